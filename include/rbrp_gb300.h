@@ -1,0 +1,177 @@
+/*
+ * rbrp_gb300.h - C ABI of the GB300-native adaptive RBRP column ID.
+ *
+ * Adaptive Robust Blockwise Random Pivoting selects k columns S of an m x n
+ * matrix A (column major) and an interpolation matrix T (k x (n-k)) with
+ * A(:, rd) ~= A(:, S) T, stopping once the squared relative residual falls
+ * below tol.  Every entry point takes plain pointers and sizes, returns an
+ * rbrp_status, never exits, throws or prints, and runs its kernels on the
+ * stream set on the handle (default: the legacy default stream).
+ *
+ * Pointers named d* are device pointers on the handle's device.
+ *
+ * Reference interfaces replaced (reference repository paths):
+ *   RBRP(m, n, A, blk, ranks, error, t_ranks, t_rbrp, flops)   gpu/rbrp.hpp:6-8
+ *       -> rbrp_RBRP (drop-in; runs to min(m, n) like the reference loop
+ *          gpu/rbrp.cu:367) and rbrp_id_f64 (adds tol and the S/T outputs).
+ *   RandAdapLUPP(A, m, n, sk, rd, T, rank, flops, tol, blk)    gpu/rid.hpp:5-7
+ *       (declared, never defined in the reference) -> rbrp_RandAdapRBRP, the
+ *          same argument meaning with callee-allocated device sk/rd/T as the
+ *          sibling RandLUPP does (gpu/randLUPP.cu:25-30).
+ *   Compute_interpolation_matrix(r, n, k, Y, P, T)             gpu/interp.hpp:7
+ *       -> rbrp_copy_T (T = R11^{-1} R12 of the RBRP factor, k x (n-k), ld >= k).
+ *   Handle_t::instance() singletons                            gpu/handle.hpp:28-61
+ *       -> rbrp_handle (one per thread / stream; no process-global state).
+ */
+#ifndef RBRP_GB300_H
+#define RBRP_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RBRP_GB300_ABI_VERSION 1
+
+typedef enum {
+  RBRP_OK = 0,
+  RBRP_ERR_INVALID_ARG = 1,   /* bad size, pointer, alignment or parameter */
+  RBRP_ERR_CUDA = 2,          /* a CUDA runtime call failed (see rbrp_last_error) */
+  RBRP_ERR_ALLOC = 3,         /* device or pinned allocation failed */
+  RBRP_ERR_NOT_COMPUTED = 4,  /* result requested before a successful run */
+  RBRP_ERR_NUMERIC = 5,       /* non-finite input or breakdown detected on device */
+  RBRP_ERR_CAPACITY = 6       /* caller buffer too small for the result */
+} rbrp_status;
+
+typedef enum {
+  RBRP_SAMPLER_NP = 0,      /* numpy Generator.choice(replace=False, p) semantics over the
+                               Philox4x64 stream (python/RBRP.ipynb cell 11 line 108) */
+  RBRP_SAMPLER_ES = 1,      /* exponential-key top-b (Efraimidis-Spirakis) over Philox */
+  RBRP_SAMPLER_GREEDY = 2   /* top-b residual norms (mode='gp', cell 11 line 112) */
+} rbrp_sampler;
+
+typedef enum {
+  RBRP_PREC_F64 = 0,        /* FP64 throughout: the plain form */
+  RBRP_PREC_F32_MIXED = 1   /* FP32 storage and projections, FP64 panels, sums and solve */
+} rbrp_precision;
+
+typedef struct {
+  double tol;          /* stop when residual < tol * ||A||_F^2 (SQUARED relative
+                          residual, python/RBRP.ipynb cell 11 line 164); <= 0: no tol */
+  int b;               /* block size (>= 1) */
+  int kmax;            /* rank cap; <= 0 means min(m, n) */
+  uint64_t seed;       /* Philox key word 0 */
+  int sampler;         /* rbrp_sampler */
+  int precision;       /* rbrp_precision (rbrp_id_f32 always uses F32_MIXED) */
+  double tol_loc;      /* robust-filter tolerance; <= 0 means 1/b (cell 11 line 90) */
+  int compute_T;       /* nonzero: compute T = R11^{-1} R12 after the loop */
+  int recompute;       /* F32_MIXED: recompute residual norms near tol (1 = on) */
+} rbrp_params;
+
+typedef struct {
+  int k;               /* rank found (|S|) */
+  int nblocks;         /* blocks completed */
+  double res0;         /* ||A||_F^2 (FP64 sum of squared column norms) */
+  double err_est;      /* final squared relative residual estimate */
+  uint64_t draws;      /* uniforms consumed from the np-compat stream */
+  double ms_total;     /* device time of the whole call (CUDA events), ms */
+  double ms_loop;      /* device time of the pivoting loop, ms */
+  double ms_T;         /* device time of the T solve, ms */
+  int recomputes;      /* residual-norm recomputations (F32_MIXED) */
+} rbrp_result;
+
+typedef struct rbrp_handle_st* rbrp_handle;
+
+/* Defaults: b = 64, tol = 1e-12, kmax = 0, seed = 0, NP sampler, F64, tol_loc = 1/b, T on. */
+void rbrp_params_default(rbrp_params* p);
+
+rbrp_status rbrp_create(rbrp_handle* h, int device);
+rbrp_status rbrp_destroy(rbrp_handle h);
+/* cudaStream_t passed as void* so this header needs no CUDA headers. */
+rbrp_status rbrp_set_stream(rbrp_handle h, void* stream);
+const char* rbrp_status_string(rbrp_status s);
+const char* rbrp_last_error(rbrp_handle h);
+int rbrp_abi_version(void);
+
+/* Adaptive RBRP column ID of a device matrix (column major, lda >= m).
+ * dPerm (n ints, device or NULL) receives the column permutation: its first
+ * k entries are the skeleton S (in selection order), the rest are rd.
+ * T stays in the handle until the next run (rbrp_copy_T / rbrp_T_device). */
+rbrp_status rbrp_id_f64(rbrp_handle h, int m, int n, const double* dA, int64_t lda,
+                        const rbrp_params* p, int* dPerm, rbrp_result* out);
+rbrp_status rbrp_id_f32(rbrp_handle h, int m, int n, const float* dA, int64_t lda,
+                        const rbrp_params* p, int* dPerm, rbrp_result* out);
+
+/* T (k x (n-k), column major) of the last run, into a device buffer with ldt >= k. */
+rbrp_status rbrp_copy_T(rbrp_handle h, double* dT, int64_t ldt);
+/* Device pointer of T of the last run (ld = k), valid until the next run. */
+rbrp_status rbrp_T_device(rbrp_handle h, const double** dT, int* ld);
+/* Per-block trace of the last run: cumulative ranks and squared relative
+ * residual estimates (gpu/rbrp.cu:467, 473-475) and cumulative device time per
+ * block in ms.  Host arrays of capacity cap; *nblocks receives the count. */
+rbrp_status rbrp_get_trace(rbrp_handle h, int* ranks, double* errors, double* t_ms,
+                           int cap, int* nblocks);
+
+/* Squared relative ID error ||A(:,rd) - A(:,S) T||_F^2 / ||A||_F^2 of the last run,
+ * recomputed in FP64 on the device (python/RBRP.ipynb cell 7 lines 40-53).
+ * dA must be the matrix of the last run (FP64 or FP32 as that run). */
+rbrp_status rbrp_id_error_f64(rbrp_handle h, int m, int n, const double* dA, int64_t lda,
+                              double* err);
+rbrp_status rbrp_id_error_f32(rbrp_handle h, int m, int n, const float* dA, int64_t lda,
+                              double* err);
+
+/* Host-buffer convenience: copies hA (host, column major, lda) in, runs, copies
+ * perm (n) and, when hT != NULL, T (k x (n-k), ldt >= k) back to host memory. */
+rbrp_status rbrp_id_f64_host(rbrp_handle h, int m, int n, const double* hA, int64_t lda,
+                             const rbrp_params* p, int* hPerm, double* hT, int64_t ldt,
+                             int64_t t_cap, rbrp_result* out);
+rbrp_status rbrp_id_f32_host(rbrp_handle h, int m, int n, const float* hA, int64_t lda,
+                             const rbrp_params* p, int* hPerm, double* hT, int64_t ldt,
+                             int64_t t_cap, rbrp_result* out);
+
+/* ---- per-phase timing (CUDA events on the handle's stream) ------------- */
+enum {
+  RBRP_PHASE_NORMS = 0,    /* initial column norms + totals */
+  RBRP_PHASE_SAMPLE = 1,   /* block sampler */
+  RBRP_PHASE_CGS = 2,      /* Gram-Schmidt coefficients + panel update + Gram */
+  RBRP_PHASE_PANEL = 3,    /* pivoted CholQR2 + filter + swap */
+  RBRP_PHASE_PROJECT = 4,  /* projection of the remaining columns + downdate */
+  RBRP_PHASE_FINISH = 5,   /* residual, stop rule, trace */
+  RBRP_PHASE_TSOLVE = 6,   /* T = R11^{-1} R12 */
+  RBRP_NPHASES = 7
+};
+typedef struct {
+  double ms[RBRP_NPHASES];      /* summed device time */
+  double bytes[RBRP_NPHASES];   /* algorithmic HBM bytes (minimum traffic) */
+  double flops[RBRP_NPHASES];   /* algorithmic flops */
+  int launches[RBRP_NPHASES];   /* kernel launches */
+} rbrp_phase_stats;
+/* When on, every phase is bracketed by CUDA events and accumulated until reset. */
+rbrp_status rbrp_set_profiling(rbrp_handle h, int on);
+rbrp_status rbrp_get_phase_stats(rbrp_handle h, rbrp_phase_stats* out);
+rbrp_status rbrp_reset_phase_stats(rbrp_handle h);
+
+/* ---- drop-in shims ----------------------------------------------------- */
+
+/* gpu/rbrp.hpp:6-8: RBRP on a device FP64 matrix (ld = m) to rank min(m, n) with
+ * block size blk.  ranks/error/t_ranks are host arrays of capacity cap filled
+ * with the cumulative per-block rank, squared relative residual and time (s);
+ * *nblocks receives their length, *t_rbrp the total time (s), *flops the
+ * algorithmic flop count (the reference leaves it unset). */
+rbrp_status rbrp_RBRP(int m, int n, double* dA, int blk, int* ranks, double* error,
+                      double* t_ranks, int cap, int* nblocks, double* t_rbrp, double* flops);
+
+/* gpu/rid.hpp:5-7 (RandAdapLUPP's argument meaning, RBRP pivoting): adaptive
+ * ID to squared relative tolerance tol with block size blk.  *sk (rank ints),
+ * *rd (n - rank ints) and *T (rank x (n - rank), ld = rank) are allocated on
+ * the device by the callee; release them with rbrp_free. */
+rbrp_status rbrp_RandAdapRBRP(const double* dA, int m, int n, int** sk, int** rd,
+                              double** T, int* rank, double* flops, double tol, int blk);
+rbrp_status rbrp_free(void* dptr);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RBRP_GB300_H */

@@ -1,0 +1,114 @@
+"""ctypes binding of ``librbrp_gb300.so`` (the C ABI of ``include/rbrp_gb300.h``).
+
+There is no fallback: if the shared library is missing, importing the
+package's compute API raises, so a GPU run can never silently route around
+the CUDA kernels.  Build it with ``python -m robust_blockwise_random_pivoting_gb300.build``.
+"""
+import ctypes
+import os
+import re
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "librbrp_gb300.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "rbrp_gb300.h")
+
+c_int, c_double, c_uint64, c_int64, c_void_p = (ctypes.c_int, ctypes.c_double, ctypes.c_uint64,
+                                                ctypes.c_int64, ctypes.c_void_p)
+
+SAMPLERS = {"np": 0, "es": 1, "greedy": 2, "gp": 2}
+PRECISIONS = {"f64": 0, "f32_mixed": 1}
+STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "allocation failed",
+          4: "no result computed", 5: "numerical failure", 6: "buffer too small"}
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("tol", c_double), ("b", c_int), ("kmax", c_int), ("seed", c_uint64),
+                ("sampler", c_int), ("precision", c_int), ("tol_loc", c_double),
+                ("compute_T", c_int), ("recompute", c_int)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("k", c_int), ("nblocks", c_int), ("res0", c_double), ("err_est", c_double),
+                ("draws", c_uint64), ("ms_total", c_double), ("ms_loop", c_double),
+                ("ms_T", c_double), ("recomputes", c_int)]
+
+
+NPHASES = 7
+PHASES = ["norms", "sample", "cgs", "panel", "project", "finish", "tsolve"]
+
+
+class PhaseStats(ctypes.Structure):
+    _fields_ = [("ms", c_double * NPHASES), ("bytes", c_double * NPHASES), ("flops", c_double * NPHASES),
+                ("launches", c_int * NPHASES)]
+
+
+class RBRPError(RuntimeError):
+    def __init__(self, status, detail=""):
+        self.status = status
+        super().__init__(f"RBRP {STATUS.get(status, status)}" + (f": {detail}" if detail else ""))
+
+
+_lib = None
+
+_SIGS = {
+    "rbrp_params_default": (None, [ctypes.POINTER(Params)]),
+    "rbrp_create": (c_int, [ctypes.POINTER(c_void_p), c_int]),
+    "rbrp_destroy": (c_int, [c_void_p]),
+    "rbrp_set_stream": (c_int, [c_void_p, c_void_p]),
+    "rbrp_status_string": (ctypes.c_char_p, [c_int]),
+    "rbrp_last_error": (ctypes.c_char_p, [c_void_p]),
+    "rbrp_abi_version": (c_int, []),
+    "rbrp_id_f64": (c_int, [c_void_p, c_int, c_int, c_void_p, c_int64, ctypes.POINTER(Params), c_void_p,
+                            ctypes.POINTER(Result)]),
+    "rbrp_id_f32": (c_int, [c_void_p, c_int, c_int, c_void_p, c_int64, ctypes.POINTER(Params), c_void_p,
+                            ctypes.POINTER(Result)]),
+    "rbrp_copy_T": (c_int, [c_void_p, c_void_p, c_int64]),
+    "rbrp_T_device": (c_int, [c_void_p, ctypes.POINTER(c_void_p), ctypes.POINTER(c_int)]),
+    "rbrp_get_trace": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int, ctypes.POINTER(c_int)]),
+    "rbrp_id_error_f64": (c_int, [c_void_p, c_int, c_int, c_void_p, c_int64, ctypes.POINTER(c_double)]),
+    "rbrp_id_error_f32": (c_int, [c_void_p, c_int, c_int, c_void_p, c_int64, ctypes.POINTER(c_double)]),
+    "rbrp_id_f64_host": (c_int, [c_void_p, c_int, c_int, c_void_p, c_int64, ctypes.POINTER(Params), c_void_p,
+                                 c_void_p, c_int64, c_int64, ctypes.POINTER(Result)]),
+    "rbrp_id_f32_host": (c_int, [c_void_p, c_int, c_int, c_void_p, c_int64, ctypes.POINTER(Params), c_void_p,
+                                 c_void_p, c_int64, c_int64, ctypes.POINTER(Result)]),
+    "rbrp_RBRP": (c_int, [c_int, c_int, c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_int,
+                          ctypes.POINTER(c_int), ctypes.POINTER(c_double), ctypes.POINTER(c_double)]),
+    "rbrp_RandAdapRBRP": (c_int, [c_void_p, c_int, c_int, ctypes.POINTER(c_void_p), ctypes.POINTER(c_void_p),
+                                  ctypes.POINTER(c_void_p), ctypes.POINTER(c_int), ctypes.POINTER(c_double),
+                                  c_double, c_int]),
+    "rbrp_free": (c_int, [c_void_p]),
+    "rbrp_set_profiling": (c_int, [c_void_p, c_int]),
+    "rbrp_get_phase_stats": (c_int, [c_void_p, ctypes.POINTER(PhaseStats)]),
+    "rbrp_reset_phase_stats": (c_int, [c_void_p]),
+}
+
+
+def header_symbols(path=HEADER):
+    """Function names declared in the C header."""
+    txt = open(path).read()
+    return sorted(set(re.findall(r"^\s*(?:rbrp_status|void|int|const char\s*\*)\s*(rbrp_\w+)\s*\(", txt, re.M)))
+
+
+def load():
+    """Load the shared library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with "
+                          "`python -m robust_blockwise_random_pivoting_gb300.build` (no CPU fallback exists)")
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(status, handle=None):
+    if status != 0:
+        detail = ""
+        if handle is not None:
+            detail = load().rbrp_last_error(handle).decode(errors="replace")
+        raise RBRPError(status, detail)

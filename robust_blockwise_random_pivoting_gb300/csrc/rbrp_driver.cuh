@@ -1,0 +1,187 @@
+// rbrp_driver.cuh - host loop of adaptive RBRP (instantiated per element type).
+//
+// One adaptive block per iteration, all sizes read by the kernels from the
+// device-resident State; the host reads the 80-byte State back once per block
+// (pinned memory) to learn whether to continue.  Follows the control flow of
+// RBRP() in gpu/rbrp.cu:333-503 and blocked_rpid in python/RBRP.ipynb cell 11
+// lines 76-173, with the stopping rule of cell 11 line 164 (squared tol).
+#pragma once
+#include <algorithm>
+
+#include "rbrp_internal.h"
+#include "rbrp_kernels.cuh"
+
+namespace rbrp {
+
+template <typename T>
+rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, const rbrp_params& p,
+                     int* dPerm, rbrp_result* out) {
+  const int kmax = p.kmax > 0 ? std::min(p.kmax, std::min(m, n)) : std::min(m, n);
+  const Layout L = make_layout(m, n, kmax, sizeof(T));
+  rbrp_status s = ensure_workspace(h, L);
+  if (s != RBRP_OK) return s;
+  {  // function attributes are per device context: set them on every call (cheap)
+    s = cuda_check(h, cudaFuncSetAttribute(k_panel1, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)sizeof(PanelSmem)), "cudaFuncSetAttribute(k_panel1)");
+    if (s != RBRP_OK) return s;
+    s = cuda_check(h, cudaFuncSetAttribute(k_panel2<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)sizeof(PanelSmem)), "cudaFuncSetAttribute(k_panel2)");
+    if (s != RBRP_OK) return s;
+  }
+  cudaStream_t st = h->stream;
+  T* Q = static_cast<T*>(h->Q);
+  T* Cpart = static_cast<T*>(h->Cpart);
+  T* C = static_cast<T*>(h->C);
+  const double tol = p.tol > 0.0 ? p.tol : 0.0;
+  const double tol_loc = p.tol_loc > 0.0 ? p.tol_loc : 1.0 / (double)p.b;
+  const int ntiles = L.ntiles;
+  const size_t panel_smem = sizeof(PanelSmem);
+  h->have_result = false;
+
+  const double es = (double)sizeof(T), dm = (double)m;
+  h->marks.clear();
+  h->prof_next = 0;
+  cudaEventRecord(h->ev_start, st);
+  cudaMemsetAsync(h->st, 0, sizeof(State), st);
+  int ev = prof_begin(h);
+  k_colnorm<T><<<(n + 7) / 8, 256, 0, st>>>(dA, lda, m, n, h->diags, h->perm, h->st);
+  k_init<<<1, 1024, 0, st>>>(h->st, h->diags, n, kmax);
+  prof_end(h, RBRP_PHASE_NORMS, ev, dm * n * es + 16.0 * n, 2.0 * dm * n, 2);
+  cudaMemcpyAsync(h->hst, h->st, sizeof(State), cudaMemcpyDeviceToHost, st);
+  s = cuda_check(h, cudaStreamSynchronize(st), "initial column norms");
+  if (s != RBRP_OK) return s;
+  if (h->hst->status) return set_error(h, RBRP_ERR_NUMERIC, "non-finite entries in A");
+
+  const int max_attempts = 4 * kmax + 64;
+  std::vector<int> attempt_of_block;
+  attempt_of_block.reserve(kmax);
+  int attempts = 0, nb_host = 0;
+  while (!h->hst->done) {
+    if (attempts >= max_attempts)
+      return set_error(h, RBRP_ERR_NUMERIC, "no progress: block attempts exceeded 4*kmax+64");
+    const int i = h->hst->i;
+    const size_t mark0 = h->marks.size();
+    ev = prof_begin(h);
+    k_sample<<<1, SAMPLE_THREADS, 0, st>>>(h->st, h->diags, h->perm, n, kmax, p.b, p.seed, p.sampler,
+                                           h->pbuf, h->kbuf, h->js, h->cols);
+    prof_end(h, RBRP_PHASE_SAMPLE, ev, 28.0 * (n - i), 0.0, 1);
+    ev = prof_begin(h);
+    if (i > 0) {
+      const int tiles = (i + 31) / 32;
+      int splits = splits_for(i, m);
+      int rps = ((m + splits - 1) / splits + 31) / 32 * 32;
+      splits = (m + rps - 1) / rps;
+      k_cgs_coef<T><<<dim3(tiles, 1, splits), 256, 0, st>>>(Q, m, dA, lda, h->cols, h->st, m, rps,
+                                                             (int64_t)i * MAXB, Cpart);
+      const int64_t cnt = (int64_t)i * MAXB;
+      k_reduce_parts<T><<<(int)std::min<int64_t>(1024, (cnt + 255) / 256), 256, 0, st>>>(Cpart, splits, cnt, cnt, C);
+    }
+    k_cgs_update<T><<<ntiles, 256, 0, st>>>(dA, lda, h->cols, Q, m, C, h->st, m, h->V, h->Gpart);
+    k_reduce_parts<double><<<16, 256, 0, st>>>(h->Gpart, ntiles, MAXB * MAXB, MAXB * MAXB, h->G);
+    prof_end(h, RBRP_PHASE_CGS, ev, 0.0, 0.0, i > 0 ? 4 : 2);
+    ev = prof_begin(h);
+    k_panel1<<<ntiles, 256, panel_smem, st>>>(h->G, h->V, m, h->st, tol_loc, h->js, h->perm, h->diags,
+                                              h->R11, h->J, h->K1, h->K2, h->Q1, h->G2part);
+    k_reduce_parts<double><<<16, 256, 0, st>>>(h->G2part, ntiles, MAXB * MAXB, MAXB * MAXB, h->G2);
+    if (i > 0) k_swap_R<<<(i + 127) / 128, 128, 0, st>>>(h->R, n, h->st, h->J, h->K1, h->K2);
+    k_panel2<T><<<ntiles, 256, panel_smem, st>>>(h->G2, h->Q1, m, h->st, Q, m, h->R, n, h->R11);
+    prof_end(h, RBRP_PHASE_PANEL, ev, 0.0, 0.0, i > 0 ? 4 : 3);
+    const int nproj = (n - i + 63) / 64;
+    ev = prof_begin(h);
+    k_project<T><<<nproj, 256, 0, st>>>(Q, m, dA, lda, h->perm, h->st, m, n, h->R, n, h->diags,
+                                        h->part_res, h->part_nnz);
+    prof_end(h, RBRP_PHASE_PROJECT, ev, 0.0, 0.0, 1);
+    ev = prof_begin(h);
+    k_finish<<<1, 1024, 0, st>>>(h->st, h->part_res, h->part_nnz, nproj, h->diags, h->js, n, kmax, tol,
+                                 h->trace_rank, h->trace_err, h->trace_samp);
+    prof_end(h, RBRP_PHASE_FINISH, ev, 16.0 * nproj, 0.0, 1);
+    while ((int)h->block_events.size() <= attempts) {
+      cudaEvent_t e;
+      s = cuda_check(h, cudaEventCreate(&e), "cudaEventCreate");
+      if (s != RBRP_OK) return s;
+      h->block_events.push_back(e);
+    }
+    cudaEventRecord(h->block_events[attempts], st);
+    cudaMemcpyAsync(h->hst, h->st, sizeof(State), cudaMemcpyDeviceToHost, st);
+    s = cuda_check(h, cudaStreamSynchronize(st), "RBRP block");
+    if (s != RBRP_OK) return s;
+    if (h->hst->status) return set_error(h, RBRP_ERR_NUMERIC, "non-finite residual during pivoting");
+    if (h->hst->nblocks > nb_host) {
+      attempt_of_block.push_back(attempts);
+      nb_host = h->hst->nblocks;
+    }
+    if (h->profiling) {  // algorithmic bytes / flops of this block, now that its sizes are known
+      const double bss = h->hst->bs_sampled, kept = h->hst->i - i, di = i;
+      const double nrem = (double)n - i - kept;
+      for (size_t q = mark0; q < h->marks.size(); ++q) {
+        auto& mk = h->marks[q];
+        if (mk.phase == RBRP_PHASE_CGS) {
+          mk.bytes = 2.0 * dm * di * es + 2.0 * dm * bss * es + 8.0 * dm * bss;
+          mk.flops = 4.0 * dm * di * bss + 2.0 * dm * bss * bss;
+        } else if (mk.phase == RBRP_PHASE_PANEL) {
+          mk.bytes = 8.0 * dm * bss + 16.0 * dm * kept + es * dm * kept;
+          mk.flops = 4.0 * dm * kept * kept;
+        } else if (mk.phase == RBRP_PHASE_PROJECT) {
+          mk.bytes = es * dm * (nrem + kept) + 8.0 * kept * nrem + 20.0 * nrem;
+          mk.flops = 2.0 * dm * nrem * kept + 2.0 * kept * nrem;
+        }
+      }
+    }
+    ++attempts;
+  }
+  cudaEventRecord(h->ev_loop, st);
+  const int k = h->hst->i;
+  h->m = m;
+  h->n = n;
+  h->k = k;
+  h->kmax = kmax;
+  if (p.compute_T && k > 0 && k < n) {
+    ev = prof_begin(h);
+    s = solve_T(h, k, n);
+    if (s != RBRP_OK) return s;
+    const double dk = k, nc = (double)n - k;
+    prof_end(h, RBRP_PHASE_TSOLVE, ev, 16.0 * dk * nc + 4.0 * dk * dk, dk * dk * nc, 2);
+  }
+  if (dPerm) cudaMemcpyAsync(dPerm, h->perm, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice, st);
+  cudaEventRecord(h->ev_end, st);
+  s = cuda_check(h, cudaStreamSynchronize(st), "RBRP finalisation");
+  if (s != RBRP_OK) return s;
+
+  prof_collect(h);
+  const int nb = h->hst->nblocks;
+  h->h_ranks.assign(nb, 0);
+  h->h_err.assign(nb, 0.0);
+  h->h_tms.assign(nb, 0.0);
+  h->h_samp.assign(nb, 0);
+  if (nb) {
+    cudaMemcpy(h->h_samp.data(), h->trace_samp, sizeof(int) * nb, cudaMemcpyDeviceToHost);
+    cudaMemcpy(h->h_ranks.data(), h->trace_rank, sizeof(int) * nb, cudaMemcpyDeviceToHost);
+    cudaMemcpy(h->h_err.data(), h->trace_err, sizeof(double) * nb, cudaMemcpyDeviceToHost);
+    for (int t = 0; t < nb; ++t) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, h->ev_start, h->block_events[attempt_of_block[t]]);
+      h->h_tms[t] = ms;
+    }
+  }
+  rbrp_result r{};
+  r.k = k;
+  r.nblocks = nb;
+  r.res0 = h->hst->res0;
+  r.err_est = h->hst->res0 > 0.0 ? h->hst->residual / h->hst->res0 : 0.0;
+  r.draws = h->hst->draws;
+  r.recomputes = h->hst->recomputes;
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, h->ev_start, h->ev_end);
+  r.ms_total = ms;
+  cudaEventElapsedTime(&ms, h->ev_start, h->ev_loop);
+  r.ms_loop = ms;
+  cudaEventElapsedTime(&ms, h->ev_loop, h->ev_end);
+  r.ms_T = ms;
+  h->res = r;
+  h->prec = sizeof(T) == 8 ? RBRP_PREC_F64 : RBRP_PREC_F32_MIXED;
+  h->have_result = true;
+  if (out) *out = r;
+  return cuda_check(h, cudaGetLastError(), "RBRP kernels");
+}
+
+}  // namespace rbrp

@@ -1,0 +1,8 @@
+// FP32-storage instantiation of the RBRP block loop (the mixed-precision form:
+// FP32 A, Q and projections; FP64 weights, panel factorisation and sums).
+#include "rbrp_driver.cuh"
+
+namespace rbrp {
+template rbrp_status run_rbrp<float>(rbrp_handle, int, int, const float*, int64_t, const rbrp_params&,
+                                     int*, rbrp_result*);
+}

@@ -1,0 +1,110 @@
+// rbrp_internal.h - host-side handle and workspace of the RBRP library.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/rbrp_gb300.h"
+#include "rbrp_common.cuh"
+
+struct rbrp_handle_st {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+
+  // device workspace (one allocation, carved; grown on demand)
+  void* ws = nullptr;
+  size_t ws_bytes = 0;
+  rbrp::State* st = nullptr;
+  rbrp::State* hst = nullptr;  // pinned host mirror of the state
+  double* diags = nullptr;
+  int* perm = nullptr;
+  void* Q = nullptr;           // m x kmax, element type of A
+  double* R = nullptr;         // kmax x n, row major
+  double* V = nullptr;         // m x MAXB
+  double* Q1 = nullptr;        // m x MAXB
+  void* Cpart = nullptr;       // split partials of Q^T A_J
+  void* C = nullptr;           // kmax x MAXB
+  double* Gpart = nullptr;
+  double* G = nullptr;
+  double* G2part = nullptr;
+  double* G2 = nullptr;
+  double* R11 = nullptr;
+  double* pbuf = nullptr;      // 2n: weights and cdf
+  unsigned long long* kbuf = nullptr;
+  int* js = nullptr;
+  int* cols = nullptr;
+  int* J = nullptr;
+  int* K1 = nullptr;
+  int* K2 = nullptr;
+  double* part_res = nullptr;
+  int* part_nnz = nullptr;
+  int* trace_rank = nullptr;
+  double* trace_err = nullptr;
+  int* trace_samp = nullptr;
+  double* err_part = nullptr;  // partial sums of the ID-error kernel
+
+  // interpolation matrix of the last run
+  double* T = nullptr;
+  size_t T_bytes = 0;
+
+  // device copy of a host matrix (host-buffer entry points)
+  void* hostA_dev = nullptr;
+  size_t hostA_bytes = 0;
+
+  // last-run results
+  bool have_result = false;
+  int m = 0, n = 0, k = 0, kmax = 0, prec = 0;
+  rbrp_result res{};
+  std::vector<int> h_ranks;
+  std::vector<double> h_err;
+  std::vector<double> h_tms;
+  std::vector<int> h_samp;
+  std::vector<cudaEvent_t> block_events;
+  cudaEvent_t ev_start = nullptr, ev_loop = nullptr, ev_end = nullptr;
+  bool smem_attr_set = false;
+
+  // per-phase profiling
+  bool profiling = false;
+  rbrp_phase_stats stats{};
+  struct PhaseMark {
+    int phase;
+    int ev0, ev1;
+    double bytes, flops;
+    int launches;
+  };
+  std::vector<cudaEvent_t> prof_events;
+  std::vector<PhaseMark> marks;
+  int prof_next = 0;
+};
+
+namespace rbrp {
+
+struct Layout {
+  int m, n, kmax, ntiles, nproj, cpart_rows;
+  size_t elem;  // sizeof element of A / Q
+};
+
+rbrp_status ensure_workspace(rbrp_handle h, const Layout& L);
+rbrp_status set_error(rbrp_handle h, rbrp_status s, const std::string& msg);
+rbrp_status cuda_check(rbrp_handle h, cudaError_t e, const char* what);
+
+template <typename T>
+rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, const rbrp_params& p,
+                     int* dPerm, rbrp_result* out);
+
+rbrp_status solve_T(rbrp_handle h, int k, int n);
+
+template <typename T>
+rbrp_status id_error(rbrp_handle h, int m, int n, const T* dA, int64_t lda, double* err);
+
+int splits_for(int i, int m);
+
+// Profiling helpers: prof_begin records an event and returns its index (-1 when off).
+int prof_begin(rbrp_handle h);
+void prof_end(rbrp_handle h, int phase, int ev0, double bytes, double flops, int launches);
+void prof_collect(rbrp_handle h);  // after a stream sync: fold the marks into h->stats
+Layout make_layout(int m, int n, int kmax, size_t elem);
+
+}  // namespace rbrp

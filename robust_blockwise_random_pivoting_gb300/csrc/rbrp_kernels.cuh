@@ -1,0 +1,874 @@
+// rbrp_kernels.cuh - sm_103a kernels of one adaptive RBRP block step.
+//
+// Per block (positions [i, i+bs) are filled), in launch order:
+//   k_sample      weighted block sampling (np-compat / exponential keys / greedy)
+//   k_cgs_coef    C = Q(:, :i)^T A(:, J)            (split-m partials)
+//   k_cgs_update  V = A(:, J) - Q(:, :i) C, Gram partials V^T V
+//   k_panel1      pivoted Cholesky of V^T V = CPQR pivots + robust filter,
+//                 Q1 = V_p R11^{-1}, Gram partials Q1^T Q1, block swap
+//   k_swap_R      R(:i, K2) = R(:i, K1), R(:i, I2) = R(:i, J)
+//   k_panel2      second CholQR pass: Q_blk = Q1 R2^{-1}, R(I2, I2) = R2 R11
+//   k_project     W = Q_blk^T A(:, perm[p]) for the remaining positions p,
+//                 R(I2, p) = W, diags(p) -= ||W(:, p)||^2 (clipped at 0)
+//   k_finish      residual, stop rule, per-block trace
+#pragma once
+#include "rbrp_common.cuh"
+
+namespace rbrp {
+// Internal linkage: this header is compiled into one translation unit per
+// element type, and each keeps its own copy of the type-independent kernels.
+namespace {
+
+// ===========================================================================
+// a1: squared column norms (initial weights) - one HBM pass over A.
+// gpu/rbrp.cu:82-99,352-356; python/RBRP.ipynb cell 11 lines 93-94.
+// One warp per column, 16-byte vector loads when the column starts are
+// 16-byte aligned, four loads in flight per lane.
+// ===========================================================================
+__device__ __forceinline__ double col_sumsq(const double* __restrict__ col, int m, int lane, bool vec) {
+  double s0 = 0.0, s1 = 0.0;
+  if (vec) {
+    const double2* c2 = reinterpret_cast<const double2*>(col);
+    const int m2 = m >> 1;
+    int r = lane;
+    for (; r + 96 < m2; r += 128) {
+      const double2 a = __ldg(c2 + r), b = __ldg(c2 + r + 32), c = __ldg(c2 + r + 64), d = __ldg(c2 + r + 96);
+      s0 = fma(a.x, a.x, s0); s1 = fma(a.y, a.y, s1);
+      s0 = fma(b.x, b.x, s0); s1 = fma(b.y, b.y, s1);
+      s0 = fma(c.x, c.x, s0); s1 = fma(c.y, c.y, s1);
+      s0 = fma(d.x, d.x, s0); s1 = fma(d.y, d.y, s1);
+    }
+    for (; r < m2; r += 32) {
+      const double2 a = __ldg(c2 + r);
+      s0 = fma(a.x, a.x, s0); s1 = fma(a.y, a.y, s1);
+    }
+    if ((m & 1) && lane == 0) { const double v = col[m - 1]; s0 = fma(v, v, s0); }
+  } else {
+    for (int r = lane; r < m; r += 32) { const double v = col[r]; s0 = fma(v, v, s0); }
+  }
+  return warp_sum(s0 + s1);
+}
+
+__device__ __forceinline__ double col_sumsq(const float* __restrict__ col, int m, int lane, bool vec) {
+  DF acc{0.f, 0.f};
+  if (vec) {
+    const float4* c4 = reinterpret_cast<const float4*>(col);
+    const int m4 = m >> 2;
+    int r = lane;
+    for (; r + 96 < m4; r += 128) {
+      const float4 a = __ldg(c4 + r), b = __ldg(c4 + r + 32), c = __ldg(c4 + r + 64), d = __ldg(c4 + r + 96);
+      df_add_sq(acc, a.x); df_add_sq(acc, a.y); df_add_sq(acc, a.z); df_add_sq(acc, a.w);
+      df_add_sq(acc, b.x); df_add_sq(acc, b.y); df_add_sq(acc, b.z); df_add_sq(acc, b.w);
+      df_add_sq(acc, c.x); df_add_sq(acc, c.y); df_add_sq(acc, c.z); df_add_sq(acc, c.w);
+      df_add_sq(acc, d.x); df_add_sq(acc, d.y); df_add_sq(acc, d.z); df_add_sq(acc, d.w);
+    }
+    for (; r < m4; r += 32) {
+      const float4 a = __ldg(c4 + r);
+      df_add_sq(acc, a.x); df_add_sq(acc, a.y); df_add_sq(acc, a.z); df_add_sq(acc, a.w);
+    }
+    for (int t = (m4 << 2) + lane; t < m; t += 32) df_add_sq(acc, col[t]);
+  } else {
+    for (int r = lane; r < m; r += 32) df_add_sq(acc, col[r]);
+  }
+  return warp_sum((double)acc.hi + (double)acc.lo);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_colnorm(const T* __restrict__ A, int64_t lda, int m, int n,
+                                                 double* __restrict__ diags, int* __restrict__ perm,
+                                                 State* st) {
+  const int lane = threadIdx.x & 31;
+  const int c = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (c >= n) return;
+  const bool vec = ((reinterpret_cast<uintptr_t>(A) & 15) == 0) && ((lda * (int64_t)sizeof(T)) % 16 == 0);
+  const double s = col_sumsq(A + (int64_t)c * lda, m, lane, vec);
+  if (lane == 0) {
+    diags[c] = s;
+    perm[c] = c;
+    if (!isfinite(s)) st->status = ST_ERR_NUMERIC;
+  }
+}
+
+// Initial totals and loop state.  One CTA.
+__global__ void __launch_bounds__(1024) k_init(State* st, const double* __restrict__ diags, int n, int kmax) {
+  __shared__ double shd[32];
+  __shared__ int shi[32];
+  double s = 0.0;
+  int c = 0;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    const double d = diags[j];
+    s += d;
+    c += d > 0.0;
+  }
+  s = block_sum(s, shd);
+  c = block_sum(c, shi);
+  if (threadIdx.x == 0) {
+    st->i = 0;
+    st->bs_sampled = 0;
+    st->bs = 0;
+    st->nblocks = 0;
+    st->zero_panel = 0;
+    st->nK = 0;
+    st->recomputes = 0;
+    st->attempts = 0;
+    st->draws = 0ull;
+    st->res0 = s;
+    st->residual = s;
+    st->nnz_rem = c;
+    st->done = (c == 0 || kmax <= 0 || st->status != 0) ? 1 : 0;
+  }
+}
+
+// ===========================================================================
+// a2: block sampler.  One CTA of 1024 threads over the n - i remaining positions.
+// NP: numpy Generator.choice(replace=False, p=w/sum(w)) rounds (python/RBRP.ipynb
+//     cell 11 line 108): uniforms from the Philox np-compat stream, cdf by a
+//     block scan, searchsorted(side='right') by binary search, first occurrences
+//     kept in draw order.  (The reference CUDA sampler draws WITH replacement
+//     and may return fewer indices, gpu/rbrp.cu:102-146.)
+// ES: keys -log(1-u)/w (u from the exponential-key stream of the original
+//     column), the bs smallest by an 8-bit radix select on the key bits.
+// GREEDY: the bs largest weights (ties: lower position), same radix select.
+// ===========================================================================
+constexpr int SAMPLE_THREADS = 1024;
+
+__global__ void __launch_bounds__(SAMPLE_THREADS)
+k_sample(State* st, const double* __restrict__ diags, const int* __restrict__ perm, int n, int kmax,
+         int b, uint64_t seed, int sampler, double* __restrict__ pbuf,
+         unsigned long long* __restrict__ kbuf, int* __restrict__ js, int* __restrict__ cols) {
+  __shared__ double shd[32];
+  __shared__ int shi[32];
+  __shared__ unsigned int hist[256];
+  __shared__ int s_rel[MAXB];
+  __shared__ int s_cand[MAXB];
+  __shared__ unsigned long long s_key[MAXB];
+  __shared__ int s_found, s_size, s_digit, s_krank, s_i, s_done;
+  __shared__ unsigned long long s_draws;
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    s_done = st->done;
+    s_i = st->i;
+    s_draws = st->draws;
+  }
+  __syncthreads();
+  if (s_done) return;
+  const int i = s_i;
+  const int nrem = n - i;
+  const int req = min(min(kmax - i, b), st->nnz_rem);
+  const int chunk = (nrem + SAMPLE_THREADS - 1) / SAMPLE_THREADS;
+  const int lo = min(nrem, tid * chunk), hi = min(nrem, lo + chunk);
+  const double* w = diags + i;
+
+  if (sampler == SAMPLER_NP) {
+    // p = w / sum(w)
+    double part = 0.0;
+    for (int j = lo; j < hi; ++j) part += w[j];
+    const double S = block_sum(part, shd);
+    int npos = 0;
+    for (int j = lo; j < hi; ++j) {
+      const double pj = w[j] / S;
+      pbuf[j] = pj;
+      npos += pj > 0.0;
+    }
+    npos = block_sum(npos, shi);
+    if (tid == 0) {
+      s_size = min(req, npos);
+      s_found = 0;
+    }
+    double* cdf = pbuf + n;  // second half of the buffer
+    __syncthreads();
+    // Rejection rounds.  Each round draws at least one new index unless every
+    // remaining positive weight is absorbed by rounding in the cdf; the cap
+    // turns that (pathological) case into a smaller sample instead of a spin.
+    for (int round = 0; s_found < s_size && round < 4096; ++round) {
+      const int found = s_found, need = s_size - s_found;
+      if (tid < found) pbuf[s_rel[tid]] = 0.0;
+      __syncthreads();
+      // inclusive cumsum: chunk-local sequential sums + block scan of chunk totals
+      double run = 0.0;
+      for (int j = lo; j < hi; ++j) {
+        run += pbuf[j];
+        cdf[j] = run;
+      }
+      const double off = block_exclusive_scan(run, shd, (double*)nullptr);
+      for (int j = lo; j < hi; ++j) cdf[j] += off;
+      __syncthreads();
+      // normalise by the last entry, as numpy's cdf /= cdf[-1]: the last entry is exactly 1
+      const double last = cdf[nrem - 1];
+      __syncthreads();
+      for (int j = lo; j < hi; ++j) cdf[j] /= last;
+      __syncthreads();
+      if (tid < need) {
+        const double x = np_uniform(seed, s_draws + (unsigned long long)tid);
+        int a = 0, z = nrem;  // first index with cdf > x (searchsorted side='right')
+        while (a < z) {
+          const int mid = (a + z) >> 1;
+          if (cdf[mid] <= x) a = mid + 1; else z = mid;
+        }
+        s_cand[tid] = a < nrem ? a : nrem - 1;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        int f = found;
+        for (int t = 0; t < need; ++t) {
+          const int c = s_cand[t];
+          bool dup = false;
+          for (int u = 0; u < t; ++u) dup |= (s_cand[u] == c);
+          if (!dup) s_rel[f++] = c;
+        }
+        s_found = f;
+        s_draws += (unsigned long long)need;
+      }
+      __syncthreads();
+    }
+    if (tid == 0) s_size = s_found;
+    __syncthreads();
+  } else {
+    // keys (ascending = preferred)
+    int npos = 0;
+    for (int j = lo; j < hi; ++j) {
+      const double wj = w[j];
+      unsigned long long key = ~0ull;
+      if (wj > 0.0) {
+        ++npos;
+        if (sampler == SAMPLER_ES) {
+          const double u = es_uniform(seed, (uint64_t)st->attempts, (uint64_t)perm[i + j]);
+          const double e = -log(1.0 - u) / wj;
+          key = (unsigned long long)__double_as_longlong(e);
+        } else {
+          key = 0x7FF0000000000000ull - (unsigned long long)__double_as_longlong(wj);
+        }
+      }
+      kbuf[j] = key;
+    }
+    npos = block_sum(npos, shi);
+    const int size = min(req, npos);
+    // radix select of the size-th smallest key
+    unsigned long long prefix = 0ull, mask = 0ull;
+    int krank = size;
+    for (int shift = 56; shift >= 0 && size > 0; shift -= 8) {
+      for (int d = tid; d < 256; d += SAMPLE_THREADS) hist[d] = 0u;
+      __syncthreads();
+      for (int j = lo; j < hi; ++j) {
+        const unsigned long long k = kbuf[j];
+        if ((k & mask) == prefix) atomicAdd(&hist[(k >> shift) & 0xFF], 1u);
+      }
+      __syncthreads();
+      if (tid == 0) {
+        int cum = 0, d = 0;
+        for (; d < 255; ++d) {
+          if (cum + (int)hist[d] >= krank) break;
+          cum += (int)hist[d];
+        }
+        s_digit = d;
+        s_krank = krank - cum;
+      }
+      __syncthreads();
+      prefix |= (unsigned long long)s_digit << shift;
+      mask |= 0xFFull << shift;
+      krank = s_krank;
+      __syncthreads();
+    }
+    const unsigned long long kth = prefix;
+    int nlt = 0, neq = 0;
+    for (int j = lo; j < hi; ++j) {
+      const unsigned long long k = kbuf[j];
+      nlt += k < kth;
+      neq += k == kth;
+    }
+    int tot_lt, tot_eq;
+    const int off_lt = block_exclusive_scan(nlt, shi, &tot_lt);
+    const int off_eq = block_exclusive_scan(neq, shi, &tot_eq);
+    const int ties = size - tot_lt;
+    int a = off_lt, e = off_eq;
+    if (size > 0) {
+      for (int j = lo; j < hi; ++j) {
+        const unsigned long long k = kbuf[j];
+        if (k < kth) {
+          s_key[a] = k;
+          s_cand[a] = j;
+          ++a;
+        } else if (k == kth) {
+          if (e < ties) {
+            s_key[tot_lt + e] = k;
+            s_cand[tot_lt + e] = j;
+          }
+          ++e;
+        }
+      }
+    }
+    __syncthreads();
+    if (tid < size) {
+      const unsigned long long k = s_key[tid];
+      const int j = s_cand[tid];
+      int rank = 0;
+      for (int u = 0; u < size; ++u) {
+        const unsigned long long ku = s_key[u];
+        rank += (ku < k) || (ku == k && s_cand[u] < j);
+      }
+      s_rel[rank] = j;
+    }
+    if (tid == 0) {
+      s_size = size;
+      s_found = size;
+    }
+    __syncthreads();
+  }
+  const int size = s_size;
+  if (tid < size) {
+    const int p = i + s_rel[tid];
+    js[tid] = p;
+    cols[tid] = perm[p];
+  }
+  if (tid == 0) {
+    st->bs_sampled = size;
+    st->draws = s_draws;
+  }
+}
+
+// ===========================================================================
+// a3: block Gram-Schmidt against the current basis (one CGS pass, as
+// python/RBRP.ipynb cell 11 line 120 and matlab/RBRP.m:55).
+// ===========================================================================
+// Cpart[z][a*MAXB + c] = sum over rows of split z of Q(r, a) * A(r, cols[c]).
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_cgs_coef(const T* __restrict__ Q, int64_t ldq, const T* __restrict__ A, int64_t lda,
+           const int* __restrict__ cols, const State* __restrict__ st, int m, int rows_per_split,
+           int64_t pstride, T* __restrict__ Cpart) {
+  __shared__ T Qs[32][33];
+  __shared__ T As[32][MAXB + 1];
+  __shared__ int cs[MAXB];
+  const int tid = threadIdx.x;
+  const int i = st->i, bss = st->bs_sampled;
+  const int a0 = blockIdx.x * 32;
+  const int rb = blockIdx.z * rows_per_split, re = min(m, rb + rows_per_split);
+  if (tid < MAXB) cs[tid] = tid < bss ? cols[tid] : -1;
+  const int al = tid >> 3, cl = tid & 7;
+  T acc[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) acc[q] = T(0);
+  for (int r0 = rb; r0 < re; r0 += 32) {
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int idx = tid + 256 * q, kk = idx & 31, aa = idx >> 5;
+      const int r = r0 + kk, a = a0 + aa;
+      Qs[kk][aa] = (r < re && a < i) ? Q[r + (int64_t)a * ldq] : T(0);
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int idx = tid + 256 * q, kk = idx & 31, cc = idx >> 5;
+      const int r = r0 + kk, c = cs[cc];
+      As[kk][cc] = (r < re && c >= 0) ? A[r + (int64_t)c * lda] : T(0);
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int kk = 0; kk < 32; ++kk) {
+      const T qa = Qs[kk][al];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) acc[q] = fma(qa, As[kk][cl + 8 * q], acc[q]);
+    }
+  }
+  const int a = a0 + al;
+  if (a < i) {
+    T* out = Cpart + (int64_t)blockIdx.z * pstride + (int64_t)a * MAXB;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) out[cl + 8 * q] = acc[q];
+  }
+}
+
+// Deterministic sum of split partials: out[x] = sum_z part[z*stride + x].
+template <typename V>
+__global__ void k_reduce_parts(const V* __restrict__ part, int nparts, int64_t stride, int64_t count,
+                               V* __restrict__ out) {
+  for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < count;
+       x += (int64_t)gridDim.x * blockDim.x) {
+    V s = V(0);
+    for (int z = 0; z < nparts; ++z) s += part[(int64_t)z * stride + x];
+    out[x] = s;
+  }
+}
+
+// V(r, c) = A(r, cols[c]) - sum_a Q(r, a) C(a, c) for 64 rows; Gram partial of the tile.
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_cgs_update(const T* __restrict__ A, int64_t lda, const int* __restrict__ cols,
+             const T* __restrict__ Q, int64_t ldq, const T* __restrict__ C,
+             const State* __restrict__ st, int m, double* __restrict__ V, double* __restrict__ Gpart) {
+  // the operand tiles and the V tile are never live together
+  constexpr size_t kOps = sizeof(T) * (64 * 33 + 32 * MAXB);
+  constexpr size_t kV = sizeof(double) * 64 * (MAXB + 1);
+  __shared__ __align__(16) unsigned char raw[kOps > kV ? kOps : kV];
+  T(*Qs)[33] = reinterpret_cast<T(*)[33]>(raw);
+  T(*Cs)[MAXB] = reinterpret_cast<T(*)[MAXB]>(raw + sizeof(T) * 64 * 33);
+  double(*Vs)[MAXB + 1] = reinterpret_cast<double(*)[MAXB + 1]>(raw);
+  __shared__ int cs[MAXB];
+  const int tid = threadIdx.x;
+  const int i = st->i, bss = st->bs_sampled;
+  const int r0 = blockIdx.x * 64;
+  if (tid < MAXB) cs[tid] = tid < bss ? cols[tid] : -1;
+  const int ty = tid >> 4, tx = tid & 15;
+  T acc[4][4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) acc[u][v] = T(0);
+  for (int a0 = 0; a0 < i; a0 += 32) {
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int idx = tid + 256 * q, rr = idx & 63, aa = idx >> 6;
+      const int r = r0 + rr, a = a0 + aa;
+      Qs[rr][aa] = (r < m && a < i) ? Q[r + (int64_t)a * ldq] : T(0);
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int idx = tid + 256 * q, cc = idx & 63, aa = idx >> 6;
+      Cs[aa][cc] = (a0 + aa < i) ? C[(int64_t)(a0 + aa) * MAXB + cc] : T(0);
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int aa = 0; aa < 32; ++aa) {
+      T qv[4], cv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) qv[u] = Qs[ty * 4 + u][aa];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) cv[v] = Cs[aa][tx + 16 * v];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = fma(qv[u], cv[v], acc[u][v]);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int rr = ty * 4 + u, r = r0 + rr;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int c = tx + 16 * v;
+      double val = 0.0;
+      if (r < m && c < bss) val = (double)A[r + (int64_t)cs[c] * lda] - (double)acc[u][v];
+      Vs[rr][c] = val;
+    }
+  }
+  __syncthreads();
+  // store V (column major, ld = m) coalesced along rows
+  for (int idx = tid; idx < 64 * MAXB; idx += 256) {
+    const int rr = idx & 63, c = idx >> 6, r = r0 + rr;
+    if (r < m && c < bss) V[r + (int64_t)c * m] = Vs[rr][c];
+  }
+  // Gram partial (bss x bss, stored MAXB x MAXB)
+  double* G = Gpart + (int64_t)blockIdx.x * MAXB * MAXB;
+  const int c1 = tid >> 2;
+  for (int q = 0; q < 16; ++q) {
+    const int c2 = (tid & 3) + 4 * q;
+    double s = 0.0;
+    if (c1 < bss && c2 < bss) {
+#pragma unroll 8
+      for (int rr = 0; rr < 64; ++rr) s = fma(Vs[rr][c1], Vs[rr][c2], s);
+    }
+    G[c1 * MAXB + c2] = s;
+  }
+}
+
+// ===========================================================================
+// a4 + a5: panel CPQR and robust filter.
+// CPQR of the m x bs panel V is computed as pivoted Cholesky of its Gram
+// matrix in shared memory: at step t the Schur complement's diagonal holds the
+// squared norms of the panel columns orthogonalised against the t pivots, so
+// the argmax is the CPQR pivot (LAPACK dgeqp3's greedy rule, swap semantics,
+// first index among ties), and its trace is the reverse cumulative sum of the
+// squared row norms of R that the robust filter tests
+// (python/RBRP.ipynb cell 11 lines 69-73, 122-123):
+//   keep t rows <=> trace_t / trace_0 >= tol_loc for every earlier step.
+// Q is then V_p R^{-1}, made orthonormal by a second CholQR pass (CholQR2).
+// ===========================================================================
+struct PanelSmem {
+  double S[MAXB][MAXB + 1];   // Gram / Schur complement
+  double R[MAXB][MAXB + 1];   // Cholesky factor rows
+  double W[64][MAXB + 1];     // row tile of the panel
+  int ord[MAXB];
+  int stop, piv;
+  double total;
+};
+
+// Pivoted Cholesky with the robust-filter stop; all threads of the CTA call it.
+__device__ int pivoted_chol_filter(PanelSmem& sm, int nb, int rows, double tol_loc) {
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  if (tid < MAXB) sm.ord[tid] = tid;
+  if (wid == 0) {
+    double d = 0.0;
+    for (int s = lane; s < nb; s += 32) d += sm.S[s][s];
+    d = warp_sum(d);
+    if (lane == 0) sm.total = d;
+  }
+  __syncthreads();
+  int kept = rows;
+  for (int t = 0; t < rows; ++t) {
+    if (wid == 0) {
+      double rem = 0.0, best = -1.0;
+      int bi = nb;
+      for (int s = t + lane; s < nb; s += 32) {
+        const double d = sm.S[s][s];
+        rem += d;
+        if (d > best) { best = d; bi = s; }
+      }
+      rem = warp_sum(rem);
+      rem = __shfl_sync(0xffffffffu, rem, 0);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_down_sync(0xffffffffu, best, o);
+        const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+      }
+      if (lane == 0) {
+        const double total = sm.total;
+        const bool stop = !(total > 0.0) || (rem / total < tol_loc) || !(best > 0.0);
+        sm.stop = stop;
+        sm.piv = bi;
+      }
+    }
+    __syncthreads();
+    if (sm.stop) { kept = t; break; }
+    const int p = sm.piv;
+    if (p != t) {
+      for (int j = tid; j < nb; j += blockDim.x) {
+        const double x = sm.S[t][j]; sm.S[t][j] = sm.S[p][j]; sm.S[p][j] = x;
+      }
+      __syncthreads();
+      for (int j = tid; j < nb; j += blockDim.x) {
+        const double x = sm.S[j][t]; sm.S[j][t] = sm.S[j][p]; sm.S[j][p] = x;
+      }
+      for (int j = tid; j < t; j += blockDim.x) {
+        const double x = sm.R[j][t]; sm.R[j][t] = sm.R[j][p]; sm.R[j][p] = x;
+      }
+      if (tid == 0) { const int o = sm.ord[t]; sm.ord[t] = sm.ord[p]; sm.ord[p] = o; }
+      __syncthreads();
+    }
+    const double rtt = sqrt(sm.S[t][t]);
+    for (int s = t + tid; s < nb; s += blockDim.x) sm.R[t][s] = (s == t) ? rtt : sm.S[t][s] / rtt;
+    __syncthreads();
+    const int w = nb - t - 1;
+    for (int idx = tid; idx < w * w; idx += blockDim.x) {
+      const int s1 = t + 1 + idx / w, s2 = t + 1 + idx % w;
+      sm.S[s1][s2] -= sm.R[t][s1] * sm.R[t][s2];
+    }
+    __syncthreads();
+  }
+  return kept;
+}
+
+// Plain Cholesky of S (n x n) into sm.R (upper); all threads call it.
+__device__ void chol_upper(PanelSmem& sm, int nb) {
+  const int tid = threadIdx.x;
+  for (int t = 0; t < nb; ++t) {
+    const double rtt = sqrt(fmax(sm.S[t][t], 0.0));
+    for (int s = t + tid; s < nb; s += blockDim.x) sm.R[t][s] = (s == t) ? rtt : sm.S[t][s] / rtt;
+    __syncthreads();
+    const int w = nb - t - 1;
+    for (int idx = tid; idx < w * w; idx += blockDim.x) {
+      const int s1 = t + 1 + idx / w, s2 = t + 1 + idx % w;
+      sm.S[s1][s2] -= sm.R[t][s1] * sm.R[t][s2];
+    }
+    __syncthreads();
+  }
+}
+
+// Forward substitution of the CTA's 64 rows: W(r, :) <- W(r, :) R^{-1} (R upper, kept x kept).
+__device__ void rows_trsm(PanelSmem& sm, int kept) {
+  const int r = threadIdx.x;
+  if (r < 64) {
+    for (int s = 0; s < kept; ++s) {
+      double x = sm.W[r][s];
+      for (int u = 0; u < s; ++u) x = fma(-sm.W[r][u], sm.R[u][s], x);
+      sm.W[r][s] = x / sm.R[s][s];
+    }
+  }
+  __syncthreads();
+}
+
+// Gram partial of the W tile (kept x kept).
+__device__ void tile_gram(const PanelSmem& sm, int kept, int rows_valid, double* G) {
+  const int tid = threadIdx.x, c1 = tid >> 2;
+  for (int q = 0; q < 16; ++q) {
+    const int c2 = (tid & 3) + 4 * q;
+    double s = 0.0;
+    if (c1 < kept && c2 < kept)
+      for (int rr = 0; rr < rows_valid; ++rr) s = fma(sm.W[rr][c1], sm.W[rr][c2], s);
+    G[c1 * MAXB + c2] = s;
+  }
+}
+
+// Every CTA factors G redundantly (identical results); CTA 0 publishes the
+// pivots, the kept count, R11 and performs the block swap of perm and diags
+// (matlab/RBRP.m:81-99: K1 = block positions not kept, ascending; K2 = kept
+// positions outside the block, in pivot order).
+__global__ void __launch_bounds__(256)
+k_panel1(const double* __restrict__ G, const double* __restrict__ V, int m, State* st, double tol_loc,
+         const int* __restrict__ js, int* __restrict__ perm, double* __restrict__ diags,
+         double* __restrict__ R11g, int* __restrict__ Jg, int* __restrict__ K1g, int* __restrict__ K2g,
+         double* __restrict__ Q1, double* __restrict__ G2part) {
+  extern __shared__ __align__(16) unsigned char dyn_smem[];
+  PanelSmem& sm = *reinterpret_cast<PanelSmem*>(dyn_smem);
+  const int tid = threadIdx.x;
+  const int nb = st->bs_sampled, i = st->i;
+  for (int idx = tid; idx < nb * nb; idx += blockDim.x) sm.S[idx / nb][idx % nb] = G[(idx / nb) * MAXB + idx % nb];
+  __syncthreads();
+  const int kept = pivoted_chol_filter(sm, nb, min(nb, m), tol_loc);
+  if (blockIdx.x == 0) {
+    for (int idx = tid; idx < MAXB * MAXB; idx += blockDim.x) {
+      const int a = idx / MAXB, c = idx % MAXB;
+      R11g[idx] = (a < kept && c < kept && c >= a) ? sm.R[a][c] : 0.0;
+    }
+    if (tid == 0) {
+      int J[MAXB], K1[MAXB], K2[MAXB];
+      int nK = 0;
+      for (int s = 0; s < kept; ++s) J[s] = js[sm.ord[s]];
+      int nk1 = 0;
+      for (int p = i; p < i + kept; ++p) {
+        bool in = false;
+        for (int s = 0; s < kept; ++s) in |= (J[s] == p);
+        if (!in) K1[nk1++] = p;
+      }
+      for (int s = 0; s < kept; ++s)
+        if (J[s] < i || J[s] >= i + kept) K2[nK++] = J[s];
+      int Tperm[MAXB];
+      for (int s = 0; s < kept; ++s) Tperm[s] = perm[J[s]];
+      for (int t = 0; t < nK; ++t) {
+        perm[K2[t]] = perm[K1[t]];
+        diags[K2[t]] = diags[K1[t]];
+      }
+      for (int s = 0; s < kept; ++s) perm[i + s] = Tperm[s];
+      for (int s = 0; s < kept; ++s) Jg[s] = J[s];
+      for (int t = 0; t < nK; ++t) { K1g[t] = K1[t]; K2g[t] = K2[t]; }
+      st->bs = kept;
+      st->nK = nK;
+      st->zero_panel = kept == 0;
+    }
+  }
+  if (kept == 0) return;
+  // Q1 rows of this tile: V_p(r, :kept) R11^{-1}
+  const int r0 = blockIdx.x * 64;
+  const int rows_valid = max(0, min(64, m - r0));
+  for (int idx = tid; idx < 64 * kept; idx += blockDim.x) {
+    const int rr = idx & 63, s = idx >> 6, r = r0 + rr;
+    sm.W[rr][s] = r < m ? V[r + (int64_t)sm.ord[s] * m] : 0.0;
+  }
+  __syncthreads();
+  rows_trsm(sm, kept);
+  for (int idx = tid; idx < 64 * kept; idx += blockDim.x) {
+    const int rr = idx & 63, s = idx >> 6, r = r0 + rr;
+    if (r < m) Q1[r + (int64_t)s * m] = sm.W[rr][s];
+  }
+  tile_gram(sm, kept, rows_valid, G2part + (int64_t)blockIdx.x * MAXB * MAXB);
+}
+
+// Column swap of the rows above the block: R(:i, K2) = R(:i, K1); R(:i, I2) = R(:i, J).
+__global__ void k_swap_R(double* __restrict__ R, int64_t ldr, const State* __restrict__ st,
+                         const int* __restrict__ Jg, const int* __restrict__ K1g, const int* __restrict__ K2g) {
+  const int i = st->i, kept = st->bs, nK = st->nK;
+  const int row = blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= i || kept == 0) return;
+  double* Rr = R + (int64_t)row * ldr;
+  double tmp[MAXB];
+  for (int s = 0; s < kept; ++s) tmp[s] = Rr[Jg[s]];
+  for (int t = 0; t < nK; ++t) Rr[K2g[t]] = Rr[K1g[t]];
+  for (int s = 0; s < kept; ++s) Rr[i + s] = tmp[s];
+}
+
+// Second CholQR pass: Q_blk = Q1 R2^{-1} (R2 = chol(Q1^T Q1)); CTA 0 writes
+// the panel R = R2 R11 into R(I2, I2) (matlab/RBRP.m:78).
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_panel2(const double* __restrict__ G2, const double* __restrict__ Q1, int m, const State* __restrict__ st,
+         T* __restrict__ Q, int64_t ldq, double* __restrict__ R, int64_t ldr, const double* __restrict__ R11g) {
+  extern __shared__ __align__(16) unsigned char dyn_smem[];
+  PanelSmem& sm = *reinterpret_cast<PanelSmem*>(dyn_smem);
+  const int tid = threadIdx.x;
+  const int kept = st->bs, i = st->i;
+  if (kept == 0) return;
+  for (int idx = tid; idx < kept * kept; idx += blockDim.x) sm.S[idx / kept][idx % kept] = G2[(idx / kept) * MAXB + idx % kept];
+  __syncthreads();
+  chol_upper(sm, kept);
+  const int r0 = blockIdx.x * 64;
+  for (int idx = tid; idx < 64 * kept; idx += blockDim.x) {
+    const int rr = idx & 63, s = idx >> 6, r = r0 + rr;
+    sm.W[rr][s] = r < m ? Q1[r + (int64_t)s * m] : 0.0;
+  }
+  __syncthreads();
+  rows_trsm(sm, kept);
+  for (int idx = tid; idx < 64 * kept; idx += blockDim.x) {
+    const int rr = idx & 63, s = idx >> 6, r = r0 + rr;
+    if (r < m) Q[r + (int64_t)(i + s) * ldq] = (T)sm.W[rr][s];
+  }
+  if (blockIdx.x == 0) {
+    for (int idx = tid; idx < kept * kept; idx += blockDim.x) {
+      const int a = idx / kept, c = idx % kept;
+      double v = 0.0;
+      if (c >= a)
+        for (int u = a; u <= c; ++u) v = fma(sm.R[a][u], R11g[u * MAXB + c], v);
+      R[(int64_t)(i + a) * ldr + (i + c)] = v;
+    }
+  }
+}
+
+// ===========================================================================
+// a7 + a8: projection of the remaining columns on the new block and the
+// residual-norm downdate (python/RBRP.ipynb cell 11 lines 132, 154-158;
+// matlab/RBRP.m:103-104,112; the reference applies Householder reflectors to
+// the whole trailing matrix instead, gpu/rbrp.cu:297-330, 453-466).
+// CTA tile: all kept (<= 64) basis vectors x 64 positions, K loop over m.
+// ===========================================================================
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_project(const T* __restrict__ Q, int64_t ldq, const T* __restrict__ A, int64_t lda,
+          const int* __restrict__ perm, const State* __restrict__ st, int m, int n,
+          double* __restrict__ R, int64_t ldr, double* __restrict__ diags,
+          double* __restrict__ part_res, int* __restrict__ part_nnz) {
+  constexpr size_t kOps = sizeof(T) * (32 * MAXB + 32 * (MAXB + 1));
+  constexpr size_t kW = sizeof(double) * MAXB * (MAXB + 1);
+  __shared__ __align__(16) unsigned char raw[kOps > kW ? kOps : kW];
+  T(*Qs)[MAXB] = reinterpret_cast<T(*)[MAXB]>(raw);
+  T(*As)[MAXB + 1] = reinterpret_cast<T(*)[MAXB + 1]>(raw + sizeof(T) * 32 * MAXB);
+  double(*Ws)[MAXB + 1] = reinterpret_cast<double(*)[MAXB + 1]>(raw);
+  __shared__ int cs[MAXB];
+  __shared__ double snew[MAXB];
+  const int tid = threadIdx.x;
+  const int i = st->i, kept = st->bs;
+  const int pbase = i + kept + blockIdx.x * 64;
+  if (kept == 0 || pbase >= n) {
+    if (tid == 0) { part_res[blockIdx.x] = 0.0; part_nnz[blockIdx.x] = 0; }
+    return;
+  }
+  if (tid < 64) cs[tid] = (pbase + tid < n) ? perm[pbase + tid] : -1;
+  const int ty = tid >> 4, tx = tid & 15;
+  T acc[4][4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) acc[u][v] = T(0);
+  const T* Qb = Q + (int64_t)i * ldq;
+  for (int r0 = 0; r0 < m; r0 += 32) {
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int idx = tid + 256 * q, kk = idx & 31, aa = idx >> 5;
+      const int r = r0 + kk;
+      Qs[kk][aa] = (r < m && aa < kept) ? Qb[r + (int64_t)aa * ldq] : T(0);
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int idx = tid + 256 * q, kk = idx & 31, cc = idx >> 5;
+      const int r = r0 + kk, c = cs[cc];
+      As[kk][cc] = (r < m && c >= 0) ? A[r + (int64_t)c * lda] : T(0);
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int kk = 0; kk < 32; ++kk) {
+      T qv[4], av[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) qv[u] = Qs[kk][ty + 16 * u];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) av[v] = As[kk][tx + 16 * v];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = fma(qv[u], av[v], acc[u][v]);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) Ws[ty + 16 * u][tx + 16 * v] = (double)acc[u][v];
+  __syncthreads();
+  for (int idx = tid; idx < kept * 64; idx += 256) {
+    const int a = idx >> 6, c = idx & 63;
+    if (pbase + c < n) R[(int64_t)(i + a) * ldr + pbase + c] = Ws[a][c];
+  }
+  if (tid < 64) {
+    const int p = pbase + tid;
+    double d = 0.0;
+    if (p < n) {
+      double s = 0.0;
+      for (int a = 0; a < kept; ++a) s = fma(Ws[a][tid], Ws[a][tid], s);
+      d = diags[p] - s;
+      d = d > 0.0 ? d : (d == d ? 0.0 : d);
+      diags[p] = d;
+    }
+    snew[tid] = d;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    double s = 0.0;
+    int c = 0;
+    for (int t = 0; t < 64; ++t) { s += snew[t]; c += snew[t] > 0.0; }
+    part_res[blockIdx.x] = s;
+    part_nnz[blockIdx.x] = c;
+  }
+}
+
+// ===========================================================================
+// a8 + a9 + a12: residual, stopping rule and per-block trace.  One CTA.
+// ===========================================================================
+__global__ void __launch_bounds__(1024)
+k_finish(State* st, const double* __restrict__ part_res, const int* __restrict__ part_nnz, int nparts,
+         double* __restrict__ diags, const int* __restrict__ js, int n, int kmax, double tol,
+         int* __restrict__ trace_rank, double* __restrict__ trace_err, int* __restrict__ trace_samp) {
+  __shared__ double shd[32];
+  __shared__ int shi[32];
+  __shared__ int s_done, s_zero, s_i, s_bs, s_bss;
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    s_done = st->done;
+    s_zero = st->zero_panel;
+    s_i = st->i;
+    s_bs = st->bs;
+    s_bss = st->bs_sampled;
+  }
+  __syncthreads();
+  if (s_done) return;
+  if (tid == 0) st->attempts += 1;
+  if (s_zero) {
+    // numerically zero panel: drop the sampled columns' weights and go on
+    if (tid < s_bss) diags[js[tid]] = 0.0;
+    __syncthreads();
+    double s = 0.0;
+    int c = 0;
+    for (int p = s_i + tid; p < n; p += blockDim.x) {
+      const double d = diags[p];
+      s += d;
+      c += d > 0.0;
+    }
+    s = block_sum(s, shd);
+    c = block_sum(c, shi);
+    if (tid == 0) {
+      st->residual = s;
+      st->nnz_rem = c;
+      st->zero_panel = 0;
+      if (c == 0 || s_bss == 0) st->done = 1;  // nothing left that can be sampled
+    }
+    return;
+  }
+  if (tid == 0) {
+    double s = 0.0;
+    int c = 0;
+    for (int z = 0; z < nparts; ++z) { s += part_res[z]; c += part_nnz[z]; }
+    const int i = s_i + s_bs;
+    const int nb = st->nblocks;
+    st->i = i;
+    st->residual = s;
+    st->nnz_rem = c;
+    trace_rank[nb] = i;
+    trace_err[nb] = st->res0 > 0.0 ? s / st->res0 : 0.0;
+    trace_samp[nb] = s_bss;
+    st->nblocks = nb + 1;
+    if ((tol > 0.0 && s < st->res0 * tol) || c == 0 || i >= kmax || !(s == s)) st->done = 1;
+    if (!(s == s)) st->status = ST_ERR_NUMERIC;
+  }
+}
+
+}  // namespace
+}  // namespace rbrp

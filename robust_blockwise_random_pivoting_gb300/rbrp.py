@@ -1,0 +1,322 @@
+"""Python host API of the GB300 RBRP column ID (over the C ABI).
+
+Mirrors the reference's entry points:
+
+* :func:`RBRP` - ``RBRP(m, n, A, blk, ranks, error, t_ranks, t_rbrp, flops)``
+  (``gpu/rbrp.hpp:6-8``): runs to rank min(m, n) and returns the per-block
+  trace.
+* :func:`rand_adap_rbrp` - ``RandAdapLUPP``'s contract (``gpu/rid.hpp:5-7``)
+  with RBRP pivoting: tolerance and block size in; skeleton ``sk``, redundant
+  set ``rd``, interpolation matrix ``T`` and rank out.
+* :func:`blocked_rpid` - the notebook's ``blocked_rpid(X, k, b, tol, mode,
+  ortho=1, tol_loc)`` (``python/RBRP.ipynb`` cell 11 lines 76-173): rows of
+  ``X`` are the items (``X = A.T``), ``tol`` bounds the squared residual.
+* :class:`Handle` - the reusable handle (workspace, stream, last result).
+
+Device memory and streams come from PyTorch; all arithmetic runs in the
+sm_103a kernels of ``librbrp_gb300.so``.
+"""
+import ctypes
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import Params, Result, check
+
+
+def _colmajor(A):
+    """A column-major (Fortran-ordered) view of a 2-D tensor, copying if needed."""
+    if A.dim() != 2:
+        raise ValueError("A must be 2-D")
+    m, _ = A.shape
+    if A.stride(0) == 1 and A.stride(1) >= max(1, m):
+        return A
+    return A.t().contiguous().t()
+
+
+@dataclass
+class IDResult:
+    perm: torch.Tensor            # (n,) int32: S = perm[:k], rd = perm[k:]
+    k: int
+    ranks: np.ndarray             # cumulative rank after each block
+    residuals: np.ndarray         # squared relative residual estimate after each block
+    t_ms: np.ndarray              # cumulative device time after each block, ms
+    res0: float
+    err_est: float
+    draws: int
+    ms_total: float
+    ms_loop: float
+    ms_T: float
+    nblocks: int
+    T: torch.Tensor = field(default=None)  # (k, n-k) FP64, column major, or None
+
+    @property
+    def S(self):
+        return self.perm[: self.k]
+
+    @property
+    def rd(self):
+        return self.perm[self.k:]
+
+
+class Handle:
+    """Owns a library handle (device workspace, CUDA stream, last result)."""
+
+    def __init__(self, device=None):
+        self.lib = _lib.load()
+        if device is None:
+            device = torch.cuda.current_device()
+        self.device = int(device)
+        h = ctypes.c_void_p()
+        check(self.lib.rbrp_create(ctypes.byref(h), self.device))
+        self.h = h
+        self.n_last = None
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.rbrp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _params(self, b, tol, kmax, seed, sampler, tol_loc, compute_T, precision, recompute):
+        p = Params()
+        self.lib.rbrp_params_default(ctypes.byref(p))
+        p.b = int(b)
+        p.tol = 0.0 if tol is None else float(tol)
+        p.kmax = int(kmax or 0)
+        p.seed = int(seed)
+        p.sampler = _lib.SAMPLERS[sampler]
+        p.tol_loc = 0.0 if tol_loc is None else float(tol_loc)
+        p.compute_T = int(bool(compute_T))
+        p.precision = _lib.PRECISIONS[precision]
+        p.recompute = int(bool(recompute))
+        return p
+
+    def _bind_stream(self, stream):
+        check(self.lib.rbrp_set_stream(self.h, ctypes.c_void_p(stream.cuda_stream)), self.h)
+
+    def column_id(self, A, b=64, tol=1e-12, kmax=None, seed=0, sampler="np", tol_loc=None,
+                  compute_T=True, recompute=True, stream=None):
+        """Adaptive RBRP column ID of the CUDA matrix ``A`` (m x n, FP64 or FP32).
+
+        FP64 runs the plain form, FP32 the mixed-precision form.  ``tol``
+        bounds the squared relative residual.  Returns an :class:`IDResult`.
+        """
+        if not A.is_cuda:
+            raise ValueError("A must be a CUDA tensor (use column_id_host for host arrays)")
+        if A.dtype not in (torch.float64, torch.float32):
+            raise TypeError("A must be float64 or float32")
+        A = _colmajor(A)
+        m, n = A.shape
+        prec = "f64" if A.dtype == torch.float64 else "f32_mixed"
+        p = self._params(b, tol, kmax, seed, sampler, tol_loc, compute_T, prec, recompute)
+        self._bind_stream(torch.cuda.current_stream(A.device) if stream is None else stream)
+        perm = torch.empty(n, dtype=torch.int32, device=A.device)
+        r = Result()
+        fn = self.lib.rbrp_id_f64 if A.dtype == torch.float64 else self.lib.rbrp_id_f32
+        check(fn(self.h, m, n, ctypes.c_void_p(A.data_ptr()), max(1, A.stride(1)), ctypes.byref(p),
+                 ctypes.c_void_p(perm.data_ptr()), ctypes.byref(r)), self.h)
+        self.n_last = n
+        res = self._result(r, perm)
+        if compute_T:
+            res.T = self.T()
+        return res
+
+    def _result(self, r, perm):
+        nb = ctypes.c_int()
+        check(self.lib.rbrp_get_trace(self.h, None, None, None, 0, ctypes.byref(nb)), self.h)
+        ranks = np.zeros(nb.value, np.int32)
+        errs = np.zeros(nb.value, np.float64)
+        tms = np.zeros(nb.value, np.float64)
+        check(self.lib.rbrp_get_trace(self.h, ranks.ctypes.data_as(ctypes.c_void_p),
+                                      errs.ctypes.data_as(ctypes.c_void_p),
+                                      tms.ctypes.data_as(ctypes.c_void_p), nb.value, ctypes.byref(nb)), self.h)
+        return IDResult(perm=perm, k=r.k, ranks=ranks, residuals=errs, t_ms=tms, res0=r.res0,
+                        err_est=r.err_est, draws=int(r.draws), ms_total=r.ms_total, ms_loop=r.ms_loop,
+                        ms_T=r.ms_T, nblocks=r.nblocks)
+
+    def T(self):
+        """T of the last run as a (k, n-k) column-major FP64 CUDA tensor (a copy)."""
+        ptr, ld = ctypes.c_void_p(), ctypes.c_int()
+        check(self.lib.rbrp_T_device(self.h, ctypes.byref(ptr), ctypes.byref(ld)), self.h)
+        k, nc = ld.value, self.n_last - ld.value
+        out = torch.empty((nc, k), dtype=torch.float64, device=f"cuda:{self.device}").t()
+        if k > 0 and nc > 0:
+            check(self.lib.rbrp_copy_T(self.h, ctypes.c_void_p(out.data_ptr()), k), self.h)
+        return out
+
+    def set_profiling(self, on=True):
+        """Bracket every phase with CUDA events (accumulated until reset)."""
+        check(self.lib.rbrp_set_profiling(self.h, int(bool(on))), self.h)
+
+    def reset_phase_stats(self):
+        check(self.lib.rbrp_reset_phase_stats(self.h), self.h)
+
+    def phase_stats(self):
+        """{phase: dict(ms, bytes, flops, launches)} accumulated since the last reset."""
+        st = _lib.PhaseStats()
+        check(self.lib.rbrp_get_phase_stats(self.h, ctypes.byref(st)), self.h)
+        return {name: dict(ms=st.ms[q], bytes=st.bytes[q], flops=st.flops[q], launches=st.launches[q])
+                for q, name in enumerate(_lib.PHASES)}
+
+    def id_error(self, A):
+        """Squared relative ID error of the last run, recomputed in FP64 on the device."""
+        A = _colmajor(A)
+        m, n = A.shape
+        e = ctypes.c_double()
+        fn = self.lib.rbrp_id_error_f64 if A.dtype == torch.float64 else self.lib.rbrp_id_error_f32
+        check(fn(self.h, m, n, ctypes.c_void_p(A.data_ptr()), max(1, A.stride(1)), ctypes.byref(e)), self.h)
+        return e.value
+
+    def column_id_host(self, A, b=64, tol=1e-12, kmax=None, seed=0, sampler="np", tol_loc=None,
+                       compute_T=True, recompute=True, perm_out=None, T_out=None):
+        """Host-buffer form: ``A`` is a host CPU tensor or numpy array (FP64 or FP32).
+
+        The host-to-device copy of A and the device-to-host copies of perm
+        and T happen inside the call (pinned buffers make them fast).
+        ``T_out`` needs room for ``min(m, n) * n`` FP64 values; T is written
+        column major with leading dimension ``min(m, n)``.  Returns
+        ``(k, perm_out, T, result)`` where ``T`` is a (k, n-k) view of ``T_out``.
+        """
+        if isinstance(A, torch.Tensor):
+            if A.is_cuda:
+                raise ValueError("column_id_host takes host memory")
+            A = _colmajor(A)
+            ptr, (m, n), lda, is64 = A.data_ptr(), A.shape, max(1, A.stride(1)), A.dtype == torch.float64
+        else:
+            A = np.asfortranarray(A)
+            if A.dtype not in (np.float64, np.float32):
+                raise TypeError("A must be float64 or float32")
+            ptr, (m, n), lda, is64 = A.ctypes.data, A.shape, A.shape[0], A.dtype == np.float64
+        prec = "f64" if is64 else "f32_mixed"
+        p = self._params(b, tol, kmax, seed, sampler, tol_loc, compute_T, prec, recompute)
+        self._bind_stream(torch.cuda.current_stream(self.device))
+        kcap = min(m, n)
+        if perm_out is None:
+            perm_out = np.empty(n, np.int32)
+        if T_out is None and compute_T:
+            T_out = np.empty(kcap * n, np.float64)
+        _ptr = lambda x: 0 if x is None else (x.data_ptr() if isinstance(x, torch.Tensor) else x.ctypes.data)
+        _len = lambda x: 0 if x is None else (x.numel() if isinstance(x, torch.Tensor) else x.size)
+        r = Result()
+        fn = self.lib.rbrp_id_f64_host if is64 else self.lib.rbrp_id_f32_host
+        check(fn(self.h, m, n, ctypes.c_void_p(ptr), lda, ctypes.byref(p), ctypes.c_void_p(_ptr(perm_out)),
+                 ctypes.c_void_p(_ptr(T_out)) if compute_T else None, kcap, _len(T_out), ctypes.byref(r)), self.h)
+        self.n_last = n
+        T = None
+        if compute_T and T_out is not None:
+            k, nc = r.k, n - r.k
+            T = T_out[: kcap * nc].reshape(nc, kcap).T[:k] if nc > 0 else T_out[:0]
+        return r.k, perm_out, T, r
+
+
+_rt = None
+
+
+def _cudart():
+    """The CUDA runtime already loaded by the library (for raw device copies)."""
+    global _rt
+    if _rt is None:
+        _lib.load()
+        _rt = ctypes.CDLL("libcudart.so.13")
+        _rt.cudaMemcpy.restype = ctypes.c_int
+        _rt.cudaMemcpy.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]
+    return _rt
+
+
+def _copy_device(src_ptr, dst, nbytes):
+    if nbytes > 0 and src_ptr:
+        rc = _cudart().cudaMemcpy(ctypes.c_void_p(dst.data_ptr()), ctypes.c_void_p(src_ptr), nbytes, 3)
+        if rc != 0:
+            raise _lib.RBRPError(2, f"cudaMemcpy failed ({rc})")
+
+
+def _fp64_colmajor(A):
+    A = _colmajor(A)
+    if A.dtype != torch.float64 or A.stride(1) != A.shape[0]:
+        A = A.to(torch.float64).t().contiguous().t()
+    return A
+
+
+def RBRP(A, blk):
+    """``RBRP(m, n, A, blk, ...)`` of ``gpu/rbrp.hpp:6-8`` on a CUDA matrix (FP64, ld = m).
+
+    Returns ``(ranks, error, t_ranks, t_rbrp, flops)``: cumulative ranks,
+    squared relative residual per block, cumulative seconds per block, total
+    seconds and the algorithmic flop count.
+    """
+    lib = _lib.load()
+    A = _fp64_colmajor(A)
+    m, n = A.shape
+    cap = min(m, n)
+    ranks = np.zeros(cap, np.int32)
+    err = np.zeros(cap, np.float64)
+    tr = np.zeros(cap, np.float64)
+    nb, t, f = ctypes.c_int(), ctypes.c_double(), ctypes.c_double()
+    with torch.cuda.device(A.device):
+        check(lib.rbrp_RBRP(m, n, ctypes.c_void_p(A.data_ptr()), int(blk), ranks.ctypes.data_as(ctypes.c_void_p),
+                            err.ctypes.data_as(ctypes.c_void_p), tr.ctypes.data_as(ctypes.c_void_p), cap,
+                            ctypes.byref(nb), ctypes.byref(t), ctypes.byref(f)))
+    k = nb.value
+    return ranks[:k], err[:k], tr[:k], t.value, f.value
+
+
+def rand_adap_rbrp(A, tol=1e-8, blk=16):
+    """``RandAdapLUPP(A, m, n, sk, rd, T, rank, flops, tol, blk)`` (``gpu/rid.hpp:5-7``) with RBRP pivoting.
+
+    Returns ``(sk, rd, T, rank, flops)`` as CUDA tensors (sk, rd int32; T FP64
+    rank x (n - rank), column major).  ``tol`` bounds the squared residual.
+    """
+    lib = _lib.load()
+    A = _fp64_colmajor(A)
+    m, n = A.shape
+    sk, rd, T = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+    rank, flops = ctypes.c_int(), ctypes.c_double()
+    with torch.cuda.device(A.device):
+        check(lib.rbrp_RandAdapRBRP(ctypes.c_void_p(A.data_ptr()), m, n, ctypes.byref(sk), ctypes.byref(rd),
+                                    ctypes.byref(T), ctypes.byref(rank), ctypes.byref(flops), float(tol), int(blk)))
+        k = rank.value
+        try:
+            sk_t = torch.empty(k, dtype=torch.int32, device=A.device)
+            rd_t = torch.empty(n - k, dtype=torch.int32, device=A.device)
+            T_t = torch.empty((n - k, k), dtype=torch.float64, device=A.device).t()
+            torch.cuda.synchronize(A.device)
+            _copy_device(sk.value, sk_t, 4 * k)
+            _copy_device(rd.value, rd_t, 4 * (n - k))
+            _copy_device(T.value, T_t, 8 * k * (n - k))
+        finally:
+            lib.rbrp_free(sk)
+            lib.rbrp_free(rd)
+            lib.rbrp_free(T)
+    return sk_t, rd_t, T_t, k, flops.value
+
+
+def blocked_rpid(X, k, b=20, tol=None, mode="rp", ortho=1, tol_loc=None, seed=0, handle=None):
+    """The notebook's ``blocked_rpid`` contract on the GPU (rows of ``X`` are the items).
+
+    ``X`` is an (n, d) CUDA tensor; the ID is the column ID of ``A = X.T``.
+    Only ``ortho=1`` (RBRP) exists.  Returns ``(row_perm, T, residuals,
+    time_pivot, ranks)``; the notebook's ``L`` factor is replaced by the
+    interpolation matrix ``T`` (k x (n-k)) that the notebook derives from it.
+    """
+    if ortho != 1:
+        raise ValueError("only ortho=1 (RBRP) is implemented")
+    sampler = {"rp": "np", "gp": "greedy"}[mode]
+    A = X.t()
+    h = handle or Handle(A.device.index)
+    r = h.column_id(A, b=b, tol=tol, kmax=k, seed=seed, sampler=sampler, tol_loc=tol_loc)
+    return (r.perm.cpu().numpy().astype(np.int64), r.T, r.residuals, r.t_ms * 1e-3,
+            r.ranks.astype(np.int64))

@@ -1,0 +1,48 @@
+"""CPU: the C-ABI library loads and exports every symbol the header declares."""
+import ctypes
+import subprocess
+
+import pytest
+
+from robust_blockwise_random_pivoting_gb300 import _lib
+
+
+def test_header_symbols_exported(rbrp_lib):
+    names = _lib.header_symbols()
+    assert "rbrp_id_f64" in names and "rbrp_RBRP" in names and "rbrp_RandAdapRBRP" in names
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.LIB_PATH], capture_output=True, text=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if line.strip()}
+    missing = [n for n in names if n not in exported]
+    assert not missing, missing
+    for n in names:
+        assert hasattr(rbrp_lib, n)
+
+
+def test_ctypes_struct_layout_matches_header(rbrp_lib):
+    assert ctypes.sizeof(_lib.Params) == 48
+    p = _lib.Params()
+    rbrp_lib.rbrp_params_default(ctypes.byref(p))
+    assert p.b == 64 and p.tol == 1e-12 and p.sampler == 0 and p.compute_T == 1 and p.kmax == 0
+    assert rbrp_lib.rbrp_abi_version() == 1
+
+
+def test_status_strings(rbrp_lib):
+    for code, text in _lib.STATUS.items():
+        assert rbrp_lib.rbrp_status_string(code).decode() == text
+
+
+def test_null_arguments_rejected_without_gpu(rbrp_lib):
+    # argument checks run before any CUDA call
+    assert rbrp_lib.rbrp_create(None, 0) == 1
+    assert rbrp_lib.rbrp_destroy(None) == 1
+    r = _lib.Result()
+    assert rbrp_lib.rbrp_id_f64(None, 4, 4, None, 4, None, None, ctypes.byref(r)) == 1
+    assert rbrp_lib.rbrp_copy_T(None, None, 0) == 1
+
+
+def test_create_without_gpu_fails_cleanly(rbrp_lib):
+    from conftest import gpu_available
+    if gpu_available():
+        pytest.skip("a GPU is present")
+    h = ctypes.c_void_p()
+    assert rbrp_lib.rbrp_create(ctypes.byref(h), 0) == 2   # RBRP_ERR_CUDA, no crash

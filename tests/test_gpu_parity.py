@@ -1,0 +1,185 @@
+"""GPU: parity of the sm_103a RBRP path (through the C ABI) with the CPU oracle.
+
+Tolerances: skeleton indices, ranks, the permutation and the number of
+uniforms consumed are compared bit for bit; squared residual estimates to
+rtol 1e-6 + atol 1e-14 (the FP64 downdate carries ~1e-16 absolute noise per
+block); ID errors to within 1.05x of the oracle's (the acceptance bound) and
+T through the reconstruction A(:, S) T to 1e-8 relative.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from oracle import id_error, interp_sid, rbrp_column_id  # noqa: E402
+from robust_blockwise_random_pivoting_gb300 import workloads as W  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def handle(rbrp_lib):
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from robust_blockwise_random_pivoting_gb300.rbrp import Handle
+    h = Handle(0)
+    yield h
+    h.close()
+
+
+def dev(A, dtype=torch.float64):
+    return torch.from_numpy(np.asfortranarray(A)).to(dtype).cuda().t().contiguous().t()
+
+
+def check_against_oracle(h, A, b, tol, sampler="np", mode="rp", seed=0, kmax=None, exact_T=True):
+    o = rbrp_column_id(A, b, tol=tol, seed=seed, sampler=sampler, mode=mode, kmax=kmax)
+    r = h.column_id(dev(A), b=b, tol=tol, seed=seed, sampler="greedy" if mode == "gp" else sampler, kmax=kmax)
+    perm = r.perm.cpu().numpy()
+    assert r.k == o["k"]
+    assert np.array_equal(r.ranks, o["ranks"])
+    assert np.array_equal(perm[: r.k], o["perm"][: o["k"]])
+    assert np.array_equal(perm, o["perm"])
+    np.testing.assert_allclose(r.residuals, o["residuals"], rtol=1e-6, atol=1e-14)
+    if sampler == "np" and mode == "rp":
+        assert r.draws == o["draws"]
+    k = r.k
+    if 0 < k < A.shape[1]:
+        T = r.T.cpu().numpy()
+        e_gpu = id_error(A, perm, T)
+        To = interp_sid(A, o["perm"], k)
+        e_ref = id_error(A, o["perm"], To)
+        assert e_gpu <= 1.05 * e_ref + 1e-28, (e_gpu, e_ref)
+        if exact_T:
+            S = o["perm"][:k]
+            rec, rec_o = A[:, S] @ T, A[:, S] @ To
+            assert np.linalg.norm(rec - rec_o) <= 1e-8 * np.linalg.norm(rec_o) + 1e-12
+        e_dev = h.id_error(dev(A))
+        np.testing.assert_allclose(e_dev, e_gpu, rtol=1e-6, atol=1e-26)
+    return r, o
+
+
+def test_gexp1000_skeleton_bit_exact(handle):
+    """The 1000 x 1000 FP64 workload, b = 40, squared tol 1e-12, Philox seed 0."""
+    A = W.gaussian_exp()
+    r, o = check_against_oracle(handle, A, 40, 1e-12)
+    assert r.k == 310
+
+
+@pytest.mark.parametrize("m,n,b,decay", [(300, 200, 16, 8.0), (129, 257, 7, 6.0), (90, 333, 64, 10.0),
+                                         (513, 65, 33, 5.0), (64, 64, 64, 3.0)])
+def test_ragged_shapes(handle, m, n, b, decay):
+    A = W.gaussian_exp(m, n, decay=decay, seed=m + n)
+    check_against_oracle(handle, A, b, 1e-10)
+
+
+@pytest.mark.parametrize("sampler", ["es", "np"])
+def test_samplers(handle, sampler):
+    A = W.snn(160, 240, r=80, r1=10, density=0.1, seed=5)
+    check_against_oracle(handle, A, 12, 1e-12, sampler=sampler, seed=3)
+
+
+def test_greedy_mode(handle):
+    A = W.gaussian_exp(200, 300, decay=7.0, seed=2)
+    check_against_oracle(handle, A, 20, 1e-10, mode="gp")
+
+
+def test_gmm_small(handle):
+    A, labels = W.gmm(64, 1500, nclusters=10, seed=1)
+    r, o = check_against_oracle(handle, A, 32, 1e-4)
+    S = r.perm[: r.k].cpu().numpy()
+    assert len(set(labels[S].tolist())) == 10   # every cluster represented
+
+
+def test_run_to_full_rank_and_kmax(handle):
+    A = W.gaussian_exp(120, 150, decay=30.0, seed=4)
+    check_against_oracle(handle, A, 16, None)
+    check_against_oracle(handle, A, 16, None, kmax=37)
+
+
+def test_zero_and_duplicate_columns(handle):
+    rng = np.random.default_rng(0)
+    B = rng.standard_normal((70, 12))
+    A = np.asfortranarray(np.concatenate([np.zeros((70, 5)), B, B, np.zeros((70, 3)), B], axis=1))
+    r, o = check_against_oracle(handle, A, 16, 1e-13)
+    assert r.k == 12
+    S = r.perm[: r.k].cpu().numpy()
+    assert all(5 <= s for s in S)
+
+
+def test_exact_rank(handle):
+    rng = np.random.default_rng(1)
+    A = np.asfortranarray(rng.standard_normal((100, 6)) @ rng.standard_normal((6, 140)))
+    r, _ = check_against_oracle(handle, A, 16, 1e-13)
+    assert r.k == 6
+
+
+def test_zero_matrix_and_tiny_shapes(handle):
+    r = handle.column_id(dev(np.zeros((30, 20))), b=8, tol=1e-12)
+    assert r.k == 0 and r.nblocks == 0
+    check_against_oracle(handle, np.ones((1, 5)), 4, 1e-12)
+    check_against_oracle(handle, np.arange(1.0, 8.0).reshape(7, 1), 4, 1e-12)
+
+
+def test_fp32_mixed_error_bound(handle):
+    A = W.gaussian_exp(400, 400, decay=12.0, seed=9)
+    o = rbrp_column_id(A, 32, tol=1e-8, seed=0)
+    To = interp_sid(A, o["perm"], o["k"])
+    e_ref = id_error(A, o["perm"], To)
+    r = handle.column_id(dev(A, torch.float32), b=32, tol=1e-8, seed=0)
+    T = r.T.cpu().numpy()
+    A32 = A.astype(np.float32).astype(np.float64)
+    e_gpu = id_error(A32, r.perm.cpu().numpy(), T)
+    assert abs(r.k - o["k"]) <= 32
+    assert e_gpu <= 1e-8 * 1.5 and e_ref <= 1e-8
+    np.testing.assert_allclose(handle.id_error(dev(A, torch.float32)), e_gpu, rtol=1e-5)
+
+
+def test_invalid_inputs_rejected(handle):
+    from robust_blockwise_random_pivoting_gb300._lib import RBRPError
+    A = dev(W.gaussian_exp(50, 60, seed=1))
+    with pytest.raises(RBRPError):
+        handle.column_id(A, b=65)
+    with pytest.raises(RBRPError):
+        handle.column_id(A, b=0)
+    bad = A.clone()
+    bad[3, 7] = float("nan")
+    with pytest.raises(RBRPError) as ei:
+        handle.column_id(bad, b=8)
+    assert ei.value.status == 5
+    # the handle stays usable after errors
+    check_against_oracle(handle, W.gaussian_exp(50, 60, seed=1), 8, 1e-10)
+
+
+def test_host_buffer_entry_point(handle):
+    A = W.gaussian_exp(200, 180, decay=9.0, seed=6)
+    o = rbrp_column_id(A, 24, tol=1e-11, seed=0)
+    k, perm, T, res = handle.column_id_host(A, b=24, tol=1e-11, seed=0)
+    assert k == o["k"] and np.array_equal(perm, o["perm"])
+    To = interp_sid(A, o["perm"], k)
+    assert id_error(A, perm, np.ascontiguousarray(T)) <= 1.05 * id_error(A, o["perm"], To) + 1e-28
+
+
+def test_dropin_RBRP_and_rand_adap(rbrp_lib, handle):
+    from robust_blockwise_random_pivoting_gb300.rbrp import RBRP, rand_adap_rbrp
+    A = W.gaussian_exp(150, 170, decay=10.0, seed=7)
+    ranks, err, t_ranks, t_total, flops = RBRP(dev(A), 20)
+    o = rbrp_column_id(A, 20, tol=None, seed=0)
+    assert np.array_equal(ranks, o["ranks"])
+    np.testing.assert_allclose(err, o["residuals"], rtol=1e-6, atol=1e-14)
+    assert t_total > 0 and flops > 0 and np.all(np.diff(t_ranks) >= 0)
+    sk, rd, T, k, flops = rand_adap_rbrp(dev(A), tol=1e-10, blk=20)
+    o = rbrp_column_id(A, 20, tol=1e-10, seed=0)
+    assert k == o["k"]
+    assert np.array_equal(sk.cpu().numpy(), o["perm"][:k]) and np.array_equal(rd.cpu().numpy(), o["perm"][k:])
+    perm = np.concatenate([sk.cpu().numpy(), rd.cpu().numpy()])
+    assert id_error(A, perm, T.cpu().numpy()) <= 1.05 * id_error(A, o["perm"], interp_sid(A, o["perm"], k)) + 1e-28
+
+
+def test_golden_oracle_fixture_cfg0(handle, golden_dir):
+    """The committed oracle output for the 1000 x 1000 workload matches the GPU."""
+    import os
+    g = np.load(os.path.join(golden_dir, "oracle_gexp1000_philox0.npz"))
+    r = handle.column_id(dev(W.gaussian_exp()), b=40, tol=1e-12, seed=0)
+    assert r.k == int(g["k"])
+    assert np.array_equal(r.perm.cpu().numpy(), g["perm"])
+    assert r.draws == int(g["draws"])

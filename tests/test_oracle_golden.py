@@ -159,3 +159,11 @@ def test_duplicate_columns_cut_by_filter():
     S = r["perm"][: r["k"]]
     assert r["k"] == 10
     assert len(set((S % 10).tolist())) == 10
+
+
+def test_oracle_fixture_cfg0_reproduces(golden_dir):
+    from robust_blockwise_random_pivoting_gb300 import workloads as W
+    g = _load(golden_dir, "oracle_gexp1000_philox0.npz")
+    r = rbrp_column_id(W.gaussian_exp(), 40, tol=1e-12, seed=0)
+    assert r["k"] == int(g["k"]) and r["draws"] == int(g["draws"])
+    assert np.array_equal(r["perm"], g["perm"])
