@@ -160,15 +160,17 @@ int splits_for(int i, int m) {
   return s > cap ? cap : s;
 }
 
-Layout make_layout(int m, int n, int kmax, size_t elem) {
+Layout make_layout(int m, int n, int kmax, size_t elem, bool residual) {
   Layout L;
   L.m = m;
   L.n = n;
   L.kmax = kmax;
   L.ntiles = (m + 63) / 64;
   L.nproj = (n + 63) / 64;
-  L.cpart_rows = kmax > 304 * 32 ? kmax : 304 * 32;
+  L.cpart_rows = residual ? 1 : (kmax > 304 * 32 ? kmax : 304 * 32);
   L.elem = elem;
+  L.residual = residual;
+  L.ld_res = residual ? ((int64_t)m + 31) / 32 * 32 : 0;  // 128-byte aligned columns
   return L;
 }
 
@@ -198,12 +200,13 @@ rbrp_status ensure_workspace(rbrp_handle h, const Layout& L) {
       {(void**)&h->perm, n * 4},
       {(void**)&h->pbuf, 2 * n * 8},
       {(void**)&h->kbuf, n * 8},
-      {(void**)&h->Q, m * kmax * el},
+      {(void**)&h->Q, m * (L.residual ? (size_t)MAXB : kmax) * el},
+      {(void**)&h->Ares, L.residual ? (size_t)L.ld_res * n * sizeof(float) : 0},
       {(void**)&h->R, kmax * n * 8},
       {(void**)&h->V, m * MAXB * 8},
       {(void**)&h->Q1, m * MAXB * 8},
       {(void**)&h->Cpart, (size_t)L.cpart_rows * MAXB * el},
-      {(void**)&h->C, kmax * MAXB * el},
+      {(void**)&h->C, (L.residual ? 1 : kmax) * MAXB * el},
       {(void**)&h->Gpart, (size_t)L.ntiles * M2 * 8},
       {(void**)&h->G, M2 * 8},
       {(void**)&h->G2part, (size_t)L.ntiles * M2 * 8},
@@ -231,6 +234,7 @@ rbrp_status ensure_workspace(rbrp_handle h, const Layout& L) {
     if (s != RBRP_OK) return s;
     h->ws_bytes = total;
   }
+  h->ld_res = L.ld_res;
   char* base = static_cast<char*>(h->ws);
   size_t off = 0;
   for (auto& it : items) {

@@ -16,8 +16,11 @@ namespace rbrp {
 template <typename T>
 rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, const rbrp_params& p,
                      int* dPerm, rbrp_result* out) {
+  // FP64: the notebook's implicit form (projections of A, downdated norms) -
+  // the parity path.  FP32: the explicit residual form (see k_proj_w).
+  constexpr bool RES = sizeof(T) == sizeof(float);
   const int kmax = p.kmax > 0 ? std::min(p.kmax, std::min(m, n)) : std::min(m, n);
-  const Layout L = make_layout(m, n, kmax, sizeof(T));
+  const Layout L = make_layout(m, n, kmax, sizeof(T), RES);
   rbrp_status s = ensure_workspace(h, L);
   if (s != RBRP_OK) return s;
   {  // function attributes are per device context: set them on every call (cheap)
@@ -27,6 +30,11 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
     s = cuda_check(h, cudaFuncSetAttribute(k_panel2<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)sizeof(PanelSmem)), "cudaFuncSetAttribute(k_panel2)");
     if (s != RBRP_OK) return s;
+    if (RES) {
+      s = cuda_check(h, cudaFuncSetAttribute(k_resid_update, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)P2_SMEM), "cudaFuncSetAttribute(k_resid_update)");
+      if (s != RBRP_OK) return s;
+    }
   }
   cudaStream_t st = h->stream;
   T* Q = static_cast<T*>(h->Q);
@@ -44,9 +52,12 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
   cudaEventRecord(h->ev_start, st);
   cudaMemsetAsync(h->st, 0, sizeof(State), st);
   int ev = prof_begin(h);
+  if (RES)  // the residual starts as A, in position (= column) order
+    cudaMemcpy2DAsync(h->Ares, (size_t)L.ld_res * sizeof(float), dA, (size_t)lda * sizeof(T), (size_t)m * sizeof(T),
+                      n, cudaMemcpyDeviceToDevice, st);
   k_colnorm<T><<<(n + 7) / 8, 256, 0, st>>>(dA, lda, m, n, h->diags, h->perm, h->st);
   k_init<<<1, 1024, 0, st>>>(h->st, h->diags, n, kmax);
-  prof_end(h, RBRP_PHASE_NORMS, ev, dm * n * es + 16.0 * n, 2.0 * dm * n, 2);
+  prof_end(h, RBRP_PHASE_NORMS, ev, (RES ? 3.0 : 1.0) * dm * n * es + 16.0 * n, 2.0 * dm * n, RES ? 3 : 2);
   cudaMemcpyAsync(h->hst, h->st, sizeof(State), cudaMemcpyDeviceToHost, st);
   s = cuda_check(h, cudaStreamSynchronize(st), "initial column norms");
   if (s != RBRP_OK) return s;
@@ -66,7 +77,7 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
                                            h->pbuf, h->kbuf, h->js, h->cols);
     prof_end(h, RBRP_PHASE_SAMPLE, ev, 28.0 * (n - i), 0.0, 1);
     ev = prof_begin(h);
-    if (i > 0) {
+    if (!RES && i > 0) {
       const int tiles = (i + 31) / 32;
       int splits = splits_for(i, m);
       int rps = ((m + splits - 1) / splits + 31) / 32 * 32;
@@ -76,21 +87,35 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
       const int64_t cnt = (int64_t)i * MAXB;
       k_reduce_parts<T><<<(int)std::min<int64_t>(1024, (cnt + 255) / 256), 256, 0, st>>>(Cpart, splits, cnt, cnt, C);
     }
-    k_cgs_update<T><<<ntiles, 256, 0, st>>>(dA, lda, h->cols, Q, m, C, h->st, m, h->V, h->Gpart);
+    if (RES)  // panel = residual columns at the sampled positions
+      k_cgs_update<T><<<ntiles, 256, 0, st>>>((const T*)h->Ares, L.ld_res, h->js, Q, m, C, h->st, m, h->V,
+                                              h->Gpart, 0);
+    else
+      k_cgs_update<T><<<ntiles, 256, 0, st>>>(dA, lda, h->cols, Q, m, C, h->st, m, h->V, h->Gpart, 1);
     k_reduce_parts<double><<<16, 256, 0, st>>>(h->Gpart, ntiles, MAXB * MAXB, MAXB * MAXB, h->G);
-    prof_end(h, RBRP_PHASE_CGS, ev, 0.0, 0.0, i > 0 ? 4 : 2);
+    prof_end(h, RBRP_PHASE_CGS, ev, 0.0, 0.0, (!RES && i > 0) ? 4 : 2);
     ev = prof_begin(h);
     k_panel1<<<ntiles, 256, panel_smem, st>>>(h->G, h->V, m, h->st, tol_loc, h->js, h->perm, h->diags,
                                               h->R11, h->J, h->K1, h->K2, h->Q1, h->G2part);
     k_reduce_parts<double><<<16, 256, 0, st>>>(h->G2part, ntiles, MAXB * MAXB, MAXB * MAXB, h->G2);
     if (i > 0) k_swap_R<<<(i + 127) / 128, 128, 0, st>>>(h->R, n, h->st, h->J, h->K1, h->K2);
-    k_panel2<T><<<ntiles, 256, panel_smem, st>>>(h->G2, h->Q1, m, h->st, Q, m, h->R, n, h->R11);
-    prof_end(h, RBRP_PHASE_PANEL, ev, 0.0, 0.0, i > 0 ? 4 : 3);
-    const int nproj = (n - i + 63) / 64;
+    if (RES)
+      k_swap_cols<<<dim3((m + 1023) / 1024, MAXB), 256, 0, st>>>(h->Ares, L.ld_res, h->st, m, h->K1, h->K2);
+    k_panel2<T><<<ntiles, 256, panel_smem, st>>>(h->G2, h->Q1, m, h->st, Q, m, h->R, n, h->R11, RES ? 0 : 1);
+    prof_end(h, RBRP_PHASE_PANEL, ev, 0.0, 0.0, (i > 0 ? 4 : 3) + (RES ? 1 : 0));
+    int nproj;
     ev = prof_begin(h);
-    k_project<T><<<nproj, 256, 0, st>>>(Q, m, dA, lda, h->perm, h->st, m, n, h->R, n, h->diags,
-                                        h->part_res, h->part_nnz);
-    prof_end(h, RBRP_PHASE_PROJECT, ev, 0.0, 0.0, 1);
+    if (RES) {
+      nproj = (n - i + P2_COLS - 1) / P2_COLS;
+      k_proj_w<<<(n - i + 63) / 64, 128, 0, st>>>((const float*)Q, m, h->Ares, L.ld_res, h->st, m, n, h->R, n);
+      k_resid_update<<<nproj, 256, P2_SMEM, st>>>((const float*)Q, m, h->Ares, L.ld_res, h->st, m, n, h->R, n,
+                                                 h->diags, h->part_res, h->part_nnz);
+    } else {
+      nproj = (n - i + 63) / 64;
+      k_project<T><<<nproj, 256, 0, st>>>(Q, m, dA, lda, h->perm, h->st, m, n, h->R, n, h->diags,
+                                          h->part_res, h->part_nnz);
+    }
+    prof_end(h, RBRP_PHASE_PROJECT, ev, 0.0, 0.0, RES ? 2 : 1);
     ev = prof_begin(h);
     k_finish<<<1, 1024, 0, st>>>(h->st, h->part_res, h->part_nnz, nproj, h->diags, h->js, n, kmax, tol,
                                  h->trace_rank, h->trace_err, h->trace_samp);
@@ -116,14 +141,18 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
       for (size_t q = mark0; q < h->marks.size(); ++q) {
         auto& mk = h->marks[q];
         if (mk.phase == RBRP_PHASE_CGS) {
-          mk.bytes = 2.0 * dm * di * es + 2.0 * dm * bss * es + 8.0 * dm * bss;
-          mk.flops = 4.0 * dm * di * bss + 2.0 * dm * bss * bss;
+          const double dq = RES ? 0.0 : di;  // the residual form gathers, no Gram-Schmidt
+          mk.bytes = 2.0 * dm * dq * es + (RES ? 1.0 : 2.0) * dm * bss * es + 8.0 * dm * bss;
+          mk.flops = 4.0 * dm * dq * bss + 2.0 * dm * bss * bss;
         } else if (mk.phase == RBRP_PHASE_PANEL) {
           mk.bytes = 8.0 * dm * bss + 16.0 * dm * kept + es * dm * kept;
           mk.flops = 4.0 * dm * kept * kept;
         } else if (mk.phase == RBRP_PHASE_PROJECT) {
-          mk.bytes = es * dm * (nrem + kept) + 8.0 * kept * nrem + 20.0 * nrem;
-          mk.flops = 2.0 * dm * nrem * kept + 2.0 * kept * nrem;
+          // implicit form: one read of the remaining columns; residual form: read for W,
+          // read + write for the update
+          mk.bytes = (RES ? 3.0 : 1.0) * es * dm * nrem + es * dm * kept + (RES ? 16.0 : 8.0) * kept * nrem +
+                     20.0 * nrem;
+          mk.flops = (RES ? 4.0 : 2.0) * dm * nrem * kept + 2.0 * kept * nrem;
         }
       }
     }

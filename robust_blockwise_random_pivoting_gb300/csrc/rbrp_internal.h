@@ -44,6 +44,8 @@ struct rbrp_handle_st {
   double* trace_err = nullptr;
   int* trace_samp = nullptr;
   double* err_part = nullptr;  // partial sums of the ID-error kernel
+  float* Ares = nullptr;       // residual form: position-ordered FP32 residual, ld_res x n
+  int64_t ld_res = 0;
 
   // interpolation matrix of the last run
   double* T = nullptr;
@@ -83,7 +85,9 @@ namespace rbrp {
 
 struct Layout {
   int m, n, kmax, ntiles, nproj, cpart_rows;
-  size_t elem;  // sizeof element of A / Q
+  size_t elem;    // sizeof element of A / Q
+  bool residual;  // FP32 residual form: Q holds one block, A_res is allocated
+  int64_t ld_res;
 };
 
 rbrp_status ensure_workspace(rbrp_handle h, const Layout& L);
@@ -105,6 +109,6 @@ int splits_for(int i, int m);
 int prof_begin(rbrp_handle h);
 void prof_end(rbrp_handle h, int phase, int ev0, double bytes, double flops, int launches);
 void prof_collect(rbrp_handle h);  // after a stream sync: fold the marks into h->stats
-Layout make_layout(int m, int n, int kmax, size_t elem);
+Layout make_layout(int m, int n, int kmax, size_t elem, bool residual);
 
 }  // namespace rbrp

@@ -395,7 +395,8 @@ template <typename T>
 __global__ void __launch_bounds__(256)
 k_cgs_update(const T* __restrict__ A, int64_t lda, const int* __restrict__ cols,
              const T* __restrict__ Q, int64_t ldq, const T* __restrict__ C,
-             const State* __restrict__ st, int m, double* __restrict__ V, double* __restrict__ Gpart) {
+             const State* __restrict__ st, int m, double* __restrict__ V, double* __restrict__ Gpart,
+             int use_q) {
   // the operand tiles and the V tile are never live together
   constexpr size_t kOps = sizeof(T) * (64 * 33 + 32 * MAXB);
   constexpr size_t kV = sizeof(double) * 64 * (MAXB + 1);
@@ -405,7 +406,7 @@ k_cgs_update(const T* __restrict__ A, int64_t lda, const int* __restrict__ cols,
   double(*Vs)[MAXB + 1] = reinterpret_cast<double(*)[MAXB + 1]>(raw);
   __shared__ int cs[MAXB];
   const int tid = threadIdx.x;
-  const int i = st->i, bss = st->bs_sampled;
+  const int i = use_q ? st->i : 0, bss = st->bs_sampled;
   const int r0 = blockIdx.x * 64;
   if (tid < MAXB) cs[tid] = tid < bss ? cols[tid] : -1;
   const int ty = tid >> 4, tx = tid & 15;
@@ -683,7 +684,8 @@ __global__ void k_swap_R(double* __restrict__ R, int64_t ldr, const State* __res
 template <typename T>
 __global__ void __launch_bounds__(256)
 k_panel2(const double* __restrict__ G2, const double* __restrict__ Q1, int m, const State* __restrict__ st,
-         T* __restrict__ Q, int64_t ldq, double* __restrict__ R, int64_t ldr, const double* __restrict__ R11g) {
+         T* __restrict__ Q, int64_t ldq, double* __restrict__ R, int64_t ldr, const double* __restrict__ R11g,
+         int q_at_i) {
   extern __shared__ __align__(16) unsigned char dyn_smem[];
   PanelSmem& sm = *reinterpret_cast<PanelSmem*>(dyn_smem);
   const int tid = threadIdx.x;
@@ -701,7 +703,7 @@ k_panel2(const double* __restrict__ G2, const double* __restrict__ Q1, int m, co
   rows_trsm(sm, kept);
   for (int idx = tid; idx < 64 * kept; idx += blockDim.x) {
     const int rr = idx & 63, s = idx >> 6, r = r0 + rr;
-    if (r < m) Q[r + (int64_t)(i + s) * ldq] = (T)sm.W[rr][s];
+    if (r < m) Q[r + (int64_t)((q_at_i ? i : 0) + s) * ldq] = (T)sm.W[rr][s];
   }
   if (blockIdx.x == 0) {
     for (int idx = tid; idx < kept * kept; idx += blockDim.x) {
@@ -807,6 +809,193 @@ k_project(const T* __restrict__ Q, int64_t ldq, const T* __restrict__ A, int64_t
     for (int t = 0; t < 64; ++t) { s += snew[t]; c += snew[t] > 0.0; }
     part_res[blockIdx.x] = s;
     part_nnz[blockIdx.x] = c;
+  }
+}
+
+// ===========================================================================
+// Residual form (FP32 storage).  The residual A_res = (I - Q Q^T) A is kept
+// explicitly, position ordered, and updated after every block - the
+// trailing-matrix update of gpu/rbrp.cu:297-330,448 (Householder there,
+// Q_blk W here) - so every residual norm is recomputed exactly from the
+// residual instead of downdated: a downdate ||a||^2 - ||Q^T a||^2 in FP32
+// arithmetic cannot resolve residuals below ~1e-7 of ||a||^2.
+// ===========================================================================
+
+// Block swap of the residual's columns: A_res(:, K2) = A_res(:, K1).  Kept
+// columns need no copy (their residual was gathered into the panel already).
+__global__ void k_swap_cols(float* __restrict__ Ares, int64_t ld, const State* __restrict__ st, int m,
+                            const int* __restrict__ K1g, const int* __restrict__ K2g) {
+  const int t = blockIdx.y;
+  if (t >= st->nK) return;
+  const float* src = Ares + (int64_t)K1g[t] * ld;
+  float* dst = Ares + (int64_t)K2g[t] * ld;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) dst[r] = src[r];
+}
+
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
+  const float t = hi + x;
+  const float bb = t - hi;
+  lo += (hi - (t - bb)) + (x - bb);
+  hi = t;
+}
+
+// P1: W = Q_blk^T A_res(:, p) for the remaining positions p, into R(I2, p).
+// CTA tile 64 basis vectors x 64 positions, 32-row K stages; each stage's FP32
+// partial sums are folded into double-float accumulators (TwoSum), so W is
+// accurate to ~1e-8 relative over m = 16384 rows.
+__global__ void __launch_bounds__(128)
+k_proj_w(const float* __restrict__ Qb, int64_t ldq, const float* __restrict__ Ares, int64_t ld,
+         const State* __restrict__ st, int m, int n, double* __restrict__ R, int64_t ldr) {
+  __shared__ __align__(16) float Qs[32][MAXB];
+  __shared__ __align__(16) float As[32][MAXB + 4];
+  const int tid = threadIdx.x;
+  const int i = st->i, kept = st->bs;
+  const int p0 = i + kept + blockIdx.x * 64;
+  if (kept == 0 || p0 >= n) return;
+  const int ncol = min(64, n - p0);
+  const int ta = tid >> 4, tc = tid & 15;  // rows a = ta*8 + u, columns c = tc*4 + v
+  float hi[8][4], lo[8][4];
+#pragma unroll
+  for (int u = 0; u < 8; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) hi[u][v] = lo[u][v] = 0.f;
+  for (int r0 = 0; r0 < m; r0 += 32) {
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      const int idx = tid + 128 * q, kk = idx & 31, aa = idx >> 5, r = r0 + kk;
+      Qs[kk][aa] = (r < m && aa < kept) ? Qb[r + (int64_t)aa * ldq] : 0.f;
+    }
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      const int idx = tid + 128 * q, kk = idx & 31, cc = idx >> 5, r = r0 + kk;
+      As[kk][cc] = (r < m && cc < ncol) ? Ares[r + (int64_t)(p0 + cc) * ld] : 0.f;
+    }
+    __syncthreads();
+    float c[8][4];
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) c[u][v] = 0.f;
+#pragma unroll 8
+    for (int kk = 0; kk < 32; ++kk) {
+      const float4 q0 = *reinterpret_cast<const float4*>(&Qs[kk][ta * 8]);
+      const float4 q1 = *reinterpret_cast<const float4*>(&Qs[kk][ta * 8 + 4]);
+      const float4 a4 = *reinterpret_cast<const float4*>(&As[kk][tc * 4]);
+      const float qv[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
+      const float av[4] = {a4.x, a4.y, a4.z, a4.w};
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) c[u][v] = fmaf(qv[u], av[v], c[u][v]);
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) two_sum_acc(hi[u][v], lo[u][v], c[u][v]);
+  }
+#pragma unroll
+  for (int u = 0; u < 8; ++u) {
+    const int a = ta * 8 + u;
+    if (a < kept) {
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const int cc = tc * 4 + v;
+        if (cc < ncol) R[(int64_t)(i + a) * ldr + p0 + cc] = (double)hi[u][v] + (double)lo[u][v];
+      }
+    }
+  }
+}
+
+// P2: A_res(:, p) -= Q_blk W(:, p) and diags(p) = ||A_res(:, p)||^2 (double-float
+// sums), for 128 positions per CTA over all m rows.  Warp w owns 16 columns,
+// lane l rows l + 32u of each 128-row stage (coalesced along the column).
+constexpr int P2_COLS = 128;
+constexpr int P2_ROWS = 128;
+constexpr size_t P2_SMEM = sizeof(float) * (size_t)MAXB * (P2_COLS + P2_ROWS);
+
+__global__ void __launch_bounds__(256)
+k_resid_update(const float* __restrict__ Qb, int64_t ldq, float* __restrict__ Ares, int64_t ld,
+               const State* __restrict__ st, int m, int n, const double* __restrict__ R, int64_t ldr,
+               double* __restrict__ diags, double* __restrict__ part_res, int* __restrict__ part_nnz) {
+  extern __shared__ __align__(16) float p2_smem[];
+  float* Ws = p2_smem;                       // Ws[a * P2_COLS + c]
+  float* Qs = p2_smem + MAXB * P2_COLS;      // Qs[a * P2_ROWS + rr]
+  __shared__ double snew[P2_COLS];
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const int i = st->i, kept = st->bs;
+  const int p0 = i + kept + blockIdx.x * P2_COLS;
+  if (kept == 0 || p0 >= n) {
+    if (tid == 0) { part_res[blockIdx.x] = 0.0; part_nnz[blockIdx.x] = 0; }
+    return;
+  }
+  const int ncol = min(P2_COLS, n - p0);
+  for (int idx = tid; idx < kept * P2_COLS; idx += 256) {
+    const int a = idx / P2_COLS, c = idx % P2_COLS;
+    Ws[idx] = c < ncol ? (float)R[(int64_t)(i + a) * ldr + p0 + c] : 0.f;
+  }
+  DF nrm[16];
+#pragma unroll
+  for (int c = 0; c < 16; ++c) nrm[c].hi = nrm[c].lo = 0.f;
+  for (int r0 = 0; r0 < m; r0 += P2_ROWS) {
+    __syncthreads();
+    for (int idx = tid; idx < kept * P2_ROWS; idx += 256) {
+      const int a = idx / P2_ROWS, rr = idx % P2_ROWS;
+      Qs[idx] = (r0 + rr < m) ? Qb[r0 + rr + (int64_t)a * ldq] : 0.f;
+    }
+    __syncthreads();
+    float acc[4][16];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int c = 0; c < 16; ++c) acc[u][c] = 0.f;
+    for (int a = 0; a < kept; ++a) {
+      float qv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) qv[u] = Qs[a * P2_ROWS + lane + 32 * u];
+      const float4* w4 = reinterpret_cast<const float4*>(Ws + a * P2_COLS + w * 16);
+      const float4 x0 = w4[0], x1 = w4[1], x2 = w4[2], x3 = w4[3];
+      const float wv[16] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w,
+                            x2.x, x2.y, x2.z, x2.w, x3.x, x3.y, x3.z, x3.w};
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int c = 0; c < 16; ++c) acc[u][c] = fmaf(qv[u], wv[c], acc[u][c]);
+    }
+#pragma unroll
+    for (int c = 0; c < 16; ++c) {
+      const int cc = w * 16 + c;
+      if (cc < ncol) {
+        float* col = Ares + (int64_t)(p0 + cc) * ld;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int r = r0 + lane + 32 * u;
+          if (r < m) {
+            const float x = col[r] - acc[u][c];
+            col[r] = x;
+            df_add_sq(nrm[c], x);
+          }
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 16; ++c) {
+    double v = (double)nrm[c].hi + (double)nrm[c].lo;
+    v = warp_sum(v);
+    if (lane == 0) {
+      const int cc = w * 16 + c;
+      if (cc < ncol) diags[p0 + cc] = v;
+      snew[cc] = cc < ncol ? v : 0.0;
+    }
+  }
+  __syncthreads();
+  if (tid == 0) {
+    double sres = 0.0;
+    int cnt = 0;
+    for (int c = 0; c < P2_COLS; ++c) { sres += snew[c]; cnt += snew[c] > 0.0; }
+    part_res[blockIdx.x] = sres;
+    part_nnz[blockIdx.x] = cnt;
   }
 }
 

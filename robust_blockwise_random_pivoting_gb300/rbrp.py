@@ -30,10 +30,16 @@ def _colmajor(A):
     """A column-major (Fortran-ordered) view of a 2-D tensor, copying if needed."""
     if A.dim() != 2:
         raise ValueError("A must be 2-D")
-    m, _ = A.shape
-    if A.stride(0) == 1 and A.stride(1) >= max(1, m):
+    m, n = A.shape
+    if (A.stride(0) == 1 or m == 1) and (A.stride(1) >= max(1, m) or n == 1):
         return A
     return A.t().contiguous().t()
+
+
+def _ld(A):
+    """Leading dimension of a column-major tensor (size-1 dimensions carry arbitrary strides)."""
+    m, n = A.shape
+    return max(1, m) if n == 1 else max(1, m, A.stride(1)) if m == 1 else A.stride(1)
 
 
 @dataclass
@@ -127,7 +133,7 @@ class Handle:
         perm = torch.empty(n, dtype=torch.int32, device=A.device)
         r = Result()
         fn = self.lib.rbrp_id_f64 if A.dtype == torch.float64 else self.lib.rbrp_id_f32
-        check(fn(self.h, m, n, ctypes.c_void_p(A.data_ptr()), max(1, A.stride(1)), ctypes.byref(p),
+        check(fn(self.h, m, n, ctypes.c_void_p(A.data_ptr()), _ld(A), ctypes.byref(p),
                  ctypes.c_void_p(perm.data_ptr()), ctypes.byref(r)), self.h)
         self.n_last = n
         res = self._result(r, perm)
@@ -178,7 +184,7 @@ class Handle:
         m, n = A.shape
         e = ctypes.c_double()
         fn = self.lib.rbrp_id_error_f64 if A.dtype == torch.float64 else self.lib.rbrp_id_error_f32
-        check(fn(self.h, m, n, ctypes.c_void_p(A.data_ptr()), max(1, A.stride(1)), ctypes.byref(e)), self.h)
+        check(fn(self.h, m, n, ctypes.c_void_p(A.data_ptr()), _ld(A), ctypes.byref(e)), self.h)
         return e.value
 
     def column_id_host(self, A, b=64, tol=1e-12, kmax=None, seed=0, sampler="np", tol_loc=None,
@@ -195,7 +201,7 @@ class Handle:
             if A.is_cuda:
                 raise ValueError("column_id_host takes host memory")
             A = _colmajor(A)
-            ptr, (m, n), lda, is64 = A.data_ptr(), A.shape, max(1, A.stride(1)), A.dtype == torch.float64
+            ptr, (m, n), lda, is64 = A.data_ptr(), A.shape, _ld(A), A.dtype == torch.float64
         else:
             A = np.asfortranarray(A)
             if A.dtype not in (np.float64, np.float32):
