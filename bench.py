@@ -317,7 +317,8 @@ def main():
     except OSError:
         pass
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    dom = max(("project", "tsolve", "cgs", "panel", "sample", "norms", "finish"), key=lambda q: stats[q]["ms"])
+    dom = max(("project", "update", "tsolve", "cgs", "panel", "sample", "norms", "finish"),
+              key=lambda q: stats[q]["ms"])
     st = stats[dom]
     launches = max(1, st["launches"])
     per_launch_ms = st["ms"] / launches

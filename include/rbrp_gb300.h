@@ -42,7 +42,8 @@ typedef enum {
   RBRP_ERR_ALLOC = 3,         /* device or pinned allocation failed */
   RBRP_ERR_NOT_COMPUTED = 4,  /* result requested before a successful run */
   RBRP_ERR_NUMERIC = 5,       /* non-finite input or breakdown detected on device */
-  RBRP_ERR_CAPACITY = 6       /* caller buffer too small for the result */
+  RBRP_ERR_CAPACITY = 6,      /* caller buffer too small for the result */
+  RBRP_ERR_DEVICE_TIMEOUT = 7 /* a bounded device-side wait expired; the kernel exited cleanly */
 } rbrp_status;
 
 typedef enum {
@@ -137,10 +138,11 @@ enum {
   RBRP_PHASE_SAMPLE = 1,   /* block sampler */
   RBRP_PHASE_CGS = 2,      /* Gram-Schmidt coefficients + panel update + Gram */
   RBRP_PHASE_PANEL = 3,    /* pivoted CholQR2 + filter + swap */
-  RBRP_PHASE_PROJECT = 4,  /* projection of the remaining columns + downdate */
+  RBRP_PHASE_PROJECT = 4,  /* projection W = Q_blk^T A of the remaining columns (+ downdate, FP64) */
   RBRP_PHASE_FINISH = 5,   /* residual, stop rule, trace */
   RBRP_PHASE_TSOLVE = 6,   /* T = R11^{-1} R12 */
-  RBRP_NPHASES = 7
+  RBRP_PHASE_UPDATE = 7,   /* residual update A_res -= Q_blk W + exact norms (FP32 form) */
+  RBRP_NPHASES = 8
 };
 typedef struct {
   double ms[RBRP_NPHASES];      /* summed device time */

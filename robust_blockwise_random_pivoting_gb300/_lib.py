@@ -18,7 +18,7 @@ c_int, c_double, c_uint64, c_int64, c_void_p = (ctypes.c_int, ctypes.c_double, c
 SAMPLERS = {"np": 0, "es": 1, "greedy": 2, "gp": 2}
 PRECISIONS = {"f64": 0, "f32_mixed": 1}
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "allocation failed",
-          4: "no result computed", 5: "numerical failure", 6: "buffer too small"}
+          4: "no result computed", 5: "numerical failure", 6: "buffer too small", 7: "device wait timed out"}
 
 
 class Params(ctypes.Structure):
@@ -33,8 +33,8 @@ class Result(ctypes.Structure):
                 ("ms_T", c_double), ("recomputes", c_int)]
 
 
-NPHASES = 7
-PHASES = ["norms", "sample", "cgs", "panel", "project", "finish", "tsolve"]
+NPHASES = 8
+PHASES = ["norms", "sample", "cgs", "panel", "project", "finish", "tsolve", "update"]
 
 
 class PhaseStats(ctypes.Structure):
@@ -80,6 +80,7 @@ _SIGS = {
     "rbrp_set_profiling": (c_int, [c_void_p, c_int]),
     "rbrp_get_phase_stats": (c_int, [c_void_p, ctypes.POINTER(PhaseStats)]),
     "rbrp_reset_phase_stats": (c_int, [c_void_p]),
+    "rbrp_set_variant": (c_int, [c_void_p, c_int]),
 }
 
 

@@ -5,7 +5,11 @@
 #include <cstring>
 #include <new>
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "rbrp_internal.h"
+#include "../../include/rbrp_gb300_testing.h"
 
 namespace rbrp {
 
@@ -202,6 +206,8 @@ rbrp_status ensure_workspace(rbrp_handle h, const Layout& L) {
       {(void**)&h->kbuf, n * 8},
       {(void**)&h->Q, m * (L.residual ? (size_t)MAXB : kmax) * el},
       {(void**)&h->Ares, L.residual ? (size_t)L.ld_res * n * sizeof(float) : 0},
+      {(void**)&h->Qh, L.residual ? (size_t)L.ld_res * MAXB * sizeof(float) : 0},
+      {(void**)&h->Ql, L.residual ? (size_t)L.ld_res * MAXB * sizeof(float) : 0},
       {(void**)&h->R, kmax * n * 8},
       {(void**)&h->V, m * MAXB * 8},
       {(void**)&h->Q1, m * MAXB * 8},
@@ -212,6 +218,8 @@ rbrp_status ensure_workspace(rbrp_handle h, const Layout& L) {
       {(void**)&h->G2part, (size_t)L.ntiles * M2 * 8},
       {(void**)&h->G2, M2 * 8},
       {(void**)&h->R11, M2 * 8},
+      {(void**)&h->R2, M2 * 8},
+      {(void**)&h->ord, MAXB * 4},
       {(void**)&h->js, MAXB * 4},
       {(void**)&h->cols, MAXB * 4},
       {(void**)&h->J, MAXB * 4},
@@ -245,6 +253,35 @@ rbrp_status ensure_workspace(rbrp_handle h, const Layout& L) {
     rbrp_status s = cuda_check(h, cudaMallocHost((void**)&h->hst, sizeof(State)), "cudaMallocHost(state)");
     if (s != RBRP_OK) return s;
   }
+  return RBRP_OK;
+}
+
+static PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    else
+      cudaGetLastError();
+  }
+  return fn;
+}
+
+rbrp_status make_tmap_f32(rbrp_handle h, void* map, const float* base, uint64_t inner, uint64_t outer,
+                          uint64_t ld_elems, uint32_t box_inner, uint32_t box_outer) {
+  auto fn = tmap_encoder();
+  if (!fn) return set_error(h, RBRP_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
+  cuuint64_t dims[2] = {inner, outer};
+  cuuint64_t strides[1] = {ld_elems * sizeof(float)};
+  cuuint32_t box[2] = {box_inner, box_outer};
+  cuuint32_t es[2] = {1, 1};
+  CUresult r = fn(static_cast<CUtensorMap*>(map), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims,
+                  strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return set_error(h, RBRP_ERR_CUDA, "cuTensorMapEncodeTiled failed");
   return RBRP_OK;
 }
 
@@ -452,6 +489,7 @@ const char* rbrp_status_string(rbrp_status s) {
     case RBRP_ERR_NOT_COMPUTED: return "no result computed";
     case RBRP_ERR_NUMERIC: return "numerical failure";
     case RBRP_ERR_CAPACITY: return "buffer too small";
+    case RBRP_ERR_DEVICE_TIMEOUT: return "device wait timed out";
   }
   return "unknown status";
 }
@@ -601,6 +639,12 @@ rbrp_status rbrp_get_phase_stats(rbrp_handle h, rbrp_phase_stats* out) {
 rbrp_status rbrp_reset_phase_stats(rbrp_handle h) {
   if (!h) return RBRP_ERR_INVALID_ARG;
   std::memset(&h->stats, 0, sizeof(h->stats));
+  return RBRP_OK;
+}
+
+rbrp_status rbrp_set_variant(rbrp_handle h, int variant) {
+  if (!h || variant < 0 || variant > 1) return RBRP_ERR_INVALID_ARG;
+  h->variant = variant;
   return RBRP_OK;
 }
 

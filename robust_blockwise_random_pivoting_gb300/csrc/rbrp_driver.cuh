@@ -10,6 +10,7 @@
 
 #include "rbrp_internal.h"
 #include "rbrp_kernels.cuh"
+#include "rbrp_tc.cuh"
 
 namespace rbrp {
 
@@ -24,9 +25,11 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
   rbrp_status s = ensure_workspace(h, L);
   if (s != RBRP_OK) return s;
   {  // function attributes are per device context: set them on every call (cheap)
-    s = cuda_check(h, cudaFuncSetAttribute(k_panel1, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)sizeof(PanelSmem)), "cudaFuncSetAttribute(k_panel1)");
-    if (s != RBRP_OK) return s;
+    for (const void* fn : {(const void*)k_pchol, (const void*)k_panel1, (const void*)k_chol2}) {
+      s = cuda_check(h, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(PanelSmem)),
+                     "cudaFuncSetAttribute(panel)");
+      if (s != RBRP_OK) return s;
+    }
     s = cuda_check(h, cudaFuncSetAttribute(k_panel2<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)sizeof(PanelSmem)), "cudaFuncSetAttribute(k_panel2)");
     if (s != RBRP_OK) return s;
@@ -34,9 +37,22 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
       s = cuda_check(h, cudaFuncSetAttribute(k_resid_update, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)P2_SMEM), "cudaFuncSetAttribute(k_resid_update)");
       if (s != RBRP_OK) return s;
+      s = cuda_check(h, cudaFuncSetAttribute(tc::k_proj_w_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)tc::P1_SMEM), "cudaFuncSetAttribute(k_proj_w_tc)");
+      if (s != RBRP_OK) return s;
     }
   }
   cudaStream_t st = h->stream;
+  const bool use_tc = RES && h->variant == 0;
+  CUtensorMap tmA, tmQh, tmQl;
+  if (use_tc) {  // TMA views: A_res (m x n) and the split basis (m x 64), boxes of 32 rows
+    s = make_tmap_f32(h, &tmA, h->Ares, m, n, L.ld_res, tc::BK, tc::BM);
+    if (s == RBRP_OK) s = make_tmap_f32(h, &tmQh, h->Qh, m, MAXB, L.ld_res, tc::BK, tc::BN);
+    if (s == RBRP_OK) s = make_tmap_f32(h, &tmQl, h->Ql, m, MAXB, L.ld_res, tc::BK, tc::BN);
+    if (s != RBRP_OK) return s;
+    cudaMemsetAsync(h->Qh, 0, (size_t)L.ld_res * MAXB * sizeof(float), st);
+    cudaMemsetAsync(h->Ql, 0, (size_t)L.ld_res * MAXB * sizeof(float), st);
+  }
   T* Q = static_cast<T*>(h->Q);
   T* Cpart = static_cast<T*>(h->Cpart);
   T* C = static_cast<T*>(h->C);
@@ -95,27 +111,37 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
     k_reduce_parts<double><<<16, 256, 0, st>>>(h->Gpart, ntiles, MAXB * MAXB, MAXB * MAXB, h->G);
     prof_end(h, RBRP_PHASE_CGS, ev, 0.0, 0.0, (!RES && i > 0) ? 4 : 2);
     ev = prof_begin(h);
-    k_panel1<<<ntiles, 256, panel_smem, st>>>(h->G, h->V, m, h->st, tol_loc, h->js, h->perm, h->diags,
-                                              h->R11, h->J, h->K1, h->K2, h->Q1, h->G2part);
+    k_pchol<<<1, 256, panel_smem, st>>>(h->G, m, h->st, tol_loc, h->js, h->perm, h->diags, h->R11, h->ord,
+                                        h->J, h->K1, h->K2);
+    k_panel1<<<ntiles, 256, panel_smem, st>>>(h->V, m, h->st, h->R11, h->ord, h->Q1, h->G2part);
     k_reduce_parts<double><<<16, 256, 0, st>>>(h->G2part, ntiles, MAXB * MAXB, MAXB * MAXB, h->G2);
+    k_chol2<<<1, 256, panel_smem, st>>>(h->G2, h->st, h->R11, h->R2, h->R, n);
     if (i > 0) k_swap_R<<<(i + 127) / 128, 128, 0, st>>>(h->R, n, h->st, h->J, h->K1, h->K2);
     if (RES)
       k_swap_cols<<<dim3((m + 1023) / 1024, MAXB), 256, 0, st>>>(h->Ares, L.ld_res, h->st, m, h->K1, h->K2);
-    k_panel2<T><<<ntiles, 256, panel_smem, st>>>(h->G2, h->Q1, m, h->st, Q, m, h->R, n, h->R11, RES ? 0 : 1);
-    prof_end(h, RBRP_PHASE_PANEL, ev, 0.0, 0.0, (i > 0 ? 4 : 3) + (RES ? 1 : 0));
+    k_panel2<T><<<ntiles, 256, panel_smem, st>>>(h->Q1, m, h->st, h->R2, Q, m, RES ? 0 : 1,
+                                                 use_tc ? h->Qh : nullptr, use_tc ? h->Ql : nullptr, L.ld_res);
+    prof_end(h, RBRP_PHASE_PANEL, ev, 0.0, 0.0, (i > 0 ? 6 : 5) + (RES ? 1 : 0));
     int nproj;
     ev = prof_begin(h);
     if (RES) {
       nproj = (n - i + P2_COLS - 1) / P2_COLS;
-      k_proj_w<<<(n - i + 63) / 64, 128, 0, st>>>((const float*)Q, m, h->Ares, L.ld_res, h->st, m, n, h->R, n);
+      if (use_tc)
+        tc::k_proj_w_tc<<<(n - i + tc::BM - 1) / tc::BM, tc::NTHREADS, tc::P1_SMEM, st>>>(tmA, tmQh, tmQl, h->st, m,
+                                                                                        n, h->R, n);
+      else
+        k_proj_w<<<(n - i + 63) / 64, 128, 0, st>>>((const float*)Q, m, h->Ares, L.ld_res, h->st, m, n, h->R, n);
+      prof_end(h, RBRP_PHASE_PROJECT, ev, 0.0, 0.0, 1);
+      ev = prof_begin(h);
       k_resid_update<<<nproj, 256, P2_SMEM, st>>>((const float*)Q, m, h->Ares, L.ld_res, h->st, m, n, h->R, n,
                                                  h->diags, h->part_res, h->part_nnz);
+      prof_end(h, RBRP_PHASE_UPDATE, ev, 0.0, 0.0, 1);
     } else {
       nproj = (n - i + 63) / 64;
       k_project<T><<<nproj, 256, 0, st>>>(Q, m, dA, lda, h->perm, h->st, m, n, h->R, n, h->diags,
                                           h->part_res, h->part_nnz);
+      prof_end(h, RBRP_PHASE_PROJECT, ev, 0.0, 0.0, 1);
     }
-    prof_end(h, RBRP_PHASE_PROJECT, ev, 0.0, 0.0, RES ? 2 : 1);
     ev = prof_begin(h);
     k_finish<<<1, 1024, 0, st>>>(h->st, h->part_res, h->part_nnz, nproj, h->diags, h->js, n, kmax, tol,
                                  h->trace_rank, h->trace_err, h->trace_samp);
@@ -130,6 +156,8 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
     cudaMemcpyAsync(h->hst, h->st, sizeof(State), cudaMemcpyDeviceToHost, st);
     s = cuda_check(h, cudaStreamSynchronize(st), "RBRP block");
     if (s != RBRP_OK) return s;
+    if (h->hst->status == tc::ST_ERR_TIMEOUT)
+      return set_error(h, RBRP_ERR_DEVICE_TIMEOUT, "a device-side wait timed out; the kernel aborted cleanly");
     if (h->hst->status) return set_error(h, RBRP_ERR_NUMERIC, "non-finite residual during pivoting");
     if (h->hst->nblocks > nb_host) {
       attempt_of_block.push_back(attempts);
@@ -148,11 +176,14 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
           mk.bytes = 8.0 * dm * bss + 16.0 * dm * kept + es * dm * kept;
           mk.flops = 4.0 * dm * kept * kept;
         } else if (mk.phase == RBRP_PHASE_PROJECT) {
-          // implicit form: one read of the remaining columns; residual form: read for W,
-          // read + write for the update
-          mk.bytes = (RES ? 3.0 : 1.0) * es * dm * nrem + es * dm * kept + (RES ? 16.0 : 8.0) * kept * nrem +
-                     20.0 * nrem;
-          mk.flops = (RES ? 4.0 : 2.0) * dm * nrem * kept + 2.0 * kept * nrem;
+          // one read of the remaining columns and the basis, W written to R
+          mk.bytes = es * dm * nrem + (RES ? 2.0 : 1.0) * es * dm * kept + 8.0 * kept * nrem +
+                     (RES ? 0.0 : 20.0 * nrem);
+          mk.flops = 2.0 * dm * nrem * kept;
+        } else if (mk.phase == RBRP_PHASE_UPDATE) {
+          // read + write of the remaining residual columns, W read, norms written
+          mk.bytes = 2.0 * es * dm * nrem + es * dm * kept + 8.0 * kept * nrem + 8.0 * nrem;
+          mk.flops = 2.0 * dm * nrem * kept + 2.0 * dm * nrem;
         }
       }
     }

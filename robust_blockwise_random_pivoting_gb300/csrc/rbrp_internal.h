@@ -31,6 +31,8 @@ struct rbrp_handle_st {
   double* G2part = nullptr;
   double* G2 = nullptr;
   double* R11 = nullptr;
+  double* R2 = nullptr;
+  int* ord = nullptr;
   double* pbuf = nullptr;      // 2n: weights and cdf
   unsigned long long* kbuf = nullptr;
   int* js = nullptr;
@@ -46,6 +48,9 @@ struct rbrp_handle_st {
   double* err_part = nullptr;  // partial sums of the ID-error kernel
   float* Ares = nullptr;       // residual form: position-ordered FP32 residual, ld_res x n
   int64_t ld_res = 0;
+  float* Qh = nullptr;         // residual form: TF32 hi / lo parts of the block basis, ld_res x 64
+  float* Ql = nullptr;
+  int variant = 0;             // 0: tensor-core projection, 1: CUDA-core projection
 
   // interpolation matrix of the last run
   double* T = nullptr;
@@ -99,6 +104,10 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
                      int* dPerm, rbrp_result* out);
 
 rbrp_status solve_T(rbrp_handle h, int k, int n);
+
+// 2-D FP32 TMA descriptor (inner dimension contiguous, 128-byte swizzle).
+rbrp_status make_tmap_f32(rbrp_handle h, void* map, const float* base, uint64_t inner, uint64_t outer,
+                          uint64_t ld_elems, uint32_t box_inner, uint32_t box_outer);
 
 template <typename T>
 rbrp_status id_error(rbrp_handle h, int m, int n, const T* dA, int64_t lda, double* err);

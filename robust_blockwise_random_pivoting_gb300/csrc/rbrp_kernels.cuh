@@ -590,27 +590,28 @@ __device__ void rows_trsm(PanelSmem& sm, int kept) {
   __syncthreads();
 }
 
-// Gram partial of the W tile (kept x kept).
+// Gram partial of the W tile (kept x kept): upper triangle computed, mirrored.
 __device__ void tile_gram(const PanelSmem& sm, int kept, int rows_valid, double* G) {
   const int tid = threadIdx.x, c1 = tid >> 2;
   for (int q = 0; q < 16; ++q) {
     const int c2 = (tid & 3) + 4 * q;
+    if (c2 < c1) continue;
     double s = 0.0;
     if (c1 < kept && c2 < kept)
       for (int rr = 0; rr < rows_valid; ++rr) s = fma(sm.W[rr][c1], sm.W[rr][c2], s);
     G[c1 * MAXB + c2] = s;
+    G[c2 * MAXB + c1] = s;
   }
 }
 
-// Every CTA factors G redundantly (identical results); CTA 0 publishes the
-// pivots, the kept count, R11 and performs the block swap of perm and diags
-// (matlab/RBRP.m:81-99: K1 = block positions not kept, ascending; K2 = kept
-// positions outside the block, in pivot order).
+// k_pchol (one CTA): pivoted Cholesky of the panel Gram matrix with the robust
+// filter; publishes the pivots (ord), the kept count, R11 and performs the block
+// swap of perm and diags (matlab/RBRP.m:81-99: K1 = block positions not kept,
+// ascending; K2 = kept positions outside the block, in pivot order).
 __global__ void __launch_bounds__(256)
-k_panel1(const double* __restrict__ G, const double* __restrict__ V, int m, State* st, double tol_loc,
-         const int* __restrict__ js, int* __restrict__ perm, double* __restrict__ diags,
-         double* __restrict__ R11g, int* __restrict__ Jg, int* __restrict__ K1g, int* __restrict__ K2g,
-         double* __restrict__ Q1, double* __restrict__ G2part) {
+k_pchol(const double* __restrict__ G, int m, State* st, double tol_loc, const int* __restrict__ js,
+        int* __restrict__ perm, double* __restrict__ diags, double* __restrict__ R11g, int* __restrict__ ordg,
+        int* __restrict__ Jg, int* __restrict__ K1g, int* __restrict__ K2g) {
   extern __shared__ __align__(16) unsigned char dyn_smem[];
   PanelSmem& sm = *reinterpret_cast<PanelSmem*>(dyn_smem);
   const int tid = threadIdx.x;
@@ -618,44 +619,58 @@ k_panel1(const double* __restrict__ G, const double* __restrict__ V, int m, Stat
   for (int idx = tid; idx < nb * nb; idx += blockDim.x) sm.S[idx / nb][idx % nb] = G[(idx / nb) * MAXB + idx % nb];
   __syncthreads();
   const int kept = pivoted_chol_filter(sm, nb, min(nb, m), tol_loc);
-  if (blockIdx.x == 0) {
-    for (int idx = tid; idx < MAXB * MAXB; idx += blockDim.x) {
-      const int a = idx / MAXB, c = idx % MAXB;
-      R11g[idx] = (a < kept && c < kept && c >= a) ? sm.R[a][c] : 0.0;
-    }
-    if (tid == 0) {
-      int J[MAXB], K1[MAXB], K2[MAXB];
-      int nK = 0;
-      for (int s = 0; s < kept; ++s) J[s] = js[sm.ord[s]];
-      int nk1 = 0;
-      for (int p = i; p < i + kept; ++p) {
-        bool in = false;
-        for (int s = 0; s < kept; ++s) in |= (J[s] == p);
-        if (!in) K1[nk1++] = p;
-      }
-      for (int s = 0; s < kept; ++s)
-        if (J[s] < i || J[s] >= i + kept) K2[nK++] = J[s];
-      int Tperm[MAXB];
-      for (int s = 0; s < kept; ++s) Tperm[s] = perm[J[s]];
-      for (int t = 0; t < nK; ++t) {
-        perm[K2[t]] = perm[K1[t]];
-        diags[K2[t]] = diags[K1[t]];
-      }
-      for (int s = 0; s < kept; ++s) perm[i + s] = Tperm[s];
-      for (int s = 0; s < kept; ++s) Jg[s] = J[s];
-      for (int t = 0; t < nK; ++t) { K1g[t] = K1[t]; K2g[t] = K2[t]; }
-      st->bs = kept;
-      st->nK = nK;
-      st->zero_panel = kept == 0;
-    }
+  for (int idx = tid; idx < MAXB * MAXB; idx += blockDim.x) {
+    const int a = idx / MAXB, c = idx % MAXB;
+    R11g[idx] = (a < kept && c < kept && c >= a) ? sm.R[a][c] : 0.0;
   }
+  if (tid < MAXB) ordg[tid] = sm.ord[tid];
+  if (tid == 0) {
+    int J[MAXB], K1[MAXB], K2[MAXB];
+    int nK = 0;
+    for (int s = 0; s < kept; ++s) J[s] = js[sm.ord[s]];
+    int nk1 = 0;
+    for (int p = i; p < i + kept; ++p) {
+      bool in = false;
+      for (int s = 0; s < kept; ++s) in |= (J[s] == p);
+      if (!in) K1[nk1++] = p;
+    }
+    for (int s = 0; s < kept; ++s)
+      if (J[s] < i || J[s] >= i + kept) K2[nK++] = J[s];
+    int Tperm[MAXB];
+    for (int s = 0; s < kept; ++s) Tperm[s] = perm[J[s]];
+    for (int t = 0; t < nK; ++t) {
+      perm[K2[t]] = perm[K1[t]];
+      diags[K2[t]] = diags[K1[t]];
+    }
+    for (int s = 0; s < kept; ++s) perm[i + s] = Tperm[s];
+    for (int s = 0; s < kept; ++s) Jg[s] = J[s];
+    for (int t = 0; t < nK; ++t) { K1g[t] = K1[t]; K2g[t] = K2[t]; }
+    st->bs = kept;
+    st->nK = nK;
+    st->zero_panel = kept == 0;
+  }
+}
+
+// Load an upper-triangular kept x kept factor (MAXB stride) into sm.R.
+__device__ __forceinline__ void load_factor(PanelSmem& sm, const double* __restrict__ Rg, int kept) {
+  for (int idx = threadIdx.x; idx < kept * kept; idx += blockDim.x) sm.R[idx / kept][idx % kept] = Rg[(idx / kept) * MAXB + idx % kept];
+}
+
+// Q1 = V(:, ord[:kept]) R11^{-1} for 64 rows per CTA, and the Gram partial of Q1.
+__global__ void __launch_bounds__(256)
+k_panel1(const double* __restrict__ V, int m, const State* __restrict__ st, const double* __restrict__ R11g,
+         const int* __restrict__ ordg, double* __restrict__ Q1, double* __restrict__ G2part) {
+  extern __shared__ __align__(16) unsigned char dyn_smem[];
+  PanelSmem& sm = *reinterpret_cast<PanelSmem*>(dyn_smem);
+  const int tid = threadIdx.x;
+  const int kept = st->bs;
   if (kept == 0) return;
-  // Q1 rows of this tile: V_p(r, :kept) R11^{-1}
+  load_factor(sm, R11g, kept);
   const int r0 = blockIdx.x * 64;
   const int rows_valid = max(0, min(64, m - r0));
   for (int idx = tid; idx < 64 * kept; idx += blockDim.x) {
     const int rr = idx & 63, s = idx >> 6, r = r0 + rr;
-    sm.W[rr][s] = r < m ? V[r + (int64_t)sm.ord[s] * m] : 0.0;
+    sm.W[rr][s] = r < m ? V[r + (int64_t)ordg[s] * m] : 0.0;
   }
   __syncthreads();
   rows_trsm(sm, kept);
@@ -664,6 +679,32 @@ k_panel1(const double* __restrict__ G, const double* __restrict__ V, int m, Stat
     if (r < m) Q1[r + (int64_t)s * m] = sm.W[rr][s];
   }
   tile_gram(sm, kept, rows_valid, G2part + (int64_t)blockIdx.x * MAXB * MAXB);
+}
+
+// k_chol2 (one CTA): R2 = chol(Q1^T Q1) and the panel R = R2 R11 into R(I2, I2)
+// (matlab/RBRP.m:78); R2 is published for the second row solve.
+__global__ void __launch_bounds__(256)
+k_chol2(const double* __restrict__ G2, const State* __restrict__ st, const double* __restrict__ R11g,
+        double* __restrict__ R2g, double* __restrict__ R, int64_t ldr) {
+  extern __shared__ __align__(16) unsigned char dyn_smem[];
+  PanelSmem& sm = *reinterpret_cast<PanelSmem*>(dyn_smem);
+  const int tid = threadIdx.x;
+  const int kept = st->bs, i = st->i;
+  if (kept == 0) return;
+  for (int idx = tid; idx < kept * kept; idx += blockDim.x) sm.S[idx / kept][idx % kept] = G2[(idx / kept) * MAXB + idx % kept];
+  __syncthreads();
+  chol_upper(sm, kept);
+  for (int idx = tid; idx < MAXB * MAXB; idx += blockDim.x) {
+    const int a = idx / MAXB, c = idx % MAXB;
+    R2g[idx] = (a < kept && c < kept && c >= a) ? sm.R[a][c] : 0.0;
+  }
+  for (int idx = tid; idx < kept * kept; idx += blockDim.x) {
+    const int a = idx / kept, c = idx % kept;
+    double v = 0.0;
+    if (c >= a)
+      for (int u = a; u <= c; ++u) v = fma(sm.R[a][u], R11g[u * MAXB + c], v);
+    R[(int64_t)(i + a) * ldr + (i + c)] = v;
+  }
 }
 
 // Column swap of the rows above the block: R(:i, K2) = R(:i, K1); R(:i, I2) = R(:i, J).
@@ -679,21 +720,19 @@ __global__ void k_swap_R(double* __restrict__ R, int64_t ldr, const State* __res
   for (int s = 0; s < kept; ++s) Rr[i + s] = tmp[s];
 }
 
-// Second CholQR pass: Q_blk = Q1 R2^{-1} (R2 = chol(Q1^T Q1)); CTA 0 writes
-// the panel R = R2 R11 into R(I2, I2) (matlab/RBRP.m:78).
+// Second CholQR pass: Q_blk = Q1 R2^{-1}, 64 rows per CTA.
+// With Qh != nullptr also the exact TF32 split of the basis for the tensor-core
+// projection: Qh = tf32(Q), Ql = fp32(Q - Qh) (ld = ldh), zero beyond the kept columns.
 template <typename T>
 __global__ void __launch_bounds__(256)
-k_panel2(const double* __restrict__ G2, const double* __restrict__ Q1, int m, const State* __restrict__ st,
-         T* __restrict__ Q, int64_t ldq, double* __restrict__ R, int64_t ldr, const double* __restrict__ R11g,
-         int q_at_i) {
+k_panel2(const double* __restrict__ Q1, int m, const State* __restrict__ st, const double* __restrict__ R2g,
+         T* __restrict__ Q, int64_t ldq, int q_at_i, float* __restrict__ Qh, float* __restrict__ Ql, int64_t ldh) {
   extern __shared__ __align__(16) unsigned char dyn_smem[];
   PanelSmem& sm = *reinterpret_cast<PanelSmem*>(dyn_smem);
   const int tid = threadIdx.x;
   const int kept = st->bs, i = st->i;
   if (kept == 0) return;
-  for (int idx = tid; idx < kept * kept; idx += blockDim.x) sm.S[idx / kept][idx % kept] = G2[(idx / kept) * MAXB + idx % kept];
-  __syncthreads();
-  chol_upper(sm, kept);
+  load_factor(sm, R2g, kept);
   const int r0 = blockIdx.x * 64;
   for (int idx = tid; idx < 64 * kept; idx += blockDim.x) {
     const int rr = idx & 63, s = idx >> 6, r = r0 + rr;
@@ -705,13 +744,15 @@ k_panel2(const double* __restrict__ G2, const double* __restrict__ Q1, int m, co
     const int rr = idx & 63, s = idx >> 6, r = r0 + rr;
     if (r < m) Q[r + (int64_t)((q_at_i ? i : 0) + s) * ldq] = (T)sm.W[rr][s];
   }
-  if (blockIdx.x == 0) {
-    for (int idx = tid; idx < kept * kept; idx += blockDim.x) {
-      const int a = idx / kept, c = idx % kept;
-      double v = 0.0;
-      if (c >= a)
-        for (int u = a; u <= c; ++u) v = fma(sm.R[a][u], R11g[u * MAXB + c], v);
-      R[(int64_t)(i + a) * ldr + (i + c)] = v;
+  if (Qh) {
+    for (int idx = tid; idx < 64 * MAXB; idx += blockDim.x) {
+      const int rr = idx & 63, s = idx >> 6, r = r0 + rr;
+      if (r < m) {
+        const double q = s < kept ? sm.W[rr][s] : 0.0;
+        const float h = __uint_as_float(__float_as_uint((float)q) & 0xFFFFE000u);
+        Qh[r + (int64_t)s * ldh] = h;
+        Ql[r + (int64_t)s * ldh] = (float)(q - (double)h);
+      }
     }
   }
 }

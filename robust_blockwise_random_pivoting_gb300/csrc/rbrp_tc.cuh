@@ -1,0 +1,297 @@
+// rbrp_tc.cuh - tcgen05 / TMEM / TMA projection kernel of the residual form (sm_103a).
+//
+// P1: W(p, a) = sum_r A_res(r, p) Q_blk(r, a) for a tile of 128 residual
+// columns p (the MMA M dimension, TMEM lanes) and the <= 64 basis vectors a of
+// the block (MMA N), reduced over the m rows (MMA K) in stages of 32 rows.
+//
+//   warp 0   TMA producer: A_res tile (128 columns x 32 rows, FP32) and the hi
+//            and lo parts of the Q tile (64 x 32) into a 4-stage ring, 128-byte
+//            swizzled, completion on an mbarrier with a transaction count.
+//   warp 1   MMA issuer: tcgen05.mma kind::tf32, 3 products per K step
+//            (Ahi Qhi + Ahi Qlo + Alo Qhi: the FP32 data is split exactly into
+//            two TF32 parts, so the products carry ~22 mantissa bits), FP32
+//            accumulation in TMEM, two accumulators used in turn.
+//   warps 2-5 split each staged A tile into its TF32 hi / lo parts (in shared
+//            memory, same swizzled layout), then drain a TMEM accumulator every
+//            512 rows with tcgen05.ld into double-float registers, so the FP32
+//            accumulation never runs over more than 512 rows.
+//
+// Every wait is bounded (about 2 s of clock64 time); on a timeout the CTA sets
+// an abort flag, raises st->status, waits (bounded) for its own TMA copies,
+// frees its TMEM and returns.
+#pragma once
+#include <cuda.h>
+
+#include "rbrp_common.cuh"
+
+namespace rbrp {
+namespace tc {
+namespace {  // internal linkage: included by each element-type translation unit
+
+constexpr int BM = 128;                  // residual columns per CTA (MMA M)
+constexpr int BN = 64;                   // basis vectors (MMA N)
+constexpr int BK = 32;                   // rows per stage = one 128-byte swizzle row of FP32
+constexpr int STAGES = 4;
+constexpr int CHUNK = 16;                // stages per accumulator drain (512 rows)
+constexpr int A_BYTES = BM * BK * 4;     // 16 KB
+constexpr int B_BYTES = BN * BK * 4;     // 8 KB
+constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;  // A hi, A lo, Q hi, Q lo
+constexpr int NTHREADS = 192;
+constexpr int TMEM_COLS = 2 * BN;
+constexpr int ST_ERR_TIMEOUT = 7;
+
+// tcgen05 instruction descriptor: D = F32 (bits 4-5 = 1), A = B = TF32 (bits 7-9,
+// 10-12 = 2), both K-major (bits 15, 16 = 0), N >> 3 in bits 17-22, M >> 4 in
+// bits 24-28.
+constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                           ((uint32_t)(BM >> 4) << 24);
+
+struct __align__(1024) P1Smem {
+  uint8_t stage[STAGES][STAGE_BYTES];
+  unsigned long long full[STAGES], split[STAGES], empty[STAGES];
+  unsigned long long accf[2], acce[2];
+  uint32_t tmem_base;
+  int abort;
+};
+constexpr size_t P1_SMEM = sizeof(P1Smem) + 1024;  // + alignment slack of the dynamic window
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* b, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(unsigned long long* b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait for the phase of parity `parity`; false on timeout or abort.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* b, uint32_t parity, volatile int* abort) {
+  if (mbar_try_wait(b, parity)) return true;
+  const long long t0 = clock64();
+  for (;;) {
+    if (mbar_try_wait(b, parity)) return true;
+    if (*abort) return false;
+    if (clock64() - t0 > (4ll << 30)) {  // ~2 s at 2 GHz
+      *abort = 1;
+      return false;
+    }
+  }
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, unsigned long long* bar, int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Shared-memory matrix descriptor, K-major operand, 128-byte swizzle: start
+// address >> 4 (bits 0-13), leading byte offset (unused for this layout, 16 B),
+// stride byte offset 1024 B = 8 rows of 128 B (bits 32-45), descriptor version 1
+// (bits 46-47), layout SWIZZLE_128B = 2 (bits 61-63).
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)(1024 >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(unsigned long long* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+// 32 consecutive TMEM columns of this warp's 32 lanes into registers.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+__device__ __forceinline__ float tf32_trunc(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
+
+__device__ __forceinline__ void df_acc(float& hi, float& lo, float x) {
+  const float t = hi + x;
+  const float bb = t - hi;
+  lo += (hi - (t - bb)) + (x - bb);
+  hi = t;
+}
+
+__global__ void __launch_bounds__(NTHREADS, 1)
+k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmQh,
+            const __grid_constant__ CUtensorMap tmQl, State* st, int m, int n, double* __restrict__ R, int64_t ldr) {
+  extern __shared__ uint8_t p1_raw[];
+  P1Smem& sm = *reinterpret_cast<P1Smem*>((reinterpret_cast<uintptr_t>(p1_raw) + 1023) & ~(uintptr_t)1023);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = st->i, kept = st->bs;
+  const int p0 = i + kept + blockIdx.x * BM;
+  if (kept == 0 || p0 >= n) return;
+  const int nk = (m + BK - 1) / BK;
+  volatile int* abort = &sm.abort;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&sm.full[s], 1);
+      mbar_init(&sm.split[s], 128);
+      mbar_init(&sm.empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&sm.accf[b], 1);
+      mbar_init(&sm.acce[b], 128);
+    }
+    sm.abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sm.tmem_base)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = sm.tmem_base;
+  int issued = 0;  // producer: stages whose TMA loads were issued
+
+  if (warp == 0) {
+    if (lane == 0) {
+      for (int s = 0; s < nk; ++s) {
+        const int slot = s % STAGES;
+        const uint32_t use = (uint32_t)(s / STAGES);
+        if (s >= STAGES && !mbar_wait(&sm.empty[slot], (use & 1) ^ 1, abort)) break;
+        uint8_t* base = sm.stage[slot];
+        mbar_expect_tx(&sm.full[slot], A_BYTES + 2 * B_BYTES);
+        tma_load_2d(base, &tmA, &sm.full[slot], s * BK, p0);
+        tma_load_2d(base + 2 * A_BYTES, &tmQh, &sm.full[slot], s * BK, 0);
+        tma_load_2d(base + 2 * A_BYTES + B_BYTES, &tmQl, &sm.full[slot], s * BK, 0);
+        issued = s + 1;
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      for (int s = 0; s < nk; ++s) {
+        const int slot = s % STAGES;
+        const uint32_t use = (uint32_t)(s / STAGES);
+        const int chunk = s / CHUNK, b = chunk & 1;
+        const bool first = (s % CHUNK) == 0;
+        if (first && chunk >= 2 && !mbar_wait(&sm.acce[b], (uint32_t)((chunk >> 1) - 1) & 1, abort)) break;
+        if (!mbar_wait(&sm.split[slot], use & 1, abort)) break;
+        tc_fence_after();
+        const uint8_t* base = sm.stage[slot];
+        const uint64_t dah = sw128_desc(smem_u32(base));
+        const uint64_t dal = sw128_desc(smem_u32(base + A_BYTES));
+        const uint64_t dqh = sw128_desc(smem_u32(base + 2 * A_BYTES));
+        const uint64_t dql = sw128_desc(smem_u32(base + 2 * A_BYTES + B_BYTES));
+        const uint32_t dt = tbase + (uint32_t)(b * BN);
+#pragma unroll
+        for (int k = 0; k < BK / 8; ++k) {  // K = 8 TF32 = 32 bytes: +2 in the 16-byte address field
+          mma_tf32(dt, dah + 2 * k, dqh + 2 * k, (first && k == 0) ? 0u : 1u);
+          mma_tf32(dt, dah + 2 * k, dql + 2 * k, 1u);
+          mma_tf32(dt, dal + 2 * k, dqh + 2 * k, 1u);
+        }
+        mma_commit(&sm.empty[slot]);
+        if ((s % CHUNK) == CHUNK - 1 || s == nk - 1) mma_commit(&sm.accf[b]);
+      }
+    }
+  } else {
+    const int et = threadIdx.x - 64;  // 0..127
+    const int q = warp & 3;           // TMEM lane quarter of this warp
+    float hi[BN], lo[BN];
+#pragma unroll
+    for (int a = 0; a < BN; ++a) hi[a] = lo[a] = 0.f;
+    for (int s = 0; s < nk; ++s) {
+      const int slot = s % STAGES;
+      const uint32_t use = (uint32_t)(s / STAGES);
+      if (!mbar_wait(&sm.full[slot], use & 1, abort)) break;
+      float4* a4 = reinterpret_cast<float4*>(sm.stage[slot]);
+      float4* l4 = reinterpret_cast<float4*>(sm.stage[slot] + A_BYTES);
+#pragma unroll 4
+      for (int e = et; e < A_BYTES / 16; e += 128) {
+        const float4 v = a4[e];
+        const float4 h = make_float4(tf32_trunc(v.x), tf32_trunc(v.y), tf32_trunc(v.z), tf32_trunc(v.w));
+        a4[e] = h;
+        l4[e] = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      mbar_arrive(&sm.split[slot]);
+      if ((s % CHUNK) == CHUNK - 1 || s == nk - 1) {
+        const int chunk = s / CHUNK, b = chunk & 1;
+        if (!mbar_wait(&sm.accf[b], (uint32_t)(chunk >> 1) & 1, abort)) break;
+        tc_fence_after();
+#pragma unroll
+        for (int h = 0; h < BN / 32; ++h) {
+          float v[32];
+          tmem_ld32(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * BN + 32 * h), v);
+#pragma unroll
+          for (int j = 0; j < 32; ++j) df_acc(hi[32 * h + j], lo[32 * h + j], v[j]);
+        }
+        tc_fence_before();
+        mbar_arrive(&sm.acce[b]);
+      }
+    }
+    const int p = p0 + 32 * q + lane;
+    if (!*abort && p < n) {
+#pragma unroll
+      for (int a = 0; a < BN; ++a)
+        if (a < kept) R[(int64_t)(i + a) * ldr + p] = (double)hi[a] + (double)lo[a];
+    }
+  }
+  __syncthreads();
+  if (*abort) {
+    if (threadIdx.x == 0) atomicExch(&st->status, ST_ERR_TIMEOUT);
+    if (warp == 0 && lane == 0) {  // let this CTA's own TMA copies land before the CTA exits
+      int dummy = 0;
+      volatile int* never = &dummy;
+      for (int s = issued - STAGES > 0 ? issued - STAGES : 0; s < issued; ++s)
+        mbar_wait(&sm.full[s % STAGES], (uint32_t)(s / STAGES) & 1, never);
+    }
+    __syncthreads();
+  }
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(TMEM_COLS) : "memory");
+  }
+}
+
+}  // namespace
+}  // namespace tc
+}  // namespace rbrp

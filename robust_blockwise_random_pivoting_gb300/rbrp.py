@@ -168,6 +168,10 @@ class Handle:
         """Bracket every phase with CUDA events (accumulated until reset)."""
         check(self.lib.rbrp_set_profiling(self.h, int(bool(on))), self.h)
 
+    def set_variant(self, variant):
+        """Projection kernel of the FP32 form: 0 = tcgen05 (default), 1 = CUDA-core FFMA."""
+        check(self.lib.rbrp_set_variant(self.h, int(variant)), self.h)
+
     def reset_phase_stats(self):
         check(self.lib.rbrp_reset_phase_stats(self.h), self.h)
 

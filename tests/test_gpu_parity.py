@@ -90,10 +90,11 @@ def test_greedy_mode(handle):
 
 
 def test_gmm_small(handle):
-    A, labels = W.gmm(64, 1500, nclusters=10, seed=1)
+    """Imbalanced mixture (cluster sizes down to one point): every cluster is in S."""
+    A, labels = W.gmm(256, 4000, nclusters=12, seed=2)
     r, o = check_against_oracle(handle, A, 32, 1e-4)
     S = r.perm[: r.k].cpu().numpy()
-    assert len(set(labels[S].tolist())) == 10   # every cluster represented
+    assert len(set(labels[S].tolist())) == 12
 
 
 def test_run_to_full_rank_and_kmax(handle):
@@ -155,9 +156,28 @@ def test_fp32_mixed_snn(handle):
 
 
 def test_fp32_mixed_gmm_clusters(handle):
-    A, labels = W.gmm(128, 3000, nclusters=12, seed=2)
+    A, labels = W.gmm(256, 4000, nclusters=12, seed=2)
     r, o = _mixed_vs_fp64(handle, A, 32, 1e-4, 64)
     assert len(set(labels[r.perm[: r.k].cpu().numpy()].tolist())) == 12
+
+
+def test_tensor_core_projection_matches_cuda_core(handle):
+    """The tcgen05 projection (3xTF32, TMEM drained every 512 rows) against the FFMA one."""
+    A = W.snn(1200, 1500, r=300, r1=30, density=0.05, seed=13)
+    A32 = dev(A, torch.float32)
+    runs = []
+    for variant in (1, 0):
+        handle.set_variant(variant)
+        try:
+            r = handle.column_id(A32, b=64, tol=1e-12, seed=0)
+        finally:
+            handle.set_variant(0)
+        runs.append((r, handle.id_error(A32)))
+    (r1, e1), (r0, e0) = runs
+    assert r0.k == r1.k
+    assert np.array_equal(r0.perm.cpu().numpy()[: r0.k], r1.perm.cpu().numpy()[: r1.k])
+    np.testing.assert_allclose(r0.residuals, r1.residuals, rtol=1e-4, atol=1e-15)
+    np.testing.assert_allclose(e0, e1, rtol=1e-3, atol=1e-16)
 
 
 def test_invalid_inputs_rejected(handle):
