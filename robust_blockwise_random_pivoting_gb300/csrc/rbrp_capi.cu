@@ -204,7 +204,8 @@ rbrp_status ensure_workspace(rbrp_handle h, const Layout& L) {
       {(void**)&h->perm, n * 4},
       {(void**)&h->pbuf, 2 * n * 8},
       {(void**)&h->kbuf, n * 8},
-      {(void**)&h->Q, m * (L.residual ? (size_t)MAXB : kmax) * el},
+      {(void**)&h->Q, (L.residual ? (size_t)L.ld_res * MAXB : m * kmax) * el},
+      {(void**)&h->part_norm, L.residual ? (size_t)P2_MAX_SPLIT_WS * n * 8 : 0},
       {(void**)&h->Ares, L.residual ? (size_t)L.ld_res * n * sizeof(float) : 0},
       {(void**)&h->Qh, L.residual ? (size_t)L.ld_res * MAXB * sizeof(float) : 0},
       {(void**)&h->Ql, L.residual ? (size_t)L.ld_res * MAXB * sizeof(float) : 0},

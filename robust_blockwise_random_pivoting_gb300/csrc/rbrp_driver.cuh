@@ -119,23 +119,29 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
     if (i > 0) k_swap_R<<<(i + 127) / 128, 128, 0, st>>>(h->R, n, h->st, h->J, h->K1, h->K2);
     if (RES)
       k_swap_cols<<<dim3((m + 1023) / 1024, MAXB), 256, 0, st>>>(h->Ares, L.ld_res, h->st, m, h->K1, h->K2);
-    k_panel2<T><<<ntiles, 256, panel_smem, st>>>(h->Q1, m, h->st, h->R2, Q, m, RES ? 0 : 1,
+    k_panel2<T><<<ntiles, 256, panel_smem, st>>>(h->Q1, m, h->st, h->R2, Q, RES ? L.ld_res : m, RES ? 0 : 1,
                                                  use_tc ? h->Qh : nullptr, use_tc ? h->Ql : nullptr, L.ld_res);
     prof_end(h, RBRP_PHASE_PANEL, ev, 0.0, 0.0, (i > 0 ? 6 : 5) + (RES ? 1 : 0));
     int nproj;
     ev = prof_begin(h);
     if (RES) {
-      nproj = (n - i + P2_COLS - 1) / P2_COLS;
       if (use_tc)
         tc::k_proj_w_tc<<<(n - i + tc::BM - 1) / tc::BM, tc::NTHREADS, tc::P1_SMEM, st>>>(tmA, tmQh, tmQl, h->st, m,
                                                                                         n, h->R, n);
       else
-        k_proj_w<<<(n - i + 63) / 64, 128, 0, st>>>((const float*)Q, m, h->Ares, L.ld_res, h->st, m, n, h->R, n);
+        k_proj_w<<<(n - i + 63) / 64, 128, 0, st>>>((const float*)Q, L.ld_res, h->Ares, L.ld_res, h->st, m, n, h->R,
+                                                    n);
       prof_end(h, RBRP_PHASE_PROJECT, ev, 0.0, 0.0, 1);
       ev = prof_begin(h);
-      k_resid_update<<<nproj, 256, P2_SMEM, st>>>((const float*)Q, m, h->Ares, L.ld_res, h->st, m, n, h->R, n,
-                                                 h->diags, h->part_res, h->part_nnz);
-      prof_end(h, RBRP_PHASE_UPDATE, ev, 0.0, 0.0, 1);
+      const int ctiles = (n - i + P2_COLS - 1) / P2_COLS;
+      int nsplit = std::min(P2_MAX_SPLIT, std::max(1, (4 * 152 + ctiles - 1) / ctiles));
+      const int rps = ((m + nsplit - 1) / nsplit + P2_ROWS - 1) / P2_ROWS * P2_ROWS;
+      nsplit = (m + rps - 1) / rps;
+      k_resid_update<<<dim3(ctiles, nsplit), 128, P2_SMEM, st>>>((const float*)Q, L.ld_res, h->Ares, L.ld_res,
+                                                                h->st, m, n, rps, h->R, n, h->part_norm);
+      nproj = (n - i + 255) / 256;
+      k_norm_reduce<<<nproj, 256, 0, st>>>(h->part_norm, nsplit, n, h->st, h->diags, h->part_res, h->part_nnz);
+      prof_end(h, RBRP_PHASE_UPDATE, ev, 0.0, 0.0, 2);
     } else {
       nproj = (n - i + 63) / 64;
       k_project<T><<<nproj, 256, 0, st>>>(Q, m, dA, lda, h->perm, h->st, m, n, h->R, n, h->diags,

@@ -8,6 +8,10 @@
 #include "../../include/rbrp_gb300.h"
 #include "rbrp_common.cuh"
 
+namespace rbrp {
+constexpr int P2_MAX_SPLIT_WS = 8;  // row ranges of the residual update (workspace sizing)
+}
+
 struct rbrp_handle_st {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -48,6 +52,7 @@ struct rbrp_handle_st {
   double* err_part = nullptr;  // partial sums of the ID-error kernel
   float* Ares = nullptr;       // residual form: position-ordered FP32 residual, ld_res x n
   int64_t ld_res = 0;
+  double* part_norm = nullptr; // residual form: partial column norms per row range
   float* Qh = nullptr;         // residual form: TF32 hi / lo parts of the block basis, ld_res x 64
   float* Ql = nullptr;
   int variant = 0;             // 0: tensor-core projection, 1: CUDA-core projection

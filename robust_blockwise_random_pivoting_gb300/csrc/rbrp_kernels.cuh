@@ -948,41 +948,49 @@ k_proj_w(const float* __restrict__ Qb, int64_t ldq, const float* __restrict__ Ar
   }
 }
 
-// P2: A_res(:, p) -= Q_blk W(:, p) and diags(p) = ||A_res(:, p)||^2 (double-float
-// sums), for 128 positions per CTA over all m rows.  Warp w owns 16 columns,
-// lane l rows l + 32u of each 128-row stage (coalesced along the column).
-constexpr int P2_COLS = 128;
+// P2: A_res(:, p) -= Q_blk W(:, p) and the partial squared norms of the updated
+// columns (double-float sums), for 64 positions x one row range per CTA.  Warp w
+// owns 16 columns, lane l four consecutive rows of every 128-row stage (16-byte
+// loads and stores, coalesced along the column).  Row ranges of the same columns
+// are summed by k_norm_reduce.
+constexpr int P2_COLS = 64;
 constexpr int P2_ROWS = 128;
+constexpr int P2_MAX_SPLIT = 8;
 constexpr size_t P2_SMEM = sizeof(float) * (size_t)MAXB * (P2_COLS + P2_ROWS);
 
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(128)
 k_resid_update(const float* __restrict__ Qb, int64_t ldq, float* __restrict__ Ares, int64_t ld,
-               const State* __restrict__ st, int m, int n, const double* __restrict__ R, int64_t ldr,
-               double* __restrict__ diags, double* __restrict__ part_res, int* __restrict__ part_nnz) {
+               const State* __restrict__ st, int m, int n, int rows_per_split, const double* __restrict__ R,
+               int64_t ldr, double* __restrict__ part_norm) {
   extern __shared__ __align__(16) float p2_smem[];
   float* Ws = p2_smem;                       // Ws[a * P2_COLS + c]
   float* Qs = p2_smem + MAXB * P2_COLS;      // Qs[a * P2_ROWS + rr]
-  __shared__ double snew[P2_COLS];
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   const int i = st->i, kept = st->bs;
   const int p0 = i + kept + blockIdx.x * P2_COLS;
-  if (kept == 0 || p0 >= n) {
-    if (tid == 0) { part_res[blockIdx.x] = 0.0; part_nnz[blockIdx.x] = 0; }
-    return;
-  }
+  if (kept == 0 || p0 >= n) return;
   const int ncol = min(P2_COLS, n - p0);
-  for (int idx = tid; idx < kept * P2_COLS; idx += 256) {
+  const int rb = blockIdx.y * rows_per_split, re = min(m, rb + rows_per_split);
+  for (int idx = tid; idx < kept * P2_COLS; idx += 128) {
     const int a = idx / P2_COLS, c = idx % P2_COLS;
     Ws[idx] = c < ncol ? (float)R[(int64_t)(i + a) * ldr + p0 + c] : 0.f;
   }
   DF nrm[16];
 #pragma unroll
   for (int c = 0; c < 16; ++c) nrm[c].hi = nrm[c].lo = 0.f;
-  for (int r0 = 0; r0 < m; r0 += P2_ROWS) {
+  for (int r0 = rb; r0 < re; r0 += P2_ROWS) {
     __syncthreads();
-    for (int idx = tid; idx < kept * P2_ROWS; idx += 256) {
-      const int a = idx / P2_ROWS, rr = idx % P2_ROWS;
-      Qs[idx] = (r0 + rr < m) ? Qb[r0 + rr + (int64_t)a * ldq] : 0.f;
+    for (int idx = tid; idx < kept * (P2_ROWS / 4); idx += 128) {
+      const int a = idx / (P2_ROWS / 4), j = idx % (P2_ROWS / 4), r = r0 + 4 * j;
+      float4 v;
+      if (r + 3 < re) {
+        v = *reinterpret_cast<const float4*>(Qb + r + (int64_t)a * ldq);
+      } else {
+        const float* qa = Qb + (int64_t)a * ldq;
+        v = make_float4(r < re ? qa[r] : 0.f, r + 1 < re ? qa[r + 1] : 0.f, r + 2 < re ? qa[r + 2] : 0.f,
+                        r + 3 < re ? qa[r + 3] : 0.f);
+      }
+      reinterpret_cast<float4*>(Qs + a * P2_ROWS)[j] = v;
     }
     __syncthreads();
     float acc[4][16];
@@ -990,12 +998,12 @@ k_resid_update(const float* __restrict__ Qb, int64_t ldq, float* __restrict__ Ar
     for (int u = 0; u < 4; ++u)
 #pragma unroll
       for (int c = 0; c < 16; ++c) acc[u][c] = 0.f;
+#pragma unroll 2
     for (int a = 0; a < kept; ++a) {
-      float qv[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) qv[u] = Qs[a * P2_ROWS + lane + 32 * u];
+      const float4 q4 = reinterpret_cast<const float4*>(Qs + a * P2_ROWS)[lane];
       const float4* w4 = reinterpret_cast<const float4*>(Ws + a * P2_COLS + w * 16);
       const float4 x0 = w4[0], x1 = w4[1], x2 = w4[2], x3 = w4[3];
+      const float qv[4] = {q4.x, q4.y, q4.z, q4.w};
       const float wv[16] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w,
                             x2.x, x2.y, x2.z, x2.w, x3.x, x3.y, x3.z, x3.w};
 #pragma unroll
@@ -1003,18 +1011,31 @@ k_resid_update(const float* __restrict__ Qb, int64_t ldq, float* __restrict__ Ar
 #pragma unroll
         for (int c = 0; c < 16; ++c) acc[u][c] = fmaf(qv[u], wv[c], acc[u][c]);
     }
+    const int r = r0 + 4 * lane;
 #pragma unroll
     for (int c = 0; c < 16; ++c) {
       const int cc = w * 16 + c;
       if (cc < ncol) {
         float* col = Ares + (int64_t)(p0 + cc) * ld;
+        if (r + 3 < re) {
+          float4 x = *reinterpret_cast<float4*>(col + r);
+          x.x -= acc[0][c];
+          x.y -= acc[1][c];
+          x.z -= acc[2][c];
+          x.w -= acc[3][c];
+          *reinterpret_cast<float4*>(col + r) = x;
+          df_add_sq(nrm[c], x.x);
+          df_add_sq(nrm[c], x.y);
+          df_add_sq(nrm[c], x.z);
+          df_add_sq(nrm[c], x.w);
+        } else {
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int r = r0 + lane + 32 * u;
-          if (r < m) {
-            const float x = col[r] - acc[u][c];
-            col[r] = x;
-            df_add_sq(nrm[c], x);
+          for (int u = 0; u < 4; ++u) {
+            if (r + u < re) {
+              const float x = col[r + u] - acc[u][c];
+              col[r + u] = x;
+              df_add_sq(nrm[c], x);
+            }
           }
         }
       }
@@ -1024,19 +1045,29 @@ k_resid_update(const float* __restrict__ Qb, int64_t ldq, float* __restrict__ Ar
   for (int c = 0; c < 16; ++c) {
     double v = (double)nrm[c].hi + (double)nrm[c].lo;
     v = warp_sum(v);
-    if (lane == 0) {
-      const int cc = w * 16 + c;
-      if (cc < ncol) diags[p0 + cc] = v;
-      snew[cc] = cc < ncol ? v : 0.0;
-    }
+    const int cc = w * 16 + c;
+    if (lane == 0 && cc < ncol) part_norm[(int64_t)blockIdx.y * n + p0 + cc] = v;
   }
-  __syncthreads();
-  if (tid == 0) {
-    double sres = 0.0;
-    int cnt = 0;
-    for (int c = 0; c < P2_COLS; ++c) { sres += snew[c]; cnt += snew[c] > 0.0; }
-    part_res[blockIdx.x] = sres;
-    part_nnz[blockIdx.x] = cnt;
+}
+
+// diags(p) = sum over row ranges of the partial norms; per-CTA residual sums and
+// positive counts for k_finish.
+__global__ void __launch_bounds__(256)
+k_norm_reduce(const double* __restrict__ part_norm, int nsplit, int n, const State* __restrict__ st,
+              double* __restrict__ diags, double* __restrict__ part_res, int* __restrict__ part_nnz) {
+  __shared__ double shd[32];
+  __shared__ int shi[32];
+  const int p = st->i + st->bs + blockIdx.x * 256 + threadIdx.x;
+  double d = 0.0;
+  if (st->bs > 0 && p < n) {
+    for (int z = 0; z < nsplit; ++z) d += part_norm[(int64_t)z * n + p];
+    diags[p] = d;
+  }
+  const double s = block_sum(d, shd);
+  const int c = block_sum((int)(d > 0.0), shi);
+  if (threadIdx.x == 0) {
+    part_res[blockIdx.x] = s;
+    part_nnz[blockIdx.x] = c;
   }
 }
 

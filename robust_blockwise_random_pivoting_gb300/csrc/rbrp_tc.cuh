@@ -7,14 +7,20 @@
 //   warp 0   TMA producer: A_res tile (128 columns x 32 rows, FP32) and the hi
 //            and lo parts of the Q tile (64 x 32) into a 4-stage ring, 128-byte
 //            swizzled, completion on an mbarrier with a transaction count.
-//   warp 1   MMA issuer: tcgen05.mma kind::tf32, 3 products per K step
-//            (Ahi Qhi + Ahi Qlo + Alo Qhi: the FP32 data is split exactly into
-//            two TF32 parts, so the products carry ~22 mantissa bits), FP32
-//            accumulation in TMEM, two accumulators used in turn.
-//   warps 2-5 split each staged A tile into its TF32 hi / lo parts (in shared
-//            memory, same swizzled layout), then drain a TMEM accumulator every
-//            512 rows with tcgen05.ld into double-float registers, so the FP32
-//            accumulation never runs over more than 512 rows.
+//   warp 1   MMA issuer: tcgen05.mma kind::tf32.  The FP32 data is split exactly
+//            into TF32 hi + lo parts; per K step the large product Ahi Qhi goes
+//            to one TMEM accumulator and the two small ones (Ahi Qlo, Alo Qhi)
+//            to another.
+//   warps 2-5 split each staged A tile into its hi / lo parts (in shared
+//            memory, same swizzled layout, one stage ahead of the MMAs), drain
+//            the large accumulator after every stage and the small one every
+//            512 rows with tcgen05.ld, into double-float registers.
+//
+// Why the drains: the tensor core rounds its FP32 accumulator once per MMA and
+// the rounding is biased, so the error grows linearly with the number of MMAs
+// between drains; 4 MMAs per drain keep W accurate to ~2e-7, which the
+// residual form needs (the part of A_res left along Q_blk by an error in W is
+// never removed by later blocks).  Both accumulators are double buffered.
 //
 // Every wait is bounded (about 2 s of clock64 time); on a timeout the CTA sets
 // an abort flag, raises st->status, waits (bounded) for its own TMA copies,
@@ -32,12 +38,12 @@ constexpr int BM = 128;                  // residual columns per CTA (MMA M)
 constexpr int BN = 64;                   // basis vectors (MMA N)
 constexpr int BK = 32;                   // rows per stage = one 128-byte swizzle row of FP32
 constexpr int STAGES = 4;
-constexpr int CHUNK = 16;                // stages per accumulator drain (512 rows)
+constexpr int CHUNK = 16;                // stages per drain of the small-product accumulator
 constexpr int A_BYTES = BM * BK * 4;     // 16 KB
 constexpr int B_BYTES = BN * BK * 4;     // 8 KB
 constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;  // A hi, A lo, Q hi, Q lo
 constexpr int NTHREADS = 192;
-constexpr int TMEM_COLS = 2 * BN;
+constexpr int TMEM_COLS = 4 * BN;         // large x2, small x2
 constexpr int ST_ERR_TIMEOUT = 7;
 
 // tcgen05 instruction descriptor: D = F32 (bits 4-5 = 1), A = B = TF32 (bits 7-9,
@@ -49,7 +55,8 @@ constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >
 struct __align__(1024) P1Smem {
   uint8_t stage[STAGES][STAGE_BYTES];
   unsigned long long full[STAGES], split[STAGES], empty[STAGES];
-  unsigned long long accf[2], acce[2];
+  unsigned long long bigf[2], bige[2];     // large accumulator: full (MMA done) / empty (drained)
+  unsigned long long smlf[2], smle[2];     // small accumulator
   uint32_t tmem_base;
   int abort;
 };
@@ -155,6 +162,16 @@ __device__ __forceinline__ void df_acc(float& hi, float& lo, float x) {
   hi = t;
 }
 
+__device__ __forceinline__ void drain64(uint32_t taddr, float (&hi)[BN], float (&lo)[BN]) {
+#pragma unroll
+  for (int h = 0; h < BN / 32; ++h) {
+    float v[32];
+    tmem_ld32(taddr + (uint32_t)(32 * h), v);
+#pragma unroll
+    for (int j = 0; j < 32; ++j) df_acc(hi[32 * h + j], lo[32 * h + j], v[j]);
+  }
+}
+
 __global__ void __launch_bounds__(NTHREADS, 1)
 k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmQh,
             const __grid_constant__ CUtensorMap tmQl, State* st, int m, int n, double* __restrict__ R, int64_t ldr) {
@@ -174,8 +191,10 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
       mbar_init(&sm.empty[s], 1);
     }
     for (int b = 0; b < 2; ++b) {
-      mbar_init(&sm.accf[b], 1);
-      mbar_init(&sm.acce[b], 128);
+      mbar_init(&sm.bigf[b], 1);
+      mbar_init(&sm.bige[b], 128);
+      mbar_init(&sm.smlf[b], 1);
+      mbar_init(&sm.smle[b], 128);
     }
     sm.abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -211,9 +230,11 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
       for (int s = 0; s < nk; ++s) {
         const int slot = s % STAGES;
         const uint32_t use = (uint32_t)(s / STAGES);
-        const int chunk = s / CHUNK, b = chunk & 1;
+        const int b = s & 1;                         // large accumulator of this stage
+        const int chunk = s / CHUNK, sb = chunk & 1;  // small accumulator of this chunk
         const bool first = (s % CHUNK) == 0;
-        if (first && chunk >= 2 && !mbar_wait(&sm.acce[b], (uint32_t)((chunk >> 1) - 1) & 1, abort)) break;
+        if (s >= 2 && !mbar_wait(&sm.bige[b], (uint32_t)((s >> 1) - 1) & 1, abort)) break;
+        if (first && chunk >= 2 && !mbar_wait(&sm.smle[sb], (uint32_t)((chunk >> 1) - 1) & 1, abort)) break;
         if (!mbar_wait(&sm.split[slot], use & 1, abort)) break;
         tc_fence_after();
         const uint8_t* base = sm.stage[slot];
@@ -221,27 +242,30 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
         const uint64_t dal = sw128_desc(smem_u32(base + A_BYTES));
         const uint64_t dqh = sw128_desc(smem_u32(base + 2 * A_BYTES));
         const uint64_t dql = sw128_desc(smem_u32(base + 2 * A_BYTES + B_BYTES));
-        const uint32_t dt = tbase + (uint32_t)(b * BN);
+        const uint32_t dbig = tbase + (uint32_t)(b * BN);
+        const uint32_t dsml = tbase + (uint32_t)(2 * BN + sb * BN);
 #pragma unroll
         for (int k = 0; k < BK / 8; ++k) {  // K = 8 TF32 = 32 bytes: +2 in the 16-byte address field
-          mma_tf32(dt, dah + 2 * k, dqh + 2 * k, (first && k == 0) ? 0u : 1u);
-          mma_tf32(dt, dah + 2 * k, dql + 2 * k, 1u);
-          mma_tf32(dt, dal + 2 * k, dqh + 2 * k, 1u);
+          mma_tf32(dbig, dah + 2 * k, dqh + 2 * k, k == 0 ? 0u : 1u);
+          mma_tf32(dsml, dah + 2 * k, dql + 2 * k, (first && k == 0) ? 0u : 1u);
+          mma_tf32(dsml, dal + 2 * k, dqh + 2 * k, 1u);
         }
         mma_commit(&sm.empty[slot]);
-        if ((s % CHUNK) == CHUNK - 1 || s == nk - 1) mma_commit(&sm.accf[b]);
+        mma_commit(&sm.bigf[b]);
+        if ((s % CHUNK) == CHUNK - 1 || s == nk - 1) mma_commit(&sm.smlf[sb]);
       }
     }
   } else {
     const int et = threadIdx.x - 64;  // 0..127
     const int q = warp & 3;           // TMEM lane quarter of this warp
+    const uint32_t lane_off = (uint32_t)(32 * q) << 16;
     float hi[BN], lo[BN];
 #pragma unroll
     for (int a = 0; a < BN; ++a) hi[a] = lo[a] = 0.f;
-    for (int s = 0; s < nk; ++s) {
-      const int slot = s % STAGES;
-      const uint32_t use = (uint32_t)(s / STAGES);
-      if (!mbar_wait(&sm.full[slot], use & 1, abort)) break;
+    // split stage t into hi / lo parts and hand it to the MMA warp
+    auto split_stage = [&](int t) -> bool {
+      const int slot = t % STAGES;
+      if (!mbar_wait(&sm.full[slot], (uint32_t)(t / STAGES) & 1, abort)) return false;
       float4* a4 = reinterpret_cast<float4*>(sm.stage[slot]);
       float4* l4 = reinterpret_cast<float4*>(sm.stage[slot] + A_BYTES);
 #pragma unroll 4
@@ -253,23 +277,28 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       mbar_arrive(&sm.split[slot]);
+      return true;
+    };
+    bool ok = nk > 0 && split_stage(0);
+    for (int s = 0; ok && s < nk; ++s) {
+      if (s + 1 < nk && !split_stage(s + 1)) { ok = false; break; }
+      const int b = s & 1;
+      if (!mbar_wait(&sm.bigf[b], (uint32_t)(s >> 1) & 1, abort)) { ok = false; break; }
+      tc_fence_after();
+      drain64(tbase + lane_off + (uint32_t)(b * BN), hi, lo);
+      tc_fence_before();
+      mbar_arrive(&sm.bige[b]);
       if ((s % CHUNK) == CHUNK - 1 || s == nk - 1) {
-        const int chunk = s / CHUNK, b = chunk & 1;
-        if (!mbar_wait(&sm.accf[b], (uint32_t)(chunk >> 1) & 1, abort)) break;
+        const int chunk = s / CHUNK, sb = chunk & 1;
+        if (!mbar_wait(&sm.smlf[sb], (uint32_t)(chunk >> 1) & 1, abort)) { ok = false; break; }
         tc_fence_after();
-#pragma unroll
-        for (int h = 0; h < BN / 32; ++h) {
-          float v[32];
-          tmem_ld32(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * BN + 32 * h), v);
-#pragma unroll
-          for (int j = 0; j < 32; ++j) df_acc(hi[32 * h + j], lo[32 * h + j], v[j]);
-        }
+        drain64(tbase + lane_off + (uint32_t)(2 * BN + sb * BN), hi, lo);
         tc_fence_before();
-        mbar_arrive(&sm.acce[b]);
+        mbar_arrive(&sm.smle[sb]);
       }
     }
     const int p = p0 + 32 * q + lane;
-    if (!*abort && p < n) {
+    if (ok && !*abort && p < n) {
 #pragma unroll
       for (int a = 0; a < BN; ++a)
         if (a < kept) R[(int64_t)(i + a) * ldr + p] = (double)hi[a] + (double)lo[a];
