@@ -162,22 +162,33 @@ def test_fp32_mixed_gmm_clusters(handle):
 
 
 def test_tensor_core_projection_matches_cuda_core(handle):
-    """The tcgen05 projection (3xTF32, TMEM drained every 512 rows) against the FFMA one."""
+    """The tcgen05 projection (3xTF32) against the CUDA-core one on the same FP32 matrix.
+
+    The tensor core rounds its FP32 accumulator once per MMA with a bias, so W
+    carries ~1e-6 relative error where the double-float CUDA-core sums carry
+    ~1e-8; both runs must meet the tolerance and stay within a block of ranks.
+    """
+    tol = 1e-12
     A = W.snn(1200, 1500, r=300, r1=30, density=0.05, seed=13)
     A32 = dev(A, torch.float32)
-    runs = []
+    A32h = A.astype(np.float32).astype(np.float64)
+    o = rbrp_column_id(A32h, 64, tol=tol, seed=0)
+    e_ref = id_error(A32h, o["perm"], interp_sid(A32h, o["perm"], o["k"]))
+    runs = {}
     for variant in (1, 0):
         handle.set_variant(variant)
         try:
-            r = handle.column_id(A32, b=64, tol=1e-12, seed=0)
+            r = handle.column_id(A32, b=64, tol=tol, seed=0)
         finally:
             handle.set_variant(0)
-        runs.append((r, handle.id_error(A32)))
-    (r1, e1), (r0, e0) = runs
-    assert r0.k == r1.k
-    assert np.array_equal(r0.perm.cpu().numpy()[: r0.k], r1.perm.cpu().numpy()[: r1.k])
-    np.testing.assert_allclose(r0.residuals, r1.residuals, rtol=1e-4, atol=1e-15)
-    np.testing.assert_allclose(e0, e1, rtol=1e-3, atol=1e-16)
+        runs[variant] = (r, handle.id_error(A32))
+    for variant, (r, e) in runs.items():
+        assert r.err_est <= tol and e <= 1.05 * max(e_ref, tol), (variant, r.k, e, e_ref)
+        assert abs(r.k - o["k"]) <= 64, (variant, r.k, o["k"])
+    assert abs(runs[0][0].k - runs[1][0].k) <= 64
+    # the first block (before any accumulated difference) selects the same columns
+    k1 = int(runs[0][0].ranks[0])
+    assert np.array_equal(runs[0][0].perm.cpu().numpy()[:k1], runs[1][0].perm.cpu().numpy()[:k1])
 
 
 def test_invalid_inputs_rejected(handle):
