@@ -84,10 +84,15 @@ _SIGS = {
 }
 
 
-def header_symbols(path=HEADER):
-    """Function names declared in the C header."""
-    txt = open(path).read()
-    return sorted(set(re.findall(r"^\s*(?:rbrp_status|void|int|const char\s*\*)\s*(rbrp_\w+)\s*\(", txt, re.M)))
+def header_symbols(paths=None):
+    """Function names declared in the C headers (include/*.h)."""
+    import glob
+    paths = paths or sorted(glob.glob(os.path.join(os.path.dirname(HEADER), "*.h")))
+    names = set()
+    for path in paths:
+        txt = open(path).read()
+        names.update(re.findall(r"^\s*(?:rbrp_status|void|int|const char\s*\*)\s*(rbrp_\w+)\s*\(", txt, re.M))
+    return sorted(names)
 
 
 def load():

@@ -46,3 +46,15 @@ def test_create_without_gpu_fails_cleanly(rbrp_lib):
         pytest.skip("a GPU is present")
     h = ctypes.c_void_p()
     assert rbrp_lib.rbrp_create(ctypes.byref(h), 0) == 2   # RBRP_ERR_CUDA, no crash
+
+
+def test_cpp_dropin_header_compiles(tmp_path):
+    """include/rbrp_gb300.hpp (the gpu/rbrp.hpp and gpu/rid.hpp shims) is valid C++."""
+    import os
+    inc = os.path.dirname(_lib.HEADER)
+    src = tmp_path / "use.cpp"
+    src.write_text('#include "rbrp_gb300.hpp"\n'
+                   'int f(double* A) { std::vector<int> r; std::vector<double> e, t; double tt, fl;\n'
+                   '  return (int)rbrp_gb300::RBRP(4, 4, A, 2, r, e, t, tt, fl); }\n')
+    out = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", inc, str(src)], capture_output=True, text=True)
+    assert out.returncode == 0, out.stderr
