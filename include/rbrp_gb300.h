@@ -123,6 +123,21 @@ rbrp_status rbrp_id_error_f64(rbrp_handle h, int m, int n, const double* dA, int
 rbrp_status rbrp_id_error_f32(rbrp_handle h, int m, int n, const float* dA, int64_t lda,
                               double* err);
 
+/* No counterpart in the reference.  For callers that cannot let a library
+ * allocate device memory (a host runtime that owns a fixed device pool, a hard
+ * memory budget, work enqueued where an allocation would synchronise): the
+ * squared relative ID error ||A(:,rd) - A(:,S) T||_F^2 / normA2 written to
+ * *dErr on `stream` (cudaStream_t), computed without a handle and without any
+ * allocation.  Inputs: A (m x n, FP64, lda), perm (n ints; S = perm[:k], rd =
+ * perm[k:]), T (k x (n-k), ldt >= k); all device pointers on the current device.
+ * Its scratch is a fixed 2 MiB device array in the library (held by every GPU
+ * that loads it until exit), so sizes with ceil((n-k)/32) * ceil(m/64) > 262144
+ * return RBRP_ERR_CAPACITY.  All calls on a device share that array: calls that
+ * overlap on the GPU race and must be serialised.  The first call on a device
+ * looks the array up (cudaGetSymbolAddress); make it before any stream capture. */
+rbrp_status rbrp_id_error_f64_noalloc(int m, int n, const double* dA, int64_t lda, const int* dPerm, int k,
+                                      const double* dT, int64_t ldt, double normA2, double* dErr, void* stream);
+
 /* Host-buffer convenience: copies hA (host, column major, lda) in, runs, copies
  * perm (n) and, when hT != NULL, T (k x (n-k), ldt >= k) back to host memory. */
 rbrp_status rbrp_id_f64_host(rbrp_handle h, int m, int n, const double* hA, int64_t lda,
