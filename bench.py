@@ -30,6 +30,7 @@ METRIC = "RBRP matrices/s & ID time at equal rel err, mixed+batched vs plain FP6
 
 WORKLOADS = {
     "snn16k": dict(kind="snn", m=16384, n=16384, r=2000, r1=100, amp=10.0, density=0.02, b=64, tol=1e-12),
+    "snn8k": dict(kind="snn", m=8192, n=8192, r=2000, r1=100, amp=10.0, density=0.02, b=64, tol=1e-12),
     "snn4k": dict(kind="snn", m=4096, n=4096, r=2000, r1=100, amp=10.0, density=0.02, b=64, tol=1e-12),
     "gexp1000": dict(kind="gexp", m=1000, n=1000, decay=20.0, b=40, tol=1e-12),
 }

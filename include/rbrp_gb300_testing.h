@@ -19,6 +19,10 @@ extern "C" {
  * (default), 1 = CUDA-core FFMA.  Both accumulate to ~1e-8 relative. */
 rbrp_status rbrp_set_variant(rbrp_handle h, int variant);
 
+/* T = R11^{-1} R12 block updates: 0 = double-float on the FP32 pipe (default,
+ * ~48 significant bits), 1 = FP64 pipe. */
+rbrp_status rbrp_set_tsolve_fp64(rbrp_handle h, int on);
+
 #ifdef __cplusplus
 }
 #endif

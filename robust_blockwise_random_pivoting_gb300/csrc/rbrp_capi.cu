@@ -104,6 +104,102 @@ __global__ void __launch_bounds__(256) k_trsm_T(const double* __restrict__ R, in
   }
 }
 
+// Double-float form of the same solve.  GB300's FP64 pipe is ~1/64 of its FP32
+// pipe, so the block updates Acc -= R11(b, later) T(later) run in double-float
+// arithmetic on the FP32 pipe: operands split x = hi + lo (two floats, 48
+// significant bits), products by an exact FMA split, sums by TwoSum - about 12
+// FP32 operations per FP64 multiply-add, ~5x the FP64 rate.  The 64 x 64
+// diagonal solves and the running right-hand side stay in FP64.
+struct TrsmDfSmem {
+  float2 Rs[64][65];     // -R11 block, (hi, lo)
+  float2 Xs[64][33];     // solved T rows, (hi, lo)
+  double Acc[64][33];    // right-hand side / solution of the current block row
+  double Rd[64][65];     // FP64 diagonal block
+};
+
+__device__ __forceinline__ float2 df_split(double x) {
+  const float hi = (float)x;
+  return make_float2(hi, (float)(x - (double)hi));
+}
+
+// (sh, sl) += a * b in double-float.
+__device__ __forceinline__ void df_mac(float& sh, float& sl, float2 a, float2 b) {
+  const float p = a.x * b.x;
+  const float e = fmaf(a.x, b.x, -p);
+  const float c = fmaf(a.x, b.y, a.y * b.x);
+  const float t = sh + p;
+  const float bb = t - sh;
+  sl += ((sh - (t - bb)) + (p - bb)) + (e + c);
+  sh = t;
+}
+
+__global__ void __launch_bounds__(256) k_trsm_T_df(const double* __restrict__ R, int64_t ldr, int k, int ncols,
+                                                   double* __restrict__ T) {
+  extern __shared__ __align__(16) unsigned char dyn_smem[];
+  TrsmDfSmem& sm = *reinterpret_cast<TrsmDfSmem*>(dyn_smem);
+  const int tid = threadIdx.x;
+  const int c0 = blockIdx.x * 32;
+  const int nc = min(32, ncols - c0);
+  const int nbk = (k + 63) / 64;
+  const int x = tid >> 2;
+  for (int bi = nbk - 1; bi >= 0; --bi) {
+    const int b0 = bi * 64, bl = min(64, k - b0);
+    for (int idx = tid; idx < 64 * 32; idx += 256) {
+      const int xr = idx & 63, c = idx >> 6;
+      sm.Acc[xr][c] = (xr < bl && c < nc) ? T[(b0 + xr) + (int64_t)(c0 + c) * k] : 0.0;
+    }
+    float sh[8], sl[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) sh[q] = sl[q] = 0.f;
+    for (int bj = bi + 1; bj < nbk; ++bj) {
+      const int cr = bj * 64, cl = min(64, k - cr);
+      __syncthreads();
+      for (int idx = tid; idx < 64 * 64; idx += 256) {
+        const int y = idx & 63, xr = idx >> 6;
+        sm.Rs[xr][y] = df_split((xr < bl && y < cl) ? -R[(int64_t)(b0 + xr) * ldr + cr + y] : 0.0);
+      }
+      for (int idx = tid; idx < 64 * 32; idx += 256) {
+        const int y = idx & 63, c = idx >> 6;
+        sm.Xs[y][c] = df_split((y < cl && c < nc) ? T[(cr + y) + (int64_t)(c0 + c) * k] : 0.0);
+      }
+      __syncthreads();
+#pragma unroll 4
+      for (int y = 0; y < 64; ++y) {
+        const float2 r = sm.Rs[x][y];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) df_mac(sh[q], sl[q], r, sm.Xs[y][(tid & 3) + 4 * q]);
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {  // renormalise so the low part stays small
+        const float t = sh[q] + sl[q];
+        sl[q] = sl[q] - (t - sh[q]);
+        sh[q] = t;
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 8; ++q) sm.Acc[x][(tid & 3) + 4 * q] += (double)sh[q] + (double)sl[q];
+    for (int idx = tid; idx < 64 * 64; idx += 256) {
+      const int y = idx & 63, xr = idx >> 6;
+      sm.Rd[xr][y] = (xr < bl && y < bl && y >= xr) ? R[(int64_t)(b0 + xr) * ldr + b0 + y] : 0.0;
+    }
+    __syncthreads();
+    if (tid < nc) {
+      for (int xr = bl - 1; xr >= 0; --xr) {
+        double v = sm.Acc[xr][tid];
+        for (int y = xr + 1; y < bl; ++y) v = fma(-sm.Rd[xr][y], sm.Acc[y][tid], v);
+        sm.Acc[xr][tid] = v / sm.Rd[xr][xr];
+      }
+    }
+    __syncthreads();
+    for (int idx = tid; idx < 64 * 32; idx += 256) {
+      const int xr = idx & 63, c = idx >> 6;
+      if (xr < bl && c < nc) T[(b0 + xr) + (int64_t)(c0 + c) * k] = sm.Acc[xr][c];
+    }
+    __syncthreads();
+  }
+}
+
 // ===========================================================================
 // a11: ||A(:, rd) - A(:, S) T||_F^2 in FP64 (python/RBRP.ipynb cell 7 lines
 // 40-53; gpu/id_cpqr.cu:145-170).  Validation only: one FP64 GEMM.
@@ -299,10 +395,18 @@ rbrp_status solve_T(rbrp_handle h, int k, int n) {
   const int ncols = n - k;
   dim3 g1((ncols + 31) / 32, (k + 31) / 32), b1(32, 8);
   k_gather_T<<<g1, b1, 0, h->stream>>>(h->R, n, k, ncols, h->T);
-  rbrp_status s = cuda_check(h, cudaFuncSetAttribute(k_trsm_T, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                     (int)sizeof(TrsmSmem)), "cudaFuncSetAttribute(k_trsm_T)");
-  if (s != RBRP_OK) return s;
-  k_trsm_T<<<(ncols + 31) / 32, 256, sizeof(TrsmSmem), h->stream>>>(h->R, n, k, ncols, h->T);
+  rbrp_status s;
+  if (h->tsolve_fp64) {
+    s = cuda_check(h, cudaFuncSetAttribute(k_trsm_T, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)sizeof(TrsmSmem)), "cudaFuncSetAttribute(k_trsm_T)");
+    if (s != RBRP_OK) return s;
+    k_trsm_T<<<(ncols + 31) / 32, 256, sizeof(TrsmSmem), h->stream>>>(h->R, n, k, ncols, h->T);
+  } else {
+    s = cuda_check(h, cudaFuncSetAttribute(k_trsm_T_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)sizeof(TrsmDfSmem)), "cudaFuncSetAttribute(k_trsm_T_df)");
+    if (s != RBRP_OK) return s;
+    k_trsm_T_df<<<(ncols + 31) / 32, 256, sizeof(TrsmDfSmem), h->stream>>>(h->R, n, k, ncols, h->T);
+  }
   return cuda_check(h, cudaGetLastError(), "T solve launch");
 }
 
@@ -646,6 +750,12 @@ rbrp_status rbrp_reset_phase_stats(rbrp_handle h) {
 rbrp_status rbrp_set_variant(rbrp_handle h, int variant) {
   if (!h || variant < 0 || variant > 1) return RBRP_ERR_INVALID_ARG;
   h->variant = variant;
+  return RBRP_OK;
+}
+
+rbrp_status rbrp_set_tsolve_fp64(rbrp_handle h, int on) {
+  if (!h) return RBRP_ERR_INVALID_ARG;
+  h->tsolve_fp64 = on != 0;
   return RBRP_OK;
 }
 

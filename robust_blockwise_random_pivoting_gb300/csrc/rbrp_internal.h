@@ -56,6 +56,7 @@ struct rbrp_handle_st {
   float* Qh = nullptr;         // residual form: TF32 hi / lo parts of the block basis, ld_res x 64
   float* Ql = nullptr;
   int variant = 0;             // 0: tensor-core projection, 1: CUDA-core projection
+  bool tsolve_fp64 = false;    // T solve on the FP64 pipe instead of double-float
 
   // interpolation matrix of the last run
   double* T = nullptr;

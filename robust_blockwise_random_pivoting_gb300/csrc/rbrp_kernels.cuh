@@ -561,6 +561,75 @@ __device__ int pivoted_chol_filter(PanelSmem& sm, int nb, int rows, double tol_l
   return kept;
 }
 
+// Single-warp form of pivoted_chol_filter (only __syncwarp between steps): lane
+// l owns columns l and l + 32.  Returns the kept count to all 32 lanes.
+__device__ int pivoted_chol_filter_warp(PanelSmem& sm, int nb, int rows, double tol_loc) {
+  const int lane = threadIdx.x & 31;
+  sm.ord[lane] = lane;
+  sm.ord[lane + 32] = lane + 32;
+  double d = 0.0;
+  for (int s = lane; s < nb; s += 32) d += sm.S[s][s];
+  const double total = __shfl_sync(0xffffffffu, warp_sum(d), 0);
+  __syncwarp();
+  for (int t = 0; t < rows; ++t) {
+    double rem = 0.0, best = -1.0;
+    int bi = nb;
+    for (int s = t + lane; s < nb; s += 32) {
+      const double v = sm.S[s][s];
+      rem += v;
+      if (v > best) { best = v; bi = s; }
+    }
+    rem = __shfl_sync(0xffffffffu, warp_sum(rem), 0);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ob = __shfl_down_sync(0xffffffffu, best, o);
+      const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    }
+    best = __shfl_sync(0xffffffffu, best, 0);
+    const int p = __shfl_sync(0xffffffffu, bi, 0);
+    if (!(total > 0.0) || (rem / total < tol_loc) || !(best > 0.0)) return t;
+    if (p != t) {
+      for (int j = lane; j < nb; j += 32) {
+        const double x = sm.S[t][j]; sm.S[t][j] = sm.S[p][j]; sm.S[p][j] = x;
+      }
+      __syncwarp();
+      for (int j = lane; j < nb; j += 32) {
+        const double x = sm.S[j][t]; sm.S[j][t] = sm.S[j][p]; sm.S[j][p] = x;
+      }
+      for (int j = lane; j < t; j += 32) {
+        const double x = sm.R[j][t]; sm.R[j][t] = sm.R[j][p]; sm.R[j][p] = x;
+      }
+      if (lane == 0) { const int o = sm.ord[t]; sm.ord[t] = sm.ord[p]; sm.ord[p] = o; }
+      __syncwarp();
+    }
+    const double rtt = sqrt(sm.S[t][t]);
+    for (int s = t + lane; s < nb; s += 32) sm.R[t][s] = (s == t) ? rtt : sm.S[t][s] / rtt;
+    __syncwarp();
+    for (int s2 = t + 1 + lane; s2 < nb; s2 += 32) {
+      const double r2 = sm.R[t][s2];
+      for (int s1 = t + 1; s1 < nb; ++s1) sm.S[s1][s2] = fma(-sm.R[t][s1], r2, sm.S[s1][s2]);
+    }
+    __syncwarp();
+  }
+  return rows;
+}
+
+// Single-warp plain Cholesky of S (n x n) into sm.R (upper).
+__device__ void chol_upper_warp(PanelSmem& sm, int nb) {
+  const int lane = threadIdx.x & 31;
+  for (int t = 0; t < nb; ++t) {
+    const double rtt = sqrt(fmax(sm.S[t][t], 0.0));
+    for (int s = t + lane; s < nb; s += 32) sm.R[t][s] = (s == t) ? rtt : sm.S[t][s] / rtt;
+    __syncwarp();
+    for (int s2 = t + 1 + lane; s2 < nb; s2 += 32) {
+      const double r2 = sm.R[t][s2];
+      for (int s1 = t + 1; s1 <= s2; ++s1) sm.S[s1][s2] = fma(-sm.R[t][s1], r2, sm.S[s1][s2]);
+    }
+    __syncwarp();
+  }
+}
+
 // Plain Cholesky of S (n x n) into sm.R (upper); all threads call it.
 __device__ void chol_upper(PanelSmem& sm, int nb) {
   const int tid = threadIdx.x;
@@ -618,7 +687,12 @@ k_pchol(const double* __restrict__ G, int m, State* st, double tol_loc, const in
   const int nb = st->bs_sampled, i = st->i;
   for (int idx = tid; idx < nb * nb; idx += blockDim.x) sm.S[idx / nb][idx % nb] = G[(idx / nb) * MAXB + idx % nb];
   __syncthreads();
-  const int kept = pivoted_chol_filter(sm, nb, min(nb, m), tol_loc);
+  if (tid < 32) {
+    const int kw = pivoted_chol_filter_warp(sm, nb, min(nb, m), tol_loc);
+    if (tid == 0) sm.stop = kw;
+  }
+  __syncthreads();
+  const int kept = sm.stop;
   for (int idx = tid; idx < MAXB * MAXB; idx += blockDim.x) {
     const int a = idx / MAXB, c = idx % MAXB;
     R11g[idx] = (a < kept && c < kept && c >= a) ? sm.R[a][c] : 0.0;
@@ -693,7 +767,8 @@ k_chol2(const double* __restrict__ G2, const State* __restrict__ st, const doubl
   if (kept == 0) return;
   for (int idx = tid; idx < kept * kept; idx += blockDim.x) sm.S[idx / kept][idx % kept] = G2[(idx / kept) * MAXB + idx % kept];
   __syncthreads();
-  chol_upper(sm, kept);
+  if (tid < 32) chol_upper_warp(sm, kept);
+  __syncthreads();
   for (int idx = tid; idx < MAXB * MAXB; idx += blockDim.x) {
     const int a = idx / MAXB, c = idx % MAXB;
     R2g[idx] = (a < kept && c < kept && c >= a) ? sm.R[a][c] : 0.0;
@@ -980,6 +1055,17 @@ k_resid_update(const float* __restrict__ Qb, int64_t ldq, float* __restrict__ Ar
   for (int c = 0; c < 16; ++c) nrm[c].hi = nrm[c].lo = 0.f;
   for (int r0 = rb; r0 < re; r0 += P2_ROWS) {
     __syncthreads();
+    // this thread's residual values, fetched before the products so the loads
+    // are in flight during the stage's FMA work
+    const int r = r0 + 4 * lane;
+    const bool vec_ok = r + 3 < re;
+    float4 xa[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c) {
+      const int cc = w * 16 + c;
+      xa[c] = (vec_ok && cc < ncol) ? *reinterpret_cast<const float4*>(Ares + (int64_t)(p0 + cc) * ld + r)
+                                    : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
     for (int idx = tid; idx < kept * (P2_ROWS / 4); idx += 128) {
       const int a = idx / (P2_ROWS / 4), j = idx % (P2_ROWS / 4), r = r0 + 4 * j;
       float4 v;
@@ -1011,14 +1097,13 @@ k_resid_update(const float* __restrict__ Qb, int64_t ldq, float* __restrict__ Ar
 #pragma unroll
         for (int c = 0; c < 16; ++c) acc[u][c] = fmaf(qv[u], wv[c], acc[u][c]);
     }
-    const int r = r0 + 4 * lane;
 #pragma unroll
     for (int c = 0; c < 16; ++c) {
       const int cc = w * 16 + c;
       if (cc < ncol) {
         float* col = Ares + (int64_t)(p0 + cc) * ld;
-        if (r + 3 < re) {
-          float4 x = *reinterpret_cast<float4*>(col + r);
+        if (vec_ok) {
+          float4 x = xa[c];
           x.x -= acc[0][c];
           x.y -= acc[1][c];
           x.z -= acc[2][c];

@@ -172,6 +172,10 @@ class Handle:
         """Projection kernel of the FP32 form: 0 = tcgen05 (default), 1 = CUDA-core FFMA."""
         check(self.lib.rbrp_set_variant(self.h, int(variant)), self.h)
 
+    def set_tsolve_fp64(self, on=True):
+        """T solve on the FP64 pipe (True) or in double-float on the FP32 pipe (False, default)."""
+        check(self.lib.rbrp_set_tsolve_fp64(self.h, int(bool(on))), self.h)
+
     def reset_phase_stats(self):
         check(self.lib.rbrp_reset_phase_stats(self.h), self.h)
 

@@ -191,6 +191,21 @@ def test_tensor_core_projection_matches_cuda_core(handle):
     assert np.array_equal(runs[0][0].perm.cpu().numpy()[:k1], runs[1][0].perm.cpu().numpy()[:k1])
 
 
+def test_double_float_T_solve_matches_fp64(handle):
+    """T = R11^{-1} R12 with double-float block updates against the FP64-pipe solve."""
+    A = dev(W.gaussian_exp(500, 900, decay=15.0, seed=17))
+    Ts = []
+    for fp64 in (True, False):
+        handle.set_tsolve_fp64(fp64)
+        try:
+            r = handle.column_id(A, b=48, tol=1e-12, seed=0)
+        finally:
+            handle.set_tsolve_fp64(False)
+        Ts.append(r.T.cpu().numpy())
+    assert Ts[0].shape == Ts[1].shape and Ts[0].shape[0] > 64
+    np.testing.assert_allclose(Ts[1], Ts[0], rtol=0, atol=1e-9 * np.abs(Ts[0]).max())
+
+
 def test_invalid_inputs_rejected(handle):
     from robust_blockwise_random_pivoting_gb300._lib import RBRPError
     A = dev(W.gaussian_exp(50, 60, seed=1))
