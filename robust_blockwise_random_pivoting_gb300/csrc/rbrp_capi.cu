@@ -302,6 +302,7 @@ rbrp_status ensure_workspace(rbrp_handle h, const Layout& L) {
       {(void**)&h->kbuf, n * 8},
       {(void**)&h->Q, (L.residual ? (size_t)L.ld_res * MAXB : m * kmax) * el},
       {(void**)&h->part_norm, L.residual ? (size_t)P2_MAX_SPLIT_WS * n * 8 : 0},
+      {(void**)&h->Wpart, L.residual ? (size_t)P1_MAX_SPLIT * MAXB * n * 8 : 0},
       {(void**)&h->Ares, L.residual ? (size_t)L.ld_res * n * sizeof(float) : 0},
       {(void**)&h->Qh, L.residual ? (size_t)L.ld_res * MAXB * sizeof(float) : 0},
       {(void**)&h->Ql, L.residual ? (size_t)L.ld_res * MAXB * sizeof(float) : 0},

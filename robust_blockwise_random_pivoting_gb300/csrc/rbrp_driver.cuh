@@ -125,20 +125,31 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
     int nproj;
     ev = prof_begin(h);
     if (RES) {
-      if (use_tc)
-        tc::k_proj_w_tc<<<(n - i + tc::BM - 1) / tc::BM, tc::NTHREADS, tc::P1_SMEM, st>>>(tmA, tmQh, tmQl, h->st, m,
-                                                                                        n, h->R, n);
-      else
+      int wsplit = 0;
+      if (use_tc) {
+        // split the rows so that about two CTAs per SM stream the remaining columns
+        const int ctiles = (n - i + tc::BM - 1) / tc::BM;
+        const int nstages = (m + tc::BK - 1) / tc::BK;
+        wsplit = std::min(std::min(P1_MAX_SPLIT, std::max(1, (2 * 152 + ctiles - 1) / ctiles)),
+                          std::max(1, nstages / tc::CHUNK));
+        const int sps = (nstages + wsplit - 1) / wsplit;
+        wsplit = (nstages + sps - 1) / sps;
+        tc::k_proj_w_tc<<<dim3(ctiles, wsplit), tc::NTHREADS, tc::P1_SMEM, st>>>(tmA, tmQh, tmQl, h->st, m, n, sps,
+                                                                                h->Wpart);
+      } else {
         k_proj_w<<<(n - i + 63) / 64, 128, 0, st>>>((const float*)Q, L.ld_res, h->Ares, L.ld_res, h->st, m, n, h->R,
                                                     n);
+      }
       prof_end(h, RBRP_PHASE_PROJECT, ev, 0.0, 0.0, 1);
       ev = prof_begin(h);
       const int ctiles = (n - i + P2_COLS - 1) / P2_COLS;
       int nsplit = std::min(P2_MAX_SPLIT, std::max(1, (4 * 152 + ctiles - 1) / ctiles));
       const int rps = ((m + nsplit - 1) / nsplit + P2_ROWS - 1) / P2_ROWS * P2_ROWS;
       nsplit = (m + rps - 1) / rps;
-      k_resid_update<<<dim3(ctiles, nsplit), 128, P2_SMEM, st>>>((const float*)Q, L.ld_res, h->Ares, L.ld_res,
-                                                                h->st, m, n, rps, h->R, n, h->part_norm);
+      k_resid_update<<<dim3(ctiles, nsplit), P2_THREADS, P2_SMEM, st>>>((const float*)Q, L.ld_res, h->Ares, L.ld_res,
+                                                                       h->st, m, n, rps, h->R, n,
+                                                                       use_tc ? h->Wpart : nullptr, wsplit,
+                                                                       h->part_norm);
       nproj = (n - i + 255) / 256;
       k_norm_reduce<<<nproj, 256, 0, st>>>(h->part_norm, nsplit, n, h->st, h->diags, h->part_res, h->part_nnz);
       prof_end(h, RBRP_PHASE_UPDATE, ev, 0.0, 0.0, 2);

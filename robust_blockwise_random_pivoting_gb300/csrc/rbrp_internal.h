@@ -10,6 +10,7 @@
 
 namespace rbrp {
 constexpr int P2_MAX_SPLIT_WS = 8;  // row ranges of the residual update (workspace sizing)
+constexpr int P1_MAX_SPLIT = 8;     // row ranges of the tensor-core projection
 }
 
 struct rbrp_handle_st {
@@ -53,6 +54,7 @@ struct rbrp_handle_st {
   float* Ares = nullptr;       // residual form: position-ordered FP32 residual, ld_res x n
   int64_t ld_res = 0;
   double* part_norm = nullptr; // residual form: partial column norms per row range
+  double* Wpart = nullptr;     // residual form: row-split partial projections, P1_MAX_SPLIT x 64 x n
   float* Qh = nullptr;         // residual form: TF32 hi / lo parts of the block basis, ld_res x 64
   float* Ql = nullptr;
   int variant = 0;             // 0: tensor-core projection, 1: CUDA-core projection

@@ -1025,18 +1025,21 @@ k_proj_w(const float* __restrict__ Qb, int64_t ldq, const float* __restrict__ Ar
 
 // P2: A_res(:, p) -= Q_blk W(:, p) and the partial squared norms of the updated
 // columns (double-float sums), for 64 positions x one row range per CTA.  Warp w
-// owns 16 columns, lane l four consecutive rows of every 128-row stage (16-byte
+// owns 8 columns, lane l four consecutive rows of every 128-row stage (16-byte
 // loads and stores, coalesced along the column).  Row ranges of the same columns
-// are summed by k_norm_reduce.
+// are summed by k_norm_reduce.  W comes either from R (one projection per
+// column) or from the row-split partials of the tensor-core projection, summed
+// here in split order; CTAs of the first row range then also write R(I2, p).
 constexpr int P2_COLS = 64;
 constexpr int P2_ROWS = 128;
 constexpr int P2_MAX_SPLIT = 8;
+constexpr int P2_THREADS = 256;
 constexpr size_t P2_SMEM = sizeof(float) * (size_t)MAXB * (P2_COLS + P2_ROWS);
 
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(P2_THREADS, 2)
 k_resid_update(const float* __restrict__ Qb, int64_t ldq, float* __restrict__ Ares, int64_t ld,
-               const State* __restrict__ st, int m, int n, int rows_per_split, const double* __restrict__ R,
-               int64_t ldr, double* __restrict__ part_norm) {
+               const State* __restrict__ st, int m, int n, int rows_per_split, double* __restrict__ R,
+               int64_t ldr, const double* __restrict__ Wpart, int wsplit, double* __restrict__ part_norm) {
   extern __shared__ __align__(16) float p2_smem[];
   float* Ws = p2_smem;                       // Ws[a * P2_COLS + c]
   float* Qs = p2_smem + MAXB * P2_COLS;      // Qs[a * P2_ROWS + rr]
@@ -1046,60 +1049,71 @@ k_resid_update(const float* __restrict__ Qb, int64_t ldq, float* __restrict__ Ar
   if (kept == 0 || p0 >= n) return;
   const int ncol = min(P2_COLS, n - p0);
   const int rb = blockIdx.y * rows_per_split, re = min(m, rb + rows_per_split);
-  for (int idx = tid; idx < kept * P2_COLS; idx += 128) {
+  for (int idx = tid; idx < kept * P2_COLS; idx += P2_THREADS) {
     const int a = idx / P2_COLS, c = idx % P2_COLS;
-    Ws[idx] = c < ncol ? (float)R[(int64_t)(i + a) * ldr + p0 + c] : 0.f;
+    float wv = 0.f;
+    if (c < ncol) {
+      double v;
+      if (Wpart) {
+        v = 0.0;
+        for (int z = 0; z < wsplit; ++z) v += Wpart[((int64_t)z * MAXB + a) * n + p0 + c];
+        if (blockIdx.y == 0) R[(int64_t)(i + a) * ldr + p0 + c] = v;
+      } else {
+        v = R[(int64_t)(i + a) * ldr + p0 + c];
+      }
+      wv = (float)v;
+    }
+    Ws[idx] = wv;
   }
-  DF nrm[16];
+  DF nrm[8];
 #pragma unroll
-  for (int c = 0; c < 16; ++c) nrm[c].hi = nrm[c].lo = 0.f;
+  for (int c = 0; c < 8; ++c) nrm[c].hi = nrm[c].lo = 0.f;
   for (int r0 = rb; r0 < re; r0 += P2_ROWS) {
     __syncthreads();
     // this thread's residual values, fetched before the products so the loads
     // are in flight during the stage's FMA work
     const int r = r0 + 4 * lane;
     const bool vec_ok = r + 3 < re;
-    float4 xa[16];
+    float4 xa[8];
 #pragma unroll
-    for (int c = 0; c < 16; ++c) {
-      const int cc = w * 16 + c;
+    for (int c = 0; c < 8; ++c) {
+      const int cc = w * 8 + c;
       xa[c] = (vec_ok && cc < ncol) ? *reinterpret_cast<const float4*>(Ares + (int64_t)(p0 + cc) * ld + r)
                                     : make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    for (int idx = tid; idx < kept * (P2_ROWS / 4); idx += 128) {
-      const int a = idx / (P2_ROWS / 4), j = idx % (P2_ROWS / 4), r = r0 + 4 * j;
+    for (int idx = tid; idx < kept * (P2_ROWS / 4); idx += P2_THREADS) {
+      const int a = idx / (P2_ROWS / 4), j = idx % (P2_ROWS / 4), rq = r0 + 4 * j;
       float4 v;
-      if (r + 3 < re) {
-        v = *reinterpret_cast<const float4*>(Qb + r + (int64_t)a * ldq);
+      if (rq + 3 < re) {
+        v = *reinterpret_cast<const float4*>(Qb + rq + (int64_t)a * ldq);
       } else {
         const float* qa = Qb + (int64_t)a * ldq;
-        v = make_float4(r < re ? qa[r] : 0.f, r + 1 < re ? qa[r + 1] : 0.f, r + 2 < re ? qa[r + 2] : 0.f,
-                        r + 3 < re ? qa[r + 3] : 0.f);
+        v = make_float4(rq < re ? qa[rq] : 0.f, rq + 1 < re ? qa[rq + 1] : 0.f, rq + 2 < re ? qa[rq + 2] : 0.f,
+                        rq + 3 < re ? qa[rq + 3] : 0.f);
       }
       reinterpret_cast<float4*>(Qs + a * P2_ROWS)[j] = v;
     }
     __syncthreads();
-    float acc[4][16];
+    float acc[4][8];
 #pragma unroll
     for (int u = 0; u < 4; ++u)
 #pragma unroll
-      for (int c = 0; c < 16; ++c) acc[u][c] = 0.f;
-#pragma unroll 2
+      for (int c = 0; c < 8; ++c) acc[u][c] = 0.f;
+#pragma unroll 4
     for (int a = 0; a < kept; ++a) {
       const float4 q4 = reinterpret_cast<const float4*>(Qs + a * P2_ROWS)[lane];
-      const float4* w4 = reinterpret_cast<const float4*>(Ws + a * P2_COLS + w * 16);
-      const float4 x0 = w4[0], x1 = w4[1], x2 = w4[2], x3 = w4[3];
+      const float4* w4 = reinterpret_cast<const float4*>(Ws + a * P2_COLS + w * 8);
+      const float4 x0 = w4[0], x1 = w4[1];
       const float qv[4] = {q4.x, q4.y, q4.z, q4.w};
-      const float wv[16] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w,
-                            x2.x, x2.y, x2.z, x2.w, x3.x, x3.y, x3.z, x3.w};
+      const float wv[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
 #pragma unroll
       for (int u = 0; u < 4; ++u)
 #pragma unroll
-        for (int c = 0; c < 16; ++c) acc[u][c] = fmaf(qv[u], wv[c], acc[u][c]);
+        for (int c = 0; c < 8; ++c) acc[u][c] = fmaf(qv[u], wv[c], acc[u][c]);
     }
 #pragma unroll
-    for (int c = 0; c < 16; ++c) {
-      const int cc = w * 16 + c;
+    for (int c = 0; c < 8; ++c) {
+      const int cc = w * 8 + c;
       if (cc < ncol) {
         float* col = Ares + (int64_t)(p0 + cc) * ld;
         if (vec_ok) {
@@ -1127,10 +1141,10 @@ k_resid_update(const float* __restrict__ Qb, int64_t ldq, float* __restrict__ Ar
     }
   }
 #pragma unroll
-  for (int c = 0; c < 16; ++c) {
+  for (int c = 0; c < 8; ++c) {
     double v = (double)nrm[c].hi + (double)nrm[c].lo;
     v = warp_sum(v);
-    const int cc = w * 16 + c;
+    const int cc = w * 8 + c;
     if (lane == 0 && cc < ncol) part_norm[(int64_t)blockIdx.y * n + p0 + cc] = v;
   }
 }

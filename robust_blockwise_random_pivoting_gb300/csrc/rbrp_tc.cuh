@@ -174,14 +174,19 @@ __device__ __forceinline__ void drain64(uint32_t taddr, float (&hi)[BN], float (
 
 __global__ void __launch_bounds__(NTHREADS, 1)
 k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmQh,
-            const __grid_constant__ CUtensorMap tmQl, State* st, int m, int n, double* __restrict__ R, int64_t ldr) {
+            const __grid_constant__ CUtensorMap tmQl, State* st, int m, int n, int stages_per_split,
+            double* __restrict__ Wpart) {
   extern __shared__ uint8_t p1_raw[];
   P1Smem& sm = *reinterpret_cast<P1Smem*>((reinterpret_cast<uintptr_t>(p1_raw) + 1023) & ~(uintptr_t)1023);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int i = st->i, kept = st->bs;
   const int p0 = i + kept + blockIdx.x * BM;
   if (kept == 0 || p0 >= n) return;
-  const int nk = (m + BK - 1) / BK;
+  // this CTA's row range: stages [s0, s0 + nk) of 32 rows (CTAs along y split the rows;
+  // their partial W are summed, in split order, by the residual update)
+  const int s0 = blockIdx.y * stages_per_split;
+  const int nk = min(stages_per_split, (m + BK - 1) / BK - s0);
+  if (nk <= 0) return;
   volatile int* abort = &sm.abort;
 
   if (threadIdx.x == 0) {
@@ -219,9 +224,9 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
         if (s >= STAGES && !mbar_wait(&sm.empty[slot], (use & 1) ^ 1, abort)) break;
         uint8_t* base = sm.stage[slot];
         mbar_expect_tx(&sm.full[slot], A_BYTES + 2 * B_BYTES);
-        tma_load_2d(base, &tmA, &sm.full[slot], s * BK, p0);
-        tma_load_2d(base + 2 * A_BYTES, &tmQh, &sm.full[slot], s * BK, 0);
-        tma_load_2d(base + 2 * A_BYTES + B_BYTES, &tmQl, &sm.full[slot], s * BK, 0);
+        tma_load_2d(base, &tmA, &sm.full[slot], (s0 + s) * BK, p0);
+        tma_load_2d(base + 2 * A_BYTES, &tmQh, &sm.full[slot], (s0 + s) * BK, 0);
+        tma_load_2d(base + 2 * A_BYTES + B_BYTES, &tmQl, &sm.full[slot], (s0 + s) * BK, 0);
         issued = s + 1;
       }
     }
@@ -299,9 +304,10 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
     }
     const int p = p0 + 32 * q + lane;
     if (ok && !*abort && p < n) {
+      double* wz = Wpart + (int64_t)blockIdx.y * BN * n;
 #pragma unroll
       for (int a = 0; a < BN; ++a)
-        if (a < kept) R[(int64_t)(i + a) * ldr + p] = (double)hi[a] + (double)lo[a];
+        if (a < kept) wz[(int64_t)a * n + p] = (double)hi[a] + (double)lo[a];
     }
   }
   __syncthreads();
