@@ -10,6 +10,7 @@
 
 #include "rbrp_internal.h"
 #include "rbrp_kernels.cuh"
+#include "rbrp_panel_df.cuh"
 #include "rbrp_tc.cuh"
 
 namespace rbrp {
@@ -34,6 +35,16 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
                                            (int)sizeof(PanelSmem)), "cudaFuncSetAttribute(k_panel2)");
     if (s != RBRP_OK) return s;
     if (RES) {
+      for (const void* fn : {(const void*)k_pchol_df, (const void*)k_chol2_df}) {
+        s = cuda_check(h, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)sizeof(PcholDfSmem)), "cudaFuncSetAttribute(panel df)");
+        if (s != RBRP_OK) return s;
+      }
+      for (const void* fn : {(const void*)k_panel1_df, (const void*)k_panel2_df}) {
+        s = cuda_check(h, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)sizeof(RowsDfSmem)), "cudaFuncSetAttribute(rows df)");
+        if (s != RBRP_OK) return s;
+      }
       s = cuda_check(h, cudaFuncSetAttribute(k_resid_update, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)P2_SMEM), "cudaFuncSetAttribute(k_resid_update)");
       if (s != RBRP_OK) return s;
@@ -103,24 +114,39 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
       const int64_t cnt = (int64_t)i * MAXB;
       k_reduce_parts<T><<<(int)std::min<int64_t>(1024, (cnt + 255) / 256), 256, 0, st>>>(Cpart, splits, cnt, cnt, C);
     }
-    if (RES)  // panel = residual columns at the sampled positions
-      k_cgs_update<T><<<ntiles, 256, 0, st>>>((const T*)h->Ares, L.ld_res, h->js, Q, m, C, h->st, m, h->V,
-                                              h->Gpart, 0);
-    else
+    const int dtiles = (m + DF_ROWS - 1) / DF_ROWS;  // row tiles of the double-float panel kernels
+    if (RES) {  // panel = residual columns at the sampled positions (FP32, exact), Gram in double-float
+      k_gram_df<<<dtiles, 256, 0, st>>>(h->Ares, L.ld_res, h->js, h->st, m, (float*)h->V, h->Gpart);
+      k_reduce_parts<double><<<16, 256, 0, st>>>(h->Gpart, dtiles, MAXB * MAXB, MAXB * MAXB, h->G);
+    } else {
       k_cgs_update<T><<<ntiles, 256, 0, st>>>(dA, lda, h->cols, Q, m, C, h->st, m, h->V, h->Gpart, 1);
-    k_reduce_parts<double><<<16, 256, 0, st>>>(h->Gpart, ntiles, MAXB * MAXB, MAXB * MAXB, h->G);
+      k_reduce_parts<double><<<16, 256, 0, st>>>(h->Gpart, ntiles, MAXB * MAXB, MAXB * MAXB, h->G);
+    }
     prof_end(h, RBRP_PHASE_CGS, ev, 0.0, 0.0, (!RES && i > 0) ? 4 : 2);
     ev = prof_begin(h);
-    k_pchol<<<1, 256, panel_smem, st>>>(h->G, m, h->st, tol_loc, h->js, h->perm, h->diags, h->R11, h->ord,
-                                        h->J, h->K1, h->K2);
-    k_panel1<<<ntiles, 256, panel_smem, st>>>(h->V, m, h->st, h->R11, h->ord, h->Q1, h->G2part);
-    k_reduce_parts<double><<<16, 256, 0, st>>>(h->G2part, ntiles, MAXB * MAXB, MAXB * MAXB, h->G2);
-    k_chol2<<<1, 256, panel_smem, st>>>(h->G2, h->st, h->R11, h->R2, h->R, n);
+    if (RES) {
+      k_pchol_df<<<1, 256, sizeof(PcholDfSmem), st>>>(h->G, m, h->st, tol_loc, h->js, h->perm, h->diags, h->R11,
+                                                      h->ord, h->J, h->K1, h->K2);
+      k_panel1_df<<<dtiles, DF_ROWS, sizeof(RowsDfSmem), st>>>((const float*)h->V, m, h->st, h->R11, h->ord,
+                                                               (float2*)h->Q1, h->G2part);
+      k_reduce_parts<double><<<16, 256, 0, st>>>(h->G2part, dtiles, MAXB * MAXB, MAXB * MAXB, h->G2);
+      k_chol2_df<<<1, 256, sizeof(PcholDfSmem), st>>>(h->G2, h->st, h->R11, h->R2, h->R, n);
+    } else {
+      k_pchol<<<1, 256, panel_smem, st>>>(h->G, m, h->st, tol_loc, h->js, h->perm, h->diags, h->R11, h->ord,
+                                          h->J, h->K1, h->K2);
+      k_panel1<<<ntiles, 256, panel_smem, st>>>(h->V, m, h->st, h->R11, h->ord, h->Q1, h->G2part);
+      k_reduce_parts<double><<<16, 256, 0, st>>>(h->G2part, ntiles, MAXB * MAXB, MAXB * MAXB, h->G2);
+      k_chol2<<<1, 256, panel_smem, st>>>(h->G2, h->st, h->R11, h->R2, h->R, n);
+    }
     if (i > 0) k_swap_R<<<(i + 127) / 128, 128, 0, st>>>(h->R, n, h->st, h->J, h->K1, h->K2);
     if (RES)
       k_swap_cols<<<dim3((m + 1023) / 1024, MAXB), 256, 0, st>>>(h->Ares, L.ld_res, h->st, m, h->K1, h->K2);
-    k_panel2<T><<<ntiles, 256, panel_smem, st>>>(h->Q1, m, h->st, h->R2, Q, RES ? L.ld_res : m, RES ? 0 : 1,
-                                                 use_tc ? h->Qh : nullptr, use_tc ? h->Ql : nullptr, L.ld_res);
+    if (RES)
+      k_panel2_df<<<dtiles, DF_ROWS, sizeof(RowsDfSmem), st>>>((const float2*)h->Q1, m, h->st, h->R2, (float*)Q,
+                                                               L.ld_res, use_tc ? h->Qh : nullptr,
+                                                               use_tc ? h->Ql : nullptr, L.ld_res);
+    else
+      k_panel2<T><<<ntiles, 256, panel_smem, st>>>(h->Q1, m, h->st, h->R2, Q, m, 1, nullptr, nullptr, 0);
     prof_end(h, RBRP_PHASE_PANEL, ev, 0.0, 0.0, (i > 0 ? 6 : 5) + (RES ? 1 : 0));
     int nproj;
     ev = prof_begin(h);

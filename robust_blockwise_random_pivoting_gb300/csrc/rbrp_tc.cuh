@@ -11,10 +11,11 @@
 //            into TF32 hi + lo parts; per K step the large product Ahi Qhi goes
 //            to one TMEM accumulator and the two small ones (Ahi Qlo, Alo Qhi)
 //            to another.
-//   warps 2-5 split each staged A tile into its hi / lo parts (in shared
+//   warps 2-9 split each staged A tile into its hi / lo parts (in shared
 //            memory, same swizzled layout, one stage ahead of the MMAs), drain
 //            the large accumulator after every stage and the small one every
-//            512 rows with tcgen05.ld, into double-float registers.
+//            512 rows with tcgen05.ld, into double-float registers.  Two warps
+//            share each TMEM lane quarter, one per half of the 64 columns.
 //
 // Why the drains: the tensor core rounds its FP32 accumulator once per MMA and
 // the rounding is biased, so the error grows linearly with the number of MMAs
@@ -42,7 +43,8 @@ constexpr int CHUNK = 16;                // stages per drain of the small-produc
 constexpr int A_BYTES = BM * BK * 4;     // 16 KB
 constexpr int B_BYTES = BN * BK * 4;     // 8 KB
 constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;  // A hi, A lo, Q hi, Q lo
-constexpr int NTHREADS = 192;
+constexpr int NTHREADS = 320;            // TMA warp, MMA warp, 8 split / drain warps
+constexpr int NEPI = NTHREADS - 64;
 constexpr int TMEM_COLS = 4 * BN;         // large x2, small x2
 constexpr int ST_ERR_TIMEOUT = 7;
 
@@ -162,14 +164,11 @@ __device__ __forceinline__ void df_acc(float& hi, float& lo, float x) {
   hi = t;
 }
 
-__device__ __forceinline__ void drain64(uint32_t taddr, float (&hi)[BN], float (&lo)[BN]) {
+__device__ __forceinline__ void drain32(uint32_t taddr, float (&hi)[32], float (&lo)[32]) {
+  float v[32];
+  tmem_ld32(taddr, v);
 #pragma unroll
-  for (int h = 0; h < BN / 32; ++h) {
-    float v[32];
-    tmem_ld32(taddr + (uint32_t)(32 * h), v);
-#pragma unroll
-    for (int j = 0; j < 32; ++j) df_acc(hi[32 * h + j], lo[32 * h + j], v[j]);
-  }
+  for (int j = 0; j < 32; ++j) df_acc(hi[j], lo[j], v[j]);
 }
 
 __global__ void __launch_bounds__(NTHREADS, 1)
@@ -192,14 +191,14 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
       mbar_init(&sm.full[s], 1);
-      mbar_init(&sm.split[s], 128);
+      mbar_init(&sm.split[s], NEPI);
       mbar_init(&sm.empty[s], 1);
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&sm.bigf[b], 1);
-      mbar_init(&sm.bige[b], 128);
+      mbar_init(&sm.bige[b], NEPI);
       mbar_init(&sm.smlf[b], 1);
-      mbar_init(&sm.smle[b], 128);
+      mbar_init(&sm.smle[b], NEPI);
     }
     sm.abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -261,12 +260,13 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
       }
     }
   } else {
-    const int et = threadIdx.x - 64;  // 0..127
+    const int et = threadIdx.x - 64;  // 0..NEPI-1
     const int q = warp & 3;           // TMEM lane quarter of this warp
-    const uint32_t lane_off = (uint32_t)(32 * q) << 16;
-    float hi[BN], lo[BN];
+    const int ch = (warp - 2) >> 2;   // column half of the accumulators this warp drains
+    const uint32_t lane_off = ((uint32_t)(32 * q) << 16) + (uint32_t)(32 * ch);
+    float hi[32], lo[32];
 #pragma unroll
-    for (int a = 0; a < BN; ++a) hi[a] = lo[a] = 0.f;
+    for (int a = 0; a < 32; ++a) hi[a] = lo[a] = 0.f;
     // split stage t into hi / lo parts and hand it to the MMA warp
     auto split_stage = [&](int t) -> bool {
       const int slot = t % STAGES;
@@ -274,7 +274,7 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
       float4* a4 = reinterpret_cast<float4*>(sm.stage[slot]);
       float4* l4 = reinterpret_cast<float4*>(sm.stage[slot] + A_BYTES);
 #pragma unroll 4
-      for (int e = et; e < A_BYTES / 16; e += 128) {
+      for (int e = et; e < A_BYTES / 16; e += NEPI) {
         const float4 v = a4[e];
         const float4 h = make_float4(tf32_trunc(v.x), tf32_trunc(v.y), tf32_trunc(v.z), tf32_trunc(v.w));
         a4[e] = h;
@@ -290,14 +290,14 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
       const int b = s & 1;
       if (!mbar_wait(&sm.bigf[b], (uint32_t)(s >> 1) & 1, abort)) { ok = false; break; }
       tc_fence_after();
-      drain64(tbase + lane_off + (uint32_t)(b * BN), hi, lo);
+      drain32(tbase + lane_off + (uint32_t)(b * BN), hi, lo);
       tc_fence_before();
       mbar_arrive(&sm.bige[b]);
       if ((s % CHUNK) == CHUNK - 1 || s == nk - 1) {
         const int chunk = s / CHUNK, sb = chunk & 1;
         if (!mbar_wait(&sm.smlf[sb], (uint32_t)(chunk >> 1) & 1, abort)) { ok = false; break; }
         tc_fence_after();
-        drain64(tbase + lane_off + (uint32_t)(2 * BN + sb * BN), hi, lo);
+        drain32(tbase + lane_off + (uint32_t)(2 * BN + sb * BN), hi, lo);
         tc_fence_before();
         mbar_arrive(&sm.smle[sb]);
       }
@@ -306,8 +306,10 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
     if (ok && !*abort && p < n) {
       double* wz = Wpart + (int64_t)blockIdx.y * BN * n;
 #pragma unroll
-      for (int a = 0; a < BN; ++a)
-        if (a < kept) wz[(int64_t)a * n + p] = (double)hi[a] + (double)lo[a];
+      for (int j = 0; j < 32; ++j) {
+        const int a = 32 * ch + j;
+        if (a < kept) wz[(int64_t)a * n + p] = (double)hi[j] + (double)lo[j];
+      }
     }
   }
   __syncthreads();
