@@ -151,18 +151,36 @@ __global__ void __launch_bounds__(256) k_trsm_T_df(const double* __restrict__ R,
     float sh[8], sl[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) sh[q] = sl[q] = 0.f;
-    for (int bj = bi + 1; bj < nbk; ++bj) {
+    // the tiles of step bj are fetched into registers during step bj - 1
+    double rpre[16], xpre[8];
+    auto fetch = [&](int bj) {
       const int cr = bj * 64, cl = min(64, k - cr);
-      __syncthreads();
-      for (int idx = tid; idx < 64 * 64; idx += 256) {
-        const int y = idx & 63, xr = idx >> 6;
-        sm.Rs[xr][y] = df_split((xr < bl && y < cl) ? -R[(int64_t)(b0 + xr) * ldr + cr + y] : 0.0);
+#pragma unroll
+      for (int u = 0; u < 16; ++u) {
+        const int idx = tid + 256 * u, y = idx & 63, xr = idx >> 6;
+        rpre[u] = (xr < bl && y < cl) ? -R[(int64_t)(b0 + xr) * ldr + cr + y] : 0.0;
       }
-      for (int idx = tid; idx < 64 * 32; idx += 256) {
-        const int y = idx & 63, c = idx >> 6;
-        sm.Xs[y][c] = df_split((y < cl && c < nc) ? T[(cr + y) + (int64_t)(c0 + c) * k] : 0.0);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int idx = tid + 256 * u, y = idx & 63, c = idx >> 6;
+        xpre[u] = (y < cl && c < nc) ? T[(cr + y) + (int64_t)(c0 + c) * k] : 0.0;
+      }
+    };
+    if (bi + 1 < nbk) fetch(bi + 1);
+    for (int bj = bi + 1; bj < nbk; ++bj) {
+      __syncthreads();
+#pragma unroll
+      for (int u = 0; u < 16; ++u) {
+        const int idx = tid + 256 * u;
+        sm.Rs[idx >> 6][idx & 63] = df_split(rpre[u]);
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int idx = tid + 256 * u;
+        sm.Xs[idx & 63][idx >> 6] = df_split(xpre[u]);
       }
       __syncthreads();
+      if (bj + 1 < nbk) fetch(bj + 1);
 #pragma unroll 4
       for (int y = 0; y < 64; ++y) {
         const float2 r = sm.Rs[x][y];

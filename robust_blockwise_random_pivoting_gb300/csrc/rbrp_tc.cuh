@@ -45,7 +45,8 @@ constexpr int B_BYTES = BN * BK * 4;     // 8 KB
 constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;  // A hi, A lo, Q hi, Q lo
 constexpr int NTHREADS = 320;            // TMA warp, MMA warp, 8 split / drain warps
 constexpr int NEPI = NTHREADS - 64;
-constexpr int TMEM_COLS = 4 * BN;         // large x2, small x2
+constexpr int NBIG = 4;                   // large-product accumulators in the TMEM ring
+constexpr int TMEM_COLS = 512;            // large x4 + small x2 = 384 columns, rounded to a power of 2
 constexpr int ST_ERR_TIMEOUT = 7;
 
 // tcgen05 instruction descriptor: D = F32 (bits 4-5 = 1), A = B = TF32 (bits 7-9,
@@ -57,7 +58,7 @@ constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >
 struct __align__(1024) P1Smem {
   uint8_t stage[STAGES][STAGE_BYTES];
   unsigned long long full[STAGES], split[STAGES], empty[STAGES];
-  unsigned long long bigf[2], bige[2];     // large accumulator: full (MMA done) / empty (drained)
+  unsigned long long bigf[NBIG], bige[NBIG];  // large accumulators: full (MMA done) / empty (drained)
   unsigned long long smlf[2], smle[2];     // small accumulator
   uint32_t tmem_base;
   int abort;
@@ -194,9 +195,11 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
       mbar_init(&sm.split[s], NEPI);
       mbar_init(&sm.empty[s], 1);
     }
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < NBIG; ++b) {
       mbar_init(&sm.bigf[b], 1);
       mbar_init(&sm.bige[b], NEPI);
+    }
+    for (int b = 0; b < 2; ++b) {
       mbar_init(&sm.smlf[b], 1);
       mbar_init(&sm.smle[b], NEPI);
     }
@@ -234,10 +237,10 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
       for (int s = 0; s < nk; ++s) {
         const int slot = s % STAGES;
         const uint32_t use = (uint32_t)(s / STAGES);
-        const int b = s & 1;                         // large accumulator of this stage
+        const int b = s % NBIG;                      // large accumulator of this stage
         const int chunk = s / CHUNK, sb = chunk & 1;  // small accumulator of this chunk
         const bool first = (s % CHUNK) == 0;
-        if (s >= 2 && !mbar_wait(&sm.bige[b], (uint32_t)((s >> 1) - 1) & 1, abort)) break;
+        if (s >= NBIG && !mbar_wait(&sm.bige[b], (uint32_t)(s / NBIG - 1) & 1, abort)) break;
         if (first && chunk >= 2 && !mbar_wait(&sm.smle[sb], (uint32_t)((chunk >> 1) - 1) & 1, abort)) break;
         if (!mbar_wait(&sm.split[slot], use & 1, abort)) break;
         tc_fence_after();
@@ -247,7 +250,7 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
         const uint64_t dqh = sw128_desc(smem_u32(base + 2 * A_BYTES));
         const uint64_t dql = sw128_desc(smem_u32(base + 2 * A_BYTES + B_BYTES));
         const uint32_t dbig = tbase + (uint32_t)(b * BN);
-        const uint32_t dsml = tbase + (uint32_t)(2 * BN + sb * BN);
+        const uint32_t dsml = tbase + (uint32_t)(NBIG * BN + sb * BN);
 #pragma unroll
         for (int k = 0; k < BK / 8; ++k) {  // K = 8 TF32 = 32 bytes: +2 in the 16-byte address field
           mma_tf32(dbig, dah + 2 * k, dqh + 2 * k, k == 0 ? 0u : 1u);
@@ -284,24 +287,31 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
       mbar_arrive(&sm.split[slot]);
       return true;
     };
-    bool ok = nk > 0 && split_stage(0);
-    for (int s = 0; ok && s < nk; ++s) {
-      if (s + 1 < nk && !split_stage(s + 1)) { ok = false; break; }
-      const int b = s & 1;
-      if (!mbar_wait(&sm.bigf[b], (uint32_t)(s >> 1) & 1, abort)) { ok = false; break; }
+    // drain stage d (large accumulator, and the small one at the end of its chunk)
+    auto drain_stage = [&](int d) -> bool {
+      const int b = d % NBIG;
+      if (!mbar_wait(&sm.bigf[b], (uint32_t)(d / NBIG) & 1, abort)) return false;
       tc_fence_after();
       drain32(tbase + lane_off + (uint32_t)(b * BN), hi, lo);
       tc_fence_before();
       mbar_arrive(&sm.bige[b]);
-      if ((s % CHUNK) == CHUNK - 1 || s == nk - 1) {
-        const int chunk = s / CHUNK, sb = chunk & 1;
-        if (!mbar_wait(&sm.smlf[sb], (uint32_t)(chunk >> 1) & 1, abort)) { ok = false; break; }
+      if ((d % CHUNK) == CHUNK - 1 || d == nk - 1) {
+        const int chunk = d / CHUNK, sb = chunk & 1;
+        if (!mbar_wait(&sm.smlf[sb], (uint32_t)(chunk >> 1) & 1, abort)) return false;
         tc_fence_after();
-        drain32(tbase + lane_off + (uint32_t)(2 * BN + sb * BN), hi, lo);
+        drain32(tbase + lane_off + (uint32_t)(NBIG * BN + sb * BN), hi, lo);
         tc_fence_before();
         mbar_arrive(&sm.smle[sb]);
       }
+      return true;
+    };
+    // split runs one stage ahead of the MMAs, the drain one stage behind them
+    bool ok = nk > 0 && split_stage(0);
+    for (int s = 0; ok && s < nk; ++s) {
+      if (s + 1 < nk && !split_stage(s + 1)) { ok = false; break; }
+      if (s >= 1 && !drain_stage(s - 1)) { ok = false; break; }
     }
+    if (ok && nk > 0) ok = drain_stage(nk - 1);
     const int p = p0 + 32 * q + lane;
     if (ok && !*abort && p < n) {
       double* wz = Wpart + (int64_t)blockIdx.y * BN * n;
