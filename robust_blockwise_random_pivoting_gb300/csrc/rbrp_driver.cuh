@@ -114,7 +114,8 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
       const int64_t cnt = (int64_t)i * MAXB;
       k_reduce_parts<T><<<(int)std::min<int64_t>(1024, (cnt + 255) / 256), 256, 0, st>>>(Cpart, splits, cnt, cnt, C);
     }
-    const int dtiles = (m + DF_ROWS - 1) / DF_ROWS;  // row tiles of the double-float panel kernels
+    const int dtiles = (m + DF_ROWS - 1) / DF_ROWS;   // row tiles of the double-float Gram kernel
+    const int ttiles = (m + DF_TROWS - 1) / DF_TROWS; // row tiles of the double-float row solves
     if (RES) {  // panel = residual columns at the sampled positions (FP32, exact), Gram in double-float
       k_gram_df<<<dtiles, 256, 0, st>>>(h->Ares, L.ld_res, h->js, h->st, m, (float*)h->V, h->Gpart);
       k_reduce_parts<double><<<16, 256, 0, st>>>(h->Gpart, dtiles, MAXB * MAXB, MAXB * MAXB, h->G);
@@ -127,9 +128,9 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
     if (RES) {
       k_pchol_df<<<1, 256, sizeof(PcholDfSmem), st>>>(h->G, m, h->st, tol_loc, h->js, h->perm, h->diags, h->R11,
                                                       h->ord, h->J, h->K1, h->K2);
-      k_panel1_df<<<dtiles, DF_ROWS, sizeof(RowsDfSmem), st>>>((const float*)h->V, m, h->st, h->R11, h->ord,
-                                                               (float2*)h->Q1, h->G2part);
-      k_reduce_parts<double><<<16, 256, 0, st>>>(h->G2part, dtiles, MAXB * MAXB, MAXB * MAXB, h->G2);
+      k_panel1_df<<<ttiles, DF_TROWS, sizeof(RowsDfSmem), st>>>((const float*)h->V, m, h->st, h->R11, h->ord,
+                                                                (float2*)h->Q1, h->G2part);
+      k_reduce_parts<double><<<16, 256, 0, st>>>(h->G2part, ttiles, MAXB * MAXB, MAXB * MAXB, h->G2);
       k_chol2_df<<<1, 256, sizeof(PcholDfSmem), st>>>(h->G2, h->st, h->R11, h->R2, h->R, n);
     } else {
       k_pchol<<<1, 256, panel_smem, st>>>(h->G, m, h->st, tol_loc, h->js, h->perm, h->diags, h->R11, h->ord,
@@ -142,7 +143,7 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
     if (RES)
       k_swap_cols<<<dim3((m + 1023) / 1024, MAXB), 256, 0, st>>>(h->Ares, L.ld_res, h->st, m, h->K1, h->K2);
     if (RES)
-      k_panel2_df<<<dtiles, DF_ROWS, sizeof(RowsDfSmem), st>>>((const float2*)h->Q1, m, h->st, h->R2, (float*)Q,
+      k_panel2_df<<<ttiles, DF_TROWS, sizeof(RowsDfSmem), st>>>((const float2*)h->Q1, m, h->st, h->R2, (float*)Q,
                                                                L.ld_res, use_tc ? h->Qh : nullptr,
                                                                use_tc ? h->Ql : nullptr, L.ld_res);
     else

@@ -50,8 +50,26 @@ __device__ __forceinline__ dfl df_mul(dfl a, dfl b) {
   e = fmaf(a.lo, b.hi, e);
   return df_fast(p, e);
 }
-// s - a * b
-__device__ __forceinline__ dfl df_fms(dfl s, dfl a, dfl b) { return df_add(s, df_neg(df_mul(a, b))); }
+// s - a * b (one error-free product, one TwoSum)
+__device__ __forceinline__ dfl df_fms(dfl s, dfl a, dfl b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  const dfl t = df_two_sum(s.hi, -p);
+  return df_fast(t.hi, t.lo + (s.lo - e));
+}
+// acc + a * b
+__device__ __forceinline__ dfl df_fma2(dfl acc, dfl a, dfl b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  const dfl t = df_two_sum(acc.hi, p);
+  return df_fast(t.hi, t.lo + (acc.lo + e));
+}
+__device__ __forceinline__ bool df_gt(dfl a, dfl b) { return a.hi > b.hi || (a.hi == b.hi && a.lo > b.lo); }
+__device__ __forceinline__ bool df_eq(dfl a, dfl b) { return a.hi == b.hi && a.lo == b.lo; }
 __device__ __forceinline__ dfl df_recip(dfl b) {
   const float q = 1.0f / b.hi;
   const dfl r = df_add({1.0f, 0.0f}, df_neg(df_mul({q, 0.0f}, b)));  // 1 - q b
@@ -72,7 +90,8 @@ __device__ __forceinline__ void df_acc_prod(dfl& acc, float x, float y) {
   acc = df_fast(s.hi, s.lo);
 }
 
-constexpr int DF_ROWS = 128;  // panel rows per CTA in the row kernels
+constexpr int DF_ROWS = 128;  // panel rows per CTA of the Gram kernel
+constexpr int DF_TROWS = 64;  // panel rows per CTA of the row-solve kernels (one thread per row)
 
 // V = A_res(:, J) (FP32, exact) for 128 rows per CTA, and the tile's Gram partial V^T V
 // (upper triangle, mirrored) in double-float, stored as FP64.
@@ -95,15 +114,21 @@ k_gram_df(const float* __restrict__ Ares, int64_t ld, const int* __restrict__ js
   __syncthreads();
   double* G = Gpart + (int64_t)blockIdx.x * MAXB * MAXB;
   const int c1 = tid >> 2;
+  dfl acc[16];
+#pragma unroll
+  for (int q = 0; q < 16; ++q) acc[q] = {0.f, 0.f};
+  if (c1 < bss) {
+    for (int rr = 0; rr < DF_ROWS; ++rr) {
+      const float x = Vs[rr][c1];
+#pragma unroll
+      for (int q = 0; q < 16; ++q) df_acc_prod(acc[q], x, Vs[rr][(tid & 3) + 4 * q]);
+    }
+  }
+#pragma unroll
   for (int q = 0; q < 16; ++q) {
     const int c2 = (tid & 3) + 4 * q;
-    if (c2 < c1) continue;
-    dfl acc = {0.f, 0.f};
-    if (c1 < bss && c2 < bss)
-      for (int rr = 0; rr < DF_ROWS; ++rr) df_acc_prod(acc, Vs[rr][c1], Vs[rr][c2]);
-    const double g = df_dbl(acc);
+    const double g = (c1 < bss && c2 < bss) ? df_dbl(acc[q]) : 0.0;
     G[c1 * MAXB + c2] = g;
-    G[c2 * MAXB + c1] = g;
   }
 }
 
@@ -112,13 +137,72 @@ struct PcholDfSmem {
   dfl R[MAXB][MAXB + 1];   // R[t][j]: row t of the factor, by panel column j
   int ord[MAXB];           // slot -> panel column
   int alive[MAXB];
-  int stop, piv;
+  int J[MAXB], K1[MAXB], K2[MAXB], inblk[MAXB], Tperm[MAXB];
+  double Tdiag[MAXB];
+  int stop, piv, nK;
   dfl inv;
 };
 
+// Block swap of perm and diags (matlab/RBRP.m:81-99), in parallel: K1 = block
+// positions not kept (ascending), K2 = kept positions outside the block (pivot
+// order), compacted with warp ballots.  All threads call it after `kept` is known.
+__device__ void block_swap_parallel(PcholDfSmem& sm, int i, int kept, const int* __restrict__ js,
+                                    int* __restrict__ perm, double* __restrict__ diags, int* __restrict__ Jg,
+                                    int* __restrict__ K1g, int* __restrict__ K2g, State* st) {
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  if (tid < MAXB) sm.inblk[tid] = 0;
+  __syncthreads();
+  if (tid < kept) {
+    const int p = js[sm.ord[tid]];
+    sm.J[tid] = p;
+    Jg[tid] = p;
+    if (p >= i && p < i + kept) sm.inblk[p - i] = 1;
+    sm.Tperm[tid] = perm[p];
+  }
+  __syncthreads();
+  if (wid < 2) {
+    // warp 0: K1 (block positions not kept), warp 1: K2 (kept positions outside the block)
+    int count = 0;
+    for (int base = 0; base < kept; base += 32) {
+      const int t = base + lane;
+      bool flag = false;
+      int val = 0;
+      if (t < kept) {
+        if (wid == 0) { flag = !sm.inblk[t]; val = i + t; }
+        else { const int p = sm.J[t]; flag = p < i || p >= i + kept; val = p; }
+      }
+      const unsigned bal = __ballot_sync(0xffffffffu, flag);
+      if (flag) {
+        const int slot = count + __popc(bal & ((1u << lane) - 1u));
+        if (wid == 0) sm.K1[slot] = val; else sm.K2[slot] = val;
+      }
+      count += __popc(bal);
+    }
+    if (wid == 1 && lane == 0) sm.nK = count;
+  }
+  __syncthreads();
+  const int nK = sm.nK;
+  if (tid < nK) {  // perm(K2) = perm(K1), diags(K2) = diags(K1): K1 inside the block, K2 outside
+    const int a = sm.K1[tid], b = sm.K2[tid];
+    const int pa = perm[a];
+    const double da = diags[a];
+    perm[b] = pa;
+    diags[b] = da;
+    K1g[tid] = a;
+    K2g[tid] = b;
+  }
+  __syncthreads();
+  if (tid < kept) perm[i + tid] = sm.Tperm[tid];
+  if (tid == 0) {
+    st->bs = kept;
+    st->nK = nK;
+    st->zero_panel = kept == 0;
+  }
+}
+
 // Pivoted Cholesky of the panel Gram matrix with the robust filter (same rule as
-// pivoted_chol_filter), 256 threads, no data movement for the swaps.  CTA 0
-// publishes R11 (slot order, FP64), ord, the kept count and does the block swap.
+// pivoted_chol_filter), 256 threads, no data movement for the swaps.  Publishes
+// R11 (slot order, FP64), ord, the kept count and performs the block swap.
 __global__ void __launch_bounds__(256)
 k_pchol_df(const double* __restrict__ G, int m, State* st, double tol_loc, const int* __restrict__ js,
            int* __restrict__ perm, double* __restrict__ diags, double* __restrict__ R11g, int* __restrict__ ordg,
@@ -128,46 +212,43 @@ k_pchol_df(const double* __restrict__ G, int m, State* st, double tol_loc, const
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int nb = st->bs_sampled, i = st->i;
   const int rows = min(nb, m);
-  for (int idx = tid; idx < nb * nb; idx += 256) sm.S[idx / nb][idx % nb] = df_of(G[(idx / nb) * MAXB + idx % nb]);
+  const int ty = tid >> 4, tx = tid & 15;  // 4 x 4 Schur entries per thread: rows ty*4+u, columns tx*4+v
+  for (int idx = tid; idx < MAXB * MAXB; idx += 256) {
+    const int a = idx / MAXB, c = idx % MAXB;
+    sm.S[a][c] = (a < nb && c < nb) ? df_of(G[a * MAXB + c]) : dfl{0.f, 0.f};
+  }
   if (tid < MAXB) {
     sm.ord[tid] = tid;
     sm.alive[tid] = tid < nb;
   }
   __syncthreads();
-  // total = trace(G) in double-float
-  float tot_hi = 0.f;
-  double total = 0.0;
+  double total = 0.0;  // trace(G), used by warp 0
   if (wid == 0) {
     dfl t = {0.f, 0.f};
-    for (int s = 0; s < nb; ++s) t = df_add(t, sm.S[s][s]);
+    for (int s2 = 0; s2 < nb; ++s2) t = df_add(t, sm.S[s2][s2]);
     total = df_dbl(t);
-    (void)tot_hi;
   }
   int kept = rows;
   for (int t = 0; t < rows; ++t) {
     if (wid == 0) {
       // remaining trace and the first maximal slot (LAPACK dgeqp3 order)
-      dfl rem = {0.f, 0.f};
-      double best = -1.0;
+      dfl rem = {0.f, 0.f}, best = {-1.f, 0.f};
       int bs = nb;
-      for (int s = t + lane; s < nb; s += 32) {
-        const dfl d = sm.S[sm.ord[s]][sm.ord[s]];
+      for (int s2 = t + lane; s2 < nb; s2 += 32) {
+        const dfl d = sm.S[sm.ord[s2]][sm.ord[s2]];
         rem = df_add(rem, d);
-        const double dv = df_dbl(d);
-        if (dv > best) { best = dv; bs = s; }
+        if (df_gt(d, best)) { best = d; bs = s2; }
       }
-      double remv = df_dbl(rem);
-      remv = warp_sum(remv);
-      remv = __shfl_sync(0xffffffffu, remv, 0);
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
-        const double ob = __shfl_down_sync(0xffffffffu, best, o);
+        const dfl orem = {__shfl_down_sync(0xffffffffu, rem.hi, o), __shfl_down_sync(0xffffffffu, rem.lo, o)};
+        rem = df_add(rem, orem);
+        const dfl ob = {__shfl_down_sync(0xffffffffu, best.hi, o), __shfl_down_sync(0xffffffffu, best.lo, o)};
         const int oi = __shfl_down_sync(0xffffffffu, bs, o);
-        if (ob > best || (ob == best && oi < bs)) { best = ob; bs = oi; }
+        if (df_gt(ob, best) || (df_eq(ob, best) && oi < bs)) { best = ob; bs = oi; }
       }
       if (lane == 0) {
-        const double tt = total;
-        const bool stop = !(tt > 0.0) || (remv / tt < tol_loc) || !(best > 0.0);
+        const bool stop = !(total > 0.0) || (df_dbl(rem) / total < tol_loc) || !(best.hi > 0.f);
         sm.stop = stop;
         if (!stop) {
           const int o = sm.ord[t];
@@ -186,14 +267,24 @@ k_pchol_df(const double* __restrict__ G, int m, State* st, double tol_loc, const
     if (sm.stop) { kept = t; break; }
     const int pv = sm.piv;
     const dfl inv = sm.inv;
-    for (int j = tid; j < nb; j += 256)
-      if (sm.alive[j]) sm.R[t][j] = df_mul(sm.S[pv][j], inv);
+    if (tid < nb && sm.alive[tid]) sm.R[t][tid] = df_mul(sm.S[pv][tid], inv);
     __syncthreads();
-    // Schur complement over the alive columns (full square: rows j1, columns j2)
-    for (int idx = tid; idx < nb * nb; idx += 256) {
-      const int j1 = idx / nb, j2 = idx % nb;
-      if (sm.alive[j1] && sm.alive[j2]) sm.S[j1][j2] = df_fms(sm.S[j1][j2], sm.R[t][j1], sm.R[t][j2]);
+    dfl ru[4], rv[4];
+    bool au[4], av[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int j = ty * 4 + u;
+      au[u] = j < nb && sm.alive[j];
+      ru[u] = sm.R[t][j];
+      const int c = tx * 4 + u;
+      av[u] = c < nb && sm.alive[c];
+      rv[u] = sm.R[t][c];
     }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v)
+        if (au[u] && av[v]) sm.S[ty * 4 + u][tx * 4 + v] = df_fms(sm.S[ty * 4 + u][tx * 4 + v], ru[u], rv[v]);
     __syncthreads();
   }
   // R11 in slot order: R11[a][c] = R[a][ord[c]] for c >= a
@@ -202,44 +293,20 @@ k_pchol_df(const double* __restrict__ G, int m, State* st, double tol_loc, const
     R11g[idx] = (a < kept && c < kept && c >= a) ? df_dbl(sm.R[a][sm.ord[c]]) : 0.0;
   }
   if (tid < MAXB) ordg[tid] = sm.ord[tid];
-  if (tid == 0) {
-    int J[MAXB], K1[MAXB], K2[MAXB];
-    int nK = 0;
-    for (int s = 0; s < kept; ++s) J[s] = js[sm.ord[s]];
-    int nk1 = 0;
-    for (int p = i; p < i + kept; ++p) {
-      bool in = false;
-      for (int s = 0; s < kept; ++s) in |= (J[s] == p);
-      if (!in) K1[nk1++] = p;
-    }
-    for (int s = 0; s < kept; ++s)
-      if (J[s] < i || J[s] >= i + kept) K2[nK++] = J[s];
-    int Tperm[MAXB];
-    for (int s = 0; s < kept; ++s) Tperm[s] = perm[J[s]];
-    for (int t = 0; t < nK; ++t) {
-      perm[K2[t]] = perm[K1[t]];
-      diags[K2[t]] = diags[K1[t]];
-    }
-    for (int s = 0; s < kept; ++s) perm[i + s] = Tperm[s];
-    for (int s = 0; s < kept; ++s) Jg[s] = J[s];
-    for (int t = 0; t < nK; ++t) { K1g[t] = K1[t]; K2g[t] = K2[t]; }
-    st->bs = kept;
-    st->nK = nK;
-    st->zero_panel = kept == 0;
-  }
+  block_swap_parallel(sm, i, kept, js, perm, diags, Jg, K1g, K2g, st);
 }
 
 // Rows of X R^{-1} (R upper, kept x kept, FP64 in global) for 128 rows per CTA,
 // one thread per row, in double-float; optionally the Gram partial of the result.
 struct RowsDfSmem {
   dfl R[MAXB][MAXB + 1];
-  dfl W[DF_ROWS][MAXB + 1];
+  dfl W[DF_TROWS][MAXB + 1];
   int ord[MAXB];
 };
 
 __device__ __forceinline__ void rows_solve_df(RowsDfSmem& sm, int kept) {
   const int r = threadIdx.x;
-  if (r < DF_ROWS) {
+  if (r < DF_TROWS) {
     for (int s = 0; s < kept; ++s) {
       dfl x = sm.W[r][s];
       for (int u = 0; u < s; ++u) x = df_fms(x, sm.W[r][u], sm.R[u][s]);
@@ -255,7 +322,7 @@ __device__ __forceinline__ void load_R_df(RowsDfSmem& sm, const double* __restri
 }
 
 // Q1 = V(:, ord[:kept]) R11^{-1} (double-float, stored as float pairs) and Q1^T Q1 partials.
-__global__ void __launch_bounds__(DF_ROWS)
+__global__ void __launch_bounds__(DF_TROWS)
 k_panel1_df(const float* __restrict__ V, int m, const State* __restrict__ st, const double* __restrict__ R11g,
             const int* __restrict__ ordg, float2* __restrict__ Q1, double* __restrict__ G2part) {
   extern __shared__ __align__(16) unsigned char dyn_smem[];
@@ -266,29 +333,38 @@ k_panel1_df(const float* __restrict__ V, int m, const State* __restrict__ st, co
   load_R_df(sm, R11g, kept);
   if (tid < MAXB) sm.ord[tid] = ordg[tid];
   __syncthreads();
-  const int r0 = blockIdx.x * DF_ROWS;
-  for (int idx = tid; idx < DF_ROWS * kept; idx += DF_ROWS) {
-    const int rr = idx % DF_ROWS, s = idx / DF_ROWS, r = r0 + rr;
+  const int r0 = blockIdx.x * DF_TROWS;
+  for (int idx = tid; idx < DF_TROWS * kept; idx += DF_TROWS) {
+    const int rr = idx % DF_TROWS, s = idx / DF_TROWS, r = r0 + rr;
     sm.W[rr][s] = {r < m ? V[r + (int64_t)sm.ord[s] * m] : 0.f, 0.f};
   }
   __syncthreads();
   rows_solve_df(sm, kept);
-  for (int idx = tid; idx < DF_ROWS * kept; idx += DF_ROWS) {
-    const int rr = idx % DF_ROWS, s = idx / DF_ROWS, r = r0 + rr;
+  for (int idx = tid; idx < DF_TROWS * kept; idx += DF_TROWS) {
+    const int rr = idx % DF_TROWS, s = idx / DF_TROWS, r = r0 + rr;
     if (r < m) Q1[r + (int64_t)s * m] = make_float2(sm.W[rr][s].hi, sm.W[rr][s].lo);
   }
-  // Gram partial (upper triangle, mirrored): thread -> (c1, c2) pairs
+  // Gram partial: thread -> column c1 = tid, all 64 columns c2 (64 independent chains
+  // would not fit; 16 at a time)
   double* G = G2part + (int64_t)blockIdx.x * MAXB * MAXB;
-  const int rows_valid = max(0, min(DF_ROWS, m - r0));
-  for (int pair = tid; pair < MAXB * MAXB; pair += DF_ROWS) {
-    const int c1 = pair / MAXB, c2 = pair % MAXB;
-    if (c2 < c1) continue;
-    dfl acc = {0.f, 0.f};
-    if (c1 < kept && c2 < kept)
-      for (int rr = 0; rr < rows_valid; ++rr) acc = df_add(acc, df_mul(sm.W[rr][c1], sm.W[rr][c2]));
-    const double g = df_dbl(acc);
-    G[c1 * MAXB + c2] = g;
-    G[c2 * MAXB + c1] = g;
+  const int rows_valid = max(0, min(DF_TROWS, m - r0));
+  const int c1 = tid;
+  for (int q0 = 0; q0 < MAXB; q0 += 16) {
+    dfl acc[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) acc[q] = {0.f, 0.f};
+    if (c1 < kept) {
+      for (int rr = 0; rr < rows_valid; ++rr) {
+        const dfl x = sm.W[rr][c1];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) acc[q] = df_fma2(acc[q], x, sm.W[rr][q0 + q]);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      const int c2 = q0 + q;
+      G[c1 * MAXB + c2] = (c1 < kept && c2 < kept) ? df_dbl(acc[q]) : 0.0;
+    }
   }
 }
 
@@ -303,6 +379,7 @@ k_chol2_df(const double* __restrict__ G2, const State* __restrict__ st, const do
   if (kept == 0) return;
   for (int idx = tid; idx < kept * kept; idx += 256) sm.S[idx / kept][idx % kept] = df_of(G2[(idx / kept) * MAXB + idx % kept]);
   __syncthreads();
+  const int ty = tid >> 4, tx = tid & 15;
   for (int t = 0; t < kept; ++t) {
     if (tid == 0) {
       const dfl r = df_sqrt(sm.S[t][t]);
@@ -311,12 +388,18 @@ k_chol2_df(const double* __restrict__ G2, const State* __restrict__ st, const do
     }
     __syncthreads();
     const dfl inv = sm.inv;
-    for (int s = t + 1 + tid; s < kept; s += 256) sm.R[t][s] = df_mul(sm.S[t][s], inv);
+    if (tid > t && tid < kept) sm.R[t][tid] = df_mul(sm.S[t][tid], inv);
     __syncthreads();
-    const int w = kept - t - 1;
-    for (int idx = tid; idx < w * w; idx += 256) {
-      const int s1 = t + 1 + idx / w, s2 = t + 1 + idx % w;
-      if (s2 >= s1) sm.S[s1][s2] = df_fms(sm.S[s1][s2], sm.R[t][s1], sm.R[t][s2]);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int s1 = ty * 4 + u;
+      if (s1 <= t || s1 >= kept) continue;
+      const dfl r1 = sm.R[t][s1];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const int s2 = tx * 4 + v;
+        if (s2 >= s1 && s2 < kept) sm.S[s1][s2] = df_fms(sm.S[s1][s2], r1, sm.R[t][s2]);
+      }
     }
     __syncthreads();
   }
@@ -335,7 +418,7 @@ k_chol2_df(const double* __restrict__ G2, const State* __restrict__ st, const do
 
 // Q_blk = Q1 R2^{-1}: FP32 basis for the residual update and its exact TF32
 // split (Qh = tf32(Q), Ql = fp32(Q - Qh), zero beyond the kept columns).
-__global__ void __launch_bounds__(DF_ROWS)
+__global__ void __launch_bounds__(DF_TROWS)
 k_panel2_df(const float2* __restrict__ Q1, int m, const State* __restrict__ st, const double* __restrict__ R2g,
             float* __restrict__ Q, int64_t ldq, float* __restrict__ Qh, float* __restrict__ Ql, int64_t ldh) {
   extern __shared__ __align__(16) unsigned char dyn_smem[];
@@ -344,16 +427,16 @@ k_panel2_df(const float2* __restrict__ Q1, int m, const State* __restrict__ st, 
   const int kept = st->bs;
   if (kept == 0) return;
   load_R_df(sm, R2g, kept);
-  const int r0 = blockIdx.x * DF_ROWS;
-  for (int idx = tid; idx < DF_ROWS * kept; idx += DF_ROWS) {
-    const int rr = idx % DF_ROWS, s = idx / DF_ROWS, r = r0 + rr;
+  const int r0 = blockIdx.x * DF_TROWS;
+  for (int idx = tid; idx < DF_TROWS * kept; idx += DF_TROWS) {
+    const int rr = idx % DF_TROWS, s = idx / DF_TROWS, r = r0 + rr;
     const float2 v = r < m ? Q1[r + (int64_t)s * m] : make_float2(0.f, 0.f);
     sm.W[rr][s] = {v.x, v.y};
   }
   __syncthreads();
   rows_solve_df(sm, kept);
-  for (int idx = tid; idx < DF_ROWS * MAXB; idx += DF_ROWS) {
-    const int rr = idx % DF_ROWS, s = idx / DF_ROWS, r = r0 + rr;
+  for (int idx = tid; idx < DF_TROWS * MAXB; idx += DF_TROWS) {
+    const int rr = idx % DF_TROWS, s = idx / DF_TROWS, r = r0 + rr;
     if (r < m) {
       const double q = s < kept ? df_dbl(sm.W[rr][s]) : 0.0;
       if (s < kept) Q[r + (int64_t)s * ldq] = (float)q;
