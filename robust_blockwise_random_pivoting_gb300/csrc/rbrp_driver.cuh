@@ -40,7 +40,7 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
                                                (int)sizeof(PcholDfSmem)), "cudaFuncSetAttribute(panel df)");
         if (s != RBRP_OK) return s;
       }
-      for (const void* fn : {(const void*)k_panel1_df, (const void*)k_panel2_df}) {
+      for (const void* fn : {(const void*)k_panel1_df, (const void*)k_panel2_df, (const void*)k_panel_q_df}) {
         s = cuda_check(h, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                (int)sizeof(RowsDfSmem)), "cudaFuncSetAttribute(rows df)");
         if (s != RBRP_OK) return s;
@@ -128,10 +128,10 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
     if (RES) {
       k_pchol_df<<<1, 256, sizeof(PcholDfSmem), st>>>(h->G, m, h->st, tol_loc, h->js, h->perm, h->diags, h->R11,
                                                       h->ord, h->J, h->K1, h->K2);
-      k_panel1_df<<<ttiles, DF_TROWS, sizeof(RowsDfSmem), st>>>((const float*)h->V, m, h->st, h->R11, h->ord,
-                                                                (float2*)h->Q1, h->G2part);
-      k_reduce_parts<double><<<16, 256, 0, st>>>(h->G2part, ttiles, MAXB * MAXB, MAXB * MAXB, h->G2);
-      k_chol2_df<<<1, 256, sizeof(PcholDfSmem), st>>>(h->G2, h->st, h->R11, h->R2, h->R, n);
+      k_panel_q_df<<<ttiles, DF_TROWS, sizeof(RowsDfSmem), st>>>((const float*)h->V, m, h->st, h->R11, h->ord,
+                                                                 (float*)Q, L.ld_res, use_tc ? h->Qh : nullptr,
+                                                                 use_tc ? h->Ql : nullptr, L.ld_res);
+      k_write_r11<<<1, 256, 0, st>>>(h->st, h->R11, h->R, n);
     } else {
       k_pchol<<<1, 256, panel_smem, st>>>(h->G, m, h->st, tol_loc, h->js, h->perm, h->diags, h->R11, h->ord,
                                           h->J, h->K1, h->K2);
@@ -142,13 +142,8 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
     if (i > 0) k_swap_R<<<(i + 127) / 128, 128, 0, st>>>(h->R, n, h->st, h->J, h->K1, h->K2);
     if (RES)
       k_swap_cols<<<dim3((m + 1023) / 1024, MAXB), 256, 0, st>>>(h->Ares, L.ld_res, h->st, m, h->K1, h->K2);
-    if (RES)
-      k_panel2_df<<<ttiles, DF_TROWS, sizeof(RowsDfSmem), st>>>((const float2*)h->Q1, m, h->st, h->R2, (float*)Q,
-                                                               L.ld_res, use_tc ? h->Qh : nullptr,
-                                                               use_tc ? h->Ql : nullptr, L.ld_res);
-    else
-      k_panel2<T><<<ntiles, 256, panel_smem, st>>>(h->Q1, m, h->st, h->R2, Q, m, 1, nullptr, nullptr, 0);
-    prof_end(h, RBRP_PHASE_PANEL, ev, 0.0, 0.0, (i > 0 ? 6 : 5) + (RES ? 1 : 0));
+    if (!RES) k_panel2<T><<<ntiles, 256, panel_smem, st>>>(h->Q1, m, h->st, h->R2, Q, m, 1, nullptr, nullptr, 0);
+    prof_end(h, RBRP_PHASE_PANEL, ev, 0.0, 0.0, RES ? (i > 0 ? 5 : 4) : (i > 0 ? 6 : 5));
     int nproj;
     ev = prof_begin(h);
     if (RES) {

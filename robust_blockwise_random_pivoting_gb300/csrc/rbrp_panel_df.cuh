@@ -368,6 +368,54 @@ k_panel1_df(const float* __restrict__ V, int m, const State* __restrict__ st, co
   }
 }
 
+// Q_blk = V(:, ord[:kept]) R11^{-1} in double-float, written as the FP32 basis and
+// its exact TF32 split (Qh = tf32(Q), Ql = fp32(Q - Qh), zero beyond the kept
+// columns).  One CholQR pass suffices here: with ~48-bit arithmetic the loss of
+// orthogonality, ~2^-48 cond(V_kept)^2, stays far below the FP32 rounding of
+// the stored basis for the conditioning the robust filter admits.
+__global__ void __launch_bounds__(DF_TROWS)
+k_panel_q_df(const float* __restrict__ V, int m, const State* __restrict__ st, const double* __restrict__ R11g,
+             const int* __restrict__ ordg, float* __restrict__ Q, int64_t ldq, float* __restrict__ Qh,
+             float* __restrict__ Ql, int64_t ldh) {
+  extern __shared__ __align__(16) unsigned char dyn_smem[];
+  RowsDfSmem& sm = *reinterpret_cast<RowsDfSmem*>(dyn_smem);
+  const int tid = threadIdx.x;
+  const int kept = st->bs;
+  if (kept == 0) return;
+  load_R_df(sm, R11g, kept);
+  if (tid < MAXB) sm.ord[tid] = ordg[tid];
+  __syncthreads();
+  const int r0 = blockIdx.x * DF_TROWS;
+  for (int idx = tid; idx < DF_TROWS * kept; idx += DF_TROWS) {
+    const int rr = idx % DF_TROWS, s = idx / DF_TROWS, r = r0 + rr;
+    sm.W[rr][s] = {r < m ? V[r + (int64_t)sm.ord[s] * m] : 0.f, 0.f};
+  }
+  __syncthreads();
+  rows_solve_df(sm, kept);
+  for (int idx = tid; idx < DF_TROWS * MAXB; idx += DF_TROWS) {
+    const int rr = idx % DF_TROWS, s = idx / DF_TROWS, r = r0 + rr;
+    if (r < m) {
+      const double q = s < kept ? df_dbl(sm.W[rr][s]) : 0.0;
+      if (s < kept) Q[r + (int64_t)s * ldq] = (float)q;
+      if (Qh) {
+        const float h = __uint_as_float(__float_as_uint((float)q) & 0xFFFFE000u);
+        Qh[r + (int64_t)s * ldh] = h;
+        Ql[r + (int64_t)s * ldh] = (float)(q - (double)h);
+      }
+    }
+  }
+}
+
+// R(I2, I2) = R11, the panel R of a single CholQR pass (upper triangle, slot order).
+__global__ void k_write_r11(const State* __restrict__ st, const double* __restrict__ R11g, double* __restrict__ R,
+                            int64_t ldr) {
+  const int kept = st->bs, i = st->i;
+  for (int idx = threadIdx.x; idx < kept * kept; idx += blockDim.x) {
+    const int a = idx / kept, c = idx % kept;
+    R[(int64_t)(i + a) * ldr + (i + c)] = c >= a ? R11g[a * MAXB + c] : 0.0;
+  }
+}
+
 // R2 = chol(Q1^T Q1) (one CTA, double-float) and the panel R = R2 R11 into R(I2, I2).
 __global__ void __launch_bounds__(256)
 k_chol2_df(const double* __restrict__ G2, const State* __restrict__ st, const double* __restrict__ R11g,

@@ -11,11 +11,13 @@
 //            into TF32 hi + lo parts; per K step the large product Ahi Qhi goes
 //            to one TMEM accumulator and the two small ones (Ahi Qlo, Alo Qhi)
 //            to another.
-//   warps 2-9 split each staged A tile into its hi / lo parts (in shared
-//            memory, same swizzled layout, one stage ahead of the MMAs), drain
-//            the large accumulator after every stage and the small one every
-//            512 rows with tcgen05.ld, into double-float registers.  Two warps
-//            share each TMEM lane quarter, one per half of the 64 columns.
+//   warps 2-5 split each staged A tile into its hi / lo parts (in shared
+//            memory, same swizzled layout) ahead of the MMAs.
+//   warps 6-13 drain the large accumulator after every stage and the small one
+//            every 512 rows with tcgen05.ld into double-float registers; two
+//            warps share each TMEM lane quarter, one per half of the 64 columns.
+//            Splitting and draining are independent chains, so neither waits
+//            for the other's latency.
 //
 // Why the drains: the tensor core rounds its FP32 accumulator once per MMA and
 // the rounding is biased, so the error grows linearly with the number of MMAs
@@ -43,8 +45,9 @@ constexpr int CHUNK = 16;                // stages per drain of the small-produc
 constexpr int A_BYTES = BM * BK * 4;     // 16 KB
 constexpr int B_BYTES = BN * BK * 4;     // 8 KB
 constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;  // A hi, A lo, Q hi, Q lo
-constexpr int NTHREADS = 320;            // TMA warp, MMA warp, 8 split / drain warps
-constexpr int NEPI = NTHREADS - 64;
+constexpr int NSPLIT = 128;              // 4 split warps
+constexpr int NDRAIN = 256;              // 8 drain warps
+constexpr int NTHREADS = 64 + NSPLIT + NDRAIN;  // TMA warp, MMA warp, split warps, drain warps
 constexpr int NBIG = 4;                   // large-product accumulators in the TMEM ring
 constexpr int TMEM_COLS = 512;            // large x4 + small x2 = 384 columns, rounded to a power of 2
 constexpr int ST_ERR_TIMEOUT = 7;
@@ -165,11 +168,28 @@ __device__ __forceinline__ void df_acc(float& hi, float& lo, float x) {
   hi = t;
 }
 
-__device__ __forceinline__ void drain32(uint32_t taddr, float (&hi)[32], float (&lo)[32]) {
-  float v[32];
-  tmem_ld32(taddr, v);
+// 16 consecutive TMEM columns of this warp's 32 lanes into registers.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-  for (int j = 0; j < 32; ++j) df_acc(hi[j], lo[j], v[j]);
+  for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+__device__ __forceinline__ void drain32(uint32_t taddr, float (&hi)[32], float (&lo)[32]) {
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    float v[16];
+    tmem_ld16(taddr + (uint32_t)(16 * h), v);
+#pragma unroll
+    for (int j = 0; j < 16; ++j) df_acc(hi[16 * h + j], lo[16 * h + j], v[j]);
+  }
 }
 
 __global__ void __launch_bounds__(NTHREADS, 1)
@@ -192,16 +212,16 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
       mbar_init(&sm.full[s], 1);
-      mbar_init(&sm.split[s], NEPI);
+      mbar_init(&sm.split[s], NSPLIT);
       mbar_init(&sm.empty[s], 1);
     }
     for (int b = 0; b < NBIG; ++b) {
       mbar_init(&sm.bigf[b], 1);
-      mbar_init(&sm.bige[b], NEPI);
+      mbar_init(&sm.bige[b], NDRAIN);
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&sm.smlf[b], 1);
-      mbar_init(&sm.smle[b], NEPI);
+      mbar_init(&sm.smle[b], NDRAIN);
     }
     sm.abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -262,22 +282,16 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
         if ((s % CHUNK) == CHUNK - 1 || s == nk - 1) mma_commit(&sm.smlf[sb]);
       }
     }
-  } else {
-    const int et = threadIdx.x - 64;  // 0..NEPI-1
-    const int q = warp & 3;           // TMEM lane quarter of this warp
-    const int ch = (warp - 2) >> 2;   // column half of the accumulators this warp drains
-    const uint32_t lane_off = ((uint32_t)(32 * q) << 16) + (uint32_t)(32 * ch);
-    float hi[32], lo[32];
-#pragma unroll
-    for (int a = 0; a < 32; ++a) hi[a] = lo[a] = 0.f;
-    // split stage t into hi / lo parts and hand it to the MMA warp
-    auto split_stage = [&](int t) -> bool {
-      const int slot = t % STAGES;
-      if (!mbar_wait(&sm.full[slot], (uint32_t)(t / STAGES) & 1, abort)) return false;
+  } else if (warp < 2 + NSPLIT / 32) {
+    // split warps: A tile of stage s -> hi / lo parts, then hand it to the MMA warp
+    const int et = threadIdx.x - 64;  // 0..NSPLIT-1
+    for (int s = 0; s < nk; ++s) {
+      const int slot = s % STAGES;
+      if (!mbar_wait(&sm.full[slot], (uint32_t)(s / STAGES) & 1, abort)) break;
       float4* a4 = reinterpret_cast<float4*>(sm.stage[slot]);
       float4* l4 = reinterpret_cast<float4*>(sm.stage[slot] + A_BYTES);
-#pragma unroll 4
-      for (int e = et; e < A_BYTES / 16; e += NEPI) {
+#pragma unroll
+      for (int e = et; e < A_BYTES / 16; e += NSPLIT) {
         const float4 v = a4[e];
         const float4 h = make_float4(tf32_trunc(v.x), tf32_trunc(v.y), tf32_trunc(v.z), tf32_trunc(v.w));
         a4[e] = h;
@@ -285,33 +299,33 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       mbar_arrive(&sm.split[slot]);
-      return true;
-    };
-    // drain stage d (large accumulator, and the small one at the end of its chunk)
-    auto drain_stage = [&](int d) -> bool {
+    }
+  } else {
+    // drain warps
+    const int dw = warp - 2 - NSPLIT / 32;  // 0..7
+    const int q = warp & 3;                  // TMEM lane quarter of this warp
+    const int ch = dw >> 2;                  // column half of the accumulators this warp drains
+    const uint32_t lane_off = ((uint32_t)(32 * q) << 16) + (uint32_t)(32 * ch);
+    float hi[32], lo[32];
+#pragma unroll
+    for (int a = 0; a < 32; ++a) hi[a] = lo[a] = 0.f;
+    bool ok = true;
+    for (int d = 0; d < nk; ++d) {
       const int b = d % NBIG;
-      if (!mbar_wait(&sm.bigf[b], (uint32_t)(d / NBIG) & 1, abort)) return false;
+      if (!mbar_wait(&sm.bigf[b], (uint32_t)(d / NBIG) & 1, abort)) { ok = false; break; }
       tc_fence_after();
       drain32(tbase + lane_off + (uint32_t)(b * BN), hi, lo);
       tc_fence_before();
       mbar_arrive(&sm.bige[b]);
       if ((d % CHUNK) == CHUNK - 1 || d == nk - 1) {
         const int chunk = d / CHUNK, sb = chunk & 1;
-        if (!mbar_wait(&sm.smlf[sb], (uint32_t)(chunk >> 1) & 1, abort)) return false;
+        if (!mbar_wait(&sm.smlf[sb], (uint32_t)(chunk >> 1) & 1, abort)) { ok = false; break; }
         tc_fence_after();
         drain32(tbase + lane_off + (uint32_t)(NBIG * BN + sb * BN), hi, lo);
         tc_fence_before();
         mbar_arrive(&sm.smle[sb]);
       }
-      return true;
-    };
-    // split runs one stage ahead of the MMAs, the drain one stage behind them
-    bool ok = nk > 0 && split_stage(0);
-    for (int s = 0; ok && s < nk; ++s) {
-      if (s + 1 < nk && !split_stage(s + 1)) { ok = false; break; }
-      if (s >= 1 && !drain_stage(s - 1)) { ok = false; break; }
     }
-    if (ok && nk > 0) ok = drain_stage(nk - 1);
     const int p = p0 + 32 * q + lane;
     if (ok && !*abort && p < n) {
       double* wz = Wpart + (int64_t)blockIdx.y * BN * n;
