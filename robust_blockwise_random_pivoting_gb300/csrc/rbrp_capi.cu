@@ -104,24 +104,56 @@ __global__ void __launch_bounds__(256) k_trsm_T(const double* __restrict__ R, in
   }
 }
 
-// Double-float form of the same solve.  GB300's FP64 pipe is ~1/64 of its FP32
-// pipe, so the block updates Acc -= R11(b, later) T(later) run in double-float
-// arithmetic on the FP32 pipe: operands split x = hi + lo (two floats, 48
-// significant bits), products by an exact FMA split, sums by TwoSum - about 12
-// FP32 operations per FP64 multiply-add, ~5x the FP64 rate.  The 64 x 64
-// diagonal solves and the running right-hand side stay in FP64.
-struct TrsmDfSmem {
-  float2 Rs[64][65];     // -R11 block, (hi, lo)
-  float2 Xs[64][33];     // solved T rows, (hi, lo)
-  double Acc[64][33];    // right-hand side / solution of the current block row
-  double Rd[64][65];     // FP64 diagonal block
-};
-
-__device__ __forceinline__ float2 df_split(double x) {
-  const float hi = (float)x;
-  return make_float2(hi, (float)(x - (double)hi));
+// Double-float form of the same solve.  GB300's FP64 pipe issues ~1/64 of its
+// FP32 pipe's rate, so the whole solve runs in double-float arithmetic on the
+// FP32 pipe: R11 and the right-hand sides are split once into float pairs
+// (hi + lo, ~48 significant bits) by k_split_df, the block updates use
+// error-free products (FMA split) and TwoSum, the 64 x 64 diagonal blocks are
+// solved in double-float too, and T is joined back to FP64 once at the end.
+__global__ void k_split_df(const double* __restrict__ R, int64_t ldr, int k, int ncols,
+                           float2* __restrict__ R11df, float2* __restrict__ Tdf) {
+  const int64_t total11 = (int64_t)k * k, totalT = (int64_t)k * ncols;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total11 + totalT;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    double x;
+    float2* dst;
+    if (idx < total11) {  // R11 row major (ld k), upper triangle
+      const int a = (int)(idx / k), c = (int)(idx % k);
+      x = c >= a ? R[(int64_t)a * ldr + c] : 0.0;
+      dst = R11df + idx;
+    } else {              // T column major (ld k), from R12 row major
+      const int64_t t = idx - total11;
+      const int c = (int)(t / k), a = (int)(t % k);
+      x = R[(int64_t)a * ldr + k + c];
+      dst = Tdf + t;
+    }
+    const float hi = (float)x;
+    *dst = make_float2(hi, (float)(x - (double)hi));
+  }
 }
 
+__global__ void k_join_df(const float2* __restrict__ Tdf, int64_t count, double* __restrict__ T) {
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < count; idx += (int64_t)gridDim.x * blockDim.x) {
+    const float2 v = Tdf[idx];
+    T[idx] = (double)v.x + (double)v.y;
+  }
+}
+
+struct TrsmDfSmem {
+  float2 Rs[64][65];     // -R11 block (update) or R11 diagonal block (solve)
+  float2 Xs[64][33];     // solved T rows
+  float2 Acc[64][33];    // right-hand side / solution of the current block row
+};
+
+__device__ __forceinline__ float2 df2_two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  return make_float2(s, (a - (s - bb)) + (b - bb));
+}
+__device__ __forceinline__ float2 df2_fast(float a, float b) {
+  const float s = a + b;
+  return make_float2(s, b - (s - a));
+}
 // (sh, sl) += a * b in double-float.
 __device__ __forceinline__ void df_mac(float& sh, float& sl, float2 a, float2 b) {
   const float p = a.x * b.x;
@@ -132,9 +164,26 @@ __device__ __forceinline__ void df_mac(float& sh, float& sl, float2 a, float2 b)
   sl += ((sh - (t - bb)) + (p - bb)) + (e + c);
   sh = t;
 }
+__device__ __forceinline__ float2 df2_add(float2 a, float2 b) {
+  float2 s = df2_two_sum(a.x, b.x);
+  s.y += a.y + b.y;
+  return df2_fast(s.x, s.y);
+}
+__device__ __forceinline__ float2 df2_mul(float2 a, float2 b) {
+  const float p = a.x * b.x;
+  float e = fmaf(a.x, b.x, -p);
+  e = fmaf(a.x, b.y, e);
+  e = fmaf(a.y, b.x, e);
+  return df2_fast(p, e);
+}
+__device__ __forceinline__ float2 df2_recip(float2 b) {
+  const float q = 1.0f / b.x;
+  const float2 r = df2_add(make_float2(1.0f, 0.0f), df2_mul(make_float2(-q, 0.0f), b));
+  return df2_fast(q, q * r.x);
+}
 
-__global__ void __launch_bounds__(256) k_trsm_T_df(const double* __restrict__ R, int64_t ldr, int k, int ncols,
-                                                   double* __restrict__ T) {
+__global__ void __launch_bounds__(256) k_trsm_T_df(const float2* __restrict__ R11, int k, int ncols,
+                                                   float2* __restrict__ T) {
   extern __shared__ __align__(16) unsigned char dyn_smem[];
   TrsmDfSmem& sm = *reinterpret_cast<TrsmDfSmem*>(dyn_smem);
   const int tid = threadIdx.x;
@@ -146,24 +195,25 @@ __global__ void __launch_bounds__(256) k_trsm_T_df(const double* __restrict__ R,
     const int b0 = bi * 64, bl = min(64, k - b0);
     for (int idx = tid; idx < 64 * 32; idx += 256) {
       const int xr = idx & 63, c = idx >> 6;
-      sm.Acc[xr][c] = (xr < bl && c < nc) ? T[(b0 + xr) + (int64_t)(c0 + c) * k] : 0.0;
+      sm.Acc[xr][c] = (xr < bl && c < nc) ? T[(b0 + xr) + (int64_t)(c0 + c) * k] : make_float2(0.f, 0.f);
     }
     float sh[8], sl[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) sh[q] = sl[q] = 0.f;
     // the tiles of step bj are fetched into registers during step bj - 1
-    double rpre[16], xpre[8];
+    float2 rpre[16], xpre[8];
     auto fetch = [&](int bj) {
       const int cr = bj * 64, cl = min(64, k - cr);
 #pragma unroll
       for (int u = 0; u < 16; ++u) {
         const int idx = tid + 256 * u, y = idx & 63, xr = idx >> 6;
-        rpre[u] = (xr < bl && y < cl) ? -R[(int64_t)(b0 + xr) * ldr + cr + y] : 0.0;
+        const float2 v = (xr < bl && y < cl) ? R11[(int64_t)(b0 + xr) * k + cr + y] : make_float2(0.f, 0.f);
+        rpre[u] = make_float2(-v.x, -v.y);
       }
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
         const int idx = tid + 256 * u, y = idx & 63, c = idx >> 6;
-        xpre[u] = (y < cl && c < nc) ? T[(cr + y) + (int64_t)(c0 + c) * k] : 0.0;
+        xpre[u] = (y < cl && c < nc) ? T[(cr + y) + (int64_t)(c0 + c) * k] : make_float2(0.f, 0.f);
       }
     };
     if (bi + 1 < nbk) fetch(bi + 1);
@@ -172,12 +222,12 @@ __global__ void __launch_bounds__(256) k_trsm_T_df(const double* __restrict__ R,
 #pragma unroll
       for (int u = 0; u < 16; ++u) {
         const int idx = tid + 256 * u;
-        sm.Rs[idx >> 6][idx & 63] = df_split(rpre[u]);
+        sm.Rs[idx >> 6][idx & 63] = rpre[u];
       }
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
         const int idx = tid + 256 * u;
-        sm.Xs[idx & 63][idx >> 6] = df_split(xpre[u]);
+        sm.Xs[idx & 63][idx >> 6] = xpre[u];
       }
       __syncthreads();
       if (bj + 1 < nbk) fetch(bj + 1);
@@ -196,17 +246,23 @@ __global__ void __launch_bounds__(256) k_trsm_T_df(const double* __restrict__ R,
     }
     __syncthreads();
 #pragma unroll
-    for (int q = 0; q < 8; ++q) sm.Acc[x][(tid & 3) + 4 * q] += (double)sh[q] + (double)sl[q];
+    for (int q = 0; q < 8; ++q) {
+      float2& a = sm.Acc[x][(tid & 3) + 4 * q];
+      a = df2_add(a, make_float2(sh[q], sl[q]));
+    }
     for (int idx = tid; idx < 64 * 64; idx += 256) {
       const int y = idx & 63, xr = idx >> 6;
-      sm.Rd[xr][y] = (xr < bl && y < bl && y >= xr) ? R[(int64_t)(b0 + xr) * ldr + b0 + y] : 0.0;
+      sm.Rs[xr][y] = (xr < bl && y < bl && y >= xr) ? R11[(int64_t)(b0 + xr) * k + b0 + y] : make_float2(0.f, 0.f);
     }
     __syncthreads();
-    if (tid < nc) {
+    if (tid < nc) {  // back substitution on the diagonal block, one right-hand side per thread
       for (int xr = bl - 1; xr >= 0; --xr) {
-        double v = sm.Acc[xr][tid];
-        for (int y = xr + 1; y < bl; ++y) v = fma(-sm.Rd[xr][y], sm.Acc[y][tid], v);
-        sm.Acc[xr][tid] = v / sm.Rd[xr][xr];
+        float vh = sm.Acc[xr][tid].x, vl = sm.Acc[xr][tid].y;
+        for (int y = xr + 1; y < bl; ++y) {
+          const float2 r = sm.Rs[xr][y];
+          df_mac(vh, vl, make_float2(-r.x, -r.y), sm.Acc[y][tid]);
+        }
+        sm.Acc[xr][tid] = df2_mul(df2_fast(vh, vl), df2_recip(sm.Rs[xr][xr]));
       }
     }
     __syncthreads();
@@ -412,19 +468,33 @@ rbrp_status solve_T(rbrp_handle h, int k, int n) {
     h->T_bytes = bytes;
   }
   const int ncols = n - k;
-  dim3 g1((ncols + 31) / 32, (k + 31) / 32), b1(32, 8);
-  k_gather_T<<<g1, b1, 0, h->stream>>>(h->R, n, k, ncols, h->T);
   rbrp_status s;
   if (h->tsolve_fp64) {
+    dim3 g1((ncols + 31) / 32, (k + 31) / 32), b1(32, 8);
+    k_gather_T<<<g1, b1, 0, h->stream>>>(h->R, n, k, ncols, h->T);
     s = cuda_check(h, cudaFuncSetAttribute(k_trsm_T, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)sizeof(TrsmSmem)), "cudaFuncSetAttribute(k_trsm_T)");
     if (s != RBRP_OK) return s;
     k_trsm_T<<<(ncols + 31) / 32, 256, sizeof(TrsmSmem), h->stream>>>(h->R, n, k, ncols, h->T);
   } else {
+    // double-float operands: R11 (k x k) and the right-hand sides (k x ncols), ~16 bytes per T entry
+    const size_t need = ((size_t)k * k + (size_t)k * ncols) * sizeof(float2);
+    if (need > h->df_bytes) {
+      if (h->df_buf) cudaFree(h->df_buf);
+      h->df_buf = nullptr;
+      h->df_bytes = 0;
+      s = cuda_check(h, cudaMalloc(&h->df_buf, need), "cudaMalloc(T solve operands)");
+      if (s != RBRP_OK) return s;
+      h->df_bytes = need;
+    }
+    float2* R11df = static_cast<float2*>(h->df_buf);
+    float2* Tdf = R11df + (size_t)k * k;
+    k_split_df<<<1216, 256, 0, h->stream>>>(h->R, n, k, ncols, R11df, Tdf);
     s = cuda_check(h, cudaFuncSetAttribute(k_trsm_T_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)sizeof(TrsmDfSmem)), "cudaFuncSetAttribute(k_trsm_T_df)");
     if (s != RBRP_OK) return s;
-    k_trsm_T_df<<<(ncols + 31) / 32, 256, sizeof(TrsmDfSmem), h->stream>>>(h->R, n, k, ncols, h->T);
+    k_trsm_T_df<<<(ncols + 31) / 32, 256, sizeof(TrsmDfSmem), h->stream>>>(R11df, k, ncols, Tdf);
+    k_join_df<<<1216, 256, 0, h->stream>>>(Tdf, (int64_t)k * ncols, h->T);
   }
   return cuda_check(h, cudaGetLastError(), "T solve launch");
 }
@@ -649,6 +719,7 @@ rbrp_status rbrp_destroy(rbrp_handle h) {
     DeviceGuard g(h->device);
     if (h->ws) cudaFree(h->ws);
     if (h->T) cudaFree(h->T);
+    if (h->df_buf) cudaFree(h->df_buf);
     if (h->hostA_dev) cudaFree(h->hostA_dev);
     if (h->hst) cudaFreeHost(h->hst);
     for (auto e : h->block_events) cudaEventDestroy(e);

@@ -63,6 +63,8 @@ struct rbrp_handle_st {
   // interpolation matrix of the last run
   double* T = nullptr;
   size_t T_bytes = 0;
+  void* df_buf = nullptr;      // double-float operands of the T solve
+  size_t df_bytes = 0;
 
   // device copy of a host matrix (host-buffer entry points)
   void* hostA_dev = nullptr;

@@ -164,9 +164,10 @@ k_sample(State* st, const double* __restrict__ diags, const int* __restrict__ pe
     double part = 0.0;
     for (int j = lo; j < hi; ++j) part += w[j];
     const double S = block_sum(part, shd);
+    const double invS = 1.0 / S;  // one FP64 division; per-entry divisions are ~1/64-rate work on GB300
     int npos = 0;
     for (int j = lo; j < hi; ++j) {
-      const double pj = w[j] / S;
+      const double pj = w[j] * invS;
       pbuf[j] = pj;
       npos += pj > 0.0;
     }
@@ -196,7 +197,10 @@ k_sample(State* st, const double* __restrict__ diags, const int* __restrict__ pe
       // normalise by the last entry, as numpy's cdf /= cdf[-1]: the last entry is exactly 1
       const double last = cdf[nrem - 1];
       __syncthreads();
-      for (int j = lo; j < hi; ++j) cdf[j] /= last;
+      const double inv_last = 1.0 / last;
+      for (int j = lo; j < hi; ++j) cdf[j] *= inv_last;
+      __syncthreads();
+      if (tid == 0) cdf[nrem - 1] = 1.0;  // the last entry is exactly 1, as numpy's cdf /= cdf[-1]
       __syncthreads();
       if (tid < need) {
         const double x = np_uniform(seed, s_draws + (unsigned long long)tid);
