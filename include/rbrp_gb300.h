@@ -147,6 +147,68 @@ rbrp_status rbrp_id_f32_host(rbrp_handle h, int m, int n, const float* hA, int64
                              const rbrp_params* p, int* hPerm, double* hT, int64_t ldt,
                              int64_t t_cap, rbrp_result* out);
 
+/* ---- batched form: many independent IDs in one persistent launch -------
+ *
+ * The reference solves one matrix per RBRP() call (gpu/rbrp.cu:333-503,
+ * driven per matrix from gpu/driver.cpp:177); it has no batched entry.  Here
+ * each problem runs the same adaptive loop as rbrp_id_f32 (FP32 residual form,
+ * double-float panel, sums and T solve) inside one CTA of a persistent kernel
+ * that pulls problems, largest first, from a device-side work queue.  The
+ * launch (queue reset + kernel) is captured once in a CUDA graph and replayed
+ * by rbrp_batch_run.  Problem q uses the Philox key seed + q.  Each problem's
+ * data is scaled by a power of two at load (exact), so blocks whose entries
+ * are far below 1 (off-diagonal kernel blocks) keep full FP32 resolution.
+ */
+typedef struct {
+  int m, n;            /* shape, m, n >= 1 */
+  int64_t lda;         /* leading dimension of A, >= m */
+  const float* A;      /* device, column major, FP32 */
+  int* perm;           /* device, n ints (output): perm[:k] = S, perm[k:] = rd */
+  double* T;           /* device (output) T = R11^{-1} R12, k x (n-k), column major, ld = k;
+                          NULL: not computed */
+  int64_t T_cap;       /* doubles available at T (k * (n-k) are written) */
+} rbrp_batch_problem;
+
+typedef struct {
+  int k;               /* rank found */
+  int nblocks;         /* blocks that kept at least one column */
+  int status;          /* RBRP_OK, RBRP_ERR_NUMERIC (non-finite input / no progress) or
+                          RBRP_ERR_CAPACITY (T_cap < k * (n-k): T not written) */
+  int attempts;        /* block attempts, including numerically zero panels */
+  double res0;         /* ||A||_F^2 */
+  double err_est;      /* squared relative residual at the stop */
+  uint64_t draws;      /* uniforms consumed from the np-compat stream */
+} rbrp_batch_result;
+
+typedef struct {
+  int b;               /* block size in use (the autotuner's choice when params b <= 0) */
+  int panel_cols;      /* panel capacity of the kernel variant in use (16 or 32) */
+  int ctas;            /* persistent CTAs of the launch */
+  int ctas_per_sm;
+  double ms_last;      /* device time of the last rbrp_batch_run, ms */
+  double ms_autotune;  /* time the autotuner spent in the last plan, ms */
+  size_t workspace_bytes;
+} rbrp_batch_info;
+
+/* Plans a batch: validates and uploads the problem list (host array), sizes the
+ * per-CTA workspace slots and, when p->b <= 0, runs the autotuner, which times
+ * the candidate block sizes (b in {8, 16, 24, 32}) and CTAs per SM on this very
+ * batch and keeps the fastest (results for a fixed b are deterministic).  The
+ * batched kernel takes b <= 32.  Keeps the problems' buffers by pointer until
+ * the next plan. */
+rbrp_status rbrp_batch_plan(rbrp_handle h, int nprob, const rbrp_batch_problem* problems,
+                            const rbrp_params* p);
+/* Enqueues the planned batch on the handle's stream as one CUDA graph launch
+ * (captured on first use after a plan); does not synchronise. */
+rbrp_status rbrp_batch_run(rbrp_handle h);
+/* Waits for the last run and copies its per-problem results (host array of
+ * cap >= nprob entries, in the caller's problem order). */
+rbrp_status rbrp_batch_results(rbrp_handle h, rbrp_batch_result* out, int cap);
+rbrp_status rbrp_batch_get_info(rbrp_handle h, rbrp_batch_info* info);
+/* plan + run + results in one call. */
+rbrp_status rbrp_id_batched_f32(rbrp_handle h, int nprob, const rbrp_batch_problem* problems,
+                                const rbrp_params* p, rbrp_batch_result* out);
+
 /* ---- per-phase timing (CUDA events on the handle's stream) ------------- */
 enum {
   RBRP_PHASE_NORMS = 0,    /* initial column norms + totals */

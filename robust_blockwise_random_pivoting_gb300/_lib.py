@@ -42,6 +42,21 @@ class PhaseStats(ctypes.Structure):
                 ("launches", c_int * NPHASES)]
 
 
+class BatchProblem(ctypes.Structure):
+    _fields_ = [("m", c_int), ("n", c_int), ("lda", c_int64), ("A", c_void_p), ("perm", c_void_p),
+                ("T", c_void_p), ("T_cap", c_int64)]
+
+
+class BatchResult(ctypes.Structure):
+    _fields_ = [("k", c_int), ("nblocks", c_int), ("status", c_int), ("attempts", c_int),
+                ("res0", c_double), ("err_est", c_double), ("draws", c_uint64)]
+
+
+class BatchInfo(ctypes.Structure):
+    _fields_ = [("b", c_int), ("panel_cols", c_int), ("ctas", c_int), ("ctas_per_sm", c_int),
+                ("ms_last", c_double), ("ms_autotune", c_double), ("workspace_bytes", ctypes.c_size_t)]
+
+
 class RBRPError(RuntimeError):
     def __init__(self, status, detail=""):
         self.status = status
@@ -84,6 +99,12 @@ _SIGS = {
     "rbrp_set_tsolve_fp64": (c_int, [c_void_p, c_int]),
     "rbrp_id_error_f64_noalloc": (c_int, [c_int, c_int, c_void_p, c_int64, c_void_p, c_int, c_void_p, c_int64,
                                           c_double, c_void_p, c_void_p]),
+    "rbrp_batch_plan": (c_int, [c_void_p, c_int, ctypes.POINTER(BatchProblem), ctypes.POINTER(Params)]),
+    "rbrp_batch_run": (c_int, [c_void_p]),
+    "rbrp_batch_results": (c_int, [c_void_p, ctypes.POINTER(BatchResult), c_int]),
+    "rbrp_batch_get_info": (c_int, [c_void_p, ctypes.POINTER(BatchInfo)]),
+    "rbrp_id_batched_f32": (c_int, [c_void_p, c_int, ctypes.POINTER(BatchProblem), ctypes.POINTER(Params),
+                                    ctypes.POINTER(BatchResult)]),
 }
 
 

@@ -1,0 +1,1033 @@
+// rbrp_batched.cu - batched adaptive RBRP: many independent column IDs of
+// uneven shape (e.g. the off-diagonal blocks of a hierarchical kernel matrix)
+// in one persistent launch.
+//
+// Each problem runs the adaptive loop of RBRP() (gpu/rbrp.cu:333-503) and of
+// the notebook's blocked_rpid (python/RBRP.ipynb cell 11 lines 76-173) in the
+// FP32 residual form of the one-matrix path, entirely inside one CTA of 256
+// threads: column norms, block sampling, panel Gram matrix, double-float
+// pivoted Cholesky with the robust filter, block swap, basis solve, projection
+// W = Q^T A_res and update A_res -= Q W with exact norms, stop rule, and the
+// T = R11^{-1} R12 solve.  A persistent grid (CTAs per SM x SMs) pulls problem
+// indices from a device-side queue (one atomicAdd per problem), largest first,
+// so thousands of uneven problems balance across the SMs without host
+// round trips.  Each CTA owns one workspace slot sized for the largest
+// problem; nothing in the kernel waits on another CTA.
+//
+// Layout of a slot (one problem at a time, ld = m rounded up to 4):
+//   A_res  ld x n FP32, column major, position ordered (written by the first
+//          update; the first block reads A through perm, scaled)
+//   R      kcap x n double-float (float2), row major, indexed by position
+//   V      ld x BB FP32 sampled panel;  Qc ld x BB / Qr m x BB FP32 basis of
+//          the block (column and row major)
+//   diags  n FP64 residual column norms by position;  pbuf 2n FP64 sampler
+#include <algorithm>
+#include <cfloat>
+#include <climits>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <vector>
+
+#include "rbrp_internal.h"
+#include "rbrp_pchol_df.cuh"
+#include "rbrp_sampler.cuh"
+
+namespace rbrp {
+
+struct BatchArgs {
+  unsigned char* slots;
+  int64_t slot_bytes;
+  int64_t off_R, off_V, off_Qc, off_Qr, off_diag, off_pbuf;
+  double tol, tol_loc;
+  uint64_t seed;
+  int b, sampler, kmax, compute_T;
+};
+
+namespace {
+
+constexpr int BT = 256;     // threads per CTA: one problem per CTA
+constexpr int BROWS = 128;  // rows per stage of the Gram / projection / update loops
+constexpr int TCOL = 64;    // remaining positions per column tile
+constexpr int BATCH_MAXB = 32;
+
+// Exact scaling by 2^s as two normal-float factors, so s may cover the full
+// exponent range of FP32 data (|s| <= 250).
+struct Pow2 {
+  float a, b;
+  __device__ __forceinline__ float apply(float x) const { return __fmul_rn(__fmul_rn(x, a), b); }
+};
+__device__ __forceinline__ Pow2 pow2_scale(int s) {
+  const int s1 = s / 2, s2 = s - s1;
+  return {__int_as_float((s1 + 127) << 23), __int_as_float((s2 + 127) << 23)};
+}
+
+template <int BB>
+struct BatchSmem {
+  static constexpr int NG = 64 / BB;  // row groups of the projection (4 basis x 4 columns per thread)
+  State st;
+  int js[MAXB];
+  int cols[MAXB];
+  const float* src[TCOL];  // source column of each panel column / tile column
+  double red_d[32];
+  int red_i[32];
+  __align__(16) float Ws[BB][TCOL];  // W of the current tile, FP32, for the update
+  union {
+    float gram_Vs[BROWS][BB + 1];
+    struct {
+      PcholDfSmemT<BB> pc;
+      dfl R11s[BB][BB + 1];  // R11 in slot order (upper)
+      dfl invd[BB];
+    } pan;
+    struct {
+      __align__(16) float Xs[BROWS][TCOL + 4];
+      __align__(16) float Qs[BROWS][BB + 4];
+    } p1;
+    dfl red[NG][BB][TCOL];
+    __align__(16) float p2_Qs[BB][BROWS];
+  } u;
+};
+
+__device__ __forceinline__ int block_max_int(int v, int* sh) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  v = __reduce_max_sync(0xffffffffu, v);
+  __syncthreads();
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  int r = sh[0];
+  for (int w = 1; w < (int)(blockDim.x >> 5); ++w) r = max(r, sh[w]);
+  __syncthreads();
+  return r;
+}
+
+// a1: column maxima, squared norms (double-float, each column scaled by its own
+// power of two so tiny entries keep their resolution) and perm = identity.
+// Returns the problem's exponent emax (max |A| = f 2^emax, f in [0.5, 1)) and
+// rescales diags to the problem scale 2^-emax; *bad flags non-finite entries.
+template <int BB>
+__device__ int batch_norms(BatchSmem<BB>& sm, const float* __restrict__ A, int64_t lda, int m, int n,
+                           int* __restrict__ perm, double* __restrict__ diags, int* __restrict__ colexp, int* bad,
+                           double* res0, int* nnz) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  int emax = INT_MIN, nonfinite = 0;
+  for (int c = warp; c < n; c += BT / 32) {
+    const float* col = A + (int64_t)c * lda;
+    unsigned mx = 0u;
+    int nf = 0;
+    for (int r = lane; r < m; r += 32) {
+      const float v = fabsf(col[r]);
+      nf |= !(v <= FLT_MAX);
+      mx = max(mx, __float_as_uint(v));
+    }
+    mx = __reduce_max_sync(0xffffffffu, mx);
+    nf = __any_sync(0xffffffffu, nf);
+    double d = 0.0;
+    int e = INT_MIN;
+    if (!nf && mx != 0u) {
+      frexpf(__uint_as_float(mx), &e);
+      const Pow2 sc = pow2_scale(-e);
+      DF acc{0.f, 0.f};
+      for (int r = lane; r < m; r += 32) df_add_sq(acc, sc.apply(col[r]));
+      d = warp_sum((double)acc.hi + (double)acc.lo);
+    }
+    if (lane == 0) {
+      diags[c] = d;
+      colexp[c] = e;
+      perm[c] = c;
+    }
+    emax = max(emax, e);
+    nonfinite |= nf;
+  }
+  *bad = __syncthreads_or(nonfinite);
+  emax = block_max_int(emax, sm.red_i);
+  double s = 0.0;
+  int cnt = 0;
+  for (int c = tid; c < n; c += BT) {
+    const int e = colexp[c];
+    const double d = (e == INT_MIN || *bad) ? 0.0 : ldexp(diags[c], 2 * (e - emax));
+    diags[c] = d;
+    s += d;
+    cnt += d > 0.0;
+  }
+  *res0 = block_sum(s, sm.red_d);
+  *nnz = block_sum(cnt, sm.red_i);
+  return emax;
+}
+
+// a3 (residual form): V = residual columns at the sampled positions (exact, FP32)
+// and their Gram matrix in double-float (exact products), written as the Schur
+// complement the pivoted Cholesky starts from.
+template <int BB>
+__device__ void batch_gram(BatchSmem<BB>& sm, int m, int bss, bool first, Pow2 sc, float* __restrict__ V,
+                           int64_t ld) {
+  constexpr int NQ = BB * BB / BT, CW = BB / NQ;
+  const int tid = threadIdx.x, c1 = tid / CW, c2 = tid % CW;
+  dfl acc[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) acc[q] = {0.f, 0.f};
+  for (int r0 = 0; r0 < m; r0 += BROWS) {
+    __syncthreads();
+    for (int idx = tid; idx < BROWS * BB; idx += BT) {
+      const int rr = idx % BROWS, c = idx / BROWS, r = r0 + rr;
+      float v = 0.f;
+      if (r < m && c < bss) {
+        v = sm.src[c][r];
+        if (first) v = sc.apply(v);
+        V[r + (int64_t)c * ld] = v;
+      }
+      sm.u.gram_Vs[rr][c] = v;
+    }
+    __syncthreads();
+    const int rows = min(BROWS, m - r0);
+    if (c1 < bss) {
+      for (int rr = 0; rr < rows; ++rr) {
+        const float x = sm.u.gram_Vs[rr][c1];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) df_acc_prod(acc[q], x, sm.u.gram_Vs[rr][c2 + CW * q]);
+      }
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) sm.u.pan.pc.S[c1][c2 + CW * q] = acc[q];
+  if (tid < BB) {
+    sm.u.pan.pc.ord[tid] = tid;
+    sm.u.pan.pc.alive[tid] = tid < bss;
+  }
+  __syncthreads();
+}
+
+// Q = V(:, ord[:kept]) R11^{-1}, one thread per row, double-float, stored as the
+// FP32 basis in column-major (update) and row-major (projection) copies, zero
+// beyond the kept columns.  Also publishes R11 (slot order) for the R rows.
+template <int BB>
+__device__ void batch_qsolve(BatchSmem<BB>& sm, int m, int kept, const float* __restrict__ V, int64_t ld,
+                             float* __restrict__ Qc, float* __restrict__ Qr) {
+  auto& P = sm.u.pan;
+  const int tid = threadIdx.x;
+  for (int idx = tid; idx < BB * BB; idx += BT) {
+    const int a = idx / BB, c = idx % BB;
+    P.R11s[a][c] = (a < kept && c < kept && c >= a) ? P.pc.R[a][P.pc.ord[c]] : dfl{0.f, 0.f};
+  }
+  if (tid < kept) P.invd[tid] = df_recip(P.pc.R[tid][P.pc.ord[tid]]);
+  __syncthreads();
+  for (int r = tid; r < m; r += BT) {
+    dfl x[BB];
+#pragma unroll
+    for (int s = 0; s < BB; ++s) {
+      x[s] = {0.f, 0.f};
+      if (s < kept) {
+        dfl v = {V[r + (int64_t)P.pc.ord[s] * ld], 0.f};
+#pragma unroll
+        for (int u = 0; u < s; ++u) v = df_fms(v, x[u], P.R11s[u][s]);
+        x[s] = df_mul(v, P.invd[s]);
+      }
+    }
+#pragma unroll
+    for (int s4 = 0; s4 < BB; s4 += 4) {
+      float4 q4;
+      q4.x = __fadd_rn(x[s4].hi, x[s4].lo);
+      q4.y = __fadd_rn(x[s4 + 1].hi, x[s4 + 1].lo);
+      q4.z = __fadd_rn(x[s4 + 2].hi, x[s4 + 2].lo);
+      q4.w = __fadd_rn(x[s4 + 3].hi, x[s4 + 3].lo);
+      reinterpret_cast<float4*>(Qr + (int64_t)r * BB)[s4 / 4] = q4;
+      Qc[r + (int64_t)s4 * ld] = q4.x;
+      Qc[r + (int64_t)(s4 + 1) * ld] = q4.y;
+      Qc[r + (int64_t)(s4 + 2) * ld] = q4.z;
+      Qc[r + (int64_t)(s4 + 3) * ld] = q4.w;
+    }
+  }
+  __syncthreads();
+}
+
+// a6/a7 bookkeeping after the pivots: R(I2, I2) = R11; the rows above the block
+// follow the block swap of the positions (R(:i, K2) = R(:i, K1), R(:i, I2) =
+// R(:i, J)); the residual columns follow it too (A_res(:, K2) = A_res(:, K1)).
+template <int BB>
+__device__ void batch_swaps(BatchSmem<BB>& sm, int i, int kept, int n, float2* __restrict__ R,
+                            float* __restrict__ Ares, int64_t ld, bool first) {
+  auto& P = sm.u.pan;
+  const int tid = threadIdx.x;
+  const int nK = P.pc.nK;
+  for (int idx = tid; idx < kept * kept; idx += BT) {
+    const int a = idx / kept, c = idx % kept;
+    const dfl v = P.R11s[a][c];
+    R[(int64_t)(i + a) * n + i + c] = make_float2(v.hi, v.lo);
+  }
+  for (int row = tid; row < i; row += BT) {
+    float2* Rr = R + (int64_t)row * n;
+    float2 tmp[BB];
+#pragma unroll
+    for (int s = 0; s < BB; ++s)
+      if (s < kept) tmp[s] = Rr[P.pc.J[s]];
+    for (int t = 0; t < nK; ++t) Rr[P.pc.K2[t]] = Rr[P.pc.K1[t]];
+#pragma unroll
+    for (int s = 0; s < BB; ++s)
+      if (s < kept) Rr[i + s] = tmp[s];
+  }
+  if (!first) {
+    const int64_t n4 = ld / 4;
+    for (int t = 0; t < nK; ++t) {
+      const float4* src = reinterpret_cast<const float4*>(Ares + (int64_t)P.pc.K1[t] * ld);
+      float4* dst = reinterpret_cast<float4*>(Ares + (int64_t)P.pc.K2[t] * ld);
+      for (int64_t r4 = tid; r4 < n4; r4 += BT) dst[r4] = src[r4];
+    }
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ void fold_two_sum(float& hi, float& lo, float x) {
+  const float t = hi + x;
+  const float bb = t - hi;
+  lo += (hi - (t - bb)) + (x - bb);
+  hi = t;
+}
+
+// a7/a8 per tile of 64 remaining positions: W = Q^T X (FP32 stage sums of 32-64
+// rows folded into double-float), R(I2, p) = W, then X -= Q W written to A_res
+// with the exact norms of the updated columns into diags.  X is the residual
+// (A_res) or, before the first update, A(:, perm[p]) scaled.
+template <int BB>
+__device__ void batch_project_update(BatchSmem<BB>& sm, int m, int n, int i, int kept, bool first, Pow2 sc,
+                                     const float* __restrict__ A, int64_t lda, const int* __restrict__ perm,
+                                     float* __restrict__ Ares, int64_t ld, const float* __restrict__ Qc,
+                                     const float* __restrict__ Qr, float2* __restrict__ R,
+                                     double* __restrict__ diags) {
+  constexpr int NG = BatchSmem<BB>::NG, GT = BT / NG, GROWS = BROWS / NG;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int g = tid / GT, lt = tid % GT, aq = lt / 16, cq = lt % 16;
+  const int cb = warp * 8;  // update: this warp's 8 columns of the tile
+  for (int p0 = i + kept; p0 < n; p0 += TCOL) {
+    const int ncol = min(TCOL, n - p0);
+    __syncthreads();
+    if (tid < TCOL)
+      sm.src[tid] = tid < ncol ? (first ? A + (int64_t)perm[p0 + tid] * lda : Ares + (int64_t)(p0 + tid) * ld)
+                               : nullptr;
+    float hi[4][4], lo[4][4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) hi[u][v] = lo[u][v] = 0.f;
+    for (int r0 = 0; r0 < m; r0 += BROWS) {
+      __syncthreads();
+      for (int idx = tid; idx < BROWS * TCOL; idx += BT) {
+        const int rr = idx % BROWS, cc = idx / BROWS, r = r0 + rr;
+        float v = 0.f;
+        if (r < m && cc < ncol) {
+          v = sm.src[cc][r];
+          if (first) v = sc.apply(v);
+        }
+        sm.u.p1.Xs[rr][cc] = v;
+      }
+      for (int idx = tid; idx < BROWS * (BB / 4); idx += BT) {
+        const int rr = idx / (BB / 4), j = idx % (BB / 4), r = r0 + rr;
+        const float4 v = r < m ? reinterpret_cast<const float4*>(Qr + (int64_t)r * BB)[j]
+                               : make_float4(0.f, 0.f, 0.f, 0.f);
+        *reinterpret_cast<float4*>(&sm.u.p1.Qs[rr][4 * j]) = v;
+      }
+      __syncthreads();
+      float c[4][4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) c[u][v] = 0.f;
+      const int rb = g * GROWS, re = min(rb + GROWS, m - r0);
+      for (int rr = rb; rr < re; ++rr) {
+        const float4 q4 = *reinterpret_cast<const float4*>(&sm.u.p1.Qs[rr][4 * aq]);
+        const float4 x4 = *reinterpret_cast<const float4*>(&sm.u.p1.Xs[rr][4 * cq]);
+        const float qv[4] = {q4.x, q4.y, q4.z, q4.w};
+        const float xv[4] = {x4.x, x4.y, x4.z, x4.w};
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int v = 0; v < 4; ++v) c[u][v] = fmaf(qv[u], xv[v], c[u][v]);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) fold_two_sum(hi[u][v], lo[u][v], c[u][v]);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) sm.u.red[g][4 * aq + u][4 * cq + v] = {hi[u][v], lo[u][v]};
+    __syncthreads();
+    for (int idx = tid; idx < BB * TCOL; idx += BT) {
+      const int a = idx / TCOL, cc = idx % TCOL;
+      dfl w = sm.u.red[0][a][cc];
+#pragma unroll
+      for (int gg = 1; gg < NG; ++gg) w = df_add(w, sm.u.red[gg][a][cc]);
+      w = df_two_sum(w.hi, w.lo);
+      if (a < kept && cc < ncol) R[(int64_t)(i + a) * n + p0 + cc] = make_float2(w.hi, w.lo);
+      sm.Ws[a][cc] = a < kept ? w.hi : 0.f;
+    }
+    // update of this warp's 8 columns: lane l owns rows r0 + l + 32 u
+    DF nrm[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) nrm[j].hi = nrm[j].lo = 0.f;
+    for (int r0 = 0; r0 < m; r0 += BROWS) {
+      float x[4][8];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int r = r0 + lane + 32 * u, cc = cb + j;
+          float v = 0.f;
+          if (r < m && cc < ncol) {
+            v = sm.src[cc][r];
+            if (first) v = sc.apply(v);
+          }
+          x[u][j] = v;
+        }
+      __syncthreads();
+      for (int idx = tid; idx < kept * (BROWS / 4); idx += BT) {
+        const int a = idx / (BROWS / 4), j = idx % (BROWS / 4), r = r0 + 4 * j;
+        const float* qa = Qc + (int64_t)a * ld;
+        float4 v;
+        if (r + 3 < m) {
+          v = *reinterpret_cast<const float4*>(qa + r);
+        } else {
+          v.x = r < m ? qa[r] : 0.f;
+          v.y = r + 1 < m ? qa[r + 1] : 0.f;
+          v.z = r + 2 < m ? qa[r + 2] : 0.f;
+          v.w = r + 3 < m ? qa[r + 3] : 0.f;
+        }
+        *reinterpret_cast<float4*>(&sm.u.p2_Qs[a][4 * j]) = v;
+      }
+      __syncthreads();
+      float acc[4][8];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[u][j] = 0.f;
+      for (int a = 0; a < kept; ++a) {
+        float q[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) q[u] = sm.u.p2_Qs[a][lane + 32 * u];
+        const float4 w0 = *reinterpret_cast<const float4*>(&sm.Ws[a][cb]);
+        const float4 w1 = *reinterpret_cast<const float4*>(&sm.Ws[a][cb + 4]);
+        const float wv[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int j = 0; j < 8; ++j) acc[u][j] = fmaf(q[u], wv[j], acc[u][j]);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int r = r0 + lane + 32 * u, cc = cb + j;
+          if (r < m && cc < ncol) {
+            const float y = x[u][j] - acc[u][j];
+            Ares[(int64_t)(p0 + cc) * ld + r] = y;
+            df_add_sq(nrm[j], y);
+          }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const double d = warp_sum((double)nrm[j].hi + (double)nrm[j].lo);
+      if (lane == 0 && cb + j < ncol) diags[p0 + cb + j] = d;
+    }
+  }
+  __syncthreads();
+}
+
+// a10: T = R11^{-1} R12 in place in R (double-float back substitution, one
+// thread per column of R12, eight rows per register chunk), then written to
+// the caller's T (k x (n-k), column major, ld = k) in FP64.
+__device__ void batch_tsolve(float2* __restrict__ R, int n, int k, dfl* __restrict__ invd, double* __restrict__ T) {
+  const int tid = threadIdx.x;
+  for (int a = tid; a < k; a += BT) {
+    const float2 d = R[(int64_t)a * n + a];
+    invd[a] = df_recip({d.x, d.y});
+  }
+  __syncthreads();
+  const int nc = n - k;
+  for (int c = tid; c < nc; c += BT) {
+    float2* col = R + k + c;  // element (a, k + c) at col[a * n]
+    for (int a1 = k; a1 > 0; a1 -= 8) {
+      const int a0 = max(0, a1 - 8);
+      dfl acc[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int a = a0 + j;
+        const float2 v = a < a1 ? col[(int64_t)a * n] : make_float2(0.f, 0.f);
+        acc[j] = {v.x, v.y};
+      }
+      for (int u = a1; u < k; ++u) {
+        const float2 xv = col[(int64_t)u * n];
+        const dfl xu = {xv.x, xv.y};
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          if (a0 + j < a1) {
+            const float2 r = R[(int64_t)(a0 + j) * n + u];
+            acc[j] = df_fms(acc[j], {r.x, r.y}, xu);
+          }
+        }
+      }
+#pragma unroll
+      for (int j = 7; j >= 0; --j) {
+        const int a = a0 + j;
+        if (a < a1) {
+          const dfl x = df_mul(acc[j], invd[a]);
+          col[(int64_t)a * n] = make_float2(x.hi, x.lo);
+#pragma unroll
+          for (int jj = 0; jj < j; ++jj) {
+            const float2 r = R[(int64_t)(a0 + jj) * n + a];
+            acc[jj] = df_fms(acc[jj], {r.x, r.y}, x);
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+  const int64_t total = (int64_t)k * nc;
+  for (int64_t idx = tid; idx < total; idx += BT) {
+    const int a = (int)(idx % k);
+    const int64_t c = idx / k;
+    const float2 x = R[(int64_t)a * n + k + c];
+    T[idx] = (double)x.x + (double)x.y;
+  }
+}
+
+template <int BB>
+__device__ void solve_problem(BatchSmem<BB>& sm, const rbrp_batch_problem& pr, int pid, unsigned char* slot,
+                              const BatchArgs& args, rbrp_batch_result* res) {
+  const int tid = threadIdx.x;
+  const int m = pr.m, n = pr.n;
+  const int64_t lda = pr.lda;
+  const float* A = pr.A;
+  int* perm = pr.perm;
+  const int64_t ld = ((int64_t)m + 3) & ~(int64_t)3;
+  float* Ares = reinterpret_cast<float*>(slot);
+  float2* R = reinterpret_cast<float2*>(slot + args.off_R);
+  float* V = reinterpret_cast<float*>(slot + args.off_V);
+  float* Qc = reinterpret_cast<float*>(slot + args.off_Qc);
+  float* Qr = reinterpret_cast<float*>(slot + args.off_Qr);
+  double* diags = reinterpret_cast<double*>(slot + args.off_diag);
+  double* pbuf = reinterpret_cast<double*>(slot + args.off_pbuf);
+  const int mn = min(m, n);
+  const int kcap = args.kmax > 0 ? min(args.kmax, mn) : mn;
+
+  int bad = 0, nnz = 0;
+  double res0 = 0.0;
+  const int emax = batch_norms<BB>(sm, A, lda, m, n, perm, diags, reinterpret_cast<int*>(pbuf), &bad, &res0, &nnz);
+  const Pow2 sc = pow2_scale(emax == INT_MIN ? 0 : -emax);
+  State& st = sm.st;
+  if (tid == 0) {
+    st.i = 0;
+    st.bs_sampled = 0;
+    st.bs = 0;
+    st.nblocks = 0;
+    st.zero_panel = 0;
+    st.nK = 0;
+    st.recomputes = 0;
+    st.attempts = 0;
+    st.draws = 0ull;
+    st.res0 = res0;
+    st.residual = res0;
+    st.nnz_rem = nnz;
+    st.status = bad ? ST_ERR_NUMERIC : 0;
+    st.done = (bad || nnz == 0 || kcap <= 0) ? 1 : 0;
+  }
+  __syncthreads();
+  const int max_attempts = 4 * kcap + 64;
+  const uint64_t seed = args.seed + (uint64_t)pid;
+  for (;;) {
+    if (st.done) break;
+    if (st.attempts >= max_attempts) {
+      __syncthreads();
+      if (tid == 0) {
+        st.status = ST_ERR_NUMERIC;
+        st.done = 1;
+      }
+      __syncthreads();
+      break;
+    }
+    const int i = st.i;
+    const bool first = i == 0;
+    sample_block(&st, diags, perm, n, kcap, args.b, seed, args.sampler, pbuf,
+                 reinterpret_cast<unsigned long long*>(pbuf), sm.js, sm.cols);
+    const int bss = st.bs_sampled;
+    if (tid < bss) {
+      const int p = sm.js[tid];
+      sm.src[tid] = first ? A + (int64_t)perm[p] * lda : Ares + (int64_t)p * ld;
+    }
+    batch_gram<BB>(sm, m, bss, first, sc, V, ld);
+    const int kept = pchol_filter_df<BB>(sm.u.pan.pc, bss, min(bss, m), args.tol_loc);
+    block_swap_parallel<BB>(sm.u.pan.pc, i, kept, sm.js, perm, diags, sm.u.pan.pc.J, sm.u.pan.pc.K1,
+                            sm.u.pan.pc.K2, &st);
+    __syncthreads();
+    double s = 0.0;
+    int c = 0;
+    if (kept > 0) {
+      batch_qsolve<BB>(sm, m, kept, V, ld, Qc, Qr);
+      batch_swaps<BB>(sm, i, kept, n, R, Ares, ld, first);
+      batch_project_update<BB>(sm, m, n, i, kept, first, sc, A, lda, perm, Ares, ld, Qc, Qr, R, diags);
+      for (int p = i + kept + tid; p < n; p += BT) {
+        const double d = diags[p];
+        s += d;
+        c += d > 0.0;
+      }
+    } else {
+      // numerically zero panel: drop the sampled columns' weights and go on
+      if (tid < bss) diags[sm.js[tid]] = 0.0;
+      __syncthreads();
+      for (int p = i + tid; p < n; p += BT) {
+        const double d = diags[p];
+        s += d;
+        c += d > 0.0;
+      }
+    }
+    s = block_sum(s, sm.red_d);
+    c = block_sum(c, sm.red_i);
+    if (tid == 0) {
+      st.attempts += 1;
+      st.residual = s;
+      st.nnz_rem = c;
+      if (kept > 0) {
+        st.i = i + kept;
+        st.nblocks += 1;
+        if ((args.tol > 0.0 && s < st.res0 * args.tol) || c == 0 || st.i >= kcap || !(s == s)) st.done = 1;
+        if (!(s == s)) st.status = ST_ERR_NUMERIC;
+      } else {
+        st.zero_panel = 0;
+        if (c == 0 || bss == 0) st.done = 1;
+      }
+    }
+    __syncthreads();
+  }
+  const int k = st.i;
+  int status = st.status == 0 ? RBRP_OK : RBRP_ERR_NUMERIC;
+  if (args.compute_T && pr.T && status == RBRP_OK && k > 0 && k < n) {
+    if ((int64_t)k * (n - k) > pr.T_cap)
+      status = RBRP_ERR_CAPACITY;
+    else
+      batch_tsolve(R, n, k, reinterpret_cast<dfl*>(V), pr.T);
+  }
+  if (tid == 0) {
+    res->k = k;
+    res->nblocks = st.nblocks;
+    res->status = status;
+    res->attempts = st.attempts;
+    res->res0 = emax == INT_MIN ? 0.0 : ldexp(st.res0, 2 * emax);
+    res->err_est = st.res0 > 0.0 ? st.residual / st.res0 : 0.0;
+    res->draws = st.draws;
+  }
+  __syncthreads();
+}
+
+template <int BB>
+__global__ void __launch_bounds__(BT, 2)
+k_rbrp_batched(const rbrp_batch_problem* __restrict__ probs, const int* __restrict__ order, int nprob,
+               int* __restrict__ queue, BatchArgs args, rbrp_batch_result* __restrict__ results) {
+  extern __shared__ __align__(16) unsigned char batch_smem[];
+  BatchSmem<BB>& sm = *reinterpret_cast<BatchSmem<BB>*>(batch_smem);
+  __shared__ int s_q;
+  unsigned char* slot = args.slots + (size_t)blockIdx.x * (size_t)args.slot_bytes;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_q = atomicAdd(queue, 1);
+    __syncthreads();
+    const int q = s_q;
+    if (q >= nprob) break;
+    const int pid = order[q];
+    solve_problem<BB>(sm, probs[pid], pid, slot, args, results + pid);
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+struct BatchState {
+  int nprob = 0;
+  std::vector<rbrp_batch_problem> probs;
+  rbrp_batch_problem* d_probs = nullptr;
+  int* d_order = nullptr;
+  rbrp_batch_result* d_res = nullptr;
+  int* d_queue = nullptr;
+  size_t cap_probs = 0;
+  unsigned char* slots = nullptr;
+  size_t slots_bytes = 0;
+  BatchArgs args{};
+  int BB = 32, grid = 0, ctas_per_sm = 0, nsm = 0;
+  cudaStream_t cap_stream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  bool planned = false, ran = false;
+  double ms_last = 0.0, ms_autotune = 0.0;
+  std::map<std::vector<int64_t>, std::pair<int, int>> tuned;  // batch signature -> (b, CTAs per SM)
+};
+
+namespace {
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+struct SlotLayout {
+  int64_t off_R, off_V, off_Qc, off_Qr, off_diag, off_pbuf, bytes;
+};
+
+SlotLayout slot_layout(const std::vector<rbrp_batch_problem>& P, int kmax, int BB) {
+  size_t a_res = 0, r = 0, v = 0, qr = 0, dg = 0;
+  for (const auto& q : P) {
+    const size_t ld = ((size_t)q.m + 3) & ~(size_t)3;
+    const int mn = std::min(q.m, q.n);
+    const size_t kc = kmax > 0 ? std::min(kmax, mn) : mn;
+    a_res = std::max(a_res, ld * q.n * sizeof(float));
+    r = std::max(r, kc * q.n * sizeof(float2));
+    v = std::max(v, ld * BB * sizeof(float));
+    qr = std::max(qr, (size_t)q.m * BB * sizeof(float));
+    dg = std::max(dg, (size_t)q.n * sizeof(double));
+  }
+  SlotLayout L;
+  size_t off = align256(a_res);
+  L.off_R = off;
+  off += align256(r);
+  L.off_V = off;
+  off += align256(v);
+  L.off_Qc = off;
+  off += align256(v);
+  L.off_Qr = off;
+  off += align256(qr);
+  L.off_diag = off;
+  off += align256(dg);
+  L.off_pbuf = off;
+  off += align256(2 * dg);
+  L.bytes = off;
+  return L;
+}
+
+template <int BB>
+size_t batch_smem_bytes() {
+  return sizeof(BatchSmem<BB>);
+}
+
+template <int BB>
+cudaError_t set_batch_attr() {
+  return cudaFuncSetAttribute(k_rbrp_batched<BB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)sizeof(BatchSmem<BB>));
+}
+
+int occupancy(int BB) {
+  int nb = 0;
+  if (BB == 16)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_rbrp_batched<16>, BT, sizeof(BatchSmem<16>));
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_rbrp_batched<32>, BT, sizeof(BatchSmem<32>));
+  return nb;
+}
+
+cudaError_t launch(BatchState& B, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(B.d_queue, 0, sizeof(int), s);
+  if (e != cudaSuccess) return e;
+  if (B.BB == 16)
+    k_rbrp_batched<16><<<B.grid, BT, sizeof(BatchSmem<16>), s>>>(B.d_probs, B.d_order, B.nprob, B.d_queue, B.args,
+                                                                 B.d_res);
+  else
+    k_rbrp_batched<32><<<B.grid, BT, sizeof(BatchSmem<32>), s>>>(B.d_probs, B.d_order, B.nprob, B.d_queue, B.args,
+                                                                 B.d_res);
+  return cudaGetLastError();
+}
+
+void drop_graph(BatchState& B) {
+  if (B.exec) cudaGraphExecDestroy(B.exec);
+  if (B.graph) cudaGraphDestroy(B.graph);
+  B.exec = nullptr;
+  B.graph = nullptr;
+}
+
+// Kernel variant and grid for block size b and a CTAs-per-SM request.
+void configure(BatchState& B, int b, int cps, int max_grid) {
+  B.BB = b <= 16 ? 16 : 32;
+  B.args.b = b;
+  const int occ = std::max(1, occupancy(B.BB));
+  B.ctas_per_sm = std::min(cps, occ);
+  B.grid = std::max(1, std::min({B.nprob, B.nsm * B.ctas_per_sm, max_grid}));
+}
+
+}  // namespace
+
+void batch_release(rbrp_handle h) {
+  BatchState* B = h->batch;
+  if (!B) return;
+  drop_graph(*B);
+  if (B->cap_stream) cudaStreamDestroy(B->cap_stream);
+  if (B->ev0) cudaEventDestroy(B->ev0);
+  if (B->ev1) cudaEventDestroy(B->ev1);
+  cudaFree(B->d_probs);
+  cudaFree(B->d_order);
+  cudaFree(B->d_res);
+  cudaFree(B->d_queue);
+  cudaFree(B->slots);
+  delete B;
+  h->batch = nullptr;
+}
+
+}  // namespace rbrp
+
+using namespace rbrp;
+
+namespace {
+
+rbrp_status batch_validate(rbrp_handle h, int nprob, const rbrp_batch_problem* problems, const rbrp_params* p) {
+  if (!h) return RBRP_ERR_INVALID_ARG;
+  if (nprob < 1 || !problems) return set_error(h, RBRP_ERR_INVALID_ARG, "empty batch");
+  if (!p) return set_error(h, RBRP_ERR_INVALID_ARG, "params is NULL");
+  if (p->b > BATCH_MAXB) return set_error(h, RBRP_ERR_INVALID_ARG, "the batched form takes b <= 32 (b <= 0: autotune)");
+  if (!std::isfinite(p->tol) || !std::isfinite(p->tol_loc))
+    return set_error(h, RBRP_ERR_INVALID_ARG, "tol and tol_loc must be finite");
+  if (p->sampler < 0 || p->sampler > 2) return set_error(h, RBRP_ERR_INVALID_ARG, "unknown sampler");
+  for (int q = 0; q < nprob; ++q) {
+    const rbrp_batch_problem& r = problems[q];
+    const std::string at = " (problem " + std::to_string(q) + ")";
+    if (r.m < 1 || r.n < 1) return set_error(h, RBRP_ERR_INVALID_ARG, "m and n must be >= 1" + at);
+    if (r.lda < r.m) return set_error(h, RBRP_ERR_INVALID_ARG, "lda < m" + at);
+    if (!r.A || !r.perm) return set_error(h, RBRP_ERR_INVALID_ARG, "A and perm are required" + at);
+    if (reinterpret_cast<uintptr_t>(r.A) % 4 || reinterpret_cast<uintptr_t>(r.perm) % 4 ||
+        reinterpret_cast<uintptr_t>(r.T) % 8)
+      return set_error(h, RBRP_ERR_INVALID_ARG, "misaligned pointer" + at);
+    if (r.T_cap < 0) return set_error(h, RBRP_ERR_INVALID_ARG, "T_cap < 0" + at);
+    if ((int64_t)r.m * r.n > ((int64_t)1 << 31)) return set_error(h, RBRP_ERR_INVALID_ARG, "problem too large" + at);
+  }
+  return RBRP_OK;
+}
+
+rbrp_status batch_alloc(rbrp_handle h, BatchState& B, size_t slot_bytes, int grid) {
+  if (B.cap_probs < (size_t)B.nprob) {
+    cudaFree(B.d_probs);
+    cudaFree(B.d_order);
+    cudaFree(B.d_res);
+    B.d_probs = nullptr;
+    B.d_order = nullptr;
+    B.d_res = nullptr;
+    B.cap_probs = 0;
+    rbrp_status s = cuda_check(h, cudaMalloc(&B.d_probs, sizeof(rbrp_batch_problem) * B.nprob), "cudaMalloc(batch)");
+    if (s == RBRP_OK) s = cuda_check(h, cudaMalloc(&B.d_order, sizeof(int) * B.nprob), "cudaMalloc(batch order)");
+    if (s == RBRP_OK) s = cuda_check(h, cudaMalloc(&B.d_res, sizeof(rbrp_batch_result) * B.nprob), "cudaMalloc(batch results)");
+    if (s != RBRP_OK) return s;
+    B.cap_probs = B.nprob;
+  }
+  if (!B.d_queue) {
+    rbrp_status s = cuda_check(h, cudaMalloc(&B.d_queue, sizeof(int)), "cudaMalloc(queue)");
+    if (s != RBRP_OK) return s;
+  }
+  const size_t need = slot_bytes * (size_t)grid;
+  if (B.slots_bytes < need) {
+    cudaFree(B.slots);
+    B.slots = nullptr;
+    B.slots_bytes = 0;
+    rbrp_status s = cuda_check(h, cudaMalloc(&B.slots, need), "cudaMalloc(batch workspace)");
+    if (s != RBRP_OK) return s;
+    B.slots_bytes = need;
+  }
+  return RBRP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+rbrp_status rbrp_batch_plan(rbrp_handle h, int nprob, const rbrp_batch_problem* problems, const rbrp_params* p) {
+  rbrp_status s = batch_validate(h, nprob, problems, p);
+  if (s != RBRP_OK) return s;
+  DeviceGuard g(h->device);
+  if (!g.ok) return set_error(h, RBRP_ERR_CUDA, "cudaSetDevice failed");
+  if (!h->batch) {
+    h->batch = new (std::nothrow) BatchState();
+    if (!h->batch) return RBRP_ERR_ALLOC;
+    BatchState& B = *h->batch;
+    if (cudaEventCreate(&B.ev0) != cudaSuccess || cudaEventCreate(&B.ev1) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&B.cap_stream, cudaStreamNonBlocking) != cudaSuccess) {
+      cudaGetLastError();
+      batch_release(h);
+      return set_error(h, RBRP_ERR_CUDA, "batch events / capture stream");
+    }
+    cudaDeviceGetAttribute(&B.nsm, cudaDevAttrMultiProcessorCount, h->device);
+    if (set_batch_attr<16>() != cudaSuccess || set_batch_attr<32>() != cudaSuccess) {
+      cudaGetLastError();
+      batch_release(h);
+      return set_error(h, RBRP_ERR_CUDA, "cudaFuncSetAttribute(batched kernel)");
+    }
+  }
+  BatchState& B = *h->batch;
+  drop_graph(B);
+  B.planned = false;
+  B.ran = false;
+  B.ms_autotune = 0.0;
+  B.nprob = nprob;
+  B.probs.assign(problems, problems + nprob);
+
+  // largest problems first: the queue hands them out before the small ones
+  std::vector<int> order(nprob);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    return (int64_t)B.probs[a].m * B.probs[a].n > (int64_t)B.probs[b].m * B.probs[b].n;
+  });
+
+  B.args.tol = p->tol > 0.0 ? p->tol : 0.0;
+  B.args.seed = p->seed;
+  B.args.sampler = p->sampler;
+  B.args.kmax = p->kmax;
+  B.args.compute_T = p->compute_T;
+  const SlotLayout L = slot_layout(B.probs, p->kmax, BATCH_MAXB);
+  B.args.off_R = L.off_R;
+  B.args.off_V = L.off_V;
+  B.args.off_Qc = L.off_Qc;
+  B.args.off_Qr = L.off_Qr;
+  B.args.off_diag = L.off_diag;
+  B.args.off_pbuf = L.off_pbuf;
+  B.args.slot_bytes = L.bytes;
+
+  // grid bounded by the memory the slots may take (80% of what is free)
+  size_t free_b = 0, total_b = 0;
+  cudaMemGetInfo(&free_b, &total_b);
+  const size_t have = B.slots_bytes + free_b;
+  const int max_grid = std::max<int64_t>(1, std::min<int64_t>((int64_t)(0.8 * (double)have / (double)L.bytes),
+                                                              (int64_t)B.nsm * 4));
+  const int occ_max = std::max(occupancy(16), occupancy(32));
+  const int grid_cap = std::max(1, std::min({nprob, B.nsm * std::max(1, occ_max), max_grid}));
+  s = batch_alloc(h, B, L.bytes, grid_cap);
+  if (s != RBRP_OK) return s;
+  B.args.slots = B.slots;
+  cudaStream_t st = h->stream;
+  s = cuda_check(h, cudaMemcpyAsync(B.d_probs, B.probs.data(), sizeof(rbrp_batch_problem) * nprob,
+                                    cudaMemcpyHostToDevice, st), "copy batch");
+  if (s == RBRP_OK)
+    s = cuda_check(h, cudaMemcpyAsync(B.d_order, order.data(), sizeof(int) * nprob, cudaMemcpyHostToDevice, st),
+                   "copy batch order");
+  if (s == RBRP_OK) s = cuda_check(h, cudaStreamSynchronize(st), "batch upload");
+  if (s != RBRP_OK) return s;
+
+  if (p->b > 0) {
+    B.args.tol_loc = p->tol_loc > 0.0 ? p->tol_loc : 1.0 / (double)p->b;
+    configure(B, p->b, 2, grid_cap);
+  } else {
+    // autotuner: time each (b, CTAs per SM) candidate on this batch, keep the fastest
+    int64_t tol_bits = 0, tol_loc_bits = 0;
+    std::memcpy(&tol_bits, &p->tol, sizeof(double));
+    std::memcpy(&tol_loc_bits, &p->tol_loc, sizeof(double));
+    std::vector<int64_t> sig = {nprob, p->kmax, p->sampler, tol_bits, tol_loc_bits, p->compute_T};
+    int64_t sm = 0, sn = 0, smn = 0;
+    for (const auto& q : B.probs) {
+      sm += q.m;
+      sn += q.n;
+      smn += (int64_t)q.m * q.n;
+    }
+    sig.insert(sig.end(), {sm, sn, smn});
+    auto it = B.tuned.find(sig);
+    if (it != B.tuned.end()) {
+      B.args.tol_loc = p->tol_loc > 0.0 ? p->tol_loc : 1.0 / (double)it->second.first;
+      configure(B, it->second.first, it->second.second, grid_cap);
+    } else {
+      float best = 1e30f, total = 0.f;
+      int best_b = 16, best_c = 2;
+      for (int b : {8, 16, 24, 32}) {
+        for (int cps : {1, 2, 3}) {
+          if (cps > occupancy(b <= 16 ? 16 : 32)) continue;
+          B.args.tol_loc = p->tol_loc > 0.0 ? p->tol_loc : 1.0 / (double)b;
+          configure(B, b, cps, grid_cap);
+          float ms = 0.f;
+          for (int rep = 0; rep < 2; ++rep) {  // the first launch warms caches and clocks
+            cudaEventRecord(B.ev0, st);
+            s = cuda_check(h, launch(B, st), "batched kernel (autotune)");
+            if (s != RBRP_OK) return s;
+            cudaEventRecord(B.ev1, st);
+            s = cuda_check(h, cudaEventSynchronize(B.ev1), "batched kernel (autotune)");
+            if (s != RBRP_OK) return s;
+            cudaEventElapsedTime(&ms, B.ev0, B.ev1);
+            total += ms;
+          }
+          if (ms < best) {
+            best = ms;
+            best_b = b;
+            best_c = cps;
+          }
+        }
+      }
+      B.tuned[sig] = {best_b, best_c};
+      B.ms_autotune = total;
+      B.args.tol_loc = p->tol_loc > 0.0 ? p->tol_loc : 1.0 / (double)best_b;
+      configure(B, best_b, best_c, grid_cap);
+    }
+  }
+  B.planned = true;
+  return RBRP_OK;
+}
+
+rbrp_status rbrp_batch_run(rbrp_handle h) {
+  if (!h) return RBRP_ERR_INVALID_ARG;
+  if (!h->batch || !h->batch->planned) return set_error(h, RBRP_ERR_NOT_COMPUTED, "no batch planned");
+  BatchState& B = *h->batch;
+  DeviceGuard g(h->device);
+  if (!B.exec) {  // capture queue reset + persistent kernel once per plan
+    rbrp_status s = cuda_check(h, cudaStreamBeginCapture(B.cap_stream, cudaStreamCaptureModeThreadLocal),
+                               "cudaStreamBeginCapture");
+    if (s != RBRP_OK) return s;
+    const cudaError_t le = launch(B, B.cap_stream);
+    const cudaError_t ce = cudaStreamEndCapture(B.cap_stream, &B.graph);
+    s = cuda_check(h, le != cudaSuccess ? le : ce, "batch graph capture");
+    if (s != RBRP_OK) {
+      drop_graph(B);
+      return s;
+    }
+    s = cuda_check(h, cudaGraphInstantiate(&B.exec, B.graph, 0), "cudaGraphInstantiate");
+    if (s != RBRP_OK) {
+      drop_graph(B);
+      return s;
+    }
+  }
+  cudaEventRecord(B.ev0, h->stream);
+  rbrp_status s = cuda_check(h, cudaGraphLaunch(B.exec, h->stream), "cudaGraphLaunch(batch)");
+  if (s != RBRP_OK) return s;
+  cudaEventRecord(B.ev1, h->stream);
+  B.ran = true;
+  return RBRP_OK;
+}
+
+rbrp_status rbrp_batch_results(rbrp_handle h, rbrp_batch_result* out, int cap) {
+  if (!h) return RBRP_ERR_INVALID_ARG;
+  if (!h->batch || !h->batch->ran) return set_error(h, RBRP_ERR_NOT_COMPUTED, "no batch run");
+  BatchState& B = *h->batch;
+  DeviceGuard g(h->device);
+  rbrp_status s = cuda_check(h, cudaEventSynchronize(B.ev1), "batched kernel");
+  if (s != RBRP_OK) return s;
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, B.ev0, B.ev1);
+  B.ms_last = ms;
+  if (out) {
+    if (cap < B.nprob) return set_error(h, RBRP_ERR_CAPACITY, "result array smaller than the batch");
+    s = cuda_check(h, cudaMemcpy(out, B.d_res, sizeof(rbrp_batch_result) * B.nprob, cudaMemcpyDeviceToHost),
+                   "copy batch results");
+  }
+  return s;
+}
+
+rbrp_status rbrp_batch_get_info(rbrp_handle h, rbrp_batch_info* info) {
+  if (!h || !info) return RBRP_ERR_INVALID_ARG;
+  if (!h->batch || !h->batch->planned) return set_error(h, RBRP_ERR_NOT_COMPUTED, "no batch planned");
+  const BatchState& B = *h->batch;
+  info->b = B.args.b;
+  info->panel_cols = B.BB;
+  info->ctas = B.grid;
+  info->ctas_per_sm = B.ctas_per_sm;
+  info->ms_last = B.ms_last;
+  info->ms_autotune = B.ms_autotune;
+  info->workspace_bytes = B.slots_bytes;
+  return RBRP_OK;
+}
+
+rbrp_status rbrp_id_batched_f32(rbrp_handle h, int nprob, const rbrp_batch_problem* problems, const rbrp_params* p,
+                                rbrp_batch_result* out) {
+  rbrp_status s = rbrp_batch_plan(h, nprob, problems, p);
+  if (s == RBRP_OK) s = rbrp_batch_run(h);
+  if (s == RBRP_OK) s = rbrp_batch_results(h, out, nprob);
+  return s;
+}
+
+}  // extern "C"

@@ -559,19 +559,6 @@ void prof_collect(rbrp_handle h) {
   h->prof_next = 0;
 }
 
-// RAII guard that makes the handle's device current for one call.
-struct DeviceGuard {
-  int prev = -1;
-  bool ok = false;
-  explicit DeviceGuard(int dev) {
-    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
-    ok = cudaSetDevice(dev) == cudaSuccess;
-  }
-  ~DeviceGuard() {
-    if (prev >= 0) cudaSetDevice(prev);
-  }
-};
-
 static rbrp_status check_device_ptr(rbrp_handle h, const void* p, const char* name) {
   cudaPointerAttributes at;
   if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
@@ -727,6 +714,7 @@ rbrp_status rbrp_destroy(rbrp_handle h) {
     if (h->ev_start) cudaEventDestroy(h->ev_start);
     if (h->ev_loop) cudaEventDestroy(h->ev_loop);
     if (h->ev_end) cudaEventDestroy(h->ev_end);
+    batch_release(h);
   }
   delete h;
   return RBRP_OK;

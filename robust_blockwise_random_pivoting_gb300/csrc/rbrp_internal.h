@@ -11,6 +11,7 @@
 namespace rbrp {
 constexpr int P2_MAX_SPLIT_WS = 8;  // row ranges of the residual update (workspace sizing)
 constexpr int P1_MAX_SPLIT = 8;     // row ranges of the tensor-core projection
+struct BatchState;                  // batched form (rbrp_batched.cu)
 }
 
 struct rbrp_handle_st {
@@ -94,9 +95,28 @@ struct rbrp_handle_st {
   std::vector<cudaEvent_t> prof_events;
   std::vector<PhaseMark> marks;
   int prof_next = 0;
+
+  // batched form (rbrp_batched.cu): plan, workspace slots, captured graph
+  rbrp::BatchState* batch = nullptr;
 };
 
 namespace rbrp {
+
+// RAII guard that makes the handle's device current for one call.
+struct DeviceGuard {
+  int prev = -1;
+  bool ok = false;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    ok = cudaSetDevice(dev) == cudaSuccess;
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+// Frees the batched form's device state of a handle (rbrp_batched.cu).
+void batch_release(rbrp_handle h);
 
 struct Layout {
   int m, n, kmax, ntiles, nproj, cpart_rows;

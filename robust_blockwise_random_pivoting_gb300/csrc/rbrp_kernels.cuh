@@ -13,6 +13,7 @@
 //   k_finish      residual, stop rule, per-block trace
 #pragma once
 #include "rbrp_common.cuh"
+#include "rbrp_sampler.cuh"
 
 namespace rbrp {
 // Internal linkage: this header is compiled into one translation unit per
@@ -119,215 +120,11 @@ __global__ void __launch_bounds__(1024) k_init(State* st, const double* __restri
   }
 }
 
-// ===========================================================================
-// a2: block sampler.  One CTA of 1024 threads over the n - i remaining positions.
-// NP: numpy Generator.choice(replace=False, p=w/sum(w)) rounds (python/RBRP.ipynb
-//     cell 11 line 108): uniforms from the Philox np-compat stream, cdf by a
-//     block scan, searchsorted(side='right') by binary search, first occurrences
-//     kept in draw order.  (The reference CUDA sampler draws WITH replacement
-//     and may return fewer indices, gpu/rbrp.cu:102-146.)
-// ES: keys -log(1-u)/w (u from the exponential-key stream of the original
-//     column), the bs smallest by an 8-bit radix select on the key bits.
-// GREEDY: the bs largest weights (ties: lower position), same radix select.
-// ===========================================================================
-constexpr int SAMPLE_THREADS = 1024;
-
 __global__ void __launch_bounds__(SAMPLE_THREADS)
 k_sample(State* st, const double* __restrict__ diags, const int* __restrict__ perm, int n, int kmax,
          int b, uint64_t seed, int sampler, double* __restrict__ pbuf,
          unsigned long long* __restrict__ kbuf, int* __restrict__ js, int* __restrict__ cols) {
-  __shared__ double shd[32];
-  __shared__ int shi[32];
-  __shared__ unsigned int hist[256];
-  __shared__ int s_rel[MAXB];
-  __shared__ int s_cand[MAXB];
-  __shared__ unsigned long long s_key[MAXB];
-  __shared__ int s_found, s_size, s_digit, s_krank, s_i, s_done;
-  __shared__ unsigned long long s_draws;
-  const int tid = threadIdx.x;
-  if (tid == 0) {
-    s_done = st->done;
-    s_i = st->i;
-    s_draws = st->draws;
-  }
-  __syncthreads();
-  if (s_done) return;
-  const int i = s_i;
-  const int nrem = n - i;
-  const int req = min(min(kmax - i, b), st->nnz_rem);
-  const int chunk = (nrem + SAMPLE_THREADS - 1) / SAMPLE_THREADS;
-  const int lo = min(nrem, tid * chunk), hi = min(nrem, lo + chunk);
-  const double* w = diags + i;
-
-  if (sampler == SAMPLER_NP) {
-    // p = w / sum(w)
-    double part = 0.0;
-    for (int j = lo; j < hi; ++j) part += w[j];
-    const double S = block_sum(part, shd);
-    const double invS = 1.0 / S;  // one FP64 division; per-entry divisions are ~1/64-rate work on GB300
-    int npos = 0;
-    for (int j = lo; j < hi; ++j) {
-      const double pj = w[j] * invS;
-      pbuf[j] = pj;
-      npos += pj > 0.0;
-    }
-    npos = block_sum(npos, shi);
-    if (tid == 0) {
-      s_size = min(req, npos);
-      s_found = 0;
-    }
-    double* cdf = pbuf + n;  // second half of the buffer
-    __syncthreads();
-    // Rejection rounds.  Each round draws at least one new index unless every
-    // remaining positive weight is absorbed by rounding in the cdf; the cap
-    // turns that (pathological) case into a smaller sample instead of a spin.
-    for (int round = 0; s_found < s_size && round < 4096; ++round) {
-      const int found = s_found, need = s_size - s_found;
-      if (tid < found) pbuf[s_rel[tid]] = 0.0;
-      __syncthreads();
-      // inclusive cumsum: chunk-local sequential sums + block scan of chunk totals
-      double run = 0.0;
-      for (int j = lo; j < hi; ++j) {
-        run += pbuf[j];
-        cdf[j] = run;
-      }
-      const double off = block_exclusive_scan(run, shd, (double*)nullptr);
-      for (int j = lo; j < hi; ++j) cdf[j] += off;
-      __syncthreads();
-      // normalise by the last entry, as numpy's cdf /= cdf[-1]: the last entry is exactly 1
-      const double last = cdf[nrem - 1];
-      __syncthreads();
-      const double inv_last = 1.0 / last;
-      for (int j = lo; j < hi; ++j) cdf[j] *= inv_last;
-      __syncthreads();
-      if (tid == 0) cdf[nrem - 1] = 1.0;  // the last entry is exactly 1, as numpy's cdf /= cdf[-1]
-      __syncthreads();
-      if (tid < need) {
-        const double x = np_uniform(seed, s_draws + (unsigned long long)tid);
-        int a = 0, z = nrem;  // first index with cdf > x (searchsorted side='right')
-        while (a < z) {
-          const int mid = (a + z) >> 1;
-          if (cdf[mid] <= x) a = mid + 1; else z = mid;
-        }
-        s_cand[tid] = a < nrem ? a : nrem - 1;
-      }
-      __syncthreads();
-      if (tid == 0) {
-        int f = found;
-        for (int t = 0; t < need; ++t) {
-          const int c = s_cand[t];
-          bool dup = false;
-          for (int u = 0; u < t; ++u) dup |= (s_cand[u] == c);
-          if (!dup) s_rel[f++] = c;
-        }
-        s_found = f;
-        s_draws += (unsigned long long)need;
-      }
-      __syncthreads();
-    }
-    if (tid == 0) s_size = s_found;
-    __syncthreads();
-  } else {
-    // keys (ascending = preferred)
-    int npos = 0;
-    for (int j = lo; j < hi; ++j) {
-      const double wj = w[j];
-      unsigned long long key = ~0ull;
-      if (wj > 0.0) {
-        ++npos;
-        if (sampler == SAMPLER_ES) {
-          const double u = es_uniform(seed, (uint64_t)st->attempts, (uint64_t)perm[i + j]);
-          const double e = -log(1.0 - u) / wj;
-          key = (unsigned long long)__double_as_longlong(e);
-        } else {
-          key = 0x7FF0000000000000ull - (unsigned long long)__double_as_longlong(wj);
-        }
-      }
-      kbuf[j] = key;
-    }
-    npos = block_sum(npos, shi);
-    const int size = min(req, npos);
-    // radix select of the size-th smallest key
-    unsigned long long prefix = 0ull, mask = 0ull;
-    int krank = size;
-    for (int shift = 56; shift >= 0 && size > 0; shift -= 8) {
-      for (int d = tid; d < 256; d += SAMPLE_THREADS) hist[d] = 0u;
-      __syncthreads();
-      for (int j = lo; j < hi; ++j) {
-        const unsigned long long k = kbuf[j];
-        if ((k & mask) == prefix) atomicAdd(&hist[(k >> shift) & 0xFF], 1u);
-      }
-      __syncthreads();
-      if (tid == 0) {
-        int cum = 0, d = 0;
-        for (; d < 255; ++d) {
-          if (cum + (int)hist[d] >= krank) break;
-          cum += (int)hist[d];
-        }
-        s_digit = d;
-        s_krank = krank - cum;
-      }
-      __syncthreads();
-      prefix |= (unsigned long long)s_digit << shift;
-      mask |= 0xFFull << shift;
-      krank = s_krank;
-      __syncthreads();
-    }
-    const unsigned long long kth = prefix;
-    int nlt = 0, neq = 0;
-    for (int j = lo; j < hi; ++j) {
-      const unsigned long long k = kbuf[j];
-      nlt += k < kth;
-      neq += k == kth;
-    }
-    int tot_lt, tot_eq;
-    const int off_lt = block_exclusive_scan(nlt, shi, &tot_lt);
-    const int off_eq = block_exclusive_scan(neq, shi, &tot_eq);
-    const int ties = size - tot_lt;
-    int a = off_lt, e = off_eq;
-    if (size > 0) {
-      for (int j = lo; j < hi; ++j) {
-        const unsigned long long k = kbuf[j];
-        if (k < kth) {
-          s_key[a] = k;
-          s_cand[a] = j;
-          ++a;
-        } else if (k == kth) {
-          if (e < ties) {
-            s_key[tot_lt + e] = k;
-            s_cand[tot_lt + e] = j;
-          }
-          ++e;
-        }
-      }
-    }
-    __syncthreads();
-    if (tid < size) {
-      const unsigned long long k = s_key[tid];
-      const int j = s_cand[tid];
-      int rank = 0;
-      for (int u = 0; u < size; ++u) {
-        const unsigned long long ku = s_key[u];
-        rank += (ku < k) || (ku == k && s_cand[u] < j);
-      }
-      s_rel[rank] = j;
-    }
-    if (tid == 0) {
-      s_size = size;
-      s_found = size;
-    }
-    __syncthreads();
-  }
-  const int size = s_size;
-  if (tid < size) {
-    const int p = i + s_rel[tid];
-    js[tid] = p;
-    cols[tid] = perm[p];
-  }
-  if (tid == 0) {
-    st->bs_sampled = size;
-    st->draws = s_draws;
-  }
+  sample_block(st, diags, perm, n, kmax, b, seed, sampler, pbuf, kbuf, js, cols);
 }
 
 // ===========================================================================

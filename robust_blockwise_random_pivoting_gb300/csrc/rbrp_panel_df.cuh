@@ -15,80 +15,11 @@
 // swap order, so the argmax still picks the first maximal slot.
 #pragma once
 #include "rbrp_common.cuh"
+#include "rbrp_df.cuh"
+#include "rbrp_pchol_df.cuh"
 
 namespace rbrp {
 namespace {
-
-struct dfl {
-  float hi, lo;
-};
-
-__device__ __forceinline__ dfl df_of(double x) {
-  const float h = (float)x;
-  return {h, (float)(x - (double)h)};
-}
-__device__ __forceinline__ double df_dbl(dfl a) { return (double)a.hi + (double)a.lo; }
-__device__ __forceinline__ dfl df_two_sum(float a, float b) {
-  const float s = a + b;
-  const float bb = s - a;
-  return {s, (a - (s - bb)) + (b - bb)};
-}
-__device__ __forceinline__ dfl df_fast(float a, float b) {
-  const float s = a + b;
-  return {s, b - (s - a)};
-}
-__device__ __forceinline__ dfl df_add(dfl a, dfl b) {
-  dfl s = df_two_sum(a.hi, b.hi);
-  s.lo += a.lo + b.lo;
-  return df_fast(s.hi, s.lo);
-}
-__device__ __forceinline__ dfl df_neg(dfl a) { return {-a.hi, -a.lo}; }
-__device__ __forceinline__ dfl df_mul(dfl a, dfl b) {
-  const float p = a.hi * b.hi;
-  float e = fmaf(a.hi, b.hi, -p);
-  e = fmaf(a.hi, b.lo, e);
-  e = fmaf(a.lo, b.hi, e);
-  return df_fast(p, e);
-}
-// s - a * b (one error-free product, one TwoSum)
-__device__ __forceinline__ dfl df_fms(dfl s, dfl a, dfl b) {
-  const float p = a.hi * b.hi;
-  float e = fmaf(a.hi, b.hi, -p);
-  e = fmaf(a.hi, b.lo, e);
-  e = fmaf(a.lo, b.hi, e);
-  const dfl t = df_two_sum(s.hi, -p);
-  return df_fast(t.hi, t.lo + (s.lo - e));
-}
-// acc + a * b
-__device__ __forceinline__ dfl df_fma2(dfl acc, dfl a, dfl b) {
-  const float p = a.hi * b.hi;
-  float e = fmaf(a.hi, b.hi, -p);
-  e = fmaf(a.hi, b.lo, e);
-  e = fmaf(a.lo, b.hi, e);
-  const dfl t = df_two_sum(acc.hi, p);
-  return df_fast(t.hi, t.lo + (acc.lo + e));
-}
-__device__ __forceinline__ bool df_gt(dfl a, dfl b) { return a.hi > b.hi || (a.hi == b.hi && a.lo > b.lo); }
-__device__ __forceinline__ bool df_eq(dfl a, dfl b) { return a.hi == b.hi && a.lo == b.lo; }
-__device__ __forceinline__ dfl df_recip(dfl b) {
-  const float q = 1.0f / b.hi;
-  const dfl r = df_add({1.0f, 0.0f}, df_neg(df_mul({q, 0.0f}, b)));  // 1 - q b
-  return df_fast(q, q * r.hi);
-}
-__device__ __forceinline__ dfl df_sqrt(dfl a) {
-  if (!(a.hi > 0.0f)) return {0.0f, 0.0f};
-  const float s = sqrtf(a.hi);
-  const dfl e = df_add(a, df_neg(df_mul({s, 0.0f}, {s, 0.0f})));  // a - s^2
-  return df_fast(s, e.hi / (2.0f * s));
-}
-// exact product of two floats, accumulated
-__device__ __forceinline__ void df_acc_prod(dfl& acc, float x, float y) {
-  const float p = x * y;
-  const float e = fmaf(x, y, -p);
-  dfl s = df_two_sum(acc.hi, p);
-  s.lo += acc.lo + e;
-  acc = df_fast(s.hi, s.lo);
-}
 
 constexpr int DF_ROWS = 128;  // panel rows per CTA of the Gram kernel
 constexpr int DF_TROWS = 64;  // panel rows per CTA of the row-solve kernels (one thread per row)
@@ -132,73 +63,7 @@ k_gram_df(const float* __restrict__ Ares, int64_t ld, const int* __restrict__ js
   }
 }
 
-struct PcholDfSmem {
-  dfl S[MAXB][MAXB + 1];   // Schur complement, indexed by panel column
-  dfl R[MAXB][MAXB + 1];   // R[t][j]: row t of the factor, by panel column j
-  int ord[MAXB];           // slot -> panel column
-  int alive[MAXB];
-  int J[MAXB], K1[MAXB], K2[MAXB], inblk[MAXB], Tperm[MAXB];
-  double Tdiag[MAXB];
-  int stop, piv, nK;
-  dfl inv;
-};
-
-// Block swap of perm and diags (matlab/RBRP.m:81-99), in parallel: K1 = block
-// positions not kept (ascending), K2 = kept positions outside the block (pivot
-// order), compacted with warp ballots.  All threads call it after `kept` is known.
-__device__ void block_swap_parallel(PcholDfSmem& sm, int i, int kept, const int* __restrict__ js,
-                                    int* __restrict__ perm, double* __restrict__ diags, int* __restrict__ Jg,
-                                    int* __restrict__ K1g, int* __restrict__ K2g, State* st) {
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  if (tid < MAXB) sm.inblk[tid] = 0;
-  __syncthreads();
-  if (tid < kept) {
-    const int p = js[sm.ord[tid]];
-    sm.J[tid] = p;
-    Jg[tid] = p;
-    if (p >= i && p < i + kept) sm.inblk[p - i] = 1;
-    sm.Tperm[tid] = perm[p];
-  }
-  __syncthreads();
-  if (wid < 2) {
-    // warp 0: K1 (block positions not kept), warp 1: K2 (kept positions outside the block)
-    int count = 0;
-    for (int base = 0; base < kept; base += 32) {
-      const int t = base + lane;
-      bool flag = false;
-      int val = 0;
-      if (t < kept) {
-        if (wid == 0) { flag = !sm.inblk[t]; val = i + t; }
-        else { const int p = sm.J[t]; flag = p < i || p >= i + kept; val = p; }
-      }
-      const unsigned bal = __ballot_sync(0xffffffffu, flag);
-      if (flag) {
-        const int slot = count + __popc(bal & ((1u << lane) - 1u));
-        if (wid == 0) sm.K1[slot] = val; else sm.K2[slot] = val;
-      }
-      count += __popc(bal);
-    }
-    if (wid == 1 && lane == 0) sm.nK = count;
-  }
-  __syncthreads();
-  const int nK = sm.nK;
-  if (tid < nK) {  // perm(K2) = perm(K1), diags(K2) = diags(K1): K1 inside the block, K2 outside
-    const int a = sm.K1[tid], b = sm.K2[tid];
-    const int pa = perm[a];
-    const double da = diags[a];
-    perm[b] = pa;
-    diags[b] = da;
-    K1g[tid] = a;
-    K2g[tid] = b;
-  }
-  __syncthreads();
-  if (tid < kept) perm[i + tid] = sm.Tperm[tid];
-  if (tid == 0) {
-    st->bs = kept;
-    st->nK = nK;
-    st->zero_panel = kept == 0;
-  }
-}
+using PcholDfSmem = PcholDfSmemT<MAXB>;
 
 // Pivoted Cholesky of the panel Gram matrix with the robust filter (same rule as
 // pivoted_chol_filter), 256 threads, no data movement for the swaps.  Publishes
@@ -209,10 +74,9 @@ k_pchol_df(const double* __restrict__ G, int m, State* st, double tol_loc, const
            int* __restrict__ Jg, int* __restrict__ K1g, int* __restrict__ K2g) {
   extern __shared__ __align__(16) unsigned char dyn_smem[];
   PcholDfSmem& sm = *reinterpret_cast<PcholDfSmem*>(dyn_smem);
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int tid = threadIdx.x;
   const int nb = st->bs_sampled, i = st->i;
   const int rows = min(nb, m);
-  const int ty = tid >> 4, tx = tid & 15;  // 4 x 4 Schur entries per thread: rows ty*4+u, columns tx*4+v
   for (int idx = tid; idx < MAXB * MAXB; idx += 256) {
     const int a = idx / MAXB, c = idx % MAXB;
     sm.S[a][c] = (a < nb && c < nb) ? df_of(G[a * MAXB + c]) : dfl{0.f, 0.f};
@@ -222,71 +86,7 @@ k_pchol_df(const double* __restrict__ G, int m, State* st, double tol_loc, const
     sm.alive[tid] = tid < nb;
   }
   __syncthreads();
-  double total = 0.0;  // trace(G), used by warp 0
-  if (wid == 0) {
-    dfl t = {0.f, 0.f};
-    for (int s2 = 0; s2 < nb; ++s2) t = df_add(t, sm.S[s2][s2]);
-    total = df_dbl(t);
-  }
-  int kept = rows;
-  for (int t = 0; t < rows; ++t) {
-    if (wid == 0) {
-      // remaining trace and the first maximal slot (LAPACK dgeqp3 order)
-      dfl rem = {0.f, 0.f}, best = {-1.f, 0.f};
-      int bs = nb;
-      for (int s2 = t + lane; s2 < nb; s2 += 32) {
-        const dfl d = sm.S[sm.ord[s2]][sm.ord[s2]];
-        rem = df_add(rem, d);
-        if (df_gt(d, best)) { best = d; bs = s2; }
-      }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const dfl orem = {__shfl_down_sync(0xffffffffu, rem.hi, o), __shfl_down_sync(0xffffffffu, rem.lo, o)};
-        rem = df_add(rem, orem);
-        const dfl ob = {__shfl_down_sync(0xffffffffu, best.hi, o), __shfl_down_sync(0xffffffffu, best.lo, o)};
-        const int oi = __shfl_down_sync(0xffffffffu, bs, o);
-        if (df_gt(ob, best) || (df_eq(ob, best) && oi < bs)) { best = ob; bs = oi; }
-      }
-      if (lane == 0) {
-        const bool stop = !(total > 0.0) || (df_dbl(rem) / total < tol_loc) || !(best.hi > 0.f);
-        sm.stop = stop;
-        if (!stop) {
-          const int o = sm.ord[t];
-          sm.ord[t] = sm.ord[bs];
-          sm.ord[bs] = o;
-          const int pv = sm.ord[t];
-          sm.alive[pv] = 0;
-          const dfl r = df_sqrt(sm.S[pv][pv]);
-          sm.R[t][pv] = r;
-          sm.inv = df_recip(r);
-          sm.piv = pv;
-        }
-      }
-    }
-    __syncthreads();
-    if (sm.stop) { kept = t; break; }
-    const int pv = sm.piv;
-    const dfl inv = sm.inv;
-    if (tid < nb && sm.alive[tid]) sm.R[t][tid] = df_mul(sm.S[pv][tid], inv);
-    __syncthreads();
-    dfl ru[4], rv[4];
-    bool au[4], av[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int j = ty * 4 + u;
-      au[u] = j < nb && sm.alive[j];
-      ru[u] = sm.R[t][j];
-      const int c = tx * 4 + u;
-      av[u] = c < nb && sm.alive[c];
-      rv[u] = sm.R[t][c];
-    }
-#pragma unroll
-    for (int u = 0; u < 4; ++u)
-#pragma unroll
-      for (int v = 0; v < 4; ++v)
-        if (au[u] && av[v]) sm.S[ty * 4 + u][tx * 4 + v] = df_fms(sm.S[ty * 4 + u][tx * 4 + v], ru[u], rv[v]);
-    __syncthreads();
-  }
+  const int kept = pchol_filter_df<MAXB>(sm, nb, rows, tol_loc);
   // R11 in slot order: R11[a][c] = R[a][ord[c]] for c >= a
   for (int idx = tid; idx < MAXB * MAXB; idx += 256) {
     const int a = idx / MAXB, c = idx % MAXB;

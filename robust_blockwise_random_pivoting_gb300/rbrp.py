@@ -12,6 +12,9 @@ Mirrors the reference's entry points:
   ortho=1, tol_loc)`` (``python/RBRP.ipynb`` cell 11 lines 76-173): rows of
   ``X`` are the items (``X = A.T``), ``tol`` bounds the squared residual.
 * :class:`Handle` - the reusable handle (workspace, stream, last result).
+* :class:`Batch` / :func:`batched_column_id` - thousands of independent FP32
+  column IDs of uneven shape in one persistent launch (no reference
+  counterpart: the reference solves one matrix per ``RBRP`` call).
 
 Device memory and streams come from PyTorch; all arithmetic runs in the
 sm_103a kernels of ``librbrp_gb300.so``.
@@ -235,6 +238,112 @@ class Handle:
             k, nc = r.k, n - r.k
             T = T_out[: kcap * nc].reshape(nc, kcap).T[:k] if nc > 0 else T_out[:0]
         return r.k, perm_out, T, r
+
+
+@dataclass
+class BatchIDResult:
+    """Per-problem outputs of a batched run (arrays indexed by problem)."""
+    k: np.ndarray
+    nblocks: np.ndarray
+    status: np.ndarray
+    attempts: np.ndarray
+    res0: np.ndarray
+    err_est: np.ndarray
+    draws: np.ndarray
+    perms: list          # (n_q,) int32 CUDA views: S = perm[:k], rd = perm[k:]
+    Ts: list             # (k_q, n_q - k_q) FP64 column-major CUDA views, or None
+    ms: float            # device time of the run (CUDA events), ms
+
+
+class Batch:
+    """A planned batch of independent column IDs run in one persistent launch.
+
+    ``As`` is a sequence of FP32 CUDA matrices of any shapes.  ``b <= 0`` lets
+    the library's autotuner pick the block size on this batch.  ``tol`` bounds
+    the squared relative residual of every problem; problem q uses the Philox
+    key ``seed + q``.  T of problem q gets room for ``min(kcap_q, t_rank_cap)``
+    rows (kcap_q = min(m_q, n_q, kmax)); a larger rank reports status 6.
+    """
+
+    def __init__(self, handle, As, b=0, tol=1e-8, kmax=None, seed=0, sampler="np", tol_loc=None,
+                 compute_T=True, t_rank_cap=None):
+        self.h = handle
+        lib = handle.lib
+        self.As = [_colmajor(A) for A in As]
+        if not self.As:
+            raise ValueError("empty batch")
+        dev = self.As[0].device
+        for A in self.As:
+            if not A.is_cuda or A.dtype != torch.float32 or A.device != dev:
+                raise TypeError("the batched form takes FP32 CUDA matrices on one device")
+        shapes = [tuple(A.shape) for A in self.As]
+        self.shapes = shapes
+        ns = np.array([n for _, n in shapes], np.int64)
+        self.perm_off = np.concatenate([[0], np.cumsum(ns)])
+        self.perm_buf = torch.empty(int(self.perm_off[-1]), dtype=torch.int32, device=dev)
+        kc = [min(m, n, kmax or min(m, n)) for m, n in shapes]
+        if t_rank_cap is not None:
+            kc = [min(k, int(t_rank_cap)) for k in kc]
+        tcap = np.array([k * n for k, (_, n) in zip(kc, shapes)], np.int64) if compute_T else np.zeros(len(shapes),
+                                                                                                       np.int64)
+        self.t_off = np.concatenate([[0], np.cumsum(tcap)])
+        self.T_buf = torch.empty(max(1, int(self.t_off[-1])), dtype=torch.float64, device=dev)
+        n_prob = len(self.As)
+        self.probs = (_lib.BatchProblem * n_prob)()
+        for q, A in enumerate(self.As):
+            pr = self.probs[q]
+            pr.m, pr.n = shapes[q]
+            pr.lda = _ld(A)
+            pr.A = A.data_ptr()
+            pr.perm = self.perm_buf.data_ptr() + 4 * int(self.perm_off[q])
+            pr.T = (self.T_buf.data_ptr() + 8 * int(self.t_off[q])) if compute_T and tcap[q] > 0 else None
+            pr.T_cap = int(tcap[q])
+        self.compute_T = compute_T
+        p = handle._params(b if b and b > 0 else 0, tol, kmax, seed, sampler, tol_loc, compute_T, "f32_mixed", True)
+        handle._bind_stream(torch.cuda.current_stream(dev))
+        check(lib.rbrp_batch_plan(handle.h, n_prob, self.probs, ctypes.byref(p)), handle.h)
+        self.n_prob = n_prob
+
+    def info(self):
+        inf = _lib.BatchInfo()
+        check(self.h.lib.rbrp_batch_get_info(self.h.h, ctypes.byref(inf)), self.h.h)
+        return dict(b=inf.b, panel_cols=inf.panel_cols, ctas=inf.ctas, ctas_per_sm=inf.ctas_per_sm,
+                    ms_last=inf.ms_last, ms_autotune=inf.ms_autotune, workspace_bytes=inf.workspace_bytes)
+
+    def run(self, stream=None):
+        """Enqueue the batch (one CUDA graph launch) on the current torch stream."""
+        self.h._bind_stream(torch.cuda.current_stream(self.As[0].device) if stream is None else stream)
+        check(self.h.lib.rbrp_batch_run(self.h.h), self.h.h)
+
+    def results(self):
+        """Wait for the last run and return a :class:`BatchIDResult`."""
+        out = (_lib.BatchResult * self.n_prob)()
+        check(self.h.lib.rbrp_batch_results(self.h.h, out, self.n_prob), self.h.h)
+        f = lambda name, dt: np.array([getattr(r, name) for r in out], dt)
+        k = f("k", np.int64)
+        status = f("status", np.int64)
+        perms, Ts = [], []
+        for q, (m, n) in enumerate(self.shapes):
+            perms.append(self.perm_buf[int(self.perm_off[q]): int(self.perm_off[q + 1])])
+            kq = int(k[q])
+            if self.compute_T and status[q] == 0:
+                Ts.append(self.T_buf[int(self.t_off[q]): int(self.t_off[q]) + kq * (n - kq)].view(n - kq, kq).t()
+                          if 0 < kq < n else torch.empty((kq, n - kq), dtype=torch.float64, device=self.T_buf.device))
+            else:
+                Ts.append(None)
+        return BatchIDResult(k=k, nblocks=f("nblocks", np.int64), status=status, attempts=f("attempts", np.int64),
+                             res0=f("res0", np.float64), err_est=f("err_est", np.float64),
+                             draws=f("draws", np.uint64), perms=perms, Ts=Ts, ms=self.info()["ms_last"])
+
+
+def batched_column_id(As, b=0, tol=1e-8, kmax=None, seed=0, sampler="np", tol_loc=None, compute_T=True,
+                      t_rank_cap=None, handle=None):
+    """Column IDs of many FP32 CUDA matrices in one persistent launch (plan, run, results)."""
+    h = handle or Handle(As[0].device.index)
+    bt = Batch(h, As, b=b, tol=tol, kmax=kmax, seed=seed, sampler=sampler, tol_loc=tol_loc, compute_T=compute_T,
+               t_rank_cap=t_rank_cap)
+    bt.run()
+    return bt.results()
 
 
 _rt = None

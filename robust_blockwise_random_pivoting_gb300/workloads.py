@@ -94,18 +94,38 @@ def kernel_block_shapes(nblocks=4096, lo=64, hi=2048, seed=0):
     return np.clip(np.round(np.exp(lm)).astype(np.int64), lo, hi)
 
 
-def kernel_block(m, n, index, lengthscale=0.5, seed=0):
-    """Gaussian-kernel block between two clusters of 3-D points in unit cubes.
-
-    Cube centres are 2 to 8 apart; ``A_ij = exp(-|x_i - y_j|^2 / (2 l^2))``.
-    """
+def kernel_block_points(m, n, index, seed=0):
+    """The two point clusters of kernel block ``index``: x (m x 3) in the unit
+    cube and y (n x 3) in a unit cube whose centre is 2 to 8 away."""
     rng = _gen(seed, 4 + int(index))
     x = rng.random((m, 3))
     direction = rng.standard_normal(3)
     direction /= np.linalg.norm(direction)
     y = rng.random((n, 3)) + rng.uniform(2.0, 8.0) * direction
+    return x, y
+
+
+def kernel_block(m, n, index, lengthscale=0.5, seed=0):
+    """Gaussian-kernel block between two clusters of 3-D points in unit cubes.
+
+    Cube centres are 2 to 8 apart; ``A_ij = exp(-|x_i - y_j|^2 / (2 l^2))``.
+    """
+    x, y = kernel_block_points(m, n, index, seed)
     d2 = ((x[:, None, :] - y[None, :, :]) ** 2).sum(-1)
     return np.asfortranarray(np.exp(-d2 / (2.0 * lengthscale ** 2)))
+
+
+def kernel_block_scaled(m, n, index, lengthscale=0.5, seed=0, dtype=np.float32):
+    """``kernel_block / max(kernel_block)``, evaluated without underflow.
+
+    The entries of far-apart blocks lie far below FP32's range (down to
+    ~1e-80), so FP32 storage keeps each block scaled by its largest entry:
+    ``exp(-(d2 - min d2) / (2 l^2))``.  A column ID is invariant under a
+    uniform scale (same S, same T, same relative error).
+    """
+    x, y = kernel_block_points(m, n, index, seed)
+    d2 = ((x[:, None, :] - y[None, :, :]) ** 2).sum(-1)
+    return np.asfortranarray(np.exp(-(d2 - d2.min()) / (2.0 * lengthscale ** 2)).astype(dtype))
 
 
 def gaussian_kernel_points(npts=8192, dim=8, seed=0):
@@ -130,3 +150,24 @@ def zero_prefixed(B, z):
     """
     m = B.shape[0]
     return np.asfortranarray(np.concatenate([np.zeros((m, z)), B], axis=1))
+
+
+def kernel_blocks_device(nblocks=4096, lo=64, hi=2048, lengthscale=0.5, seed=0, device="cuda", fp64=False):
+    """The batched workload on the device: ``nblocks`` scaled kernel blocks.
+
+    Shapes from :func:`kernel_block_shapes`, points from
+    :func:`kernel_block_points` (host, small), entries evaluated on the device
+    as in :func:`kernel_block_scaled`.  Returns a list of column-major CUDA
+    tensors (FP32, or FP64 with ``fp64=True``).
+    """
+    import torch
+    out = []
+    for q, (m, n) in enumerate(kernel_block_shapes(nblocks, lo, hi, seed)):
+        x, y = kernel_block_points(int(m), int(n), q, seed)
+        xd = torch.from_numpy(x).to(device)
+        yd = torch.from_numpy(y).to(device)
+        d2 = ((xd[:, None, :] - yd[None, :, :]) ** 2).sum(-1)
+        A = torch.exp(-(d2 - d2.min()) / (2.0 * lengthscale ** 2))
+        A = A if fp64 else A.to(torch.float32)
+        out.append(A.t().contiguous().t())
+    return out

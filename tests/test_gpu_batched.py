@@ -1,0 +1,200 @@
+"""GPU: the batched persistent form (rbrp_batch_* through the C ABI).
+
+Every problem of a batch runs the FP32 residual form inside one CTA, so the
+checks are those of the one-matrix FP32 form against the FP64 oracle on the
+same FP32-rounded matrix: the squared relative ID error (recomputed here in
+FP64 from the returned perm and T) stays within 1.05x of max(oracle error,
+tol); the rank stays within one block of the oracle's; the first block (whose
+sampling weights are the exact initial column norms in both) selects the same
+columns.  Runs are deterministic, so a replay of the captured graph must
+reproduce every output bit for bit, and scaling a matrix by a power of two
+must change nothing but res0.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from oracle import id_error, interp_sid, rbrp_column_id  # noqa: E402
+from robust_blockwise_random_pivoting_gb300 import workloads as W  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def handle(rbrp_lib):
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from robust_blockwise_random_pivoting_gb300.rbrp import Handle
+    h = Handle(0)
+    yield h
+    h.close()
+
+
+def dev32(A):
+    return torch.from_numpy(np.asfortranarray(A, dtype=np.float32)).cuda().t().contiguous().t()
+
+
+def shapes(nprob, lo, hi, seed):
+    rng = np.random.default_rng(seed)
+    return np.exp(rng.uniform(np.log(lo), np.log(hi), (nprob, 2))).astype(int)
+
+
+def run_batch(handle, mats, **kw):
+    from robust_blockwise_random_pivoting_gb300.rbrp import Batch
+    bt = Batch(handle, [dev32(A) for A in mats], **kw)
+    bt.run()
+    return bt, bt.results()
+
+
+def check_problem(A64, perm, T, k, err_est, tol, b, seed, kslack=None):
+    o = rbrp_column_id(A64, b, tol=tol, seed=seed)
+    e_ref = id_error(A64, o["perm"], interp_sid(A64, o["perm"], o["k"]))
+    n = A64.shape[1]
+    assert sorted(perm.tolist()) == list(range(n))
+    e = id_error(A64, perm, T) if 0 < k < n else (0.0 if k == n else 1.0)
+    assert e <= 1.05 * max(e_ref, tol), (e, e_ref, k, o["k"])
+    assert err_est <= tol or k == min(A64.shape), (err_est, k)
+    assert abs(k - o["k"]) <= (kslack or b), (k, o["k"])
+    k1 = int(o["ranks"][0]) if len(o["ranks"]) else 0
+    assert np.array_equal(perm[:k1], o["perm"][:k1]), (perm[:k1], o["perm"][:k1])
+    return o
+
+
+@pytest.mark.parametrize("b", [8, 16, 32])
+def test_batched_kernel_blocks_match_fp64_oracle(handle, b):
+    tol, seed = 1e-8, 5
+    sh = shapes(14, 48, 320, seed=b)
+    mats = [W.kernel_block_scaled(int(m), int(n), q) for q, (m, n) in enumerate(sh)]
+    bt, res = run_batch(handle, mats, b=b, tol=tol, seed=seed)
+    assert (res.status == 0).all(), res.status
+    for q, A in enumerate(mats):
+        k = int(res.k[q])
+        T = res.Ts[q].cpu().numpy()
+        assert T.shape == (k, A.shape[1] - k)
+        check_problem(A.astype(np.float64), res.perms[q].cpu().numpy(), T, k, res.err_est[q], tol, b, seed + q)
+    assert bt.info()["b"] == b
+
+
+def test_batched_gaussian_exp_and_snn(handle):
+    """Slower-decaying spectra: several full blocks per problem, ranks up to ~100."""
+    tol, b, seed = 1e-10, 32, 3
+    mats = [W.gaussian_exp(300, 260, decay=12.0, seed=1), W.snn(400, 350, r=200, r1=20, density=0.05, seed=4),
+            W.gaussian_exp(97, 411, decay=30.0, seed=2), W.gaussian_exp(513, 129, decay=6.0, seed=8)]
+    mats = [A.astype(np.float32) for A in mats]
+    _, res = run_batch(handle, mats, b=b, tol=tol, seed=seed)
+    assert (res.status == 0).all()
+    assert res.k.max() > 60
+    for q, A in enumerate(mats):
+        check_problem(A.astype(np.float64), res.perms[q].cpu().numpy(), res.Ts[q].cpu().numpy(), int(res.k[q]),
+                      res.err_est[q], tol, b, seed + q)
+
+
+def test_batched_uneven_shapes_to_2048(handle):
+    """The workload's shape range (log-uniform 64..2048), errors checked in FP64 on the host."""
+    tol, b = 1e-8, 16
+    sh = shapes(48, 64, 2048, seed=11)
+    mats = [W.kernel_block_scaled(int(m), int(n), 1000 + q) for q, (m, n) in enumerate(sh)]
+    _, res = run_batch(handle, mats, b=b, tol=tol, seed=0)
+    assert (res.status == 0).all()
+    for q, A in enumerate(mats):
+        A64 = A.astype(np.float64)
+        k, perm = int(res.k[q]), res.perms[q].cpu().numpy()
+        assert sorted(perm.tolist()) == list(range(A.shape[1]))
+        assert res.err_est[q] <= tol
+        e = id_error(A64, perm, res.Ts[q].cpu().numpy())
+        assert e <= 1.05 * tol, (q, A.shape, k, e)
+        np.testing.assert_allclose(res.res0[q], (A64 ** 2).sum(), rtol=1e-6)
+
+
+def test_batched_replay_is_bit_exact(handle):
+    sh = shapes(40, 32, 400, seed=21)
+    mats = [W.kernel_block_scaled(int(m), int(n), 500 + q) for q, (m, n) in enumerate(sh)]
+    bt, r1 = run_batch(handle, mats, b=16, tol=1e-8, seed=9)
+    p1 = [p.clone() for p in r1.perms]
+    T1 = [t.clone() for t in r1.Ts]
+    for _ in range(2):
+        bt.run()
+        r2 = bt.results()
+        assert np.array_equal(r1.k, r2.k) and np.array_equal(r1.err_est, r2.err_est)
+        for q in range(len(mats)):
+            assert torch.equal(p1[q], r2.perms[q]) and torch.equal(T1[q], r2.Ts[q])
+
+
+def test_batched_power_of_two_scale_invariance(handle):
+    """Blocks scaled by 2^-100 or 2^60 give the same skeleton and T bit for bit."""
+    A = W.gaussian_exp(200, 180, decay=10.0, seed=6).astype(np.float32)
+    A /= np.abs(A).max()
+    outs = []
+    for s in (0, -100, 60):
+        As = np.ldexp(A, s).astype(np.float32)
+        assert np.array_equal(np.ldexp(As, -s), A)
+        _, r = run_batch(handle, [As], b=16, tol=1e-10, seed=2)
+        outs.append((r.perms[0].cpu().numpy(), r.Ts[0].cpu().numpy(), r.err_est[0], r.res0[0]))
+    for s, (p, T, e, r0) in zip((0, -100, 60), outs):
+        assert np.array_equal(p, outs[0][0]) and np.array_equal(T, outs[0][1]) and e == outs[0][2]
+        np.testing.assert_allclose(r0, outs[0][3] * 2.0 ** (2 * s), rtol=1e-12)
+
+
+def test_batched_edge_cases(handle):
+    rng = np.random.default_rng(3)
+    low = (rng.standard_normal((90, 3)) @ rng.standard_normal((3, 70))).astype(np.float32)
+    nan = np.ones((20, 10), np.float32)
+    nan[4, 7] = np.nan
+    mats = [np.zeros((30, 20), np.float32), np.ones((1, 5), np.float32), np.arange(1, 8, dtype=np.float32)[:, None],
+            np.ones((1, 1), np.float32), low, nan, rng.standard_normal((40, 12)).astype(np.float32)]
+    _, res = run_batch(handle, mats, b=8, tol=1e-12, seed=0)
+    assert res.k[0] == 0 and res.status[0] == 0 and res.nblocks[0] == 0
+    assert res.k[1] == 1 and res.k[2] == 1 and res.k[3] == 1
+    assert 3 <= res.k[4] <= 8 and res.err_est[4] < 1e-10
+    assert res.status[5] == 5 and res.k[5] == 0
+    assert res.k[6] == 12  # full column rank: runs to min(m, n)
+    for q in (1, 2, 4, 6):
+        assert sorted(res.perms[q].cpu().numpy().tolist()) == list(range(mats[q].shape[1]))
+    e = id_error(low.astype(np.float64), res.perms[4].cpu().numpy(), res.Ts[4].cpu().numpy())
+    assert e < 1e-10
+
+
+def test_batched_T_capacity_and_kmax(handle):
+    A = W.gaussian_exp(120, 100, decay=4.0, seed=5).astype(np.float32)
+    _, res = run_batch(handle, [A, A], b=16, tol=1e-12, seed=0, t_rank_cap=4)
+    assert (res.status == 6).all() and (res.k > 20).all() and (res.k < 100).all(), res.k
+    _, res = run_batch(handle, [A], b=16, tol=1e-12, seed=0, kmax=20)
+    assert res.k[0] == 20 and res.status[0] == 0 and res.Ts[0].shape == (20, 80)
+
+
+@pytest.mark.parametrize("sampler", ["es", "greedy"])
+def test_batched_other_samplers(handle, sampler):
+    tol, b = 1e-8, 16
+    sh = shapes(10, 48, 300, seed=31)
+    mats = [W.kernel_block_scaled(int(m), int(n), 700 + q) for q, (m, n) in enumerate(sh)]
+    _, res = run_batch(handle, mats, b=b, tol=tol, seed=4, sampler=sampler)
+    assert (res.status == 0).all()
+    for q, A in enumerate(mats):
+        A64 = A.astype(np.float64)
+        perm = res.perms[q].cpu().numpy()
+        e = id_error(A64, perm, res.Ts[q].cpu().numpy())
+        assert e <= 1.05 * tol and res.err_est[q] <= tol
+        if sampler == "greedy":
+            o = rbrp_column_id(A64, b, tol=tol, seed=4 + q, mode="gp")
+            k1 = int(o["ranks"][0])
+            assert np.array_equal(perm[:k1], o["perm"][:k1])
+
+
+def test_batched_autotuner(handle):
+    sh = shapes(64, 48, 600, seed=41)
+    mats = [W.kernel_block_scaled(int(m), int(n), 900 + q) for q, (m, n) in enumerate(sh)]
+    bt, res = run_batch(handle, mats, b=0, tol=1e-8, seed=0)
+    info = bt.info()
+    assert info["b"] in (8, 16, 24, 32) and info["ctas"] >= 1 and info["ms_autotune"] > 0
+    assert (res.status == 0).all() and (res.err_est <= 1e-8).all()
+
+
+def test_batched_invalid_inputs(handle):
+    from robust_blockwise_random_pivoting_gb300._lib import RBRPError
+    from robust_blockwise_random_pivoting_gb300.rbrp import Batch
+    A = dev32(np.ones((10, 10)))
+    with pytest.raises(RBRPError):
+        Batch(handle, [A], b=40)
+    with pytest.raises(TypeError):
+        Batch(handle, [A.double()])
