@@ -205,6 +205,15 @@ rbrp_status rbrp_batch_run(rbrp_handle h);
  * cap >= nprob entries, in the caller's problem order). */
 rbrp_status rbrp_batch_results(rbrp_handle h, rbrp_batch_result* out, int cap);
 rbrp_status rbrp_batch_get_info(rbrp_handle h, rbrp_batch_info* info);
+/* In-kernel phase profile of the batched kernel: when on, thread 0 of every CTA
+ * adds the SM cycles of each phase (clock64 between the barriers that end the
+ * phases) into device counters, accumulated over runs until switched on again.
+ * Phases: 0 column norms, 1 sampler, 2 panel gather + Gram, 3 pivoted Cholesky
+ * + filter + swap, 4 basis solve + R/column swaps, 5 projection W = Q^T A_res,
+ * 6 update A_res -= Q W + norms, 7 residual sums + stop rule, 8 T solve. */
+#define RBRP_BATCH_NPHASES 9
+rbrp_status rbrp_batch_set_profiling(rbrp_handle h, int on);
+rbrp_status rbrp_batch_get_phase_cycles(rbrp_handle h, double* cycles, int cap);
 /* plan + run + results in one call. */
 rbrp_status rbrp_id_batched_f32(rbrp_handle h, int nprob, const rbrp_batch_problem* problems,
                                 const rbrp_params* p, rbrp_batch_result* out);

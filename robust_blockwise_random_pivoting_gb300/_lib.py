@@ -42,6 +42,9 @@ class PhaseStats(ctypes.Structure):
                 ("launches", c_int * NPHASES)]
 
 
+BATCH_PHASES = ["norms", "sample", "gram", "pivot", "basis", "project", "update", "finish", "tsolve"]
+
+
 class BatchProblem(ctypes.Structure):
     _fields_ = [("m", c_int), ("n", c_int), ("lda", c_int64), ("A", c_void_p), ("perm", c_void_p),
                 ("T", c_void_p), ("T_cap", c_int64)]
@@ -103,6 +106,8 @@ _SIGS = {
     "rbrp_batch_run": (c_int, [c_void_p]),
     "rbrp_batch_results": (c_int, [c_void_p, ctypes.POINTER(BatchResult), c_int]),
     "rbrp_batch_get_info": (c_int, [c_void_p, ctypes.POINTER(BatchInfo)]),
+    "rbrp_batch_set_profiling": (c_int, [c_void_p, c_int]),
+    "rbrp_batch_get_phase_cycles": (c_int, [c_void_p, ctypes.POINTER(c_double), c_int]),
     "rbrp_id_batched_f32": (c_int, [c_void_p, c_int, ctypes.POINTER(BatchProblem), ctypes.POINTER(Params),
                                     ctypes.POINTER(BatchResult)]),
 }

@@ -43,14 +43,39 @@ struct BatchArgs {
   double tol, tol_loc;
   uint64_t seed;
   int b, sampler, kmax, compute_T;
+  unsigned long long* prof;  // per-phase SM cycles summed over CTAs (NULL: off)
 };
 
 namespace {
+
+// Phases of the in-kernel profile (clock64 deltas taken by thread 0 after the
+// barriers that end each phase, summed over problems and CTAs).
+enum { BPH_NORMS, BPH_SAMPLE, BPH_GRAM, BPH_PIVOT, BPH_BASIS, BPH_PROJECT, BPH_UPDATE, BPH_FINISH, BPH_TSOLVE, BPH_N };
+static_assert(BPH_N == RBRP_BATCH_NPHASES, "phase count");
+
+struct PhaseClock {
+  unsigned long long* acc;  // shared-memory accumulators, NULL when profiling is off
+  long long t;
+  __device__ __forceinline__ void start(unsigned long long* a) {
+    acc = (a && threadIdx.x == 0) ? a : nullptr;
+    if (acc) t = clock64();
+  }
+  __device__ __forceinline__ void mark(int ph) {
+    if (acc) {
+      const long long t1 = clock64();
+      acc[ph] += (unsigned long long)(t1 - t);
+      t = t1;
+    }
+  }
+};
 
 constexpr int BT = 256;     // threads per CTA: one problem per CTA
 constexpr int BROWS = 128;  // rows per stage of the Gram / projection / update loops
 constexpr int TCOL = 64;    // remaining positions per column tile
 constexpr int BATCH_MAXB = 32;
+constexpr int QRES_FLOATS = 8192;   // resident basis (32 KB): kept x m rounded up to 128 rows
+constexpr int RING_D = 4;           // stages in flight per warp
+constexpr int RING_FLOATS = RING_D * 4 * BROWS;  // per warp: D stages x up to 4 columns x 128 rows (8 KB)
 
 // Exact scaling by 2^s as two normal-float factors, so s may cover the full
 // exponent range of FP32 data (|s| <= 250).
@@ -65,14 +90,13 @@ __device__ __forceinline__ Pow2 pow2_scale(int s) {
 
 template <int BB>
 struct BatchSmem {
-  static constexpr int NG = 64 / BB;  // row groups of the projection (4 basis x 4 columns per thread)
   State st;
   int js[MAXB];
   int cols[MAXB];
   const float* src[TCOL];  // source column of each panel column / tile column
   double red_d[32];
   int red_i[32];
-  __align__(16) float Ws[BB][TCOL];  // W of the current tile, FP32, for the update
+  unsigned long long pacc[BPH_N];
   union {
     float gram_Vs[BROWS][BB + 1];
     struct {
@@ -80,14 +104,36 @@ struct BatchSmem {
       dfl R11s[BB][BB + 1];  // R11 in slot order (upper)
       dfl invd[BB];
     } pan;
-    struct {
-      __align__(16) float Xs[BROWS][TCOL + 4];
-      __align__(16) float Qs[BROWS][BB + 4];
-    } p1;
-    dfl red[NG][BB][TCOL];
-    __align__(16) float p2_Qs[BB][BROWS];
+    struct {  // staged projection / update (any kept, any m)
+      __align__(16) float Ws[BB][TCOL];  // W of the current tile, FP32, for the update
+      union {
+        struct {
+          __align__(16) float Xs[BROWS][TCOL + 4];
+          __align__(16) float Qs[BROWS][BB + 4];
+        } p1;
+        dfl red[BT * 16];  // projection partials: 16 per thread
+        __align__(16) float p2_Qs[BB][BROWS];
+      };
+    } stg;
+    struct {  // resident basis and one asynchronous-copy ring per warp
+      __align__(16) float qres[QRES_FLOATS];  // qres[a * ldq + r], zero for r >= m
+      __align__(16) float ring[BT / 32][RING_FLOATS];  // also the warp's reduction buffer
+    } res;
   } u;
 };
+
+// Warp sum of double-float partials (hi, lo) on the FP32 pipe, by a fixed
+// butterfly; GB300's FP64 pipe is ~1/64 of the FP32 rate, so only the final
+// conversion to FP64 runs there, once per column.
+__device__ __forceinline__ double warp_sum_df(float hi, float lo) {
+  dfl s = df_two_sum(hi, lo);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const dfl t = {__shfl_xor_sync(0xffffffffu, s.hi, o), __shfl_xor_sync(0xffffffffu, s.lo, o)};
+    s = df_add(s, t);
+  }
+  return (threadIdx.x & 31) == 0 ? (double)s.hi + (double)s.lo : 0.0;
+}
 
 __device__ __forceinline__ int block_max_int(int v, int* sh) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -101,8 +147,33 @@ __device__ __forceinline__ int block_max_int(int v, int* sh) {
   return r;
 }
 
-// a1: column maxima, squared norms (double-float, each column scaled by its own
-// power of two so tiny entries keep their resolution) and perm = identity.
+// A warp's walk over one column, f(x) per entry: 16-byte loads (two in flight
+// per lane) when the column is 16-byte aligned.  Both norm passes use it, so a
+// lane sees the same entries in the same order in each.
+template <typename F>
+__device__ __forceinline__ void column_walk(const float* __restrict__ col, int m, int lane, bool vec, F&& f) {
+  if (vec) {
+    const float4* c4 = reinterpret_cast<const float4*>(col);
+    const int m4 = m >> 2;
+    int r = lane;
+    for (; r + 32 < m4; r += 64) {
+      const float4 a = c4[r], b = c4[r + 32];
+      f(a.x); f(a.y); f(a.z); f(a.w);
+      f(b.x); f(b.y); f(b.z); f(b.w);
+    }
+    for (; r < m4; r += 32) {
+      const float4 a = c4[r];
+      f(a.x); f(a.y); f(a.z); f(a.w);
+    }
+    for (int t = 4 * m4 + lane; t < m; t += 32) f(col[t]);
+  } else {
+    for (int r = lane; r < m; r += 32) f(col[r]);
+  }
+}
+
+// a1: column maxima, squared norms (double-float; a column whose maximum lies
+// outside [2^-41, 2^40) is summed again scaled by its own power of two so tiny
+// entries keep their resolution) and perm = identity.
 // Returns the problem's exponent emax (max |A| = f 2^emax, f in [0.5, 1)) and
 // rescales diags to the problem scale 2^-emax; *bad flags non-finite entries.
 template <int BB>
@@ -110,30 +181,40 @@ __device__ int batch_norms(BatchSmem<BB>& sm, const float* __restrict__ A, int64
                            int* __restrict__ perm, double* __restrict__ diags, int* __restrict__ colexp, int* bad,
                            double* res0, int* nnz) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const bool vec = (lda & 3) == 0 && (reinterpret_cast<uintptr_t>(A) & 15) == 0;
   int emax = INT_MIN, nonfinite = 0;
   for (int c = warp; c < n; c += BT / 32) {
     const float* col = A + (int64_t)c * lda;
     unsigned mx = 0u;
     int nf = 0;
-    for (int r = lane; r < m; r += 32) {
-      const float v = fabsf(col[r]);
+    DF raw{0.f, 0.f};
+    column_walk(col, m, lane, vec, [&](float x) {
+      const float v = fabsf(x);
       nf |= !(v <= FLT_MAX);
       mx = max(mx, __float_as_uint(v));
-    }
+      df_add_sq(raw, x);
+    });
     mx = __reduce_max_sync(0xffffffffu, mx);
     nf = __any_sync(0xffffffffu, nf);
     double d = 0.0;
-    int e = INT_MIN;
+    int e = INT_MIN, ce = INT_MIN;  // column exponent; exponent of the scale d is expressed in
     if (!nf && mx != 0u) {
       frexpf(__uint_as_float(mx), &e);
-      const Pow2 sc = pow2_scale(-e);
-      DF acc{0.f, 0.f};
-      for (int r = lane; r < m; r += 32) df_add_sq(acc, sc.apply(col[r]));
-      d = warp_sum((double)acc.hi + (double)acc.lo);
+      if (e >= -40 && e <= 40) {
+        // squares of every entry that matters (>= max 2^-24) stay normal: the raw sum is exact enough
+        d = warp_sum_df(raw.hi, raw.lo);
+        ce = 0;
+      } else {
+        const Pow2 sc = pow2_scale(-e);
+        DF acc{0.f, 0.f};
+        column_walk(col, m, lane, vec, [&](float x) { df_add_sq(acc, sc.apply(x)); });
+        d = warp_sum_df(acc.hi, acc.lo);
+        ce = e;
+      }
     }
     if (lane == 0) {
       diags[c] = d;
-      colexp[c] = e;
+      colexp[c] = ce;
       perm[c] = c;
     }
     emax = max(emax, e);
@@ -155,6 +236,18 @@ __device__ int batch_norms(BatchSmem<BB>& sm, const float* __restrict__ A, int64
   return emax;
 }
 
+// Compensated product accumulation (Ogita, Rump and Oishi's Dot2): the exact
+// product by FMA, the sum by TwoSum, errors gathered in lo; as accurate as a
+// double-float accumulation, normalised once by the caller.
+__device__ __forceinline__ void dot2_acc(float& hi, float& lo, float x, float y) {
+  const float p = x * y;
+  const float e = fmaf(x, y, -p);
+  const float s = hi + p;
+  const float z = s - hi;
+  lo += ((hi - (s - z)) + (p - z)) + e;
+  hi = s;
+}
+
 // a3 (residual form): V = residual columns at the sampled positions (exact, FP32)
 // and their Gram matrix in double-float (exact products), written as the Schur
 // complement the pivoted Cholesky starts from.
@@ -163,9 +256,9 @@ __device__ void batch_gram(BatchSmem<BB>& sm, int m, int bss, bool first, Pow2 s
                            int64_t ld) {
   constexpr int NQ = BB * BB / BT, CW = BB / NQ;
   const int tid = threadIdx.x, c1 = tid / CW, c2 = tid % CW;
-  dfl acc[NQ];
+  float hi[NQ], lo[NQ];
 #pragma unroll
-  for (int q = 0; q < NQ; ++q) acc[q] = {0.f, 0.f};
+  for (int q = 0; q < NQ; ++q) hi[q] = lo[q] = 0.f;
   for (int r0 = 0; r0 < m; r0 += BROWS) {
     __syncthreads();
     for (int idx = tid; idx < BROWS * BB; idx += BT) {
@@ -184,13 +277,13 @@ __device__ void batch_gram(BatchSmem<BB>& sm, int m, int bss, bool first, Pow2 s
       for (int rr = 0; rr < rows; ++rr) {
         const float x = sm.u.gram_Vs[rr][c1];
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) df_acc_prod(acc[q], x, sm.u.gram_Vs[rr][c2 + CW * q]);
+        for (int q = 0; q < NQ; ++q) dot2_acc(hi[q], lo[q], x, sm.u.gram_Vs[rr][c2 + CW * q]);
       }
     }
   }
   __syncthreads();
 #pragma unroll
-  for (int q = 0; q < NQ; ++q) sm.u.pan.pc.S[c1][c2 + CW * q] = acc[q];
+  for (int q = 0; q < NQ; ++q) sm.u.pan.pc.S[c1][c2 + CW * q] = df_two_sum(hi[q], lo[q]);
   if (tid < BB) {
     sm.u.pan.pc.ord[tid] = tid;
     sm.u.pan.pc.alive[tid] = tid < bss;
@@ -284,153 +377,470 @@ __device__ __forceinline__ void fold_two_sum(float& hi, float& lo, float x) {
   hi = t;
 }
 
-// a7/a8 per tile of 64 remaining positions: W = Q^T X (FP32 stage sums of 32-64
-// rows folded into double-float), R(I2, p) = W, then X -= Q W written to A_res
-// with the exact norms of the updated columns into diags.  X is the residual
+// ---------------------------------------------------------------------------
+// a7/a8 per tile of 64 remaining positions p: W = Q^T X (FP32 partial sums
+// folded into double-float), R(I2, p) = W, then X -= Q W written to A_res with
+// the exact norms of the updated columns into diags.  X is the residual
 // (A_res) or, before the first update, A(:, perm[p]) scaled.
+//
+// Lane layout (update, and projection when kept <= 4): the tile is walked in
+// two halves of 32 positions; warp w owns positions 4w..4w+3 of a half and
+// lane l rows r0 + l + 32u (u < 4) of every 128-row stage, so each load and
+// store instruction of a warp touches one 128-byte row segment.  The next
+// stage's 16 values per thread are loaded while the current one is used.
+// ---------------------------------------------------------------------------
+template <int BB>
+__device__ __forceinline__ float load_x(const BatchSmem<BB>& sm, int cc, int r, int m, int ncol, bool first,
+                                        Pow2 sc) {
+  float v = 0.f;
+  if (r < m && cc < ncol) {
+    v = sm.src[cc][r];
+    if (first) v = sc.apply(v);
+  }
+  return v;
+}
+
+// Rows [r0, r0 + 128) of the kept basis columns into p2_Qs[a][row].
+template <int BB>
+__device__ __forceinline__ void stage_basis(BatchSmem<BB>& sm, const float* __restrict__ Qc, int64_t ld, int m,
+                                            int r0, int kept) {
+  for (int idx = threadIdx.x; idx < kept * (BROWS / 4); idx += BT) {
+    const int a = idx / (BROWS / 4), j = idx % (BROWS / 4), r = r0 + 4 * j;
+    const float* qa = Qc + (int64_t)a * ld;
+    float4 v;
+    if (r + 3 < m) {
+      v = *reinterpret_cast<const float4*>(qa + r);
+    } else {
+      v.x = r < m ? qa[r] : 0.f;
+      v.y = r + 1 < m ? qa[r + 1] : 0.f;
+      v.z = r + 2 < m ? qa[r + 2] : 0.f;
+      v.w = r + 3 < m ? qa[r + 3] : 0.f;
+    }
+    *reinterpret_cast<float4*>(&sm.u.stg.p2_Qs[a][4 * j]) = v;
+  }
+}
+
+// Projection from staged tiles: a thread computes 4 basis rows x 4 positions from
+// staged tiles; the basis rows cover kept rounded up to 4 nq (nq a power of
+// two), and the CTA's 256 / (16 nq) thread groups split each 128-row stage,
+// their partials summed at the end of the tile.
+template <int BB>
+__device__ void proj_staged(BatchSmem<BB>& sm, int m, int n, int i, int kept, int p0, int ncol, bool first,
+                            Pow2 sc, const float* __restrict__ Qr, float2* __restrict__ R) {
+  constexpr int XPT = BROWS * TCOL / BT;  // staged values per thread and stage
+  const int tid = threadIdx.x;
+  const int nq = kept <= 4 ? 1 : kept <= 8 ? 2 : kept <= 16 ? 4 : 8;
+  const int gt = 16 * nq, ng = BT / gt, grows = BROWS / ng, na = 4 * nq;
+  const int g = tid / gt, lt = tid % gt, aq = lt / 16, cq = lt % 16;
+  const int xr_row = tid & (BROWS - 1), xr_col = tid / BROWS;  // staging: row, first column (step BT / BROWS)
+  float xr[XPT];
+  auto load_stage = [&](int r0) {
+#pragma unroll
+    for (int j = 0; j < XPT; ++j) xr[j] = load_x(sm, xr_col + (BT / BROWS) * j, r0 + xr_row, m, ncol, first, sc);
+  };
+  load_stage(0);
+  float hi[4][4], lo[4][4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) hi[u][v] = lo[u][v] = 0.f;
+  for (int r0 = 0; r0 < m; r0 += BROWS) {
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < XPT; ++j) sm.u.stg.p1.Xs[xr_row][xr_col + (BT / BROWS) * j] = xr[j];
+    for (int idx = tid; idx < BROWS * nq; idx += BT) {
+      const int rr = idx / nq, j = idx % nq, r = r0 + rr;
+      const float4 v = r < m ? reinterpret_cast<const float4*>(Qr + (int64_t)r * BB)[j]
+                             : make_float4(0.f, 0.f, 0.f, 0.f);
+      *reinterpret_cast<float4*>(&sm.u.stg.p1.Qs[rr][4 * j]) = v;
+    }
+    __syncthreads();
+    if (r0 + BROWS < m) load_stage(r0 + BROWS);
+    float c[4][4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) c[u][v] = 0.f;
+    const int rb = g * grows, re = min(rb + grows, m - r0);
+    for (int rr = rb; rr < re; ++rr) {
+      const float4 q4 = *reinterpret_cast<const float4*>(&sm.u.stg.p1.Qs[rr][4 * aq]);
+      const float4 x4 = *reinterpret_cast<const float4*>(&sm.u.stg.p1.Xs[rr][4 * cq]);
+      const float qv[4] = {q4.x, q4.y, q4.z, q4.w};
+      const float xv[4] = {x4.x, x4.y, x4.z, x4.w};
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) c[u][v] = fmaf(qv[u], xv[v], c[u][v]);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) fold_two_sum(hi[u][v], lo[u][v], c[u][v]);
+  }
+  __syncthreads();
+  // partials of group g at red[(g * na + a) * TCOL + c]
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) sm.u.stg.red[(g * na + 4 * aq + u) * TCOL + 4 * cq + v] = {hi[u][v], lo[u][v]};
+  __syncthreads();
+  for (int idx = tid; idx < kept * TCOL; idx += BT) {
+    const int a = idx / TCOL, cc = idx % TCOL;
+    dfl w = sm.u.stg.red[a * TCOL + cc];
+    for (int gg = 1; gg < ng; ++gg) w = df_add(w, sm.u.stg.red[(gg * na + a) * TCOL + cc]);
+    w = df_two_sum(w.hi, w.lo);
+    if (cc < ncol) R[(int64_t)(i + a) * n + p0 + cc] = make_float2(w.hi, w.lo);
+    sm.u.stg.Ws[a][cc] = w.hi;
+  }
+  __syncthreads();
+}
+
+// Update X -= Q W in the lane layout, the updated columns written to A_res and
+// their squared norms (double-float) into diags.
+template <int BB>
+__device__ void update_lanes(BatchSmem<BB>& sm, int m, int kept, int p0, int ncol, bool first, Pow2 sc,
+                             float* __restrict__ Ares, int64_t ld, const float* __restrict__ Qc,
+                             double* __restrict__ diags) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int h = 0; h < TCOL / 32 && 32 * h < ncol; ++h) {
+    const int c0 = 32 * h + 4 * warp;
+    DF nrm[4];
+    float x[4][4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) nrm[j].hi = nrm[j].lo = 0.f;
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) x[u][j] = load_x(sm, c0 + j, lane + 32 * u, m, ncol, first, sc);
+    for (int r0 = 0; r0 < m; r0 += BROWS) {
+      __syncthreads();
+      stage_basis(sm, Qc, ld, m, r0, kept);
+      __syncthreads();
+      float xn[4][4];
+      const bool more = r0 + BROWS < m;
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) xn[u][j] = more ? load_x(sm, c0 + j, r0 + BROWS + lane + 32 * u, m, ncol, first, sc) : 0.f;
+      float acc[4][4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[u][j] = 0.f;
+      for (int a = 0; a < kept; ++a) {
+        float q[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) q[u] = sm.u.stg.p2_Qs[a][lane + 32 * u];
+        const float4 w4 = *reinterpret_cast<const float4*>(&sm.u.stg.Ws[a][c0]);
+        const float wv[4] = {w4.x, w4.y, w4.z, w4.w};
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) acc[u][j] = fmaf(q[u], wv[j], acc[u][j]);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int r = r0 + lane + 32 * u, cc = c0 + j;
+          if (r < m && cc < ncol) {
+            const float y = x[u][j] - acc[u][j];
+            Ares[(int64_t)(p0 + cc) * ld + r] = y;
+            df_add_sq(nrm[j], y);
+          }
+          x[u][j] = xn[u][j];
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const double d = warp_sum_df(nrm[j].hi, nrm[j].lo);
+      if (lane == 0 && c0 + j < ncol) diags[p0 + c0 + j] = d;
+    }
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ void cp_async16(float* smem, const float* gmem, int src_bytes) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(sa), "l"(gmem), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async4(float* smem, const float* gmem, int src_bytes) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(sa), "l"(gmem), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// Sum over the 32 lanes of 16 double-float values per lane by a shuffle
+// reduce-scatter (rounds at offsets 16, 8, 4, 2 halve the values each lane
+// holds, the last adds the lane pair): afterwards lanes 2v and 2v + 1 hold the
+// sum of value v, in a fixed order.
+__device__ __forceinline__ dfl warp_reduce_scatter16(float (&hi)[16], float (&lo)[16]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 16, cnt = 16; o >= 2; o >>= 1, cnt >>= 1) {
+    const bool upper = (lane & o) != 0;
+    const int half = cnt / 2;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      if (k < half) {
+        const float sh = upper ? hi[k] : hi[k + half], sl = upper ? lo[k] : lo[k + half];
+        const dfl keep = upper ? dfl{hi[k + half], lo[k + half]} : dfl{hi[k], lo[k]};
+        const dfl recv = {__shfl_xor_sync(0xffffffffu, sh, o), __shfl_xor_sync(0xffffffffu, sl, o)};
+        const dfl r = upper ? df_add(recv, keep) : df_add(keep, recv);
+        hi[k] = r.hi;
+        lo[k] = r.lo;
+      }
+    }
+  }
+  const dfl mine = {hi[0], lo[0]};
+  const dfl other = {__shfl_xor_sync(0xffffffffu, hi[0], 1), __shfl_xor_sync(0xffffffffu, lo[0], 1)};
+  const dfl r = (lane & 1) ? df_add(other, mine) : df_add(mine, other);
+  return df_two_sum(r.hi, r.lo);
+}
+
+template <int CW>
+struct IssueState {
+  int t;       // next stage of the warp's stream to issue
+  int g, s;    // its group and its stage within the pass
+  int upd;     // 0: projection pass, 1: update pass
+  const float* src[CW];
+};
+
+template <int CW>
+__device__ __forceinline__ void issue_sources(IssueState<CW>& is, int p, int n, bool first,
+                                              const float* __restrict__ A, int64_t lda, const int* __restrict__ perm,
+                                              const float* Ares, int64_t ld) {
+  if (p >= n) return;
+  const int nc = min(CW, n - p);
+#pragma unroll
+  for (int j = 0; j < CW; ++j) {
+    const int pj = p + min(j, nc - 1);
+    is.src[j] = first ? A + (int64_t)perm[pj] * lda : Ares + (int64_t)pj * ld;
+  }
+}
+
+// Issues the next stage of a warp's stream into ring slot t % RING_D (past
+// the end only an empty group is committed, which keeps the group count
+// uniform): this lane's 4 rows of each of the group's columns, zero-filled
+// beyond m.  Stages run projection 0..nst-1, update 0..nst-1 per group.
+template <int CW>
+__device__ __forceinline__ void ring_issue(IssueState<CW>& is, int total, int nst, int p_first, int stride, int n,
+                                           int m, bool first, bool vec, const float* __restrict__ A, int64_t lda,
+                                           const int* __restrict__ perm, const float* Ares, int64_t ld, float* ring) {
+  const int lane = threadIdx.x & 31;
+  if (is.t < total) {
+    const int r = is.s * BROWS + 4 * lane;
+    const int valid = max(0, min(4, m - r));
+#pragma unroll
+    for (int j = 0; j < CW; ++j) {
+      float* dst = ring + ((is.t % RING_D) * CW + j) * BROWS + 4 * lane;
+      if (vec) {
+        cp_async16(dst, valid > 0 ? is.src[j] + r : is.src[j], 4 * valid);
+      } else {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) cp_async4(dst + e, e < valid ? is.src[j] + r + e : is.src[j], e < valid ? 4 : 0);
+      }
+    }
+    if (++is.s == nst) {
+      is.s = 0;
+      is.upd ^= 1;
+      if (!is.upd) issue_sources<CW>(is, p_first + (++is.g) * stride, n, first, A, lda, perm, Ares, ld);
+    }
+  }
+  ++is.t;
+  cp_async_commit();
+}
+
+// Resident basis (kept <= KA, kept * ldq <= QRES_FLOATS): every warp streams
+// its own groups of CW = 16 / KA positions, each through projection (nst
+// stages of 128 rows), a warp-level sum of the partials and update (the same
+// nst stages again), with no CTA barrier.  Lane l owns rows r0 + 4l .. +3 of a
+// stage.  All stages of the warp form one sequence fed by a ring of RING_D
+// asynchronous copies (cp.async, 16 bytes per lane and column, or 4-byte
+// copies when the caller's columns are not 16-byte aligned) that runs ahead
+// across the projection/update and group boundaries; each lane reads back
+// only what it copied itself.  The update's reads of a group hit L2, where
+// the projection's reads left them.
+template <int BB, int KA>
+__device__ void project_update_resident(BatchSmem<BB>& sm, int m, int n, int i, int kept, bool first, Pow2 sc,
+                                        const float* __restrict__ A, int64_t lda, const int* __restrict__ perm,
+                                        float* __restrict__ Ares, int64_t ld, int ldq, float2* __restrict__ R,
+                                        double* __restrict__ diags) {
+  constexpr int CW = 16 / KA;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const float* __restrict__ qres = sm.u.res.qres;
+  float* ring = sm.u.res.ring[warp];
+  const bool vec = !first || ((lda & 3) == 0 && (reinterpret_cast<uintptr_t>(A) & 15) == 0);
+  const int nst = (m + BROWS - 1) / BROWS;
+  const int stride = CW * (BT / 32);
+  const int p_first = i + kept + CW * warp;
+  const int ngroups = p_first < n ? (n - p_first + stride - 1) / stride : 0;
+  const int total = ngroups * 2 * nst;
+  // issue side: source columns of the group being fetched
+  IssueState<CW> is;
+  is.t = is.g = is.s = is.upd = 0;
+  issue_sources<CW>(is, p_first, n, first, A, lda, perm, Ares, ld);
+  auto fetch = [&](int t, float (&x)[4][CW]) {
+#pragma unroll
+    for (int j = 0; j < CW; ++j) {
+      const float4 v4 = *reinterpret_cast<const float4*>(ring + ((t % RING_D) * CW + j) * BROWS + 4 * lane);
+      x[0][j] = first ? sc.apply(v4.x) : v4.x;
+      x[1][j] = first ? sc.apply(v4.y) : v4.y;
+      x[2][j] = first ? sc.apply(v4.z) : v4.z;
+      x[3][j] = first ? sc.apply(v4.w) : v4.w;
+    }
+  };
+#pragma unroll
+  for (int t = 0; t < RING_D - 1; ++t)
+    ring_issue<CW>(is, total, nst, p_first, stride, n, m, first, vec, A, lda, perm, Ares, ld, ring);
+  int t = 0;
+  for (int g = 0; g < ngroups; ++g) {
+    const int p = p_first + g * stride, nc = min(CW, n - p);
+    // projection: W(a, j) = sum_r q_a(r) x_j(r), FP32 stage sums folded into double-float
+    float hi[16], lo[16];
+#pragma unroll
+    for (int v = 0; v < 16; ++v) hi[v] = lo[v] = 0.f;
+    for (int s = 0; s < nst; ++s, ++t) {
+      ring_issue<CW>(is, total, nst, p_first, stride, n, m, first, vec, A, lda, perm, Ares, ld, ring);
+      cp_async_wait<RING_D - 1>();
+      float x[4][CW];
+      fetch(t, x);
+      const int r0 = s * BROWS + 4 * lane;
+#pragma unroll
+      for (int a = 0; a < KA; ++a) {
+        if (a < kept) {
+          const float4 q4 = *reinterpret_cast<const float4*>(qres + a * ldq + r0);
+          const float q[4] = {q4.x, q4.y, q4.z, q4.w};
+          float c[CW];
+#pragma unroll
+          for (int j = 0; j < CW; ++j) c[j] = 0.f;
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int j = 0; j < CW; ++j) c[j] = fmaf(q[u], x[u][j], c[j]);
+#pragma unroll
+          for (int j = 0; j < CW; ++j) fold_two_sum(hi[a * CW + j], lo[a * CW + j], c[j]);
+        }
+      }
+    }
+    const dfl wsum = warp_reduce_scatter16(hi, lo);  // value v = lane >> 1
+    {
+      const int v = lane >> 1, a = v / CW, j = v % CW;
+      if ((lane & 1) == 0 && a < kept && j < nc) R[(int64_t)(i + a) * n + p + j] = make_float2(wsum.hi, wsum.lo);
+    }
+    float w[KA][CW];
+#pragma unroll
+    for (int a = 0; a < KA; ++a)
+#pragma unroll
+      for (int j = 0; j < CW; ++j) w[a][j] = __shfl_sync(0xffffffffu, wsum.hi, 2 * (a * CW + j));
+    // update X -= Q W into A_res; squared norms of the updated columns: FP32
+    // sums of each lane's 4 squares (positive terms, relative error < 3e-7),
+    // folded into double-float
+    DF nrm[CW];
+#pragma unroll
+    for (int j = 0; j < CW; ++j) nrm[j].hi = nrm[j].lo = 0.f;
+    for (int s = 0; s < nst; ++s, ++t) {
+      ring_issue<CW>(is, total, nst, p_first, stride, n, m, first, vec, A, lda, perm, Ares, ld, ring);
+      cp_async_wait<RING_D - 1>();
+      float x[4][CW];
+      fetch(t, x);
+      const int r0 = s * BROWS + 4 * lane;
+      float acc[4][CW];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int j = 0; j < CW; ++j) acc[u][j] = 0.f;
+#pragma unroll
+      for (int a = 0; a < KA; ++a) {
+        if (a < kept) {
+          const float4 q4 = *reinterpret_cast<const float4*>(qres + a * ldq + r0);
+          const float q[4] = {q4.x, q4.y, q4.z, q4.w};
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int j = 0; j < CW; ++j) acc[u][j] = fmaf(q[u], w[a][j], acc[u][j]);
+        }
+      }
+      const int valid = max(0, min(4, m - r0));
+#pragma unroll
+      for (int j = 0; j < CW; ++j) {
+        if (j < nc && valid > 0) {
+          float y[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) y[u] = x[u][j] - acc[u][j];
+          float* dst = Ares + (int64_t)(p + j) * ld + r0;
+          if (valid == 4) {
+            *reinterpret_cast<float4*>(dst) = make_float4(y[0], y[1], y[2], y[3]);
+          } else {
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+              if (u < valid) dst[u] = y[u];
+          }
+          // rows >= m give y = 0 (zero-filled x, zero basis rows)
+          fold_two_sum(nrm[j].hi, nrm[j].lo, fmaf(y[3], y[3], fmaf(y[2], y[2], fmaf(y[1], y[1], y[0] * y[0]))));
+        }
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < CW; ++j) {
+      const double d = warp_sum_df(nrm[j].hi, nrm[j].lo);
+      if (lane == 0 && j < nc) diags[p + j] = d;
+    }
+  }
+  cp_async_wait<0>();
+  __syncthreads();
+}
+
 template <int BB>
 __device__ void batch_project_update(BatchSmem<BB>& sm, int m, int n, int i, int kept, bool first, Pow2 sc,
                                      const float* __restrict__ A, int64_t lda, const int* __restrict__ perm,
                                      float* __restrict__ Ares, int64_t ld, const float* __restrict__ Qc,
                                      const float* __restrict__ Qr, float2* __restrict__ R,
-                                     double* __restrict__ diags) {
-  constexpr int NG = BatchSmem<BB>::NG, GT = BT / NG, GROWS = BROWS / NG;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int g = tid / GT, lt = tid % GT, aq = lt / 16, cq = lt % 16;
-  const int cb = warp * 8;  // update: this warp's 8 columns of the tile
+                                     double* __restrict__ diags, PhaseClock& clk) {
+  const int tid = threadIdx.x;
+  const int ldq = (m + BROWS - 1) / BROWS * BROWS;
+  const int ka = kept <= 4 ? 4 : kept <= 8 ? 8 : 16;
+  if (kept <= 16 && kept * ldq <= QRES_FLOATS) {
+    // stage the kept basis columns once (rows >= m zero), then barrier-free warp streams
+    for (int idx = tid; idx < kept * (ldq / 4); idx += BT) {
+      const int a = idx / (ldq / 4), r = 4 * (idx % (ldq / 4));
+      const float* qa = Qc + (int64_t)a * ld;
+      float4 v;
+      if (r + 3 < m) {
+        v = *reinterpret_cast<const float4*>(qa + r);
+      } else {
+        v.x = r < m ? qa[r] : 0.f;
+        v.y = r + 1 < m ? qa[r + 1] : 0.f;
+        v.z = r + 2 < m ? qa[r + 2] : 0.f;
+        v.w = r + 3 < m ? qa[r + 3] : 0.f;
+      }
+      *reinterpret_cast<float4*>(&sm.u.res.qres[a * ldq + r]) = v;
+    }
+    __syncthreads();
+    if (ka == 4)
+      project_update_resident<BB, 4>(sm, m, n, i, kept, first, sc, A, lda, perm, Ares, ld, ldq, R, diags);
+    else if (ka == 8)
+      project_update_resident<BB, 8>(sm, m, n, i, kept, first, sc, A, lda, perm, Ares, ld, ldq, R, diags);
+    else
+      project_update_resident<BB, 16>(sm, m, n, i, kept, first, sc, A, lda, perm, Ares, ld, ldq, R, diags);
+    clk.mark(BPH_UPDATE);
+    return;
+  }
   for (int p0 = i + kept; p0 < n; p0 += TCOL) {
     const int ncol = min(TCOL, n - p0);
     __syncthreads();
     if (tid < TCOL)
       sm.src[tid] = tid < ncol ? (first ? A + (int64_t)perm[p0 + tid] * lda : Ares + (int64_t)(p0 + tid) * ld)
                                : nullptr;
-    float hi[4][4], lo[4][4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u)
-#pragma unroll
-      for (int v = 0; v < 4; ++v) hi[u][v] = lo[u][v] = 0.f;
-    for (int r0 = 0; r0 < m; r0 += BROWS) {
-      __syncthreads();
-      for (int idx = tid; idx < BROWS * TCOL; idx += BT) {
-        const int rr = idx % BROWS, cc = idx / BROWS, r = r0 + rr;
-        float v = 0.f;
-        if (r < m && cc < ncol) {
-          v = sm.src[cc][r];
-          if (first) v = sc.apply(v);
-        }
-        sm.u.p1.Xs[rr][cc] = v;
-      }
-      for (int idx = tid; idx < BROWS * (BB / 4); idx += BT) {
-        const int rr = idx / (BB / 4), j = idx % (BB / 4), r = r0 + rr;
-        const float4 v = r < m ? reinterpret_cast<const float4*>(Qr + (int64_t)r * BB)[j]
-                               : make_float4(0.f, 0.f, 0.f, 0.f);
-        *reinterpret_cast<float4*>(&sm.u.p1.Qs[rr][4 * j]) = v;
-      }
-      __syncthreads();
-      float c[4][4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int v = 0; v < 4; ++v) c[u][v] = 0.f;
-      const int rb = g * GROWS, re = min(rb + GROWS, m - r0);
-      for (int rr = rb; rr < re; ++rr) {
-        const float4 q4 = *reinterpret_cast<const float4*>(&sm.u.p1.Qs[rr][4 * aq]);
-        const float4 x4 = *reinterpret_cast<const float4*>(&sm.u.p1.Xs[rr][4 * cq]);
-        const float qv[4] = {q4.x, q4.y, q4.z, q4.w};
-        const float xv[4] = {x4.x, x4.y, x4.z, x4.w};
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-#pragma unroll
-          for (int v = 0; v < 4; ++v) c[u][v] = fmaf(qv[u], xv[v], c[u][v]);
-      }
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int v = 0; v < 4; ++v) fold_two_sum(hi[u][v], lo[u][v], c[u][v]);
-    }
     __syncthreads();
-#pragma unroll
-    for (int u = 0; u < 4; ++u)
-#pragma unroll
-      for (int v = 0; v < 4; ++v) sm.u.red[g][4 * aq + u][4 * cq + v] = {hi[u][v], lo[u][v]};
-    __syncthreads();
-    for (int idx = tid; idx < BB * TCOL; idx += BT) {
-      const int a = idx / TCOL, cc = idx % TCOL;
-      dfl w = sm.u.red[0][a][cc];
-#pragma unroll
-      for (int gg = 1; gg < NG; ++gg) w = df_add(w, sm.u.red[gg][a][cc]);
-      w = df_two_sum(w.hi, w.lo);
-      if (a < kept && cc < ncol) R[(int64_t)(i + a) * n + p0 + cc] = make_float2(w.hi, w.lo);
-      sm.Ws[a][cc] = a < kept ? w.hi : 0.f;
-    }
-    // update of this warp's 8 columns: lane l owns rows r0 + l + 32 u
-    DF nrm[8];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) nrm[j].hi = nrm[j].lo = 0.f;
-    for (int r0 = 0; r0 < m; r0 += BROWS) {
-      float x[4][8];
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const int r = r0 + lane + 32 * u, cc = cb + j;
-          float v = 0.f;
-          if (r < m && cc < ncol) {
-            v = sm.src[cc][r];
-            if (first) v = sc.apply(v);
-          }
-          x[u][j] = v;
-        }
-      __syncthreads();
-      for (int idx = tid; idx < kept * (BROWS / 4); idx += BT) {
-        const int a = idx / (BROWS / 4), j = idx % (BROWS / 4), r = r0 + 4 * j;
-        const float* qa = Qc + (int64_t)a * ld;
-        float4 v;
-        if (r + 3 < m) {
-          v = *reinterpret_cast<const float4*>(qa + r);
-        } else {
-          v.x = r < m ? qa[r] : 0.f;
-          v.y = r + 1 < m ? qa[r + 1] : 0.f;
-          v.z = r + 2 < m ? qa[r + 2] : 0.f;
-          v.w = r + 3 < m ? qa[r + 3] : 0.f;
-        }
-        *reinterpret_cast<float4*>(&sm.u.p2_Qs[a][4 * j]) = v;
-      }
-      __syncthreads();
-      float acc[4][8];
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int j = 0; j < 8; ++j) acc[u][j] = 0.f;
-      for (int a = 0; a < kept; ++a) {
-        float q[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) q[u] = sm.u.p2_Qs[a][lane + 32 * u];
-        const float4 w0 = *reinterpret_cast<const float4*>(&sm.Ws[a][cb]);
-        const float4 w1 = *reinterpret_cast<const float4*>(&sm.Ws[a][cb + 4]);
-        const float wv[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-#pragma unroll
-          for (int j = 0; j < 8; ++j) acc[u][j] = fmaf(q[u], wv[j], acc[u][j]);
-      }
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const int r = r0 + lane + 32 * u, cc = cb + j;
-          if (r < m && cc < ncol) {
-            const float y = x[u][j] - acc[u][j];
-            Ares[(int64_t)(p0 + cc) * ld + r] = y;
-            df_add_sq(nrm[j], y);
-          }
-        }
-    }
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const double d = warp_sum((double)nrm[j].hi + (double)nrm[j].lo);
-      if (lane == 0 && cb + j < ncol) diags[p0 + cb + j] = d;
-    }
+    proj_staged<BB>(sm, m, n, i, kept, p0, ncol, first, sc, Qr, R);
+    clk.mark(BPH_PROJECT);
+    update_lanes<BB>(sm, m, kept, p0, ncol, first, sc, Ares, ld, Qc, diags);
+    clk.mark(BPH_UPDATE);
   }
   __syncthreads();
 }
@@ -512,6 +922,8 @@ __device__ void solve_problem(BatchSmem<BB>& sm, const rbrp_batch_problem& pr, i
   const int mn = min(m, n);
   const int kcap = args.kmax > 0 ? min(args.kmax, mn) : mn;
 
+  PhaseClock clk;
+  clk.start(args.prof ? sm.pacc : nullptr);
   int bad = 0, nnz = 0;
   double res0 = 0.0;
   const int emax = batch_norms<BB>(sm, A, lda, m, n, perm, diags, reinterpret_cast<int*>(pbuf), &bad, &res0, &nnz);
@@ -534,6 +946,7 @@ __device__ void solve_problem(BatchSmem<BB>& sm, const rbrp_batch_problem& pr, i
     st.done = (bad || nnz == 0 || kcap <= 0) ? 1 : 0;
   }
   __syncthreads();
+  clk.mark(BPH_NORMS);
   const int max_attempts = 4 * kcap + 64;
   const uint64_t seed = args.seed + (uint64_t)pid;
   for (;;) {
@@ -552,21 +965,25 @@ __device__ void solve_problem(BatchSmem<BB>& sm, const rbrp_batch_problem& pr, i
     sample_block(&st, diags, perm, n, kcap, args.b, seed, args.sampler, pbuf,
                  reinterpret_cast<unsigned long long*>(pbuf), sm.js, sm.cols);
     const int bss = st.bs_sampled;
+    clk.mark(BPH_SAMPLE);
     if (tid < bss) {
       const int p = sm.js[tid];
       sm.src[tid] = first ? A + (int64_t)perm[p] * lda : Ares + (int64_t)p * ld;
     }
     batch_gram<BB>(sm, m, bss, first, sc, V, ld);
+    clk.mark(BPH_GRAM);
     const int kept = pchol_filter_df<BB>(sm.u.pan.pc, bss, min(bss, m), args.tol_loc);
     block_swap_parallel<BB>(sm.u.pan.pc, i, kept, sm.js, perm, diags, sm.u.pan.pc.J, sm.u.pan.pc.K1,
                             sm.u.pan.pc.K2, &st);
     __syncthreads();
+    clk.mark(BPH_PIVOT);
     double s = 0.0;
     int c = 0;
     if (kept > 0) {
       batch_qsolve<BB>(sm, m, kept, V, ld, Qc, Qr);
       batch_swaps<BB>(sm, i, kept, n, R, Ares, ld, first);
-      batch_project_update<BB>(sm, m, n, i, kept, first, sc, A, lda, perm, Ares, ld, Qc, Qr, R, diags);
+      clk.mark(BPH_BASIS);
+      batch_project_update<BB>(sm, m, n, i, kept, first, sc, A, lda, perm, Ares, ld, Qc, Qr, R, diags, clk);
       for (int p = i + kept + tid; p < n; p += BT) {
         const double d = diags[p];
         s += d;
@@ -599,6 +1016,7 @@ __device__ void solve_problem(BatchSmem<BB>& sm, const rbrp_batch_problem& pr, i
       }
     }
     __syncthreads();
+    clk.mark(BPH_FINISH);
   }
   const int k = st.i;
   int status = st.status == 0 ? RBRP_OK : RBRP_ERR_NUMERIC;
@@ -618,6 +1036,7 @@ __device__ void solve_problem(BatchSmem<BB>& sm, const rbrp_batch_problem& pr, i
     res->draws = st.draws;
   }
   __syncthreads();
+  clk.mark(BPH_TSOLVE);
 }
 
 template <int BB>
@@ -628,6 +1047,7 @@ k_rbrp_batched(const rbrp_batch_problem* __restrict__ probs, const int* __restri
   BatchSmem<BB>& sm = *reinterpret_cast<BatchSmem<BB>*>(batch_smem);
   __shared__ int s_q;
   unsigned char* slot = args.slots + (size_t)blockIdx.x * (size_t)args.slot_bytes;
+  if (threadIdx.x < BPH_N) sm.pacc[threadIdx.x] = 0ull;
   for (;;) {
     __syncthreads();
     if (threadIdx.x == 0) s_q = atomicAdd(queue, 1);
@@ -637,6 +1057,7 @@ k_rbrp_batched(const rbrp_batch_problem* __restrict__ probs, const int* __restri
     const int pid = order[q];
     solve_problem<BB>(sm, probs[pid], pid, slot, args, results + pid);
   }
+  if (args.prof && threadIdx.x < BPH_N) atomicAdd(args.prof + threadIdx.x, sm.pacc[threadIdx.x]);
 }
 
 }  // namespace
@@ -662,6 +1083,8 @@ struct BatchState {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool planned = false, ran = false;
   double ms_last = 0.0, ms_autotune = 0.0;
+  unsigned long long* d_prof = nullptr;  // per-phase cycle sums when profiling is on
+  bool profiling = false;
   std::map<std::vector<int64_t>, std::pair<int, int>> tuned;  // batch signature -> (b, CTAs per SM)
 };
 
@@ -765,6 +1188,7 @@ void batch_release(rbrp_handle h) {
   cudaFree(B->d_res);
   cudaFree(B->d_queue);
   cudaFree(B->slots);
+  cudaFree(B->d_prof);
   delete B;
   h->batch = nullptr;
 }
@@ -875,6 +1299,7 @@ rbrp_status rbrp_batch_plan(rbrp_handle h, int nprob, const rbrp_batch_problem* 
   B.args.sampler = p->sampler;
   B.args.kmax = p->kmax;
   B.args.compute_T = p->compute_T;
+  B.args.prof = B.profiling ? B.d_prof : nullptr;
   const SlotLayout L = slot_layout(B.probs, p->kmax, BATCH_MAXB);
   B.args.off_R = L.off_R;
   B.args.off_V = L.off_V;
@@ -1020,6 +1445,32 @@ rbrp_status rbrp_batch_get_info(rbrp_handle h, rbrp_batch_info* info) {
   info->ms_autotune = B.ms_autotune;
   info->workspace_bytes = B.slots_bytes;
   return RBRP_OK;
+}
+
+rbrp_status rbrp_batch_set_profiling(rbrp_handle h, int on) {
+  if (!h) return RBRP_ERR_INVALID_ARG;
+  if (!h->batch || !h->batch->planned) return set_error(h, RBRP_ERR_NOT_COMPUTED, "no batch planned");
+  BatchState& B = *h->batch;
+  DeviceGuard g(h->device);
+  if (on && !B.d_prof) {
+    rbrp_status s = cuda_check(h, cudaMalloc(&B.d_prof, sizeof(unsigned long long) * BPH_N), "cudaMalloc(profile)");
+    if (s != RBRP_OK) return s;
+  }
+  B.profiling = on != 0;
+  B.args.prof = B.profiling ? B.d_prof : nullptr;
+  drop_graph(B);  // the kernel arguments changed: capture again
+  if (B.profiling) return cuda_check(h, cudaMemset(B.d_prof, 0, sizeof(unsigned long long) * BPH_N), "profile reset");
+  return RBRP_OK;
+}
+
+rbrp_status rbrp_batch_get_phase_cycles(rbrp_handle h, double* cycles, int cap) {
+  if (!h || !cycles || cap < RBRP_BATCH_NPHASES) return RBRP_ERR_INVALID_ARG;
+  if (!h->batch || !h->batch->d_prof) return set_error(h, RBRP_ERR_NOT_COMPUTED, "batch profiling is off");
+  DeviceGuard g(h->device);
+  unsigned long long c[BPH_N];
+  rbrp_status s = cuda_check(h, cudaMemcpy(c, h->batch->d_prof, sizeof(c), cudaMemcpyDeviceToHost), "copy profile");
+  for (int q = 0; q < BPH_N; ++q) cycles[q] = (double)c[q];
+  return s;
 }
 
 rbrp_status rbrp_id_batched_f32(rbrp_handle h, int nprob, const rbrp_batch_problem* problems, const rbrp_params* p,

@@ -310,6 +310,17 @@ class Batch:
         return dict(b=inf.b, panel_cols=inf.panel_cols, ctas=inf.ctas, ctas_per_sm=inf.ctas_per_sm,
                     ms_last=inf.ms_last, ms_autotune=inf.ms_autotune, workspace_bytes=inf.workspace_bytes)
 
+    def set_profiling(self, on=True):
+        """In-kernel phase cycle counters (reset when switched on)."""
+        check(self.h.lib.rbrp_batch_set_profiling(self.h.h, int(bool(on))), self.h.h)
+
+    def phase_cycles(self):
+        """{phase: SM cycles summed over CTAs} accumulated since profiling was switched on."""
+        n = len(_lib.BATCH_PHASES)
+        buf = (ctypes.c_double * n)()
+        check(self.h.lib.rbrp_batch_get_phase_cycles(self.h.h, buf, n), self.h.h)
+        return dict(zip(_lib.BATCH_PHASES, list(buf)))
+
     def run(self, stream=None):
         """Enqueue the batch (one CUDA graph launch) on the current torch stream."""
         self.h._bind_stream(torch.cuda.current_stream(self.As[0].device) if stream is None else stream)
