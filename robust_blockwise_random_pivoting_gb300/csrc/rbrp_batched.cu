@@ -147,7 +147,7 @@ __device__ __forceinline__ int block_max_int(int v, int* sh) {
   return r;
 }
 
-// A warp's walk over one column, f(x) per entry: 16-byte loads (two in flight
+// A warp's walk over one column, f(x) per entry: 16-byte loads (four in flight
 // per lane) when the column is 16-byte aligned.  Both norm passes use it, so a
 // lane sees the same entries in the same order in each.
 template <typename F>
@@ -156,10 +156,12 @@ __device__ __forceinline__ void column_walk(const float* __restrict__ col, int m
     const float4* c4 = reinterpret_cast<const float4*>(col);
     const int m4 = m >> 2;
     int r = lane;
-    for (; r + 32 < m4; r += 64) {
-      const float4 a = c4[r], b = c4[r + 32];
+    for (; r + 96 < m4; r += 128) {
+      const float4 a = c4[r], b = c4[r + 32], c = c4[r + 64], d = c4[r + 96];
       f(a.x); f(a.y); f(a.z); f(a.w);
       f(b.x); f(b.y); f(b.z); f(b.w);
+      f(c.x); f(c.y); f(c.z); f(c.w);
+      f(d.x); f(d.y); f(d.z); f(d.w);
     }
     for (; r < m4; r += 32) {
       const float4 a = c4[r];
@@ -564,6 +566,9 @@ __device__ __forceinline__ void cp_async16(float* smem, const float* gmem, int s
   const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(sa), "l"(gmem), "r"(src_bytes) : "memory");
 }
+__device__ __forceinline__ void cp_async16_sa(unsigned sa, const float* gmem, int src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(sa), "l"(gmem), "r"(src_bytes) : "memory");
+}
 __device__ __forceinline__ void cp_async4(float* smem, const float* gmem, int src_bytes) {
   const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(sa), "l"(gmem), "r"(src_bytes) : "memory");
@@ -635,11 +640,13 @@ __device__ __forceinline__ void ring_issue(IssueState<CW>& is, int total, int ns
   if (is.t < total) {
     const int r = is.s * BROWS + 4 * lane;
     const int valid = max(0, min(4, m - r));
+    const int off = valid > 0 ? r : 0;
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(ring + (is.t % RING_D) * CW * BROWS + 4 * lane);
 #pragma unroll
     for (int j = 0; j < CW; ++j) {
       float* dst = ring + ((is.t % RING_D) * CW + j) * BROWS + 4 * lane;
       if (vec) {
-        cp_async16(dst, valid > 0 ? is.src[j] + r : is.src[j], 4 * valid);
+        cp_async16_sa(sa + j * BROWS * (unsigned)sizeof(float), is.src[j] + off, 4 * valid);
       } else {
 #pragma unroll
         for (int e = 0; e < 4; ++e) cp_async4(dst + e, e < valid ? is.src[j] + r + e : is.src[j], e < valid ? 4 : 0);
@@ -701,29 +708,33 @@ __device__ void project_update_resident(BatchSmem<BB>& sm, int m, int n, int i, 
   for (int g = 0; g < ngroups; ++g) {
     const int p = p_first + g * stride, nc = min(CW, n - p);
     // projection: W(a, j) = sum_r q_a(r) x_j(r), FP32 stage sums folded into double-float
-    float hi[16], lo[16];
+    // (FP32 sums of a lane's 8 rows, two stages, are folded at a time)
+    float hi[16], lo[16], c[16];
 #pragma unroll
-    for (int v = 0; v < 16; ++v) hi[v] = lo[v] = 0.f;
+    for (int v = 0; v < 16; ++v) hi[v] = lo[v] = c[v] = 0.f;
     for (int s = 0; s < nst; ++s, ++t) {
       ring_issue<CW>(is, total, nst, p_first, stride, n, m, first, vec, A, lda, perm, Ares, ld, ring);
       cp_async_wait<RING_D - 1>();
       float x[4][CW];
       fetch(t, x);
       const int r0 = s * BROWS + 4 * lane;
+      const bool fold = (s & 1) || s == nst - 1;
 #pragma unroll
       for (int a = 0; a < KA; ++a) {
         if (a < kept) {
           const float4 q4 = *reinterpret_cast<const float4*>(qres + a * ldq + r0);
           const float q[4] = {q4.x, q4.y, q4.z, q4.w};
-          float c[CW];
-#pragma unroll
-          for (int j = 0; j < CW; ++j) c[j] = 0.f;
 #pragma unroll
           for (int u = 0; u < 4; ++u)
 #pragma unroll
-            for (int j = 0; j < CW; ++j) c[j] = fmaf(q[u], x[u][j], c[j]);
+            for (int j = 0; j < CW; ++j) c[a * CW + j] = fmaf(q[u], x[u][j], c[a * CW + j]);
+          if (fold) {
 #pragma unroll
-          for (int j = 0; j < CW; ++j) fold_two_sum(hi[a * CW + j], lo[a * CW + j], c[j]);
+            for (int j = 0; j < CW; ++j) {
+              fold_two_sum(hi[a * CW + j], lo[a * CW + j], c[a * CW + j]);
+              c[a * CW + j] = 0.f;
+            }
+          }
         }
       }
     }
