@@ -1,16 +1,26 @@
 #!/usr/bin/env python
 """Benchmark of the GB300 adaptive RBRP column ID (one JSON line on stdout).
 
-Workload (default ``snn16k``): the sparse non-negative low-rank-plus-tail
-matrix A = sum_{j<=100} (10/j) x_j y_j^T + sum_{100<j<=2000} (1/j) x_j y_j^T,
-16384 x 16384, x_j, y_j i.i.d. with density 0.02 and Uniform[0,1] nonzeros,
-stored dense FP32 (FP64 copy for the plain form and the error check);
-b = 64, squared relative tolerance 1e-12 (relative Frobenius 1e-6), Philox
-seed = rank.  Seeded synthetic data stands in for the reference's generators.
+Default workload ``blocks4096`` (batched): 4096 off-diagonal blocks of a
+Gaussian kernel k(x, y) = exp(-|x - y|^2 / (2 * 0.5^2)) between clusters of
+3-D points uniform in unit cubes whose centres are 2 to 8 apart, m and n
+log-uniform in [64, 2048], FP32 storage (each block scaled by its largest
+entry, which a column ID is invariant to), squared relative tolerance 1e-8
+(relative Frobenius 1e-4), block size b chosen by the library's autotuner,
+Philox key = rank * 4096 + problem.  A step is one persistent launch (a CUDA
+graph) that computes all 4096 IDs (S, T, k, error estimate), so ``value`` is
+matrices/s.  The inputs (5.4 GB) are larger than L2: no flush is needed.
+The plain FP64 and FP32 one-launch-per-matrix forms are timed on a seeded
+random subset of 64 of the same blocks, and the 16384^2 single-matrix ID
+time of the ``snn16k`` workload is reported beside the line.
 
-A step is one complete adaptive ID of the matrix (norms, sampling, panels,
-projections, stop, T = R11^{-1} R12), so ``value`` is matrices/s.  The matrix
-(1 GiB) is larger than L2, so no flush is needed between steps.
+Single-matrix workloads (``--workload snn16k`` ...): the sparse non-negative
+low-rank-plus-tail matrix A = sum_{j<=100} (10/j) x_j y_j^T + sum_{100<j<=2000}
+(1/j) x_j y_j^T, x_j, y_j i.i.d. with density 0.02 and Uniform[0,1] nonzeros,
+stored dense FP32 (FP64 copy for the plain form and the error check); b = 64,
+squared relative tolerance 1e-12 (relative Frobenius 1e-6).  A step is one
+complete adaptive ID of the matrix.  Seeded synthetic data stands in for the
+reference's generators throughout.
 """
 import argparse
 import json
@@ -29,6 +39,7 @@ sys.path.insert(0, ROOT)
 METRIC = "RBRP matrices/s & ID time at equal rel err, mixed+batched vs plain FP64"
 
 WORKLOADS = {
+    "blocks4096": dict(kind="blocks", nblocks=4096, lo=64, hi=2048, lengthscale=0.5, b=0, tol=1e-8),
     "snn16k": dict(kind="snn", m=16384, n=16384, r=2000, r1=100, amp=10.0, density=0.02, b=64, tol=1e-12),
     "snn8k": dict(kind="snn", m=8192, n=8192, r=2000, r1=100, amp=10.0, density=0.02, b=64, tol=1e-12),
     "snn4k": dict(kind="snn", m=4096, n=4096, r=2000, r1=100, amp=10.0, density=0.02, b=64, tol=1e-12),
@@ -37,6 +48,10 @@ WORKLOADS = {
 
 
 def describe(name, wl):
+    if wl["kind"] == "blocks":
+        return (f"{name}: {wl['nblocks']} Gaussian-kernel blocks (l={wl['lengthscale']}, 3-D unit-cube clusters "
+                f"2-8 apart), m, n log-uniform in [{wl['lo']}, {wl['hi']}], FP32 storage scaled by each block's "
+                f"max, squared tol {wl['tol']:g} (rel. Frobenius {np.sqrt(wl['tol']):g}), b autotuned")
     if wl["kind"] == "snn":
         return (f"{name}: SNN {wl['m']}x{wl['n']} (2000 rank-one terms, density {wl['density']}), FP32 storage, "
                 f"b={wl['b']}, squared tol {wl['tol']:g} (rel. Frobenius {np.sqrt(wl['tol']):g})")
@@ -194,111 +209,120 @@ def run_reference(args, wl, name):
     print(json.dumps(line))
 
 
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
-    ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="snn16k", choices=sorted(WORKLOADS))
-    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison")
-    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
-    ap.add_argument("--no-e2e", action="store_true")
-    args = ap.parse_args()
-    wl = WORKLOADS[args.workload]
-    if args.impl == "reference":
-        run_reference(args, wl, args.workload)
-        return
+class Ctx:
+    """Process / device context shared by the bench legs."""
 
-    import torch
-    import torch.distributed as dist
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    device = torch.device("cuda", local)
-    if world > 1:
-        dist.init_process_group("nccl", device_id=device)
+    def __init__(self, args):
+        import torch
+        import torch.distributed as dist
+        self.torch, self.dist = torch, dist
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        torch.cuda.set_device(self.local)
+        self.device = torch.device("cuda", self.local)
+        if self.world > 1:
+            dist.init_process_group("nccl", device_id=self.device)
+        self.stream = torch.cuda.current_stream(self.device)
+        self.uuid = None
+        try:
+            self.uuid = "GPU-" + str(torch.cuda.get_device_properties(self.local).uuid)
+        except Exception:
+            pass
+        self.peaks = {}
+        try:
+            self.peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        except OSError:
+            pass
 
-    def barrier():
-        if world > 1:
-            dist.barrier()
+    def barrier(self):
+        if self.world > 1:
+            self.dist.barrier()
 
+    def max_over_ranks(self, x):
+        t = self.torch.tensor([x], device=self.device, dtype=self.torch.float64)
+        if self.world > 1:
+            self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.dist.destroy_process_group()
+
+
+def traffic_from_profile(name):
+    """DRAM bytes per launch from the committed ncu summary of this workload (or None)."""
+    path = os.path.join(ROOT, "profiles", name)
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+def run_single(args, wl, name, ctx, light=False):
+    """One adaptive ID per step of one matrix per rank; returns the JSON line (dict)."""
+    torch = ctx.torch
     from robust_blockwise_random_pivoting_gb300.rbrp import Handle
-    seed = rank
-    A64, A32 = make_matrix(wl, seed, torch, device)
+    seed = ctx.rank
+    A64, A32 = make_matrix(wl, seed, torch, ctx.device)
     m, n = A32.shape
-    h = Handle(local)
-    stream = torch.cuda.current_stream(device)
+    h = Handle(ctx.local)
+    stream = ctx.stream
     mixed = wl["kind"] == "snn"
     A = A32 if mixed else A64
     kw = dict(b=wl["b"], tol=wl["tol"], seed=seed)
+    warmup, steps = (2, 2) if light else (args.warmup, args.steps)
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         r = h.column_id(A, **kw)
     h.set_profiling(True)
     h.reset_phase_stats()
-    uuid = None
-    try:
-        uuid = "GPU-" + str(torch.cuda.get_device_properties(local).uuid)
-    except Exception:
-        pass
-    barrier()
+    ctx.barrier()
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(uuid) as clk:
+    with ClockSampler(ctx.uuid) as clk:
         ev0.record(stream)
-        for _ in range(args.steps):
+        for _ in range(steps):
             r = h.column_id(A, **kw)
         ev1.record(stream)
         torch.cuda.synchronize()
-    barrier()
+    ctx.barrier()
     ms = ev0.elapsed_time(ev1)
     stats = h.phase_stats()
     h.set_profiling(False)
     clocks = clk.summary()
-    t = torch.tensor([ms], device=device, dtype=torch.float64)
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_max = float(t.item())
-    value = world * args.steps / (ms_max * 1e-3)
+    ms_max = ctx.max_over_ranks(ms)
+    value = ctx.world * steps / (ms_max * 1e-3)
 
-    # quality of the last timed result, against the FP64 matrix
     k = r.k
     rel_err = h.id_error(A)             # squared, on the matrix the ID was computed for
-    perm = r.perm.clone()
-    T = r.T
 
-    # end to end through the host-buffer entry point (pinned host A, perm and T out)
     e2e = None
-    if not args.no_e2e:
+    if not (args.no_e2e or light):
         hostA = torch.empty((n, m), dtype=A.dtype, pin_memory=True).t()
         hostA.copy_(A)
         kcap = min(m, n)
         T_out = torch.empty(kcap * n, dtype=torch.float64, pin_memory=True)
         perm_out = torch.empty(n, dtype=torch.int32, pin_memory=True)
-        for _ in range(1):
-            h.column_id_host(hostA, perm_out=perm_out, T_out=T_out, **kw)
-        barrier()
+        h.column_id_host(hostA, perm_out=perm_out, T_out=T_out, **kw)
+        ctx.barrier()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        for _ in range(args.steps):
+        for _ in range(steps):
             k_h, _, _, _ = h.column_id_host(hostA, perm_out=perm_out, T_out=T_out, **kw)
         torch.cuda.synchronize()
-        dt = time.perf_counter() - t0
-        tt = torch.tensor([dt], device=device, dtype=torch.float64)
-        if world > 1:
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        dt = float(tt.item())
-        e2e = {"value": world * args.steps / dt, "unit": "matrices/s",
+        dt = ctx.max_over_ranks(time.perf_counter() - t0)
+        e2e = {"value": ctx.world * steps / dt, "unit": "matrices/s",
                "h2d_bytes_per_step": int(m * n * A.element_size()),
                "d2h_bytes_per_step": int(4 * n + 8 * k_h * (n - k_h))}
         del hostA, T_out
 
-    # plain FP64 single-launch form on the same matrix (the comparison the metric names)
     plain = None
     if mixed and not args.no_plain:
-        hp = Handle(local)
+        hp = Handle(ctx.local)
         hp.column_id(A64, **kw)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -311,13 +335,7 @@ def main():
                  "rel_err": float(np.sqrt(max(hp.id_error(A64), 0.0)))}
         hp.close()
 
-    # dominant phase and its roofline (algorithmic bytes over measured launch time)
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except OSError:
-        pass
-    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    hbm_peak = ctx.peaks.get("hbm_gbs", 6800.0)
     dom = max(("project", "update", "tsolve", "cgs", "panel", "sample", "norms", "finish"),
               key=lambda q: stats[q]["ms"])
     st = stats[dom]
@@ -327,42 +345,274 @@ def main():
     roofline = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved / hbm_peak, "traffic": None,
                 "flops_per_s": st["flops"] / (st["ms"] * 1e-3) if st["ms"] else None,
-                "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s"}
-    phases = {q: {"ms_per_step": v["ms"] / args.steps, "launches_per_step": v["launches"] / args.steps,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if ctx.peaks else "fallback 6.8 TB/s"}
+    phases = {q: {"ms_per_step": v["ms"] / steps, "launches_per_step": v["launches"] / steps,
                   "GBps": (v["bytes"] / (v["ms"] * 1e-3) / 1e9) if v["ms"] else None,
                   "TFLOPs": (v["flops"] / (v["ms"] * 1e-3) / 1e12) if v["ms"] else None}
               for q, v in stats.items()}
     gpu_launches = int(sum(v["launches"] for v in stats.values()))
 
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu:
+    if ctx.rank == 0 and ctx.world == 1 and not (args.no_cpu or light):
         A_host = A64.cpu().numpy()
         kmax_sample = 2 * wl["b"]
         dt, f, o = cpu_sample(A_host, wl, seed, kmax_sample)
-        f_full = sum(v["flops"] for v in stats.values()) / args.steps
+        f_full = sum(v["flops"] for v in stats.values()) / steps
         cpu = {"value": (f / dt) / f_full, "unit": "matrices/s", "cores": threads(), "kind": "port",
                "sample": f"oracle port (numpy/scipy FP64) of the reference's blocked_rpid on the first "
                          f"{kmax_sample} ranks of the same matrix ({dt:.1f} s); matrices/s extrapolated by the "
                          f"algorithmic flop model to the GPU run's trace (k={k}, {r.nblocks} blocks)"}
-
-    if rank == 0:
-        line = {
-            "metric": METRIC, "value": value, "unit": "matrices/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if mixed else "f64",
-            "data": "synthetic (seeded Philox), one independent matrix per rank",
-            "config": {"workload": describe(args.workload, wl), "precision": "mixed" if mixed else "f64",
-                       "k": k, "blocks": r.nblocks, "id_time_ms": ms_max / args.steps,
-                       "rel_err": float(np.sqrt(max(rel_err, 0.0))), "err_est_sq": r.err_est,
-                       "plain_f64": plain, "parallelism": f"replicas x{world}",
-                       "l2": "no flush: the 1 GiB input is larger than L2", "phases": phases},
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
-            "gpu_launches": gpu_launches,
-        }
-        print(json.dumps(line))
     h.close()
-    if world > 1:
-        dist.destroy_process_group()
+    del A64, A32
+    return {
+        "metric": METRIC, "value": value, "unit": "matrices/s", "n_gpus": ctx.world, "steps": steps,
+        "warmup": warmup, "ms_per_step": ms_max / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if mixed else "f64",
+        "data": "synthetic (seeded Philox), one independent matrix per rank",
+        "config": {"workload": describe(name, wl), "precision": "mixed" if mixed else "f64",
+                   "k": k, "blocks": r.nblocks, "id_time_ms": ms_max / steps,
+                   "rel_err": float(np.sqrt(max(rel_err, 0.0))), "err_est_sq": r.err_est,
+                   "plain_f64": plain, "parallelism": f"replicas x{ctx.world}",
+                   "l2": "no flush: the 1 GiB input is larger than L2", "phases": phases},
+        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+        "gpu_launches": gpu_launches,
+    }
+
+
+def block_sample_ids(nblocks, count, seed):
+    return np.sort(np.random.default_rng(1000 + seed).choice(nblocks, size=min(count, nblocks), replace=False))
+
+
+def batched_cpu_sample(wl, seed, b, count):
+    """The oracle port on a seeded sample of the workload's blocks: (seconds, count, description)."""
+    from oracle import rbrp_column_id
+    from robust_blockwise_random_pivoting_gb300 import workloads as W
+    shapes = W.kernel_block_shapes(wl["nblocks"], wl["lo"], wl["hi"], seed)
+    ids = block_sample_ids(wl["nblocks"], count, seed)
+    mats = [W.kernel_block_scaled(int(shapes[q][0]), int(shapes[q][1]), q, wl["lengthscale"], seed).astype(np.float64)
+            for q in ids]
+    t0 = time.perf_counter()
+    for q, A in zip(ids, mats):
+        rbrp_column_id(A, b, tol=wl["tol"], seed=seed * wl["nblocks"] + int(q))
+    dt = time.perf_counter() - t0
+    return dt, len(ids), (f"oracle port (numpy/scipy FP64) of the reference's blocked_rpid on a seeded sample of "
+                          f"{len(ids)} of the {wl['nblocks']} blocks (same shape distribution), b={b}; "
+                          f"matrices/s = sample size / time")
+
+
+def run_batched(args, wl, name, ctx):
+    """All blocks of the workload in one persistent launch per step; returns the JSON line (dict)."""
+    torch = ctx.torch
+    from robust_blockwise_random_pivoting_gb300 import workloads as W
+    from robust_blockwise_random_pivoting_gb300.rbrp import Batch, Handle
+    seed = ctx.rank
+    nb = wl["nblocks"]
+    blocks = W.kernel_blocks_device(nb, wl["lo"], wl["hi"], wl["lengthscale"], seed, ctx.device)
+    shapes = [tuple(A.shape) for A in blocks]
+    # all blocks packed in one device buffer (column major each), also the target of the e2e copy
+    sizes = np.array([m * n for m, n in shapes], np.int64)
+    offs = np.concatenate([[0], np.cumsum(sizes)])
+    pack = torch.empty(int(offs[-1]), dtype=torch.float32, device=ctx.device)
+    As = []
+    for q, ((m, n), A) in enumerate(zip(shapes, blocks)):
+        v = pack[int(offs[q]): int(offs[q + 1])].view(n, m).t()
+        v.copy_(A)
+        As.append(v)
+    del blocks
+    h = Handle(ctx.local)
+    t_cap = 64
+    t_plan = time.perf_counter()
+    bt = Batch(h, As, b=wl["b"], tol=wl["tol"], seed=seed * nb, t_rank_cap=t_cap)
+    t_plan = time.perf_counter() - t_plan
+    info = bt.info()
+    stream = ctx.stream
+    for _ in range(args.warmup):
+        bt.run()
+        res = bt.results()
+    ctx.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(ctx.uuid) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            bt.run(stream)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    ctx.barrier()
+    ms = ev0.elapsed_time(ev1)
+    clocks = clk.summary()
+    res = bt.results()
+    ms_max = ctx.max_over_ranks(ms)
+    value = ctx.world * args.steps * nb / (ms_max * 1e-3)
+    ms_launch = ms / args.steps
+
+    # quality: relative Frobenius error of every ID against the block in FP64 (device GEMMs)
+    rel = np.zeros(nb)
+    for q, A in enumerate(As):
+        k = int(res.k[q])
+        m, n = shapes[q]
+        if k == 0 or k == n or res.Ts[q] is None:
+            rel[q] = 0.0 if k == n else (1.0 if k == 0 else np.nan)
+            continue
+        p = res.perms[q].long()
+        A64 = A.double()
+        E = A64[:, p[k:]] - A64[:, p[:k]] @ res.Ts[q]
+        rel[q] = float(torch.linalg.norm(E) / torch.linalg.norm(A64))
+    ok = int((res.status == 0).sum())
+
+    # one profiled launch: in-kernel phase cycle shares
+    bt.set_profiling(True)
+    bt.run()
+    bt.results()
+    cyc = bt.phase_cycles()
+    bt.set_profiling(False)
+    tot = sum(cyc.values()) or 1.0
+    phases = {q: round(v / tot, 4) for q, v in cyc.items()}
+
+    alg_bytes = float(res.alg_bytes.sum())
+    alg_flops = float(res.alg_flops.sum())
+    hbm_peak = ctx.peaks.get("hbm_gbs", 6800.0)
+    achieved = alg_bytes / (ms_launch * 1e-3) / 1e9
+    roofline = {"kernel": "k_rbrp_batched", "bound": "hbm", "achieved": achieved, "peak": hbm_peak,
+                "unit": "GB/s", "frac": achieved / hbm_peak,
+                "traffic": traffic_from_profile("k_rbrp_batched_blocks4096.md"),
+                "alg_bytes_per_launch": alg_bytes, "flops_per_s": alg_flops / (ms_launch * 1e-3),
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if ctx.peaks else "fallback 6.8 TB/s"}
+
+    # one launch per matrix: plain FP64 and FP32 mixed, on a seeded subset of the same blocks
+    single = None
+    if not args.no_plain:
+        ids = block_sample_ids(nb, 64, seed)
+        hs = Handle(ctx.local)
+        single = {"subset": len(ids), "b": info["b"]}
+        for label, dt in (("plain_f64", torch.float64), ("f32_one_launch", torch.float32)):
+            sub = [As[q].to(dt).t().contiguous().t() for q in ids]
+            kw = dict(b=info["b"], tol=wl["tol"])
+            hs.column_id(sub[0], seed=0, **kw)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            errs, ks = [], []
+            for j, (q, A) in enumerate(zip(ids, sub)):
+                r = hs.column_id(A, seed=seed * nb + int(q), **kw)
+                ks.append(r.k)
+            torch.cuda.synchronize()
+            dt_s = time.perf_counter() - t0
+            for A, q in zip(sub, ids):
+                r = hs.column_id(A, seed=seed * nb + int(q), **kw)
+                errs.append(float(np.sqrt(max(hs.id_error(A), 0.0))))
+            single[label] = {"matrices_per_s": len(ids) / dt_s, "ms_per_matrix": 1e3 * dt_s / len(ids),
+                             "k_mean": float(np.mean(ks)), "rel_err_max": float(np.max(errs))}
+            del sub
+        single["batched_same_subset"] = {"k_mean": float(res.k[ids].mean()), "rel_err_max": float(rel[ids].max())}
+        hs.close()
+
+    # end to end: pinned host blocks in, one H2D copy, the graph launch, perms + T + results out
+    e2e = None
+    if not args.no_e2e:
+        host = torch.empty(pack.numel(), dtype=torch.float32, pin_memory=True)
+        host.copy_(pack)
+        perm_h = torch.empty(bt.perm_buf.numel(), dtype=torch.int32, pin_memory=True)
+        T_h = torch.empty(bt.T_buf.numel(), dtype=torch.float64, pin_memory=True)
+
+        def step():
+            pack.copy_(host, non_blocking=True)
+            bt.run()
+            perm_h.copy_(bt.perm_buf, non_blocking=True)
+            T_h.copy_(bt.T_buf, non_blocking=True)
+            return bt.results()
+        step()
+        ctx.barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            step()
+        torch.cuda.synchronize()
+        dt = ctx.max_over_ranks(time.perf_counter() - t0)
+        e2e = {"value": ctx.world * args.steps * nb / dt, "unit": "matrices/s",
+               "h2d_bytes_per_step": int(pack.numel() * 4),
+               "d2h_bytes_per_step": int(perm_h.numel() * 4 + T_h.numel() * 8 + nb * 56)}
+        del host, perm_h, T_h
+
+    cpu = None
+    if ctx.rank == 0 and ctx.world == 1 and not args.no_cpu:
+        dt, cnt, desc = batched_cpu_sample(wl, seed, info["b"], 256)
+        cpu = {"value": cnt / dt, "unit": "matrices/s", "cores": threads(), "kind": "port", "sample": desc}
+
+    single_matrix = None
+    if not args.no_single and ctx.world == 1:
+        sl = run_single(args, WORKLOADS["snn16k"], "snn16k", ctx, light=True)
+        single_matrix = {"workload": sl["config"]["workload"], "id_time_ms": sl["config"]["id_time_ms"],
+                         "k": sl["config"]["k"], "rel_err": sl["config"]["rel_err"],
+                         "plain_f64": sl["config"]["plain_f64"], "roofline": sl["roofline"],
+                         "clocks": sl["clocks"], "timing": "2 warm-up + 2 timed IDs"}
+    h.close()
+    return {
+        "metric": METRIC, "value": value, "unit": "matrices/s", "n_gpus": ctx.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic (seeded Philox points), one independent batch per rank",
+        "config": {"workload": describe(name, wl), "precision": "mixed", "problems": nb,
+                   "elements": int(offs[-1]), "b": info["b"], "ctas": info["ctas"],
+                   "ctas_per_sm": info["ctas_per_sm"], "plan_s": t_plan, "autotune_ms": info["ms_autotune"],
+                   "k_mean": float(res.k.mean()), "k_max": int(res.k.max()), "blocks_mean": float(res.nblocks.mean()),
+                   "status_ok": ok, "rel_err_max": float(np.nanmax(rel)), "rel_err_mean": float(np.nanmean(rel)),
+                   "one_launch_per_matrix": single, "single_matrix_snn16k": single_matrix,
+                   "parallelism": f"replicas x{ctx.world}", "launch": "one CUDA graph (queue reset + kernel)",
+                   "l2": "no flush: the 5.4 GB of inputs are larger than L2", "phase_cycle_share": phases},
+        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+        "gpu_launches": args.steps,
+    }
+
+
+def run_reference_batched(args, wl, name):
+    """Reference arm for the batched workload: the oracle port on a bounded sample of blocks per step."""
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    b = 16
+    times, counts = [], []
+    for s in range(args.warmup + args.steps):
+        dt, cnt, desc = batched_cpu_sample(wl, 0, b, 64)
+        if s >= args.warmup:
+            times.append(dt)
+            counts.append(cnt)
+    value = sum(counts) / sum(times)
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "matrices/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded Philox points)", "config": {"workload": describe(name, wl)},
+        "cpu_baseline": {"value": value, "unit": "matrices/s", "cores": threads(), "kind": "port", "sample": desc},
+        "e2e": {"value": value, "unit": "matrices/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="blocks4096", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-plain", action="store_true", help="skip the one-launch-per-matrix comparisons")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-single", action="store_true", help="skip the snn16k single-matrix figure")
+    args = ap.parse_args()
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        if wl["kind"] == "blocks":
+            run_reference_batched(args, wl, args.workload)
+        else:
+            run_reference(args, wl, args.workload)
+        return
+    ctx = Ctx(args)
+    if wl["kind"] == "blocks":
+        line = run_batched(args, wl, args.workload, ctx)
+    else:
+        line = run_single(args, wl, args.workload, ctx)
+    if ctx.rank == 0:
+        print(json.dumps(line))
+    ctx.close()
 
 
 if __name__ == "__main__":

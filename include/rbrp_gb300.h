@@ -178,6 +178,9 @@ typedef struct {
   double res0;         /* ||A||_F^2 */
   double err_est;      /* squared relative residual at the stop */
   uint64_t draws;      /* uniforms consumed from the np-compat stream */
+  double alg_bytes;    /* algorithmic HBM bytes: 4 [m n + sum_t m n_t + sum_t m bs_t]
+                          (n_t columns left after block t, bs_t columns sampled) */
+  double alg_flops;    /* algorithmic flops: 2 m n + sum_t [2 m n_t b_t + 4 m bs_t^2] + k^2 (n-k) */
 } rbrp_batch_result;
 
 typedef struct {

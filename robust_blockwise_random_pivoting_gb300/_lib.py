@@ -52,7 +52,8 @@ class BatchProblem(ctypes.Structure):
 
 class BatchResult(ctypes.Structure):
     _fields_ = [("k", c_int), ("nblocks", c_int), ("status", c_int), ("attempts", c_int),
-                ("res0", c_double), ("err_est", c_double), ("draws", c_uint64)]
+                ("res0", c_double), ("err_est", c_double), ("draws", c_uint64), ("alg_bytes", c_double),
+                ("alg_flops", c_double)]
 
 
 class BatchInfo(ctypes.Structure):

@@ -960,6 +960,7 @@ __device__ void solve_problem(BatchSmem<BB>& sm, const rbrp_batch_problem& pr, i
   clk.mark(BPH_NORMS);
   const int max_attempts = 4 * kcap + 64;
   const uint64_t seed = args.seed + (uint64_t)pid;
+  double alg_bytes = 4.0 * m * n, alg_flops = 2.0 * m * n;  // thread 0's tally of the algorithmic work
   for (;;) {
     if (st.done) break;
     if (st.attempts >= max_attempts) {
@@ -1013,6 +1014,9 @@ __device__ void solve_problem(BatchSmem<BB>& sm, const rbrp_batch_problem& pr, i
     s = block_sum(s, sm.red_d);
     c = block_sum(c, sm.red_i);
     if (tid == 0) {
+      const double nt = (double)(n - i - kept), dm = (double)m;
+      alg_bytes += 4.0 * dm * (nt + bss);
+      alg_flops += 2.0 * dm * nt * kept + 4.0 * dm * bss * bss;
       st.attempts += 1;
       st.residual = s;
       st.nnz_rem = c;
@@ -1045,6 +1049,8 @@ __device__ void solve_problem(BatchSmem<BB>& sm, const rbrp_batch_problem& pr, i
     res->res0 = emax == INT_MIN ? 0.0 : ldexp(st.res0, 2 * emax);
     res->err_est = st.res0 > 0.0 ? st.residual / st.res0 : 0.0;
     res->draws = st.draws;
+    res->alg_bytes = alg_bytes;
+    res->alg_flops = alg_flops + (double)k * k * (n - k);
   }
   __syncthreads();
   clk.mark(BPH_TSOLVE);

@@ -250,6 +250,8 @@ class BatchIDResult:
     res0: np.ndarray
     err_est: np.ndarray
     draws: np.ndarray
+    alg_bytes: np.ndarray  # algorithmic HBM bytes per problem (minimum traffic)
+    alg_flops: np.ndarray  # algorithmic flops per problem
     perms: list          # (n_q,) int32 CUDA views: S = perm[:k], rd = perm[k:]
     Ts: list             # (k_q, n_q - k_q) FP64 column-major CUDA views, or None
     ms: float            # device time of the run (CUDA events), ms
@@ -344,7 +346,8 @@ class Batch:
                 Ts.append(None)
         return BatchIDResult(k=k, nblocks=f("nblocks", np.int64), status=status, attempts=f("attempts", np.int64),
                              res0=f("res0", np.float64), err_est=f("err_est", np.float64),
-                             draws=f("draws", np.uint64), perms=perms, Ts=Ts, ms=self.info()["ms_last"])
+                             draws=f("draws", np.uint64), alg_bytes=f("alg_bytes", np.float64),
+                             alg_flops=f("alg_flops", np.float64), perms=perms, Ts=Ts, ms=self.info()["ms_last"])
 
 
 def batched_column_id(As, b=0, tol=1e-8, kmax=None, seed=0, sampler="np", tol_loc=None, compute_T=True,

@@ -58,3 +58,31 @@ def test_cpp_dropin_header_compiles(tmp_path):
                    '  return (int)rbrp_gb300::RBRP(4, 4, A, 2, r, e, t, tt, fl); }\n')
     out = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", inc, str(src)], capture_output=True, text=True)
     assert out.returncode == 0, out.stderr
+
+
+def test_struct_sizes_match_c(tmp_path):
+    """ctypes mirrors of the ABI structs have the C compiler's sizes and field offsets."""
+    import os
+    inc = os.path.dirname(_lib.HEADER)
+    src = tmp_path / "sz.c"
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "rbrp_gb300.h"\n'
+                   'int main(void) { printf("%zu %zu %zu %zu %zu %zu %zu\\n", sizeof(rbrp_params), '
+                   'sizeof(rbrp_result), sizeof(rbrp_batch_problem), sizeof(rbrp_batch_result), '
+                   'sizeof(rbrp_batch_info), offsetof(rbrp_batch_problem, T_cap), '
+                   'offsetof(rbrp_batch_result, alg_flops)); return 0; }\n')
+    exe = tmp_path / "sz"
+    out = subprocess.run(["gcc", "-I", inc, str(src), "-o", str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, out.stderr
+    sizes = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()]
+    assert sizes == [ctypes.sizeof(_lib.Params), ctypes.sizeof(_lib.Result), ctypes.sizeof(_lib.BatchProblem),
+                     ctypes.sizeof(_lib.BatchResult), ctypes.sizeof(_lib.BatchInfo),
+                     _lib.BatchProblem.T_cap.offset, _lib.BatchResult.alg_flops.offset]
+
+
+def test_batch_entry_points_reject_bad_arguments_without_gpu(rbrp_lib):
+    assert rbrp_lib.rbrp_batch_plan(None, 1, None, None) == 1
+    assert rbrp_lib.rbrp_batch_run(None) == 1
+    assert rbrp_lib.rbrp_batch_results(None, None, 0) == 1
+    info = _lib.BatchInfo()
+    assert rbrp_lib.rbrp_batch_get_info(None, ctypes.byref(info)) == 1
+    assert rbrp_lib.rbrp_batch_set_profiling(None, 1) == 1
