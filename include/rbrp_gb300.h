@@ -105,6 +105,28 @@ rbrp_status rbrp_id_f64(rbrp_handle h, int m, int n, const double* dA, int64_t l
 rbrp_status rbrp_id_f32(rbrp_handle h, int m, int n, const float* dA, int64_t lda,
                         const rbrp_params* p, int* dPerm, rbrp_result* out);
 
+/* Fixed-skeleton ID (no counterpart in the reference, which always pivots):
+ * the given skeleton dS (k distinct device column indices) is taken b columns
+ * at a time, in list order, through the same panels, swaps and updates as an
+ * adaptive run (no tolerance, every nonzero pivot kept), so perm[:k] holds S
+ * (reordered by the panel pivots), perm[k:] the rest, and T = R11^{-1} R12 =
+ * A(:, S)^+ A(:, rd) as in an adaptive run (rbrp_copy_T).  The forward of the
+ * differentiable fixed-skeleton ID; synchronises the handle's stream. */
+rbrp_status rbrp_fixed_id_f32(rbrp_handle h, int m, int n, const float* dA, int64_t lda, const int* dS,
+                              int k, int b, int* dPerm, rbrp_result* out);
+rbrp_status rbrp_fixed_id_f64(rbrp_handle h, int m, int n, const double* dA, int64_t lda, const int* dS,
+                              int k, int b, int* dPerm, rbrp_result* out);
+
+/* Loss and gradient of the fixed-skeleton ID of the last FP32 run
+ * (rbrp_fixed_id_f32 on the same dA): with C = A(:, S), B = A(:, rd),
+ * T = C^+ B, w = dW(rd) (dW has n entries, those at S are ignored),
+ *   L = ||B - C T||_F^2 + ||T w||^2  -> *loss (host),
+ * and, when dG != NULL, dG (m x n, ldg >= m) = scale * dL/dA, written in full.
+ * FP32 GEMM kernels (double-float sums and triangular solve); synchronises the
+ * handle's stream.  No counterpart in the reference. */
+rbrp_status rbrp_fixed_id_adjoint_f32(rbrp_handle h, int m, int n, const float* dA, int64_t lda,
+                                      const float* dW, float scale, float* dG, int64_t ldg, double* loss);
+
 /* T (k x (n-k), column major) of the last run, into a device buffer with ldt >= k. */
 rbrp_status rbrp_copy_T(rbrp_handle h, double* dT, int64_t ldt);
 /* Device pointer of T of the last run (ld = k), valid until the next run. */

@@ -103,6 +103,12 @@ _SIGS = {
     "rbrp_set_tsolve_fp64": (c_int, [c_void_p, c_int]),
     "rbrp_id_error_f64_noalloc": (c_int, [c_int, c_int, c_void_p, c_int64, c_void_p, c_int, c_void_p, c_int64,
                                           c_double, c_void_p, c_void_p]),
+    "rbrp_fixed_id_f32": (c_int, [c_void_p, c_int, c_int, c_void_p, c_int64, c_void_p, c_int, c_int, c_void_p,
+                                  ctypes.POINTER(Result)]),
+    "rbrp_fixed_id_f64": (c_int, [c_void_p, c_int, c_int, c_void_p, c_int64, c_void_p, c_int, c_int, c_void_p,
+                                  ctypes.POINTER(Result)]),
+    "rbrp_fixed_id_adjoint_f32": (c_int, [c_void_p, c_int, c_int, c_void_p, c_int64, c_void_p, ctypes.c_float,
+                                          c_void_p, c_int64, ctypes.POINTER(c_double)]),
     "rbrp_batch_plan": (c_int, [c_void_p, c_int, ctypes.POINTER(BatchProblem), ctypes.POINTER(Params)]),
     "rbrp_batch_run": (c_int, [c_void_p]),
     "rbrp_batch_results": (c_int, [c_void_p, ctypes.POINTER(BatchResult), c_int]),

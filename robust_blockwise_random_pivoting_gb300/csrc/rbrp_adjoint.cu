@@ -1,0 +1,465 @@
+// rbrp_adjoint.cu - loss and adjoint of the fixed-skeleton interpolative
+// decomposition, FP32 kernels (no counterpart in the reference).
+//
+// With the skeleton S held fixed, C = A(:, S) (m x k), B = A(:, rd) (m x nc)
+// and T = C^+ B (the k x nc interpolation matrix of the last fixed-skeleton
+// run, T = R11^{-1} R12), the loss is
+//     L = ||E||_F^2 + ||T w||^2,   E = B - C T,   w = dW(rd).
+// Its gradient (T optimal for the first term, so only the second term sees
+// dT = -C^+ dC T + (C^T C)^{-1} dC^T E + C^+ dB), with u = T w and
+// z = (C^T C)^{-1} u = R11^{-1} R11^{-T} u:
+//     dL/dB = 2 E + 2 (C z) w^T
+//     dL/dC = -2 E T^T - 2 (C z) u^T + 2 (E w) z^T.
+// Nothing of the forward factorisation is stored: R11 and T come from the
+// handle's last run (the caller recomputes it for the backward), C and B are
+// read from A through perm.  The two products E = B - C T and E T^T are
+// 128 x 128-tiled FP32 GEMMs with the loss terms, E w and the rank-one terms
+// fused into their epilogues; z is a double-float triangular solve.
+#include <algorithm>
+#include <cmath>
+
+#include "rbrp_internal.h"
+#include "rbrp_df.cuh"
+
+namespace rbrp {
+namespace {
+
+constexpr int GT = 256;        // threads of a GEMM CTA
+constexpr int GTILE = 128;     // output tile edge
+constexpr int GK = 16;         // contraction chunk
+constexpr int PARTS = 16;      // split of the GEMV contractions
+
+// Tr[t * nc + c] = T[t + c * k] (row major copy) and Tc = FP32 T (column major);
+// wr[c] = W[perm[k + c]].
+__global__ void k_adj_prep(const double* __restrict__ T, int k, int nc, const float* __restrict__ W,
+                           const int* __restrict__ perm, float* __restrict__ Tr, float* __restrict__ Tc,
+                           float* __restrict__ wr) {
+  __shared__ float tile[32][33];
+  const int t0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8 threads
+  for (int q = ty; q < 32; q += 8) {
+    const int t = t0 + tx, c = c0 + q;
+    float v = 0.f;
+    if (t < k && c < nc) {
+      v = (float)T[t + (int64_t)c * k];
+      Tc[t + (int64_t)c * k] = v;
+    }
+    tile[q][tx] = v;
+  }
+  __syncthreads();
+  for (int q = ty; q < 32; q += 8) {
+    const int t = t0 + q, c = c0 + tx;
+    if (t < k && c < nc) Tr[(int64_t)t * nc + c] = tile[tx][q];
+  }
+  if (blockIdx.x == 0)
+    for (int c = c0 + threadIdx.x; c < min(nc, c0 + 32); c += blockDim.x) wr[c] = W[perm[k + c]];
+}
+
+// upart[p][t] = sum over columns c of part p of T[t, c] wr[c] (double-float, as float2)
+__global__ void k_adj_u(const float* __restrict__ Tc, int k, int nc, const float* __restrict__ wr,
+                        float2* __restrict__ upart) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int p = blockIdx.y, chunk = (nc + PARTS - 1) / PARTS;
+  const int cb = p * chunk, ce = min(nc, cb + chunk);
+  if (t >= k) return;
+  float hi = 0.f, lo = 0.f;
+  for (int c = cb; c < ce; ++c) {
+    const float prod = Tc[t + (int64_t)c * k] * wr[c];
+    const float e = fmaf(Tc[t + (int64_t)c * k], wr[c], -prod);
+    const float s = hi + prod, z = s - hi;
+    lo += ((hi - (s - z)) + (prod - z)) + e;
+    hi = s;
+  }
+  upart[(int64_t)p * k + t] = make_float2(hi, lo);
+}
+
+// out[i] = sum of the PARTS partials (fixed order), as float and (if out_df)
+// double-float.
+__global__ void k_adj_sum_parts(const float2* __restrict__ part, int len, float* __restrict__ out,
+                                float2* __restrict__ out_df) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= len) return;
+  dfl s = {part[i].x, part[i].y};
+  for (int p = 1; p < PARTS; ++p) {
+    const float2 v = part[(int64_t)p * len + i];
+    s = df_add(s, {v.x, v.y});
+  }
+  s = df_two_sum(s.hi, s.lo);
+  out[i] = s.hi;
+  if (out_df) out_df[i] = make_float2(s.hi, s.lo);
+}
+
+// out[i] = sum over p < nparts of part[p][i] (fixed order, double-float).
+__global__ void k_adj_sum_rows(const float2* __restrict__ part, int nparts, int len, float* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= len) return;
+  dfl s = {0.f, 0.f};
+  for (int p = 0; p < nparts; ++p) {
+    const float2 v = part[(int64_t)p * len + i];
+    s = df_add(s, {v.x, v.y});
+  }
+  out[i] = df_two_sum(s.hi, s.lo).hi;
+}
+
+// R11 (FP64, row major, ld ldr, upper) as double-float pairs, row major ld k.
+__global__ void k_adj_split_r(const double* __restrict__ R, int64_t ldr, int k, float2* __restrict__ Rdf) {
+  const int64_t total = (int64_t)k * k;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int a = (int)(idx / k), c = (int)(idx % k);
+    const double x = c >= a ? R[(int64_t)a * ldr + c] : 0.0;
+    const float hi = (float)x;
+    Rdf[idx] = make_float2(hi, (float)(x - (double)hi));
+  }
+}
+
+// z = R11^{-1} R11^{-T} u in double-float, one CTA: 32-wide diagonal blocks
+// solved by one thread, the remaining right-hand side updated by all threads.
+__global__ void __launch_bounds__(1024) k_adj_z(const float2* __restrict__ Rdf, int k, const float2* __restrict__ udf,
+                                                 float2* __restrict__ work, float* __restrict__ z) {
+  __shared__ dfl xb[32];
+  const int tid = threadIdx.x;
+  for (int i = tid; i < k; i += blockDim.x) work[i] = udf[i];
+  __syncthreads();
+  auto r_at = [&](int a, int c) { const float2 v = Rdf[(int64_t)a * k + c]; return dfl{v.x, v.y}; };
+  // forward: R11^T y = u (y overwrites work)
+  for (int j0 = 0; j0 < k; j0 += 32) {
+    const int jl = min(32, k - j0);
+    if (tid == 0) {
+      for (int jj = 0; jj < jl; ++jj) {
+        const float2 w0 = work[j0 + jj];
+        dfl v = {w0.x, w0.y};
+        for (int ii = 0; ii < jj; ++ii) v = df_fms(v, r_at(j0 + ii, j0 + jj), xb[ii]);
+        xb[jj] = df_mul(v, df_recip(r_at(j0 + jj, j0 + jj)));
+        work[j0 + jj] = make_float2(xb[jj].hi, xb[jj].lo);
+      }
+    }
+    __syncthreads();
+    for (int j = j0 + jl + tid; j < k; j += blockDim.x) {
+      const float2 w0 = work[j];
+      dfl v = {w0.x, w0.y};
+      for (int ii = 0; ii < jl; ++ii) v = df_fms(v, r_at(j0 + ii, j), xb[ii]);
+      work[j] = make_float2(v.hi, v.lo);
+    }
+    __syncthreads();
+  }
+  // backward: R11 z = y
+  for (int i1 = k; i1 > 0; i1 -= 32) {
+    const int i0 = max(0, i1 - 32), il = i1 - i0;
+    if (tid == 0) {
+      for (int ii = il - 1; ii >= 0; --ii) {
+        const float2 w0 = work[i0 + ii];
+        dfl v = {w0.x, w0.y};
+        for (int jj = ii + 1; jj < il; ++jj) v = df_fms(v, r_at(i0 + ii, i0 + jj), xb[jj]);
+        xb[ii] = df_mul(v, df_recip(r_at(i0 + ii, i0 + ii)));
+        work[i0 + ii] = make_float2(xb[ii].hi, xb[ii].lo);
+      }
+    }
+    __syncthreads();
+    for (int i = tid; i < i0; i += blockDim.x) {
+      const float2 w0 = work[i];
+      dfl v = {w0.x, w0.y};
+      for (int jj = 0; jj < il; ++jj) v = df_fms(v, r_at(i, i0 + jj), xb[jj]);
+      work[i] = make_float2(v.hi, v.lo);
+    }
+    __syncthreads();
+  }
+  for (int i = tid; i < k; i += blockDim.x) z[i] = work[i].x;
+}
+
+// czpart[p][r] = sum over the part-p skeleton columns t of A[r, perm[t]] z[t]
+__global__ void k_adj_cz(const float* __restrict__ A, int64_t lda, int m, int k, const int* __restrict__ perm,
+                         const float* __restrict__ z, float2* __restrict__ czpart) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int p = blockIdx.y, chunk = (k + PARTS - 1) / PARTS;
+  const int tb = p * chunk, te = min(k, tb + chunk);
+  if (r >= m) return;
+  float hi = 0.f, lo = 0.f;
+  for (int t = tb; t < te; ++t) {
+    const float a = A[r + (int64_t)perm[t] * lda];
+    const float prod = a * z[t];
+    const float e = fmaf(a, z[t], -prod);
+    const float s = hi + prod, zz = s - hi;
+    lo += ((hi - (s - zz)) + (prod - zz)) + e;
+    hi = s;
+  }
+  czpart[(int64_t)p * m + r] = make_float2(hi, lo);
+}
+
+// ---------------------------------------------------------------------------
+// 128 x 128 FP32 GEMM tile: acc[8][8] += X(r0:r0+128, :) Y(:, c0:c0+128), the
+// contraction in chunks of 16 staged through double-buffered shared memory.
+// Thread (ty, tx) = (tid / 16, tid % 16) owns rows ty*4 + {0..3} and
+// 64 + ty*4 + {0..3}, columns tx*4 + {0..3} and 64 + tx*4 + {0..3}.
+// ---------------------------------------------------------------------------
+struct GemmSmem {
+  __align__(16) float X[2][GK][GTILE + 4];  // X[kk][row]
+  __align__(16) float Y[2][GK][GTILE + 4];  // Y[kk][col]
+};
+
+// Loaders return one staged element for (chunk-relative kk, tile-relative index).
+struct LoadC {  // X = C: C[r][t] = A[r + perm[t] lda]
+  const float* A;
+  int64_t lda;
+  const int* perm;
+  int m, K;
+  __device__ __forceinline__ float x(int r, int t) const {
+    return (r < m && t < K) ? A[r + (int64_t)perm[t] * lda] : 0.f;
+  }
+};
+struct LoadE {  // X = E (m x nc, column major, ld m)
+  const float* E;
+  int m, K;
+  __device__ __forceinline__ float x(int r, int c) const { return (r < m && c < K) ? E[r + (int64_t)c * m] : 0.f; }
+};
+struct LoadRowMajor {  // Y[kk][col] from a row-major K x N matrix
+  const float* Y;
+  int K, N;
+  __device__ __forceinline__ float y(int kk, int c) const {
+    return (kk < K && c < N) ? Y[(int64_t)kk * N + c] : 0.f;
+  }
+};
+
+template <class LX, class LY>
+__device__ __forceinline__ void gemm_tile(GemmSmem& sm, const LX& lx, const LY& ly, int K, int r0, int c0,
+                                          float (&acc)[8][8]) {
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  // staging: 16 x 128 values per operand, 8 per thread: rows/cols contiguous across threads
+  const int s_i = tid & 127, s_k = tid >> 7;  // index within the tile, first kk (step 2)
+  float xr[8], yr[8];
+  auto load = [&](int k0) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int kk = s_k + 2 * q;
+      xr[q] = lx.x(r0 + s_i, k0 + kk);
+      yr[q] = ly.y(k0 + kk, c0 + s_i);
+    }
+  };
+  auto store = [&](int buf) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int kk = s_k + 2 * q;
+      sm.X[buf][kk][s_i] = xr[q];
+      sm.Y[buf][kk][s_i] = yr[q];
+    }
+  };
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+  const int nchunk = (K + GK - 1) / GK;
+  load(0);
+  store(0);
+  __syncthreads();
+  for (int ch = 0; ch < nchunk; ++ch) {
+    const int buf = ch & 1;
+    if (ch + 1 < nchunk) load((ch + 1) * GK);
+#pragma unroll
+    for (int kk = 0; kk < GK; ++kk) {
+      const float4 a0 = *reinterpret_cast<const float4*>(&sm.X[buf][kk][ty * 4]);
+      const float4 a1 = *reinterpret_cast<const float4*>(&sm.X[buf][kk][64 + ty * 4]);
+      const float4 b0 = *reinterpret_cast<const float4*>(&sm.Y[buf][kk][tx * 4]);
+      const float4 b1 = *reinterpret_cast<const float4*>(&sm.Y[buf][kk][64 + tx * 4]);
+      const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+      const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+    }
+    if (ch + 1 < nchunk) store(buf ^ 1);
+    __syncthreads();
+  }
+}
+
+__device__ __forceinline__ int tile_row(int ty, int i) { return (i < 4 ? 0 : 64) + ty * 4 + (i & 3); }
+__device__ __forceinline__ int tile_col(int tx, int j) { return (j < 4 ? 0 : 64) + tx * 4 + (j & 3); }
+
+// E = B - C T for a 128 x 128 tile: E stored (if Eout), ||E||^2 and E w row
+// sums as per-tile partials, and G(:, rd) = scale * 2 (E + (C z) w^T).
+__global__ void __launch_bounds__(GT) k_adj_gemm1(const float* __restrict__ A, int64_t lda, int m, int k, int nc,
+                                                  const int* __restrict__ perm, const float* __restrict__ Tr,
+                                                  const float* __restrict__ wr, const float* __restrict__ cz,
+                                                  float* __restrict__ Eout, float* __restrict__ G, int64_t ldg,
+                                                  float scale, float2* __restrict__ loss_part,
+                                                  float2* __restrict__ ew_part) {
+  __shared__ GemmSmem sm;
+  __shared__ float2 red[GT];
+  const int r0 = blockIdx.x * GTILE, c0 = blockIdx.y * GTILE;
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  float acc[8][8];
+  gemm_tile(sm, LoadC{A, lda, perm, m, k}, LoadRowMajor{Tr, k, nc}, k, r0, c0, acc);
+  dfl sq = {0.f, 0.f};
+  float ew[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) ew[i] = 0.f;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const int c = c0 + tile_col(tx, j);
+    if (c >= nc) continue;
+    const int col = perm[k + c];
+    const float w = wr[c];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int r = r0 + tile_row(ty, i);
+      if (r >= m) continue;
+      const float e = A[r + (int64_t)col * lda] - acc[i][j];
+      df_acc_prod(sq, e, e);
+      ew[i] = fmaf(e, w, ew[i]);
+      if (Eout) Eout[r + (int64_t)c * m] = e;
+      if (G) G[r + (int64_t)col * ldg] = scale * 2.f * fmaf(cz[r], w, e);
+    }
+  }
+  // row sums of E w over the tile's 16 column groups: through shared memory, fixed order
+  float* ews = reinterpret_cast<float*>(&sm);  // the staging buffers are idle now
+#pragma unroll
+  for (int i = 0; i < 8; ++i) ews[tile_row(ty, i) * 16 + tx] = ew[i];
+  red[tid] = make_float2(sq.hi, sq.lo);
+  __syncthreads();
+  if (tid < GTILE) {
+    float s = 0.f;
+    for (int q = 0; q < 16; ++q) s += ews[tid * 16 + q];
+    if (r0 + tid < m) ew_part[(int64_t)blockIdx.y * m + r0 + tid] = make_float2(s, 0.f);
+  }
+  if (tid == 0) {
+    dfl t = {red[0].x, red[0].y};
+    for (int q = 1; q < GT; ++q) t = df_add(t, {red[q].x, red[q].y});
+    loss_part[blockIdx.y * gridDim.x + blockIdx.x] = make_float2(t.hi, t.lo);
+  }
+}
+
+// G(:, S) = scale * (-2 E T^T - 2 (C z) u^T + 2 (E w) z^T) for a 128 x 128 tile.
+__global__ void __launch_bounds__(GT) k_adj_gemm2(const float* __restrict__ E, int m, int k, int nc,
+                                                  const int* __restrict__ perm, const float* __restrict__ Tc,
+                                                  const float* __restrict__ cz, const float* __restrict__ ew,
+                                                  const float* __restrict__ u, const float* __restrict__ z,
+                                                  float* __restrict__ G, int64_t ldg, float scale) {
+  __shared__ GemmSmem sm;
+  const int r0 = blockIdx.x * GTILE, c0 = blockIdx.y * GTILE;
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  float acc[8][8];
+  // E T^T: contraction over the nc rd columns; T^T (nc x k) row major is T column major
+  gemm_tile(sm, LoadE{E, m, nc}, LoadRowMajor{Tc, nc, k}, nc, r0, c0, acc);
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const int t = c0 + tile_col(tx, j);
+    if (t >= k) continue;
+    const int col = perm[t];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int r = r0 + tile_row(ty, i);
+      if (r >= m) continue;
+      const float g = -2.f * acc[i][j] - 2.f * cz[r] * u[t] + 2.f * ew[r] * z[t];
+      G[r + (int64_t)col * ldg] = scale * g;
+    }
+  }
+}
+
+__global__ void k_adj_loss(const float2* __restrict__ loss_part, int nparts, const float2* __restrict__ udf, int k,
+                           double* __restrict__ out) {
+  __shared__ float2 red[256];
+  dfl s = {0.f, 0.f};
+  for (int i = threadIdx.x; i < nparts; i += blockDim.x) s = df_add(s, {loss_part[i].x, loss_part[i].y});
+  dfl su = {0.f, 0.f};
+  for (int i = threadIdx.x; i < k; i += blockDim.x) {
+    const dfl v = {udf[i].x, udf[i].y};
+    su = df_add(su, df_mul(v, v));
+  }
+  red[threadIdx.x] = make_float2(s.hi, s.lo);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    dfl t = {red[0].x, red[0].y};
+    for (int q = 1; q < (int)blockDim.x; ++q) t = df_add(t, {red[q].x, red[q].y});
+    out[0] = (double)t.hi + (double)t.lo;
+  }
+  __syncthreads();
+  red[threadIdx.x] = make_float2(su.hi, su.lo);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    dfl t = {red[0].x, red[0].y};
+    for (int q = 1; q < (int)blockDim.x; ++q) t = df_add(t, {red[q].x, red[q].y});
+    out[1] = (double)t.hi + (double)t.lo;
+  }
+}
+
+size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
+
+}  // namespace
+}  // namespace rbrp
+
+using namespace rbrp;
+
+extern "C" rbrp_status rbrp_fixed_id_adjoint_f32(rbrp_handle h, int m, int n, const float* dA, int64_t lda,
+                                                 const float* dW, float scale, float* dG, int64_t ldg,
+                                                 double* loss) {
+  if (!h) return RBRP_ERR_INVALID_ARG;
+  if (!h->have_result || h->prec != RBRP_PREC_F32_MIXED)
+    return set_error(h, RBRP_ERR_NOT_COMPUTED, "needs a preceding FP32 run (rbrp_fixed_id_f32) on this matrix");
+  if (m != h->m || n != h->n || !dA || lda < m || !dW)
+    return set_error(h, RBRP_ERR_INVALID_ARG, "A / W do not match the last run");
+  if (dG && ldg < m) return set_error(h, RBRP_ERR_INVALID_ARG, "ldg < m");
+  const int k = h->k, nc = n - k;
+  if (k < 1 || nc < 1 || !h->T) return set_error(h, RBRP_ERR_NOT_COMPUTED, "the last run has no T (k = 0 or n)");
+  DeviceGuard g(h->device);
+  cudaStream_t st = h->stream;
+  // workspace: Tr, Tc (k x nc), wr (nc), u parts / u / udf, z, Rdf (k x k), work (k), cz parts / cz,
+  // E (m x nc), E w parts / E w, loss parts, loss out
+  const int gx = (m + GTILE - 1) / GTILE, gy1 = (nc + GTILE - 1) / GTILE, gy2 = (k + GTILE - 1) / GTILE;
+  const size_t kn = (size_t)k * nc;
+  size_t off = 0;
+  auto take = [&](size_t bytes) { const size_t o = off; off += al(bytes); return o; };
+  const size_t o_Tr = take(4 * kn), o_Tc = take(4 * kn), o_wr = take(4 * (size_t)nc);
+  const size_t o_up = take(8 * (size_t)PARTS * k), o_u = take(4 * (size_t)k), o_udf = take(8 * (size_t)k);
+  const size_t o_z = take(4 * (size_t)k), o_R = take(8 * (size_t)k * k), o_wk = take(8 * (size_t)k);
+  const size_t o_czp = take(8 * (size_t)PARTS * m), o_cz = take(4 * (size_t)m);
+  const size_t o_E = take(4 * (size_t)m * nc), o_ewp = take(8 * (size_t)gy1 * m), o_ew = take(4 * (size_t)m);
+  const size_t o_lp = take(8 * (size_t)gx * gy1), o_loss = take(16);
+  if (h->adj_bytes < off) {
+    if (h->adj_ws) cudaFree(h->adj_ws);
+    h->adj_ws = nullptr;
+    h->adj_bytes = 0;
+    rbrp_status s = cuda_check(h, cudaMalloc(&h->adj_ws, off), "cudaMalloc(adjoint workspace)");
+    if (s != RBRP_OK) return s;
+    h->adj_bytes = off;
+  }
+  unsigned char* w = static_cast<unsigned char*>(h->adj_ws);
+  float* Tr = reinterpret_cast<float*>(w + o_Tr);
+  float* Tc = reinterpret_cast<float*>(w + o_Tc);
+  float* wr = reinterpret_cast<float*>(w + o_wr);
+  float2* up = reinterpret_cast<float2*>(w + o_up);
+  float* u = reinterpret_cast<float*>(w + o_u);
+  float2* udf = reinterpret_cast<float2*>(w + o_udf);
+  float* z = reinterpret_cast<float*>(w + o_z);
+  float2* Rdf = reinterpret_cast<float2*>(w + o_R);
+  float2* wk = reinterpret_cast<float2*>(w + o_wk);
+  float2* czp = reinterpret_cast<float2*>(w + o_czp);
+  float* cz = reinterpret_cast<float*>(w + o_cz);
+  float* E = reinterpret_cast<float*>(w + o_E);
+  float2* ewp = reinterpret_cast<float2*>(w + o_ewp);
+  float* ew = reinterpret_cast<float*>(w + o_ew);
+  float2* lp = reinterpret_cast<float2*>(w + o_lp);
+  double* lout = reinterpret_cast<double*>(w + o_loss);
+
+  k_adj_prep<<<dim3((k + 31) / 32, (nc + 31) / 32), 256, 0, st>>>(h->T, k, nc, dW, h->perm, Tr, Tc, wr);
+  k_adj_u<<<dim3((k + 255) / 256, PARTS), 256, 0, st>>>(Tc, k, nc, wr, up);
+  k_adj_sum_parts<<<(k + 255) / 256, 256, 0, st>>>(up, k, u, udf);
+  if (dG) {
+    k_adj_split_r<<<1216, 256, 0, st>>>(h->R, n, k, Rdf);
+    k_adj_z<<<1, 1024, 0, st>>>(Rdf, k, udf, wk, z);
+    k_adj_cz<<<dim3((m + 255) / 256, PARTS), 256, 0, st>>>(dA, lda, m, k, h->perm, z, czp);
+    k_adj_sum_parts<<<(m + 255) / 256, 256, 0, st>>>(czp, m, cz, nullptr);
+  }
+  k_adj_gemm1<<<dim3(gx, gy1), GT, 0, st>>>(dA, lda, m, k, nc, h->perm, Tr, wr, cz, dG ? E : nullptr, dG, ldg, scale,
+                                            lp, ewp);
+  if (dG) k_adj_sum_rows<<<(m + 255) / 256, 256, 0, st>>>(ewp, gy1, m, ew);
+  k_adj_loss<<<1, 256, 0, st>>>(lp, gx * gy1, udf, k, lout);
+  if (dG) {
+    k_adj_gemm2<<<dim3(gx, gy2), GT, 0, st>>>(E, m, k, nc, h->perm, Tc, cz, ew, u, z, dG, ldg, scale);
+  }
+  double hl[2] = {0.0, 0.0};
+  rbrp_status s = cuda_check(h, cudaMemcpyAsync(hl, lout, sizeof(hl), cudaMemcpyDeviceToHost, st), "copy loss");
+  if (s == RBRP_OK) s = cuda_check(h, cudaStreamSynchronize(st), "adjoint kernels");
+  if (s != RBRP_OK) return s;
+  if (loss) *loss = hl[0] + hl[1];
+  return RBRP_OK;
+}

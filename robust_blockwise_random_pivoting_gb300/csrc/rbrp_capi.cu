@@ -1,9 +1,11 @@
 // rbrp_capi.cu - C ABI, workspace management, interpolation-matrix solve
 // (a10) and ID-error kernel (a11) of the GB300 RBRP library.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <vector>
 
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -643,6 +645,61 @@ double run_flops(const rbrp_handle h, bool with_T) {
 
 using namespace rbrp;
 
+namespace rbrp {
+// Fixed-skeleton ID: the adaptive loop with the sampler replaced by "the next
+// b columns of S" and a filter that keeps every nonzero pivot, so the run ends
+// with S (reordered by the panel pivots) in perm[:k] and T = R11^{-1} R12 =
+// A(:, S)^+ A(:, rd).
+template <typename T>
+rbrp_status fixed_id(rbrp_handle h, int m, int n, const T* dA, int64_t lda, const int* dS, int k, int b,
+                            int* dPerm, rbrp_result* out) {
+  rbrp_params p;
+  rbrp_params_default(&p);
+  p.b = b;
+  p.tol = 0.0;
+  p.kmax = k;
+  p.tol_loc = 1e-300;  // keep every pivot with a positive Schur diagonal
+  p.compute_T = 1;
+  rbrp_status s = validate(h, m, n, dA, lda, &p, sizeof(T));
+  if (s != RBRP_OK) return s;
+  if (!dS || k < 1 || k > std::min(m, n)) return set_error(h, RBRP_ERR_INVALID_ARG, "need 1 <= k <= min(m, n) and S");
+  if (dPerm && (s = check_device_ptr(h, dPerm, "perm")) != RBRP_OK) return s;
+  if ((s = check_device_ptr(h, dS, "S")) != RBRP_OK) return s;
+  DeviceGuard g(h->device);
+  std::vector<int> S(k), order(n, -1);
+  s = cuda_check(h, cudaMemcpy(S.data(), dS, sizeof(int) * (size_t)k, cudaMemcpyDeviceToHost), "copy S");
+  if (s != RBRP_OK) return s;
+  for (int t = 0; t < k; ++t) {
+    if (S[t] < 0 || S[t] >= n) return set_error(h, RBRP_ERR_INVALID_ARG, "skeleton index out of range");
+    if (order[S[t]] >= 0) return set_error(h, RBRP_ERR_INVALID_ARG, "repeated skeleton index");
+    order[S[t]] = t;
+  }
+  if (h->given_cap < (size_t)n) {
+    if (h->given_order) cudaFree(h->given_order);
+    if (h->adj_ws) cudaFree(h->adj_ws);
+    h->given_order = nullptr;
+    h->given_cap = 0;
+    s = cuda_check(h, cudaMalloc((void**)&h->given_order, sizeof(int) * (size_t)n), "cudaMalloc(skeleton order)");
+    if (s != RBRP_OK) return s;
+    h->given_cap = n;
+  }
+  s = cuda_check(h, cudaMemcpyAsync(h->given_order, order.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice,
+                                    h->stream), "copy skeleton order");
+  if (s != RBRP_OK) return s;
+  p.sampler = SAMPLER_GIVEN;
+  // the CUDA-core projection (double-float sums) for the FP32 form: T feeds gradients
+  const int variant = h->variant;
+  h->variant = 1;
+  s = run_rbrp<T>(h, m, n, dA, lda, p, dPerm, out);
+  h->variant = variant;
+  // the host vector is released on return: finish the copy before that
+  const rbrp_status s2 = cuda_check(h, cudaStreamSynchronize(h->stream), "fixed-skeleton run");
+  return s != RBRP_OK ? s : s2;
+}
+
+}  // namespace rbrp
+
+
 extern "C" {
 
 void rbrp_params_default(rbrp_params* p) {
@@ -708,6 +765,8 @@ rbrp_status rbrp_destroy(rbrp_handle h) {
     if (h->T) cudaFree(h->T);
     if (h->df_buf) cudaFree(h->df_buf);
     if (h->hostA_dev) cudaFree(h->hostA_dev);
+    if (h->given_order) cudaFree(h->given_order);
+    if (h->adj_ws) cudaFree(h->adj_ws);
     if (h->hst) cudaFreeHost(h->hst);
     for (auto e : h->block_events) cudaEventDestroy(e);
     for (auto e : h->prof_events) cudaEventDestroy(e);
@@ -742,6 +801,16 @@ rbrp_status rbrp_id_f32(rbrp_handle h, int m, int n, const float* dA, int64_t ld
   if (dPerm && (s = check_device_ptr(h, dPerm, "perm")) != RBRP_OK) return s;
   DeviceGuard g(h->device);
   return run_rbrp<float>(h, m, n, dA, lda, *p, dPerm, out);
+}
+
+rbrp_status rbrp_fixed_id_f32(rbrp_handle h, int m, int n, const float* dA, int64_t lda, const int* dS, int k, int b,
+                              int* dPerm, rbrp_result* out) {
+  return fixed_id<float>(h, m, n, dA, lda, dS, k, b, dPerm, out);
+}
+
+rbrp_status rbrp_fixed_id_f64(rbrp_handle h, int m, int n, const double* dA, int64_t lda, const int* dS, int k,
+                              int b, int* dPerm, rbrp_result* out) {
+  return fixed_id<double>(h, m, n, dA, lda, dS, k, b, dPerm, out);
 }
 
 rbrp_status rbrp_copy_T(rbrp_handle h, double* dT, int64_t ldt) {

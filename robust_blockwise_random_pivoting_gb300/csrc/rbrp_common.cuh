@@ -21,6 +21,7 @@ constexpr int MAXB = 64;          // largest block size b supported by the panel
 constexpr int SAMPLER_NP = 0;
 constexpr int SAMPLER_ES = 1;
 constexpr int SAMPLER_GREEDY = 2;
+constexpr int SAMPLER_GIVEN = 3;  // fixed skeleton: the next columns of a given list, in list order
 constexpr int ST_ERR_NUMERIC = 5; // mirrors RBRP_ERR_NUMERIC
 
 // Loop state, resident in device memory; every per-block kernel reads it, so the

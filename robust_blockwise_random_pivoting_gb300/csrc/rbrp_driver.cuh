@@ -101,7 +101,7 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
     const size_t mark0 = h->marks.size();
     ev = prof_begin(h);
     k_sample<<<1, SAMPLE_THREADS, 0, st>>>(h->st, h->diags, h->perm, n, kmax, p.b, p.seed, p.sampler,
-                                           h->pbuf, h->kbuf, h->js, h->cols);
+                                           h->pbuf, h->kbuf, h->js, h->cols, h->given_order);
     prof_end(h, RBRP_PHASE_SAMPLE, ev, 28.0 * (n - i), 0.0, 1);
     ev = prof_begin(h);
     if (!RES && i > 0) {

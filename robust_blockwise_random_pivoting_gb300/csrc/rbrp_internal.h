@@ -67,6 +67,14 @@ struct rbrp_handle_st {
   void* df_buf = nullptr;      // double-float operands of the T solve
   size_t df_bytes = 0;
 
+  // fixed-skeleton adjoint workspace (rbrp_adjoint.cu)
+  void* adj_ws = nullptr;
+  size_t adj_bytes = 0;
+
+  // fixed-skeleton runs: order_of[col] = index of col in the given skeleton, -1 otherwise
+  int* given_order = nullptr;
+  size_t given_cap = 0;
+
   // device copy of a host matrix (host-buffer entry points)
   void* hostA_dev = nullptr;
   size_t hostA_bytes = 0;

@@ -123,8 +123,9 @@ __global__ void __launch_bounds__(1024) k_init(State* st, const double* __restri
 __global__ void __launch_bounds__(SAMPLE_THREADS)
 k_sample(State* st, const double* __restrict__ diags, const int* __restrict__ perm, int n, int kmax,
          int b, uint64_t seed, int sampler, double* __restrict__ pbuf,
-         unsigned long long* __restrict__ kbuf, int* __restrict__ js, int* __restrict__ cols) {
-  sample_block(st, diags, perm, n, kmax, b, seed, sampler, pbuf, kbuf, js, cols);
+         unsigned long long* __restrict__ kbuf, int* __restrict__ js, int* __restrict__ cols,
+         const int* __restrict__ order_of) {
+  sample_block(st, diags, perm, n, kmax, b, seed, sampler, pbuf, kbuf, js, cols, order_of);
 }
 
 // ===========================================================================

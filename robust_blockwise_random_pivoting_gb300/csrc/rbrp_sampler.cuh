@@ -19,6 +19,8 @@ namespace {
 // ES: keys -log(1-u)/w (u from the exponential-key stream of the original
 //     column), the bs smallest by an 8-bit radix select on the key bits.
 // GREEDY: the bs largest weights (ties: lower position), same radix select.
+// GIVEN: a fixed skeleton: the bs listed columns that come first in the list
+//     (order_of[col] = list index, -1 for unlisted), same radix select.
 // ===========================================================================
 constexpr int SAMPLE_THREADS = 1024;
 
@@ -26,7 +28,8 @@ constexpr int SAMPLE_THREADS = 1024;
 // threads, the batched kernel with its CTA.
 __device__ void sample_block(State* st, const double* __restrict__ diags, const int* __restrict__ perm, int n,
                              int kmax, int b, uint64_t seed, int sampler, double* __restrict__ pbuf,
-                             unsigned long long* __restrict__ kbuf, int* __restrict__ js, int* __restrict__ cols) {
+                             unsigned long long* __restrict__ kbuf, int* __restrict__ js, int* __restrict__ cols,
+                             const int* __restrict__ order_of = nullptr) {
   __shared__ double shd[32];
   __shared__ int shi[32];
   __shared__ unsigned int hist[256];
@@ -124,7 +127,14 @@ __device__ void sample_block(State* st, const double* __restrict__ diags, const 
     for (int j = lo; j < hi; ++j) {
       const double wj = w[j];
       unsigned long long key = ~0ull;
-      if (wj > 0.0) {
+      if (sampler == SAMPLER_GIVEN) {
+        // fixed skeleton: columns of the list (order_of[col] >= 0), earliest first
+        const int o = order_of[perm[i + j]];
+        if (wj > 0.0 && o >= 0) {
+          ++npos;
+          key = (unsigned long long)o;
+        }
+      } else if (wj > 0.0) {
         ++npos;
         if (sampler == SAMPLER_ES) {
           const double u = es_uniform(seed, (uint64_t)st->attempts, (uint64_t)perm[i + j]);
