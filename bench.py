@@ -44,10 +44,15 @@ WORKLOADS = {
     "snn8k": dict(kind="snn", m=8192, n=8192, r=2000, r1=100, amp=10.0, density=0.02, b=64, tol=1e-12),
     "snn4k": dict(kind="snn", m=4096, n=4096, r=2000, r1=100, amp=10.0, density=0.02, b=64, tol=1e-12),
     "gexp1000": dict(kind="gexp", m=1000, n=1000, decay=20.0, b=40, tol=1e-12),
+    "adjoint8k": dict(kind="adjoint", n=8192, dim=8, lengthscale=1.5, b=64, tol=1e-6),
 }
 
 
 def describe(name, wl):
+    if wl["kind"] == "adjoint":
+        return (f"{name}: fixed-skeleton ID loss ||A - A(:,S) T||^2 + ||T w||^2 and its gradient, Gaussian kernel "
+                f"{wl['n']}^2 on N(0, I_{wl['dim']}) points, l={wl['lengthscale']}, S from FP32 RBRP at squared tol "
+                f"{wl['tol']:g} (b={wl['b']}); a step is one forward + backward (d/dA and d/dl)")
     if wl["kind"] == "blocks":
         return (f"{name}: {wl['nblocks']} Gaussian-kernel blocks (l={wl['lengthscale']}, 3-D unit-cube clusters "
                 f"2-8 apart), m, n log-uniform in [{wl['lo']}, {wl['hi']}], FP32 storage scaled by each block's "
@@ -564,6 +569,92 @@ def run_batched(args, wl, name, ctx):
     }
 
 
+def run_adjoint(args, wl, name, ctx):
+    """Forward + backward of the differentiable fixed-skeleton ID per step; returns the JSON line (dict)."""
+    torch = ctx.torch
+    from robust_blockwise_random_pivoting_gb300 import workloads as W
+    from robust_blockwise_random_pivoting_gb300.adjoint import fixed_skeleton_id_loss, gaussian_kernel_matrix
+    from robust_blockwise_random_pivoting_gb300.rbrp import Handle
+    seed = ctx.rank
+    n = wl["n"]
+    P = torch.from_numpy(W.gaussian_kernel_points(n, wl["dim"], seed)).to(ctx.device)
+    h = Handle(ctx.local)
+    A0 = gaussian_kernel_matrix(P, wl["lengthscale"]).float().t().contiguous().t()
+    t0 = time.perf_counter()
+    r = h.column_id(A0, b=wl["b"], tol=wl["tol"], seed=seed)
+    torch.cuda.synchronize()
+    t_rbrp = time.perf_counter() - t0
+    S = r.perm[: r.k].clone()
+    k = r.k
+    w = torch.randn(n, generator=torch.Generator(device="cpu").manual_seed(7 + seed)).to(ctx.device)
+
+    def step():
+        ls = torch.tensor(wl["lengthscale"], dtype=torch.float64, device=ctx.device, requires_grad=True)
+        A = gaussian_kernel_matrix(P, ls).float()
+        loss = fixed_skeleton_id_loss(A, S, w, b=wl["b"], handle=h)
+        loss.backward()
+        return loss, ls.grad
+    for _ in range(args.warmup):
+        loss, gl = step()
+    ctx.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(ctx.uuid) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            loss, gl = step()
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+    clocks = clk.summary()
+    dt = ctx.max_over_ranks(dt)
+    value = ctx.world * args.steps / dt
+
+    # the adjoint kernels alone (CUDA events): forward fixed ID + loss, then fixed ID + gradient
+    from robust_blockwise_random_pivoting_gb300.adjoint import fixed_skeleton_loss_and_grad
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    ev[0].record(ctx.stream)
+    fixed_skeleton_loss_and_grad(h, A0, S, w, wl["b"], grad=False)
+    ev[1].record(ctx.stream)
+    _, G = fixed_skeleton_loss_and_grad(h, A0, S, w, wl["b"], grad=True)
+    ev[2].record(ctx.stream)
+    torch.cuda.synchronize()
+    ms_fwd, ms_bwd = ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
+    nc = n - k
+    gemm_flops = 2.0 * (2.0 * n * nc * k)   # E = B - C T and E T^T
+
+    # FP64 reference gradient (torch autograd through a QR least-squares T) on the same FP32 matrix
+    check = None
+    if not args.no_plain:
+        A64 = A0.double().requires_grad_(True)
+        mask = torch.ones(n, dtype=torch.bool, device=ctx.device)
+        mask[S.long()] = False
+        rd = torch.nonzero(mask).flatten()
+        C, B = A64[:, S.long()], A64[:, rd]
+        Q, R = torch.linalg.qr(C)
+        T = torch.linalg.solve_triangular(R, Q.t() @ B, upper=True)
+        E = B - C @ T
+        lref = (E * E).sum() + ((T @ w.double()[rd]) ** 2).sum()
+        lref.backward()
+        check = {"loss": float(loss.item()), "loss_fp64": float(lref.item()),
+                 "grad_A_rel_err": float((torch.linalg.norm(G.double() - A64.grad) / torch.linalg.norm(A64.grad)).item()),
+                 "grad_l": float(gl.item())}
+        del A64, C, B, Q, R, T, E
+    h.close()
+    nominal_fp32 = 152 * 128 * 2 * 2.07e9 / 1e12
+    return {
+        "metric": METRIC, "value": value, "unit": "forward+backward/s", "n_gpus": ctx.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Philox points)",
+        "config": {"workload": describe(name, wl), "k": k, "rbrp_forward_s": t_rbrp, "ms_fixed_id_and_loss": ms_fwd,
+                   "ms_fixed_id_and_gradient": ms_bwd, "check": check},
+        "roofline": {"kernel": "k_adj_gemm1 + k_adj_gemm2 (FFMA)", "bound": "fp32",
+                     "achieved": gemm_flops / (ms_bwd * 1e-3) / 1e12, "peak": nominal_fp32, "unit": "TFLOP/s",
+                     "frac": gemm_flops / (ms_bwd * 1e-3) / 1e12 / nominal_fp32, "traffic": None,
+                     "peak_source": "nominal FP32 CUDA-core peak (152 SMs x 128 FMA x 2.07 GHz); "
+                                    "the time includes the fixed-skeleton forward run"},
+        "cpu_baseline": None, "e2e": None, "clocks": clocks, "gpu_launches": None,
+    }
+
+
 def run_reference_batched(args, wl, name):
     """Reference arm for the batched workload: the oracle port on a bounded sample of blocks per step."""
     if int(os.environ.get("RANK", "0")) != 0:
@@ -600,6 +691,9 @@ def main():
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
+        if wl["kind"] == "adjoint":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no differentiable ID"}))
+            return
         if wl["kind"] == "blocks":
             run_reference_batched(args, wl, args.workload)
         else:
@@ -608,6 +702,8 @@ def main():
     ctx = Ctx(args)
     if wl["kind"] == "blocks":
         line = run_batched(args, wl, args.workload, ctx)
+    elif wl["kind"] == "adjoint":
+        line = run_adjoint(args, wl, args.workload, ctx)
     else:
         line = run_single(args, wl, args.workload, ctx)
     if ctx.rank == 0:
