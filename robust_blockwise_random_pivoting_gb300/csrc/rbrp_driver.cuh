@@ -157,7 +157,7 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
         const int sps = (nstages + wsplit - 1) / wsplit;
         wsplit = (nstages + sps - 1) / sps;
         tc::k_proj_w_tc<<<dim3(ctiles, wsplit), tc::NTHREADS, tc::P1_SMEM, st>>>(tmA, tmQh, tmQl, h->st, m, n, sps,
-                                                                                h->Wpart);
+                                                                                reinterpret_cast<float2*>(h->Wpart));
       } else {
         k_proj_w<<<(n - i + 63) / 64, 128, 0, st>>>((const float*)Q, L.ld_res, h->Ares, L.ld_res, h->st, m, n, h->R,
                                                     n);
@@ -170,7 +170,8 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
       nsplit = (m + rps - 1) / rps;
       k_resid_update<<<dim3(ctiles, nsplit), P2_THREADS, P2_SMEM, st>>>((const float*)Q, L.ld_res, h->Ares, L.ld_res,
                                                                        h->st, m, n, rps, h->R, n,
-                                                                       use_tc ? h->Wpart : nullptr, wsplit,
+                                                                       use_tc ? reinterpret_cast<const float2*>(h->Wpart)
+                                                                              : nullptr, wsplit,
                                                                        h->part_norm);
       nproj = (n - i + 255) / 256;
       k_norm_reduce<<<nproj, 256, 0, st>>>(h->part_norm, nsplit, n, h->st, h->diags, h->part_res, h->part_nnz);

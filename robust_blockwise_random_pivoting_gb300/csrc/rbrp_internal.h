@@ -56,6 +56,7 @@ struct rbrp_handle_st {
   int64_t ld_res = 0;
   double* part_norm = nullptr; // residual form: partial column norms per row range
   double* Wpart = nullptr;     // residual form: row-split partial projections, P1_MAX_SPLIT x 64 x n
+                               // double-float pairs (float2, 8 bytes each)
   float* Qh = nullptr;         // residual form: TF32 hi / lo parts of the block basis, ld_res x 64
   float* Ql = nullptr;
   int variant = 0;             // 0: tensor-core projection, 1: CUDA-core projection

@@ -13,6 +13,7 @@
 //   k_finish      residual, stop rule, per-block trace
 #pragma once
 #include "rbrp_common.cuh"
+#include "rbrp_df.cuh"
 #include "rbrp_sampler.cuh"
 
 namespace rbrp {
@@ -841,7 +842,7 @@ constexpr size_t P2_SMEM = sizeof(float) * (size_t)MAXB * (P2_COLS + P2_ROWS);
 __global__ void __launch_bounds__(P2_THREADS, 2)
 k_resid_update(const float* __restrict__ Qb, int64_t ldq, float* __restrict__ Ares, int64_t ld,
                const State* __restrict__ st, int m, int n, int rows_per_split, double* __restrict__ R,
-               int64_t ldr, const double* __restrict__ Wpart, int wsplit, double* __restrict__ part_norm) {
+               int64_t ldr, const float2* __restrict__ Wpart, int wsplit, double* __restrict__ part_norm) {
   extern __shared__ __align__(16) float p2_smem[];
   float* Ws = p2_smem;                       // Ws[a * P2_COLS + c]
   float* Qs = p2_smem + MAXB * P2_COLS;      // Qs[a * P2_ROWS + rr]
@@ -855,15 +856,18 @@ k_resid_update(const float* __restrict__ Qb, int64_t ldq, float* __restrict__ Ar
     const int a = idx / P2_COLS, c = idx % P2_COLS;
     float wv = 0.f;
     if (c < ncol) {
-      double v;
       if (Wpart) {
-        v = 0.0;
-        for (int z = 0; z < wsplit; ++z) v += Wpart[((int64_t)z * MAXB + a) * n + p0 + c];
-        if (blockIdx.y == 0) R[(int64_t)(i + a) * ldr + p0 + c] = v;
+        // double-float sum of the row-split partials on the FP32 pipe; one row range writes R
+        dfl v = {0.f, 0.f};
+        for (int z = 0; z < wsplit; ++z) {
+          const float2 t = Wpart[((int64_t)z * MAXB + a) * n + p0 + c];
+          v = df_add(v, {t.x, t.y});
+        }
+        if (blockIdx.y == 0) R[(int64_t)(i + a) * ldr + p0 + c] = (double)v.hi + (double)v.lo;
+        wv = v.hi;
       } else {
-        v = R[(int64_t)(i + a) * ldr + p0 + c];
+        wv = (float)R[(int64_t)(i + a) * ldr + p0 + c];
       }
-      wv = (float)v;
     }
     Ws[idx] = wv;
   }
@@ -942,12 +946,15 @@ k_resid_update(const float* __restrict__ Qb, int64_t ldq, float* __restrict__ Ar
       }
     }
   }
+  // warp sums of the double-float norms on the FP32 pipe; lane 0 converts once per column
 #pragma unroll
   for (int c = 0; c < 8; ++c) {
-    double v = (double)nrm[c].hi + (double)nrm[c].lo;
-    v = warp_sum(v);
+    dfl v = df_two_sum(nrm[c].hi, nrm[c].lo);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+      v = df_add(v, {__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)});
     const int cc = w * 8 + c;
-    if (lane == 0 && cc < ncol) part_norm[(int64_t)blockIdx.y * n + p0 + cc] = v;
+    if (lane == 0 && cc < ncol) part_norm[(int64_t)blockIdx.y * n + p0 + cc] = (double)v.hi + (double)v.lo;
   }
 }
 

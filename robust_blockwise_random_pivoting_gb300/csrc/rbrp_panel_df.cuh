@@ -195,12 +195,15 @@ k_panel_q_df(const float* __restrict__ V, int m, const State* __restrict__ st, c
   for (int idx = tid; idx < DF_TROWS * MAXB; idx += DF_TROWS) {
     const int rr = idx % DF_TROWS, s = idx / DF_TROWS, r = r0 + rr;
     if (r < m) {
-      const double q = s < kept ? df_dbl(sm.W[rr][s]) : 0.0;
-      if (s < kept) Q[r + (int64_t)s * ldq] = (float)q;
+      // FP32 basis and its exact TF32 split, on the FP32 pipe: q = hi + lo (double-float),
+      // Q = rn(q), Qh = tf32(Q), Ql = rn(q - Qh) with hi - Qh exact (Sterbenz)
+      const dfl w = s < kept ? sm.W[rr][s] : dfl{0.f, 0.f};
+      const float qf = __fadd_rn(w.hi, w.lo);
+      if (s < kept) Q[r + (int64_t)s * ldq] = qf;
       if (Qh) {
-        const float h = __uint_as_float(__float_as_uint((float)q) & 0xFFFFE000u);
+        const float h = __uint_as_float(__float_as_uint(qf) & 0xFFFFE000u);
         Qh[r + (int64_t)s * ldh] = h;
-        Ql[r + (int64_t)s * ldh] = (float)(q - (double)h);
+        Ql[r + (int64_t)s * ldh] = __fadd_rn(w.hi - h, w.lo);
       }
     }
   }
@@ -286,12 +289,15 @@ k_panel2_df(const float2* __restrict__ Q1, int m, const State* __restrict__ st, 
   for (int idx = tid; idx < DF_TROWS * MAXB; idx += DF_TROWS) {
     const int rr = idx % DF_TROWS, s = idx / DF_TROWS, r = r0 + rr;
     if (r < m) {
-      const double q = s < kept ? df_dbl(sm.W[rr][s]) : 0.0;
-      if (s < kept) Q[r + (int64_t)s * ldq] = (float)q;
+      // FP32 basis and its exact TF32 split, on the FP32 pipe: q = hi + lo (double-float),
+      // Q = rn(q), Qh = tf32(Q), Ql = rn(q - Qh) with hi - Qh exact (Sterbenz)
+      const dfl w = s < kept ? sm.W[rr][s] : dfl{0.f, 0.f};
+      const float qf = __fadd_rn(w.hi, w.lo);
+      if (s < kept) Q[r + (int64_t)s * ldq] = qf;
       if (Qh) {
-        const float h = __uint_as_float(__float_as_uint((float)q) & 0xFFFFE000u);
+        const float h = __uint_as_float(__float_as_uint(qf) & 0xFFFFE000u);
         Qh[r + (int64_t)s * ldh] = h;
-        Ql[r + (int64_t)s * ldh] = (float)(q - (double)h);
+        Ql[r + (int64_t)s * ldh] = __fadd_rn(w.hi - h, w.lo);
       }
     }
   }

@@ -195,7 +195,7 @@ __device__ __forceinline__ void drain32(uint32_t taddr, float (&hi)[32], float (
 __global__ void __launch_bounds__(NTHREADS, 1)
 k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmQh,
             const __grid_constant__ CUtensorMap tmQl, State* st, int m, int n, int stages_per_split,
-            double* __restrict__ Wpart) {
+            float2* __restrict__ Wpart) {
   extern __shared__ uint8_t p1_raw[];
   P1Smem& sm = *reinterpret_cast<P1Smem*>((reinterpret_cast<uintptr_t>(p1_raw) + 1023) & ~(uintptr_t)1023);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -328,11 +328,14 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
     }
     const int p = p0 + 32 * q + lane;
     if (ok && !*abort && p < n) {
-      double* wz = Wpart + (int64_t)blockIdx.y * BN * n;
+      float2* wz = Wpart + (int64_t)blockIdx.y * BN * n;
 #pragma unroll
       for (int j = 0; j < 32; ++j) {
         const int a = 32 * ch + j;
-        if (a < kept) wz[(int64_t)a * n + p] = (double)hi[j] + (double)lo[j];
+        if (a < kept) {  // double-float (normalised), summed over the row splits by the update
+          const float s = hi[j] + lo[j];
+          wz[(int64_t)a * n + p] = make_float2(s, lo[j] - (s - hi[j]));
+        }
       }
     }
   }
