@@ -44,6 +44,7 @@ WORKLOADS = {
     "snn8k": dict(kind="snn", m=8192, n=8192, r=2000, r1=100, amp=10.0, density=0.02, b=64, tol=1e-12),
     "snn4k": dict(kind="snn", m=4096, n=4096, r=2000, r1=100, amp=10.0, density=0.02, b=64, tol=1e-12),
     "gexp1000": dict(kind="gexp", m=1000, n=1000, decay=20.0, b=40, tol=1e-12),
+    "gmm65k": dict(kind="gmm", m=1024, n=65536, clusters=20, b=32, tol=1e-4),
     "adjoint8k": dict(kind="adjoint", n=8192, dim=8, lengthscale=1.5, b=64, tol=1e-6),
 }
 
@@ -57,6 +58,10 @@ def describe(name, wl):
         return (f"{name}: {wl['nblocks']} Gaussian-kernel blocks (l={wl['lengthscale']}, 3-D unit-cube clusters "
                 f"2-8 apart), m, n log-uniform in [{wl['lo']}, {wl['hi']}], FP32 storage scaled by each block's "
                 f"max, squared tol {wl['tol']:g} (rel. Frobenius {np.sqrt(wl['tol']):g}), b autotuned")
+    if wl["kind"] == "gmm":
+        return (f"{name}: Gaussian mixture, {wl['n']} points as columns in R^{wl['m']}, {wl['clusters']} clusters "
+                f"(weights 2^-c, means N(0, 4I), sigma U[0.1, 1]), FP32 storage, b={wl['b']}, squared tol "
+                f"{wl['tol']:g}; every cluster must appear in S")
     if wl["kind"] == "snn":
         return (f"{name}: SNN {wl['m']}x{wl['n']} (2000 rank-one terms, density {wl['density']}), FP32 storage, "
                 f"b={wl['b']}, squared tol {wl['tol']:g} (rel. Frobenius {np.sqrt(wl['tol']):g})")
@@ -73,6 +78,9 @@ def make_matrix(wl, seed, torch, device):
         Yt = torch.from_numpy(Y).to(device)
         A64 = (Yt @ Xt.t()).t()           # (m, n) column major
         del Xt, Yt
+    elif wl["kind"] == "gmm":
+        A, _ = W.gmm(wl["m"], wl["n"], wl["clusters"], seed)
+        A64 = torch.from_numpy(A).to(device).t().contiguous().t()
     else:
         A = W.gaussian_exp(wl["m"], wl["n"], decay=wl["decay"], seed=seed)
         A64 = torch.from_numpy(A).to(device).t().contiguous().t()
@@ -182,6 +190,9 @@ def run_reference(args, wl, name):
         X, w, Y = W.snn_factors(wl["m"], wl["n"], wl["r"], wl["r1"], wl["amp"], wl["density"], 0)
         A = np.asfortranarray((X * w) @ Y.T)
         full_k = min(wl["r"], wl["m"], wl["n"])
+    elif wl["kind"] == "gmm":
+        A, _ = W.gmm(wl["m"], wl["n"], wl["clusters"], 0)
+        full_k = min(wl["m"], wl["n"])
     else:
         A = W.gaussian_exp(wl["m"], wl["n"], decay=wl["decay"], seed=0)
         full_k = None
@@ -276,7 +287,7 @@ def run_single(args, wl, name, ctx, light=False):
     m, n = A32.shape
     h = Handle(ctx.local)
     stream = ctx.stream
-    mixed = wl["kind"] == "snn"
+    mixed = wl["kind"] in ("snn", "gmm")
     A = A32 if mixed else A64
     kw = dict(b=wl["b"], tol=wl["tol"], seed=seed)
     warmup, steps = (2, 2) if light else (args.warmup, args.steps)
@@ -304,6 +315,12 @@ def run_single(args, wl, name, ctx, light=False):
 
     k = r.k
     rel_err = h.id_error(A)             # squared, on the matrix the ID was computed for
+    coverage = None
+    if wl["kind"] == "gmm":             # every cluster represented in the skeleton
+        from robust_blockwise_random_pivoting_gb300 import workloads as W
+        _, labels = W.gmm(wl["m"], wl["n"], wl["clusters"], seed)
+        got = len(set(labels[r.perm[:k].cpu().numpy()].tolist()))
+        coverage = {"clusters": wl["clusters"], "in_skeleton": got}
 
     e2e = None
     if not (args.no_e2e or light):
@@ -377,8 +394,8 @@ def run_single(args, wl, name, ctx, light=False):
         "config": {"workload": describe(name, wl), "precision": "mixed" if mixed else "f64",
                    "k": k, "blocks": r.nblocks, "id_time_ms": ms_max / steps,
                    "rel_err": float(np.sqrt(max(rel_err, 0.0))), "err_est_sq": r.err_est,
-                   "plain_f64": plain, "parallelism": f"replicas x{ctx.world}",
-                   "l2": "no flush: the 1 GiB input is larger than L2", "phases": phases},
+                   "plain_f64": plain, "parallelism": f"replicas x{ctx.world}", "cluster_coverage": coverage,
+                   "l2": f"no flush: the {m * n * 4 / 2**20:.0f} MiB input is larger than L2", "phases": phases},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
         "gpu_launches": gpu_launches,
     }
