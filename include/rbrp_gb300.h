@@ -127,6 +127,14 @@ rbrp_status rbrp_fixed_id_f64(rbrp_handle h, int m, int n, const double* dA, int
 rbrp_status rbrp_fixed_id_adjoint_f32(rbrp_handle h, int m, int n, const float* dA, int64_t lda,
                                       const float* dW, float scale, float* dG, int64_t ldg, double* loss);
 
+/* Gaussian sketch for the sketch-based comparison IDs (RandCPQR_OS / RandLUPP_OS,
+ * gpu/randCPQR_OS.cu:20-111, whose G is drawn in gpu/random.cu and applied by
+ * the cuBLAS GEMM of gpu/gemm.cu:9-15): dY (l x n, ldy >= l) = G A with
+ * G (l x m) = scale * N(0, 1) from Philox4x64-10 (key seed) by Box-Muller.
+ * FP32 CUDA-core GEMM; asynchronous on the handle's stream. */
+rbrp_status rbrp_sketch_gaussian_f32(rbrp_handle h, int l, int m, int n, const float* dA, int64_t lda,
+                                     uint64_t seed, float scale, float* dY, int64_t ldy);
+
 /* T (k x (n-k), column major) of the last run, into a device buffer with ldt >= k. */
 rbrp_status rbrp_copy_T(rbrp_handle h, double* dT, int64_t ldt);
 /* Device pointer of T of the last run (ld = k), valid until the next run. */

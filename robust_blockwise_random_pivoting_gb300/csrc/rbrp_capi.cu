@@ -676,7 +676,6 @@ rbrp_status fixed_id(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
   }
   if (h->given_cap < (size_t)n) {
     if (h->given_order) cudaFree(h->given_order);
-    if (h->adj_ws) cudaFree(h->adj_ws);
     h->given_order = nullptr;
     h->given_cap = 0;
     s = cuda_check(h, cudaMalloc((void**)&h->given_order, sizeof(int) * (size_t)n), "cudaMalloc(skeleton order)");
@@ -767,6 +766,7 @@ rbrp_status rbrp_destroy(rbrp_handle h) {
     if (h->hostA_dev) cudaFree(h->hostA_dev);
     if (h->given_order) cudaFree(h->given_order);
     if (h->adj_ws) cudaFree(h->adj_ws);
+    if (h->sketch_ws) cudaFree(h->sketch_ws);
     if (h->hst) cudaFreeHost(h->hst);
     for (auto e : h->block_events) cudaEventDestroy(e);
     for (auto e : h->prof_events) cudaEventDestroy(e);

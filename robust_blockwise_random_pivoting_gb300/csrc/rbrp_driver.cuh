@@ -199,6 +199,15 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
     if (h->hst->status == tc::ST_ERR_TIMEOUT)
       return set_error(h, RBRP_ERR_DEVICE_TIMEOUT, "a device-side wait timed out; the kernel aborted cleanly");
     if (h->hst->status) return set_error(h, RBRP_ERR_NUMERIC, "non-finite residual during pivoting");
+    {  // the loop state must stay in range: a block adds at most one trace entry and b positions
+      const State& q = *h->hst;
+      if (q.i < i || q.i > kmax || q.i - i > MAXB || q.nblocks < nb_host || q.nblocks > nb_host + 1 ||
+          q.bs_sampled < 0 || q.bs_sampled > MAXB || q.nK < 0 || q.nK > MAXB)
+        return set_error(h, RBRP_ERR_NUMERIC,
+                         "device loop state out of range after block attempt " + std::to_string(attempts) +
+                             " (i " + std::to_string(q.i) + ", nblocks " + std::to_string(q.nblocks) +
+                             ", sampled " + std::to_string(q.bs_sampled) + ", nK " + std::to_string(q.nK) + ")");
+    }
     if (h->hst->nblocks > nb_host) {
       attempt_of_block.push_back(attempts);
       nb_host = h->hst->nblocks;

@@ -68,6 +68,10 @@ struct rbrp_handle_st {
   void* df_buf = nullptr;      // double-float operands of the T solve
   size_t df_bytes = 0;
 
+  // Gaussian sketch matrix (rbrp_sketch.cu)
+  void* sketch_ws = nullptr;
+  size_t sketch_bytes = 0;
+
   // fixed-skeleton adjoint workspace (rbrp_adjoint.cu)
   void* adj_ws = nullptr;
   size_t adj_bytes = 0;

@@ -1,0 +1,117 @@
+"""GPU: the comparison IDs (CPQR ID, RandCPQR_OS, SID interpolation modes) and the sketch.
+
+The CPQR skeleton must equal LAPACK dgeqp3's (scipy ``qr(pivoting=True)``)
+pivot for pivot on inputs without near-ties, with T = R11^{-1} R12 to 1e-8.
+RandCPQR_OS must equal the same construction done by numpy/scipy on the
+library's own sketch.  The sketch must be the linear map G A with G of the
+requested scale.
+"""
+import numpy as np
+import pytest
+import scipy.linalg as sla
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def handle(rbrp_lib):
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from robust_blockwise_random_pivoting_gb300.rbrp import Handle
+    h = Handle(0)
+    yield h
+    h.close()
+
+
+def decaying(m, n, seed, rate=40.0):
+    rng = np.random.default_rng(seed)
+    U = np.linalg.qr(rng.standard_normal((m, min(m, n))))[0]
+    V = np.linalg.qr(rng.standard_normal((n, min(m, n))))[0]
+    s = np.exp(-np.arange(min(m, n)) / rate)
+    return (U * s) @ V.T
+
+
+def test_sketch_is_linear_map_with_scale(handle):
+    from robust_blockwise_random_pivoting_gb300.sketch_ids import gaussian_sketch
+    m, l = 700, 96
+    rng = np.random.default_rng(0)
+    B = rng.standard_normal((m, 150)).astype(np.float32)
+    A = np.concatenate([np.eye(m, dtype=np.float32), B], axis=1)
+    At = torch.from_numpy(A).cuda()
+    Y = gaussian_sketch(At, l, seed=5, scale=0.5, handle=handle).double().cpu().numpy()
+    G = Y[:, :m]
+    assert abs(G.mean()) < 0.02 and abs(G.std() - 0.5) < 0.02
+    np.testing.assert_allclose(Y[:, m:], G @ B, rtol=0, atol=1e-4 * np.abs(G @ B).max())
+    Y2 = gaussian_sketch(At, l, seed=5, scale=0.5, handle=handle).double().cpu().numpy()
+    assert np.array_equal(Y, Y2)
+    Y3 = gaussian_sketch(At, l, seed=6, scale=0.5, handle=handle).double().cpu().numpy()
+    assert not np.array_equal(Y, Y3)
+
+
+def test_cpqr_id_matches_lapack_pivots(handle):
+    from robust_blockwise_random_pivoting_gb300.sketch_ids import cpqr_id
+    A = decaying(300, 220, seed=1)
+    k = 60
+    sk, rd, T = cpqr_id(torch.from_numpy(A).cuda(), k, handle=handle)
+    _, R, piv = sla.qr(A, mode="economic", pivoting=True)
+    assert np.array_equal(sk.cpu().numpy(), piv[:k])
+    # T columns follow rd (the library's remaining order); LAPACK's R12 follows piv[k:]
+    Tref = sla.solve_triangular(R[:k, :k], R[:k, k:])
+    order = {c: j for j, c in enumerate(piv[k:])}
+    cols = np.array([order[c] for c in rd.cpu().numpy()])
+    np.testing.assert_allclose(T.cpu().numpy(), Tref[:, cols], rtol=0, atol=1e-8 * np.abs(Tref).max())
+
+
+def test_rand_cpqr_os_matches_numpy_on_same_sketch(handle):
+    from robust_blockwise_random_pivoting_gb300.sketch_ids import gaussian_sketch, rand_cpqr_os
+    A = decaying(500, 400, seed=2, rate=25.0)
+    At = torch.from_numpy(A).cuda()
+    r = 40
+    sk, rd, T = rand_cpqr_os(At, r, seed=9, handle=handle)
+    Y = gaussian_sketch(At, 2 * r, seed=9, handle=handle).double().cpu().numpy()
+    _, _, piv = sla.qr(Y[:r], mode="economic", pivoting=True)
+    assert np.array_equal(sk.cpu().numpy(), piv[:r])
+    S, R_ = sk.cpu().numpy(), rd.cpu().numpy()
+    Tref = np.linalg.lstsq(Y[:, S], Y[:, R_], rcond=None)[0]
+    np.testing.assert_allclose(T.cpu().numpy(), Tref, rtol=0, atol=1e-7 * np.abs(Tref).max())
+    # the sketched ID is a good ID of A itself
+    err = np.linalg.norm(A[:, R_] - A[:, S] @ T.cpu().numpy()) / np.linalg.norm(A)
+    s = np.linalg.svd(A, compute_uv=False)
+    opt = np.sqrt((s[r:] ** 2).sum() / (s ** 2).sum())
+    assert err < 30 * opt, (err, opt)
+
+
+def test_interpolation_sid_and_fsid(handle):
+    from robust_blockwise_random_pivoting_gb300.sketch_ids import interpolation
+    A = decaying(400, 300, seed=3, rate=30.0)
+    At = torch.from_numpy(A).cuda()
+    r = handle.column_id(At, b=16, tol=1e-8, seed=0)
+    k, perm = r.k, r.perm
+    p = perm.cpu().numpy()
+    T_sid = interpolation(At, perm, k, mode="sid", handle=handle).cpu().numpy()
+    Tref = np.linalg.lstsq(A[:, p[:k]], A[:, p[k:]], rcond=None)[0]
+    np.testing.assert_allclose(T_sid, Tref, rtol=0, atol=1e-7 * np.abs(Tref).max())
+    T_f = interpolation(At, perm, k, mode="fsid", oversampling=2.0, seed=4, handle=handle).cpu().numpy()
+    e_sid = np.linalg.norm(A[:, p[k:]] - A[:, p[:k]] @ T_sid)
+    e_f = np.linalg.norm(A[:, p[k:]] - A[:, p[:k]] @ T_f)
+    assert e_f < 10 * e_sid, (e_f, e_sid)
+
+
+def test_workspaces_survive_growth_of_other_buffers(rbrp_lib):
+    """A fixed-skeleton run that grows the skeleton-order buffer leaves the sketch workspace intact."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from robust_blockwise_random_pivoting_gb300.rbrp import Handle
+    from robust_blockwise_random_pivoting_gb300.sketch_ids import fixed_skeleton, gaussian_sketch
+    h = Handle(0)
+    try:
+        A = torch.from_numpy(decaying(120, 90, seed=5)).cuda()
+        Y1 = gaussian_sketch(A, 32, seed=1, handle=h).cpu()
+        W = torch.from_numpy(decaying(150, 400, seed=6)).cuda()   # wider than any earlier run
+        fixed_skeleton(h, W, torch.arange(0, 400, 10, dtype=torch.int32), b=16)
+        Y2 = gaussian_sketch(A, 32, seed=1, handle=h).cpu()
+        assert torch.equal(Y1, Y2)
+    finally:
+        h.close()
