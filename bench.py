@@ -46,10 +46,16 @@ WORKLOADS = {
     "gexp1000": dict(kind="gexp", m=1000, n=1000, decay=20.0, b=40, tol=1e-12),
     "gmm65k": dict(kind="gmm", m=1024, n=65536, clusters=20, b=32, tol=1e-4),
     "adjoint8k": dict(kind="adjoint", n=8192, dim=8, lengthscale=1.5, b=64, tol=1e-6),
+    "idcmp16k": dict(kind="idcmp", d=1000, n=16384, clusters=100, b=32, nb=6, tol=1e-12),
 }
 
 
 def describe(name, wl):
+    if wl["kind"] == "idcmp":
+        return (f"{name}: the C++ driver's Gaussian-mixture matrix {wl['d']}x{wl['n']} ({wl['clusters']} clusters, "
+                f"point i of cluster c shifted by 10(c+1) in coordinate c), FP64; a step is one RBRP (b={wl['b']}) "
+                f"to rank {wl['nb'] * wl['b']}; RandCPQR_OS, RandLUPP_OS and the CPQR ID are timed at the first "
+                f"{wl['nb']} RBRP ranks, as the driver does")
     if wl["kind"] == "adjoint":
         return (f"{name}: fixed-skeleton ID loss ||A - A(:,S) T||^2 + ||T w||^2 and its gradient, Gaussian kernel "
                 f"{wl['n']}^2 on N(0, I_{wl['dim']}) points, l={wl['lengthscale']}, S from FP32 RBRP at squared tol "
@@ -672,6 +678,76 @@ def run_adjoint(args, wl, name, ctx):
     }
 
 
+def run_idcmp(args, wl, name, ctx):
+    """The driver's comparison: RBRP, then the comparison IDs at RBRP's first ranks; returns the JSON line."""
+    torch = ctx.torch
+    from robust_blockwise_random_pivoting_gb300 import workloads as W
+    from robust_blockwise_random_pivoting_gb300.rbrp import Handle
+    from robust_blockwise_random_pivoting_gb300.sketch_ids import cpqr_id, rand_cpqr_os, rand_lupp_os
+    seed = ctx.rank
+    A_host = W.driver_gmm(wl["n"], wl["d"], wl["clusters"], seed)
+    A = torch.from_numpy(A_host).to(ctx.device).t().contiguous().t()
+    h = Handle(ctx.local)
+    nrm2 = float((A * A).sum())
+    kmax = wl["nb"] * wl["b"]
+    kw = dict(b=wl["b"], tol=wl["tol"], kmax=kmax, seed=seed)
+
+    def sq_err(sk, rd, T):
+        E = A[:, rd.long()] - A[:, sk.long()] @ T
+        return float((E * E).sum()) / nrm2
+
+    for _ in range(args.warmup):
+        r = h.column_id(A, **kw)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    ctx.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(ctx.uuid) as clk:
+        ev[0].record(ctx.stream)
+        for _ in range(args.steps):
+            r = h.column_id(A, **kw)
+        ev[1].record(ctx.stream)
+        torch.cuda.synchronize()
+    clocks = clk.summary()
+    dt = ctx.max_over_ranks(ev[0].elapsed_time(ev[1]) * 1e-3)
+    ranks = [int(x) for x in r.ranks[: wl["nb"]]]
+    rbrp_err = [float(x) for x in r.residuals[: wl["nb"]]]
+
+    def timed(fn, k):
+        fn(k)                                   # warm: workspaces and one-time attributes
+        torch.cuda.synchronize()
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        e[0].record(ctx.stream)
+        sk, rd, T = fn(k)
+        e[1].record(ctx.stream)
+        torch.cuda.synchronize()
+        return e[0].elapsed_time(e[1]), sq_err(sk, rd, T)
+
+    methods = {
+        "RandCPQR_OS": lambda k: rand_cpqr_os(A, k, seed=seed, handle=h),
+        "RandLUPP_OS": lambda k: rand_lupp_os(A, k, seed=seed, handle=h),
+        "CPQR_ID": lambda k: cpqr_id(A, k, handle=h),
+    }
+    comparison = {"ranks": ranks, "RBRP": {"sq_rel_err": rbrp_err, "ms_to_last_rank": 1e3 * dt / args.steps}}
+    for label, fn in methods.items():
+        res = [timed(fn, k) for k in ranks]
+        comparison[label] = {"ms": [x[0] for x in res], "sq_rel_err": [x[1] for x in res]}
+    cpu = None
+    if not args.no_cpu and ctx.rank == 0:
+        dtc, f, o = cpu_sample(A_host, wl, seed, 2 * wl["b"])
+        cpu = {"value": 1.0 / dtc, "unit": "samples/s", "cores": threads(), "kind": "port",
+               "sample": f"oracle port (numpy/scipy FP64) of blocked_rpid on the first {2 * wl['b']} ranks "
+                         f"of the same matrix, {dtc:.3f} s"}
+    h.close()
+    return {
+        "metric": METRIC, "value": ctx.world * args.steps / dt, "unit": "matrices/s", "n_gpus": ctx.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded Philox)",
+        "config": {"workload": describe(name, wl), "comparison": comparison},
+        "cpu_baseline": cpu, "e2e": None, "clocks": clocks, "gpu_launches": None,
+    }
+
+
 def run_reference_batched(args, wl, name):
     """Reference arm for the batched workload: the oracle port on a bounded sample of blocks per step."""
     if int(os.environ.get("RANK", "0")) != 0:
@@ -711,6 +787,10 @@ def main():
         if wl["kind"] == "adjoint":
             print(json.dumps({"impl": "reference", "unavailable": "the reference has no differentiable ID"}))
             return
+        if wl["kind"] == "idcmp":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference's comparison IDs are "
+                              "cuSOLVER/MAGMA GPU code; its CPU RBRP is the reference arm of the other workloads"}))
+            return
         if wl["kind"] == "blocks":
             run_reference_batched(args, wl, args.workload)
         else:
@@ -721,6 +801,8 @@ def main():
         line = run_batched(args, wl, args.workload, ctx)
     elif wl["kind"] == "adjoint":
         line = run_adjoint(args, wl, args.workload, ctx)
+    elif wl["kind"] == "idcmp":
+        line = run_idcmp(args, wl, args.workload, ctx)
     else:
         line = run_single(args, wl, args.workload, ctx)
     if ctx.rank == 0:

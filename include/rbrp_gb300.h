@@ -135,6 +135,18 @@ rbrp_status rbrp_fixed_id_adjoint_f32(rbrp_handle h, int m, int n, const float* 
 rbrp_status rbrp_sketch_gaussian_f32(rbrp_handle h, int l, int m, int n, const float* dA, int64_t lda,
                                      uint64_t seed, float scale, float* dY, int64_t ldy);
 
+/* Row pivots of the partial-pivoted LU of W^T, as RandLUPP_OS takes them from
+ * cusolverDnDgetrf on the first k rows of its sketch (gpu/randLUPP_OS.cu:48-90)
+ * and turns them into a permutation (pivots_to_permutation, gpu/permute.cu:8-23).
+ * dW is k x n (ldw >= k, 1 <= k <= n, k <= 25600) FP64; dPerm (n ints) receives
+ * the permutation of W's columns (perm[:k] is the skeleton); dIpiv (k ints, may
+ * be NULL) receives LAPACK's 1-based pivots.  Ties go to the first current
+ * position, as idamax.  RBRP_ERR_NUMERIC for a non-finite W or a zero pivot
+ * (the reference asserts info == 0).  One cooperative launch; synchronises the
+ * handle's stream. */
+rbrp_status rbrp_lupp_pivots_f64(rbrp_handle h, int k, int n, const double* dW, int64_t ldw, int* dPerm,
+                                 int* dIpiv);
+
 /* T (k x (n-k), column major) of the last run, into a device buffer with ldt >= k. */
 rbrp_status rbrp_copy_T(rbrp_handle h, double* dT, int64_t ldt);
 /* Device pointer of T of the last run (ld = k), valid until the next run. */

@@ -342,7 +342,7 @@ Layout make_layout(int m, int n, int kmax, size_t elem, bool residual) {
   L.n = n;
   L.kmax = kmax;
   L.ntiles = (m + 63) / 64;
-  L.nproj = (n + 63) / 64;
+  L.nproj = (n + 31) / 32;   // partials of the projection: 32 positions per CTA at the finest
   L.cpart_rows = residual ? 1 : (kmax > 304 * 32 ? kmax : 304 * 32);
   L.elem = elem;
   L.residual = residual;
@@ -767,6 +767,7 @@ rbrp_status rbrp_destroy(rbrp_handle h) {
     if (h->given_order) cudaFree(h->given_order);
     if (h->adj_ws) cudaFree(h->adj_ws);
     if (h->sketch_ws) cudaFree(h->sketch_ws);
+    if (h->lupp_ws) cudaFree(h->lupp_ws);
     if (h->hst) cudaFreeHost(h->hst);
     for (auto e : h->block_events) cudaEventDestroy(e);
     for (auto e : h->prof_events) cudaEventDestroy(e);

@@ -7,6 +7,7 @@
 // lines 76-173, with the stopping rule of cell 11 line 164 (squared tol).
 #pragma once
 #include <algorithm>
+#include <type_traits>
 
 #include "rbrp_internal.h"
 #include "rbrp_kernels.cuh"
@@ -177,9 +178,25 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
       k_norm_reduce<<<nproj, 256, 0, st>>>(h->part_norm, nsplit, n, h->st, h->diags, h->part_res, h->part_nnz);
       prof_end(h, RBRP_PHASE_UPDATE, ev, 0.0, 0.0, 2);
     } else {
-      nproj = (n - i + 63) / 64;
-      k_project<T><<<nproj, 256, 0, st>>>(Q, m, dA, lda, h->perm, h->st, m, n, h->R, n, h->diags,
-                                          h->part_res, h->part_nnz);
+      // basis tile height: the smallest KB >= b (kept <= b); b <= 8 takes the column-streaming form
+      auto project = [&](auto kb) {
+        constexpr int KB = decltype(kb)::value;
+        nproj = (n - i + ProjTile<KB>::PC - 1) / ProjTile<KB>::PC;
+        k_project<T, KB><<<nproj, 256, 0, st>>>(Q, m, dA, lda, h->perm, h->st, m, n, h->R, n, h->diags,
+                                                h->part_res, h->part_nnz);
+      };
+      auto skinny = [&](auto kb) {
+        constexpr int KB = decltype(kb)::value;
+        nproj = (n - i + SKINNY_COLS - 1) / SKINNY_COLS;
+        k_project_skinny<T, KB><<<nproj, 256, 0, st>>>(Q, m, dA, lda, h->perm, h->st, m, n, h->R, n, h->diags,
+                                                       h->part_res, h->part_nnz);
+      };
+      if (p.b <= 1) skinny(std::integral_constant<int, 1>{});
+      else if (p.b <= 4) skinny(std::integral_constant<int, 4>{});
+      else if (p.b <= 8) skinny(std::integral_constant<int, 8>{});
+      else if (p.b <= 16) project(std::integral_constant<int, 16>{});
+      else if (p.b <= 32) project(std::integral_constant<int, 32>{});
+      else project(std::integral_constant<int, 64>{});
       prof_end(h, RBRP_PHASE_PROJECT, ev, 0.0, 0.0, 1);
     }
     ev = prof_begin(h);

@@ -71,6 +71,9 @@ struct rbrp_handle_st {
   // Gaussian sketch matrix (rbrp_sketch.cu)
   void* sketch_ws = nullptr;
   size_t sketch_bytes = 0;
+  // LU-pivot workspace (rbrp_lupp.cu): W^T, argmax partials, barrier, positions
+  void* lupp_ws = nullptr;
+  size_t lupp_bytes = 0;
 
   // fixed-skeleton adjoint workspace (rbrp_adjoint.cu)
   void* adj_ws = nullptr;

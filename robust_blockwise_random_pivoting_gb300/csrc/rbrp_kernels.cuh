@@ -12,6 +12,7 @@
 //                 R(I2, p) = W, diags(p) -= ||W(:, p)||^2 (clipped at 0)
 //   k_finish      residual, stop rule, per-block trace
 #pragma once
+#include <type_traits>
 #include "rbrp_common.cuh"
 #include "rbrp_df.cuh"
 #include "rbrp_sampler.cuh"
@@ -148,6 +149,7 @@ k_cgs_coef(const T* __restrict__ Q, int64_t ldq, const T* __restrict__ A, int64_
   const int rb = blockIdx.z * rows_per_split, re = min(m, rb + rows_per_split);
   if (tid < MAXB) cs[tid] = tid < bss ? cols[tid] : -1;
   const int al = tid >> 3, cl = tid & 7;
+  const int nq = (bss + 7) >> 3;   // column groups that hold sampled columns (uniform: FP64 work only there)
   T acc[8];
 #pragma unroll
   for (int q = 0; q < 8; ++q) acc[q] = T(0);
@@ -166,12 +168,20 @@ k_cgs_coef(const T* __restrict__ Q, int64_t ldq, const T* __restrict__ A, int64_
       As[kk][cc] = (r < re && c >= 0) ? A[r + (int64_t)c * lda] : T(0);
     }
     __syncthreads();
+    // column groups as a compile-time count: predicated-off FP64 FMAs would still take issue slots
+    auto fmas = [&](auto nqc) {
+      constexpr int NQ = decltype(nqc)::value;
 #pragma unroll 8
-    for (int kk = 0; kk < 32; ++kk) {
-      const T qa = Qs[kk][al];
+      for (int kk = 0; kk < 32; ++kk) {
+        const T qa = Qs[kk][al];
 #pragma unroll
-      for (int q = 0; q < 8; ++q) acc[q] = fma(qa, As[kk][cl + 8 * q], acc[q]);
-    }
+        for (int q = 0; q < NQ; ++q) acc[q] = fma(qa, As[kk][cl + 8 * q], acc[q]);
+      }
+    };
+    if (nq <= 1) fmas(std::integral_constant<int, 1>{});
+    else if (nq <= 2) fmas(std::integral_constant<int, 2>{});
+    else if (nq <= 4) fmas(std::integral_constant<int, 4>{});
+    else fmas(std::integral_constant<int, 8>{});
   }
   const int a = a0 + al;
   if (a < i) {
@@ -213,6 +223,7 @@ k_cgs_update(const T* __restrict__ A, int64_t lda, const int* __restrict__ cols,
   const int r0 = blockIdx.x * 64;
   if (tid < MAXB) cs[tid] = tid < bss ? cols[tid] : -1;
   const int ty = tid >> 4, tx = tid & 15;
+  const int nv = (bss + 15) >> 4;   // column groups that hold sampled columns (uniform over the CTA)
   T acc[4][4];
 #pragma unroll
   for (int u = 0; u < 4; ++u)
@@ -232,18 +243,26 @@ k_cgs_update(const T* __restrict__ A, int64_t lda, const int* __restrict__ cols,
       Cs[aa][cc] = (a0 + aa < i) ? C[(int64_t)(a0 + aa) * MAXB + cc] : T(0);
     }
     __syncthreads();
+    // column groups as a compile-time count: predicated-off FP64 FMAs would still take issue slots
+    auto fmas = [&](auto nvc) {
+      constexpr int NV = decltype(nvc)::value;
 #pragma unroll 4
-    for (int aa = 0; aa < 32; ++aa) {
-      T qv[4], cv[4];
+      for (int aa = 0; aa < 32; ++aa) {
+        T qv[4], cv[NV];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) qv[u] = Qs[ty * 4 + u][aa];
+        for (int u = 0; u < 4; ++u) qv[u] = Qs[ty * 4 + u][aa];
 #pragma unroll
-      for (int v = 0; v < 4; ++v) cv[v] = Cs[aa][tx + 16 * v];
+        for (int v = 0; v < NV; ++v) cv[v] = Cs[aa][tx + 16 * v];
 #pragma unroll
-      for (int u = 0; u < 4; ++u)
+        for (int u = 0; u < 4; ++u)
 #pragma unroll
-        for (int v = 0; v < 4; ++v) acc[u][v] = fma(qv[u], cv[v], acc[u][v]);
-    }
+          for (int v = 0; v < NV; ++v) acc[u][v] = fma(qv[u], cv[v], acc[u][v]);
+      }
+    };
+    if (nv <= 1) fmas(std::integral_constant<int, 1>{});
+    else if (nv <= 2) fmas(std::integral_constant<int, 2>{});
+    else if (nv <= 3) fmas(std::integral_constant<int, 3>{});
+    else fmas(std::integral_constant<int, 4>{});
   }
   __syncthreads();
 #pragma unroll
@@ -640,93 +659,235 @@ k_panel2(const double* __restrict__ Q1, int m, const State* __restrict__ st, con
 // residual-norm downdate (python/RBRP.ipynb cell 11 lines 132, 154-158;
 // matlab/RBRP.m:103-104,112; the reference applies Householder reflectors to
 // the whole trailing matrix instead, gpu/rbrp.cu:297-330, 453-466).
-// CTA tile: all kept (<= 64) basis vectors x 64 positions, K loop over m.
+// CTA tile: KB basis vectors (KB >= kept, chosen on the host from b) x PC =
+// 4096 / KB positions, K loop over m in chunks of KC rows; every thread holds a
+// (KB / TY) x 4 accumulator block.  Each accumulator sums over the rows in
+// ascending order, so W is the same for every KB: KB only removes the work on
+// basis rows that do not exist (the FP64 pipe is the bound of this kernel).
 // ===========================================================================
-template <typename T>
+template <int KB>
+struct ProjTile {
+  static constexpr int MU = KB < 4 ? KB : 4;     // basis rows per thread
+  static constexpr int TY = KB / MU;             // thread rows
+  static constexpr int TX = 256 / TY;            // thread columns
+  static constexpr int PC = TX * 4;              // positions per CTA
+  static constexpr int KC = 4096 / PC < 32 ? 4096 / PC : 32;   // rows per K chunk
+};
+
+template <typename T, int KB>
 __global__ void __launch_bounds__(256)
 k_project(const T* __restrict__ Q, int64_t ldq, const T* __restrict__ A, int64_t lda,
           const int* __restrict__ perm, const State* __restrict__ st, int m, int n,
           double* __restrict__ R, int64_t ldr, double* __restrict__ diags,
           double* __restrict__ part_res, int* __restrict__ part_nnz) {
-  constexpr size_t kOps = sizeof(T) * (32 * MAXB + 32 * (MAXB + 1));
-  constexpr size_t kW = sizeof(double) * MAXB * (MAXB + 1);
+  using P = ProjTile<KB>;
+  constexpr int PC = P::PC, KC = P::KC, TX = P::TX, TY = P::TY, MU = P::MU;
+  constexpr size_t kOps = sizeof(T) * (KC * KB + KC * (PC + 1));
+  constexpr size_t kW = sizeof(double) * KB * (PC + 1);
   __shared__ __align__(16) unsigned char raw[kOps > kW ? kOps : kW];
-  T(*Qs)[MAXB] = reinterpret_cast<T(*)[MAXB]>(raw);
-  T(*As)[MAXB + 1] = reinterpret_cast<T(*)[MAXB + 1]>(raw + sizeof(T) * 32 * MAXB);
-  double(*Ws)[MAXB + 1] = reinterpret_cast<double(*)[MAXB + 1]>(raw);
-  __shared__ int cs[MAXB];
-  __shared__ double snew[MAXB];
+  T(*Qs)[KB] = reinterpret_cast<T(*)[KB]>(raw);
+  T(*As)[PC + 1] = reinterpret_cast<T(*)[PC + 1]>(raw + sizeof(T) * KC * KB);
+  double(*Ws)[PC + 1] = reinterpret_cast<double(*)[PC + 1]>(raw);
+  __shared__ int cs[PC];
+  __shared__ double snew[PC];
+  __shared__ double red_s[PC / 64];
+  __shared__ int red_c[PC / 64];
   const int tid = threadIdx.x;
-  const int i = st->i, kept = st->bs;
-  const int pbase = i + kept + blockIdx.x * 64;
+  // kept <= b <= KB by construction (the host picks KB from b); the clamp only keeps smem in bounds
+  const int i = st->i, kept = min(st->bs, KB);
+  const int pbase = i + st->bs + blockIdx.x * PC;
   if (kept == 0 || pbase >= n) {
     if (tid == 0) { part_res[blockIdx.x] = 0.0; part_nnz[blockIdx.x] = 0; }
     return;
   }
-  if (tid < 64) cs[tid] = (pbase + tid < n) ? perm[pbase + tid] : -1;
-  const int ty = tid >> 4, tx = tid & 15;
-  T acc[4][4];
+  for (int t = tid; t < PC; t += 256) cs[t] = (pbase + t < n) ? perm[pbase + t] : -1;
+  const int ty = tid / TX, tx = tid % TX;
+  const int me = (kept + TY - 1) / TY;   // <= MU
+  T acc[MU][4];
 #pragma unroll
-  for (int u = 0; u < 4; ++u)
+  for (int u = 0; u < MU; ++u)
 #pragma unroll
     for (int v = 0; v < 4; ++v) acc[u][v] = T(0);
   const T* Qb = Q + (int64_t)i * ldq;
-  for (int r0 = 0; r0 < m; r0 += 32) {
+  for (int r0 = 0; r0 < m; r0 += KC) {
     __syncthreads();
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      const int idx = tid + 256 * q, kk = idx & 31, aa = idx >> 5;
+    for (int idx = tid; idx < KC * KB; idx += 256) {
+      const int kk = idx % KC, aa = idx / KC;
       const int r = r0 + kk;
       Qs[kk][aa] = (r < m && aa < kept) ? Qb[r + (int64_t)aa * ldq] : T(0);
     }
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      const int idx = tid + 256 * q, kk = idx & 31, cc = idx >> 5;
+    for (int q = 0; q < (KC * PC) / 256; ++q) {
+      const int idx = tid + 256 * q, kk = idx % KC, cc = idx / KC;
       const int r = r0 + kk, c = cs[cc];
       As[kk][cc] = (r < m && c >= 0) ? A[r + (int64_t)c * lda] : T(0);
     }
     __syncthreads();
+    // basis rows per thread that exist (kept <= TY * me) as a compile-time count:
+    // predicated-off FP64 FMAs would still take issue slots on the FP64 pipe
+    auto fmas = [&](auto mec) {
+      constexpr int ME = decltype(mec)::value;
 #pragma unroll 4
-    for (int kk = 0; kk < 32; ++kk) {
-      T qv[4], av[4];
+      for (int kk = 0; kk < KC; ++kk) {
+        T qv[ME], av[4];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) qv[u] = Qs[kk][ty + 16 * u];
+        for (int u = 0; u < ME; ++u) qv[u] = Qs[kk][ty + TY * u];
 #pragma unroll
-      for (int v = 0; v < 4; ++v) av[v] = As[kk][tx + 16 * v];
+        for (int v = 0; v < 4; ++v) av[v] = As[kk][tx + TX * v];
 #pragma unroll
-      for (int u = 0; u < 4; ++u)
+        for (int u = 0; u < ME; ++u)
 #pragma unroll
-        for (int v = 0; v < 4; ++v) acc[u][v] = fma(qv[u], av[v], acc[u][v]);
-    }
+          for (int v = 0; v < 4; ++v) acc[u][v] = fma(qv[u], av[v], acc[u][v]);
+      }
+    };
+    if (MU == 1 || me <= 1) fmas(std::integral_constant<int, 1>{});
+    else if (me <= 2) fmas(std::integral_constant<int, (MU < 2 ? MU : 2)>{});
+    else if (me <= 3) fmas(std::integral_constant<int, (MU < 3 ? MU : 3)>{});
+    else fmas(std::integral_constant<int, MU>{});
   }
   __syncthreads();
 #pragma unroll
-  for (int u = 0; u < 4; ++u)
+  for (int u = 0; u < MU; ++u)
 #pragma unroll
-    for (int v = 0; v < 4; ++v) Ws[ty + 16 * u][tx + 16 * v] = (double)acc[u][v];
+    for (int v = 0; v < 4; ++v) Ws[ty + TY * u][tx + TX * v] = (double)acc[u][v];
   __syncthreads();
-  for (int idx = tid; idx < kept * 64; idx += 256) {
-    const int a = idx >> 6, c = idx & 63;
+  for (int idx = tid; idx < kept * PC; idx += 256) {
+    const int a = idx / PC, c = idx % PC;
     if (pbase + c < n) R[(int64_t)(i + a) * ldr + pbase + c] = Ws[a][c];
   }
-  if (tid < 64) {
-    const int p = pbase + tid;
+  for (int t = tid; t < PC; t += 256) {
+    const int p = pbase + t;
     double d = 0.0;
     if (p < n) {
       double s = 0.0;
-      for (int a = 0; a < kept; ++a) s = fma(Ws[a][tid], Ws[a][tid], s);
+      for (int a = 0; a < kept; ++a) s = fma(Ws[a][t], Ws[a][t], s);
       d = diags[p] - s;
       d = d > 0.0 ? d : (d == d ? 0.0 : d);
       diags[p] = d;
     }
-    snew[tid] = d;
+    snew[t] = d;
+  }
+  __syncthreads();
+  // CTA partial of the residual and of the nonzero count, positions in ascending order
+  // in chunks of 64 (the sum order of the 64-position tile this kernel generalises)
+  if (tid < PC / 64) {
+    double sacc = 0.0;
+    int c = 0;
+    for (int t = tid * 64; t < tid * 64 + 64; ++t) { sacc += snew[t]; c += snew[t] > 0.0; }
+    red_s[tid] = sacc;
+    red_c[tid] = c;
   }
   __syncthreads();
   if (tid == 0) {
-    double s = 0.0;
+    double sacc = 0.0;
     int c = 0;
-    for (int t = 0; t < 64; ++t) { s += snew[t]; c += snew[t] > 0.0; }
-    part_res[blockIdx.x] = s;
+    for (int t = 0; t < PC / 64; ++t) { sacc += red_s[t]; c += red_c[t]; }
+    part_res[blockIdx.x] = sacc;
+    part_nnz[blockIdx.x] = c;
+  }
+}
+
+// Skinny form of the same projection for b <= 8 (a GEMV shape: greedy b = 1 is
+// column-pivoted QR).  Each warp streams CW = 4 whole columns (coalesced over
+// rows) against the basis staged in shared memory, MC rows at a time; lanes keep
+// strided partial sums that a butterfly combines.  32 positions per CTA.
+constexpr int SKINNY_COLS = 32;
+
+template <typename T, int KB>
+__global__ void __launch_bounds__(256)
+k_project_skinny(const T* __restrict__ Q, int64_t ldq, const T* __restrict__ A, int64_t lda,
+                 const int* __restrict__ perm, const State* __restrict__ st, int m, int n,
+                 double* __restrict__ R, int64_t ldr, double* __restrict__ diags,
+                 double* __restrict__ part_res, int* __restrict__ part_nnz) {
+  constexpr int CW = 4, MC = 256, NW = 8;
+  static_assert(NW * CW == SKINNY_COLS, "positions per CTA");
+  __shared__ T Qs[KB][MC];   // basis chunk, row index fastest: lanes read consecutive rows
+  __shared__ double red_s[NW];
+  __shared__ int red_c[NW];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // kept <= b <= KB by construction (the host picks KB from b); the clamp only keeps smem in bounds
+  const int i = st->i, kept = min(st->bs, KB);
+  const int pbase = i + st->bs + blockIdx.x * SKINNY_COLS;
+  if (kept == 0 || pbase >= n) {
+    if (tid == 0) { part_res[blockIdx.x] = 0.0; part_nnz[blockIdx.x] = 0; }
+    return;
+  }
+  int col[CW];
+#pragma unroll
+  for (int c = 0; c < CW; ++c) {
+    const int p = pbase + warp * CW + c;
+    col[c] = p < n ? perm[p] : -1;
+  }
+  T acc[CW][KB];
+#pragma unroll
+  for (int c = 0; c < CW; ++c)
+#pragma unroll
+    for (int a = 0; a < KB; ++a) acc[c][a] = T(0);
+  const T* Qb = Q + (int64_t)i * ldq;
+  for (int r0 = 0; r0 < m; r0 += MC) {
+    __syncthreads();
+    for (int idx = tid; idx < KB * MC; idx += 256) {
+      const int a = idx / MC, rr = idx % MC, r = r0 + rr;
+      Qs[a][rr] = (r < m && a < kept) ? Qb[r + (int64_t)a * ldq] : T(0);
+    }
+    __syncthreads();
+    const int rend = min(MC, m - r0);
+#pragma unroll 2
+    for (int rr = lane; rr < rend; rr += 32) {
+      T av[CW], qv[KB];
+#pragma unroll
+      for (int c = 0; c < CW; ++c) av[c] = col[c] >= 0 ? A[(r0 + rr) + (int64_t)col[c] * lda] : T(0);
+#pragma unroll
+      for (int a = 0; a < KB; ++a) qv[a] = Qs[a][rr];
+#pragma unroll
+      for (int c = 0; c < CW; ++c)
+#pragma unroll
+        for (int a = 0; a < KB; ++a) acc[c][a] = fma(av[c], qv[a], acc[c][a]);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < CW; ++c)
+#pragma unroll
+    for (int a = 0; a < KB; ++a)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc[c][a] += __shfl_xor_sync(0xffffffffu, acc[c][a], o);
+  double dsum = 0.0;
+  int dcnt = 0;
+#pragma unroll
+  for (int c = 0; c < CW; ++c) {
+    const int p = pbase + warp * CW + c;
+    if (lane == c && p < n) {
+      double s = 0.0;
+#pragma unroll
+      for (int a = 0; a < KB; ++a) {
+        if (a < kept) {
+          const double w = (double)acc[c][a];
+          R[(int64_t)(i + a) * ldr + p] = w;
+          s = fma(w, w, s);
+        }
+      }
+      double d = diags[p] - s;
+      d = d > 0.0 ? d : (d == d ? 0.0 : d);
+      diags[p] = d;
+      dsum = d;
+      dcnt = d > 0.0;
+    }
+  }
+#pragma unroll
+  for (int o = 1; o < CW; o <<= 1) {
+    dsum += __shfl_xor_sync(0xffffffffu, dsum, o);
+    dcnt += __shfl_xor_sync(0xffffffffu, dcnt, o);
+  }
+  if (lane == 0) {
+    red_s[warp] = dsum;
+    red_c[warp] = dcnt;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    double sacc = 0.0;
+    int c = 0;
+    for (int w = 0; w < NW; ++w) { sacc += red_s[w]; c += red_c[w]; }
+    part_res[blockIdx.x] = sacc;
     part_nnz[blockIdx.x] = c;
   }
 }

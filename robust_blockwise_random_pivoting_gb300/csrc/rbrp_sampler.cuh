@@ -122,8 +122,10 @@ __device__ void sample_block(State* st, const double* __restrict__ diags, const 
     if (tid == 0) s_size = s_found;
     __syncthreads();
   } else {
-    // keys (ascending = preferred)
+    // keys (ascending = preferred); each thread also keeps its smallest (key, position)
     int npos = 0;
+    unsigned long long bk = ~0ull;
+    int bj = 0x7fffffff;
     for (int j = lo; j < hi; ++j) {
       const double wj = w[j];
       unsigned long long key = ~0ull;
@@ -145,79 +147,104 @@ __device__ void sample_block(State* st, const double* __restrict__ diags, const 
         }
       }
       kbuf[j] = key;
+      if (key < bk) bk = key, bj = j;
     }
     npos = block_sum(npos, shi);
     const int size = min(req, npos);
-    // radix select of the size-th smallest key
-    unsigned long long prefix = 0ull, mask = 0ull;
-    int krank = size;
-    for (int shift = 56; shift >= 0 && size > 0; shift -= 8) {
-      for (int d = tid; d < 256; d += blockDim.x) hist[d] = 0u;
-      __syncthreads();
-      for (int j = lo; j < hi; ++j) {
-        const unsigned long long k = kbuf[j];
-        if ((k & mask) == prefix) atomicAdd(&hist[(k >> shift) & 0xFF], 1u);
+    if (size == 1) {
+      // one index (greedy b = 1 is column-pivoted QR): argmin of (key, position),
+      // the element the radix select below would return
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long ok = __shfl_xor_sync(0xffffffffu, bk, o);
+        const int oj = __shfl_xor_sync(0xffffffffu, bj, o);
+        if (ok < bk || (ok == bk && oj < bj)) bk = ok, bj = oj;
+      }
+      if ((tid & 31) == 0) {
+        s_key[tid >> 5] = bk;
+        s_cand[tid >> 5] = bj;
       }
       __syncthreads();
       if (tid == 0) {
-        int cum = 0, d = 0;
-        for (; d < 255; ++d) {
-          if (cum + (int)hist[d] >= krank) break;
-          cum += (int)hist[d];
-        }
-        s_digit = d;
-        s_krank = krank - cum;
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+          if (s_key[w] < s_key[0] || (s_key[w] == s_key[0] && s_cand[w] < s_cand[0])) s_key[0] = s_key[w], s_cand[0] = s_cand[w];
+        s_rel[0] = s_cand[0];
+        s_size = 1;
+        s_found = 1;
       }
       __syncthreads();
-      prefix |= (unsigned long long)s_digit << shift;
-      mask |= 0xFFull << shift;
-      krank = s_krank;
-      __syncthreads();
-    }
-    const unsigned long long kth = prefix;
-    int nlt = 0, neq = 0;
-    for (int j = lo; j < hi; ++j) {
-      const unsigned long long k = kbuf[j];
-      nlt += k < kth;
-      neq += k == kth;
-    }
-    int tot_lt, tot_eq;
-    const int off_lt = block_exclusive_scan(nlt, shi, &tot_lt);
-    const int off_eq = block_exclusive_scan(neq, shi, &tot_eq);
-    const int ties = size - tot_lt;
-    int a = off_lt, e = off_eq;
-    if (size > 0) {
+    } else {
+      // radix select of the size-th smallest key
+      unsigned long long prefix = 0ull, mask = 0ull;
+      int krank = size;
+      for (int shift = 56; shift >= 0 && size > 0; shift -= 8) {
+        for (int d = tid; d < 256; d += blockDim.x) hist[d] = 0u;
+        __syncthreads();
+        for (int j = lo; j < hi; ++j) {
+          const unsigned long long k = kbuf[j];
+          if ((k & mask) == prefix) atomicAdd(&hist[(k >> shift) & 0xFF], 1u);
+        }
+        __syncthreads();
+        if (tid == 0) {
+          int cum = 0, d = 0;
+          for (; d < 255; ++d) {
+            if (cum + (int)hist[d] >= krank) break;
+            cum += (int)hist[d];
+          }
+          s_digit = d;
+          s_krank = krank - cum;
+        }
+        __syncthreads();
+        prefix |= (unsigned long long)s_digit << shift;
+        mask |= 0xFFull << shift;
+        krank = s_krank;
+        __syncthreads();
+      }
+      const unsigned long long kth = prefix;
+      int nlt = 0, neq = 0;
       for (int j = lo; j < hi; ++j) {
         const unsigned long long k = kbuf[j];
-        if (k < kth) {
-          s_key[a] = k;
-          s_cand[a] = j;
-          ++a;
-        } else if (k == kth) {
-          if (e < ties) {
-            s_key[tot_lt + e] = k;
-            s_cand[tot_lt + e] = j;
+        nlt += k < kth;
+        neq += k == kth;
+      }
+      int tot_lt, tot_eq;
+      const int off_lt = block_exclusive_scan(nlt, shi, &tot_lt);
+      const int off_eq = block_exclusive_scan(neq, shi, &tot_eq);
+      const int ties = size - tot_lt;
+      int a = off_lt, e = off_eq;
+      if (size > 0) {
+        for (int j = lo; j < hi; ++j) {
+          const unsigned long long k = kbuf[j];
+          if (k < kth) {
+            s_key[a] = k;
+            s_cand[a] = j;
+            ++a;
+          } else if (k == kth) {
+            if (e < ties) {
+              s_key[tot_lt + e] = k;
+              s_cand[tot_lt + e] = j;
+            }
+            ++e;
           }
-          ++e;
         }
       }
-    }
-    __syncthreads();
-    if (tid < size) {
-      const unsigned long long k = s_key[tid];
-      const int j = s_cand[tid];
-      int rank = 0;
-      for (int u = 0; u < size; ++u) {
-        const unsigned long long ku = s_key[u];
-        rank += (ku < k) || (ku == k && s_cand[u] < j);
+      __syncthreads();
+      if (tid < size) {
+        const unsigned long long k = s_key[tid];
+        const int j = s_cand[tid];
+        int rank = 0;
+        for (int u = 0; u < size; ++u) {
+          const unsigned long long ku = s_key[u];
+          rank += (ku < k) || (ku == k && s_cand[u] < j);
+        }
+        s_rel[rank] = j;
       }
-      s_rel[rank] = j;
+      if (tid == 0) {
+        s_size = size;
+        s_found = size;
+      }
+      __syncthreads();
     }
-    if (tid == 0) {
-      s_size = size;
-      s_found = size;
-    }
-    __syncthreads();
   }
   const int size = s_size;
   if (tid < size) {

@@ -13,6 +13,9 @@
   (``python/RBRP.ipynb`` cell 7 lines 1-37) for a given skeleton: ``'sid'``
   (least squares on A) and ``'fsid'`` (least squares on an oversampled sketch
   of A), both through the fixed-skeleton ID.
+* :func:`rand_lupp_os` - ``RandLUPP_OS`` (``gpu/randLUPP_OS.cu:14-119``): the
+  same sketch with 2k rows, the skeleton from the partial-pivoted LU of
+  Y(1:k, :)^T (:func:`lupp_pivots`), and T = Y(:, S)^+ Y(:, rd).
 * :func:`gaussian_sketch` - ``Y = G A`` with Philox Gaussian G
   (``rbrp_sketch_gaussian_f32``).
 """
@@ -87,6 +90,35 @@ def rand_cpqr_os(A, r, seed=0, handle=None):
     S = piv.perm[: piv.k].clone()
     rd = piv.perm[piv.k:].clone()
     perm_run, T_run = fixed_skeleton(h, _cm(Y, torch.float64), S, b=min(64, max(1, S.numel())))
+    return S, rd, _reorder(perm_run, T_run, S, rd)
+
+
+def lupp_pivots(W, handle=None, return_ipiv=False):
+    """Column permutation of ``W`` (k x n) from the partial-pivoted LU of ``W^T`` (``rbrp_lupp_pivots_f64``).
+
+    ``perm[:k]`` are the pivot columns in pivot order; with ``return_ipiv`` also
+    LAPACK's 1-based ``ipiv`` (k,).  Computed in FP64.
+    """
+    h = handle or Handle(W.device.index)
+    W = _cm(W, torch.float64)
+    k, n = W.shape
+    perm = torch.empty(n, dtype=torch.int32, device=W.device)
+    ipiv = torch.empty(k, dtype=torch.int32, device=W.device) if return_ipiv else None
+    h._bind_stream(torch.cuda.current_stream(W.device))
+    check(h.lib.rbrp_lupp_pivots_f64(h.h, k, n, ctypes.c_void_p(W.data_ptr()), _ld(W),
+                                     ctypes.c_void_p(perm.data_ptr()),
+                                     ctypes.c_void_p(ipiv.data_ptr() if ipiv is not None else None)), h.h)
+    return (perm, ipiv) if return_ipiv else perm
+
+
+def rand_lupp_os(A, k, seed=0, handle=None):
+    """``RandLUPP_OS`` (``gpu/randLUPP_OS.cu:14-119``): returns ``(sk, rd, T)`` with T k x (n - k)."""
+    h = handle or Handle(A.device.index)
+    Y = _cm(gaussian_sketch(A, 2 * k, seed=seed, handle=h), torch.float64)
+    perm = lupp_pivots(Y[:k], handle=h)
+    S = perm[:k].clone()
+    rd = perm[k:].clone()
+    perm_run, T_run = fixed_skeleton(h, Y, S, b=min(64, k))
     return S, rd, _reorder(perm_run, T_run, S, rd)
 
 

@@ -87,6 +87,21 @@ def gmm(d=1024, npts=65536, nclusters=20, seed=0):
     return np.asfortranarray(A), labels
 
 
+def driver_gmm(npts=1000, d=1000, nclusters=100, seed=0):
+    """The C++ driver's Gaussian-mixture test matrix (``gpu/driver.cpp:94-109``), d x npts.
+
+    i.i.d. N(0, 1) entries; point i belongs to cluster c = i // (npts // nclusters)
+    and has 10 (c + 1) added to coordinate c.
+    """
+    per = npts // nclusters
+    if d < 1 or per < 1 or (npts - 1) // per >= d:
+        raise ValueError("need npts >= nclusters and d above the cluster count")
+    A = _gen(seed, 5).standard_normal((d, npts))
+    c = np.arange(npts) // per
+    A[c, np.arange(npts)] += 10.0 * (c + 1)
+    return np.asfortranarray(A)
+
+
 def kernel_block_shapes(nblocks=4096, lo=64, hi=2048, seed=0):
     """(m, n) of each off-diagonal kernel block, log-uniform in [lo, hi]."""
     rng = _gen(seed, 3)

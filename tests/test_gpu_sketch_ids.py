@@ -115,3 +115,75 @@ def test_workspaces_survive_growth_of_other_buffers(rbrp_lib):
         assert torch.equal(Y1, Y2)
     finally:
         h.close()
+
+
+def _lapack_lupp(W):
+    """Column permutation of W (k x n) from scipy's dgetrf on W^T, applied as sequential swaps."""
+    k, n = W.shape
+    _, piv = sla.lu_factor(W.T, check_finite=False)
+    P = np.arange(n)
+    for j in range(k):
+        P[[j, piv[j]]] = P[[piv[j], j]]
+    return P, piv + 1
+
+
+@pytest.mark.parametrize("k,n", [(1, 1), (1, 37), (7, 7), (48, 700), (130, 3000)])
+def test_lupp_pivots_match_lapack(handle, k, n):
+    from robust_blockwise_random_pivoting_gb300.sketch_ids import lupp_pivots
+    rng = np.random.default_rng(k * 1000 + n)
+    W = rng.standard_normal((k, n))
+    perm, ipiv = lupp_pivots(torch.from_numpy(W).cuda(), handle=handle, return_ipiv=True)
+    P, piv = _lapack_lupp(W)
+    assert np.array_equal(perm.cpu().numpy(), P)
+    assert np.array_equal(ipiv.cpu().numpy(), piv)
+
+
+def test_lupp_ties_go_to_the_first_position(handle):
+    from robust_blockwise_random_pivoting_gb300.sketch_ids import lupp_pivots
+    rng = np.random.default_rng(11)
+    W = np.round(rng.standard_normal((6, 90)) * 2)   # small integers: many exact ties in |value|
+    W[0, 3] = W[0, 7] = -9.0                          # first step: columns 3 and 7 tie; LAPACK takes 3
+    W[0, 40] = 9.0
+    perm = lupp_pivots(torch.from_numpy(W).cuda(), handle=handle).cpu().numpy()
+    P, _ = _lapack_lupp(W)
+    assert perm[0] == 3
+    assert np.array_equal(perm, P)
+
+
+def test_lupp_errors(handle):
+    from robust_blockwise_random_pivoting_gb300._lib import RBRPError
+    from robust_blockwise_random_pivoting_gb300.sketch_ids import lupp_pivots
+    rng = np.random.default_rng(2)
+    W = rng.standard_normal((5, 50))
+    Wz = W.copy()
+    Wz[4] = 0.0                      # rank 4 < k = 5: step 5 meets an exact zero pivot (dgetrf info = 5)
+    with pytest.raises(RBRPError, match="zero pivot"):
+        lupp_pivots(torch.from_numpy(Wz).cuda(), handle=handle)
+    Wn = W.copy()
+    Wn[1, 20] = np.nan
+    with pytest.raises(RBRPError, match="non-finite"):
+        lupp_pivots(torch.from_numpy(Wn).cuda(), handle=handle)
+    with pytest.raises(RBRPError):
+        lupp_pivots(torch.from_numpy(W[:, :2].copy()).cuda(), handle=handle)   # k = 5 > n = 2
+    # the handle stays usable
+    perm = lupp_pivots(torch.from_numpy(W).cuda(), handle=handle).cpu().numpy()
+    assert np.array_equal(perm, _lapack_lupp(W)[0])
+
+
+def test_rand_lupp_os_matches_numpy_on_same_sketch(handle):
+    from robust_blockwise_random_pivoting_gb300.sketch_ids import gaussian_sketch, rand_lupp_os
+    A = decaying(500, 400, seed=7, rate=25.0)
+    At = torch.from_numpy(A).cuda()
+    k = 40
+    sk, rd, T = rand_lupp_os(At, k, seed=3, handle=handle)
+    Y = gaussian_sketch(At, 2 * k, seed=3, handle=handle).double().cpu().numpy()
+    P, _ = _lapack_lupp(Y[:k])
+    assert np.array_equal(sk.cpu().numpy(), P[:k])
+    assert np.array_equal(rd.cpu().numpy(), P[k:])
+    S, R_ = sk.cpu().numpy(), rd.cpu().numpy()
+    Tref = np.linalg.lstsq(Y[:, S], Y[:, R_], rcond=None)[0]
+    np.testing.assert_allclose(T.cpu().numpy(), Tref, rtol=0, atol=1e-7 * np.abs(Tref).max())
+    err = np.linalg.norm(A[:, R_] - A[:, S] @ T.cpu().numpy()) / np.linalg.norm(A)
+    s = np.linalg.svd(A, compute_uv=False)
+    opt = np.sqrt((s[k:] ** 2).sum() / (s ** 2).sum())
+    assert err < 30 * opt, (err, opt)
