@@ -542,23 +542,34 @@ def run_batched(args, wl, name, ctx):
         perm_h = torch.empty(bt.perm_buf.numel(), dtype=torch.int32, pin_memory=True)
         T_h = torch.empty(bt.T_buf.numel(), dtype=torch.float64, pin_memory=True)
 
+        seg = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+
         def step():
+            seg[0].record()
             pack.copy_(host, non_blocking=True)
+            seg[1].record()
             bt.run()
+            seg[2].record()
             perm_h.copy_(bt.perm_buf, non_blocking=True)
             T_h.copy_(bt.T_buf, non_blocking=True)
+            seg[3].record()
             return bt.results()
         step()
         ctx.barrier()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
+        split = np.zeros(3)
         for _ in range(args.steps):
             step()
+            split += [seg[i].elapsed_time(seg[i + 1]) for i in range(3)]
         torch.cuda.synchronize()
         dt = ctx.max_over_ranks(time.perf_counter() - t0)
+        split /= args.steps
         e2e = {"value": ctx.world * args.steps * nb / dt, "unit": "matrices/s",
                "h2d_bytes_per_step": int(pack.numel() * 4),
-               "d2h_bytes_per_step": int(perm_h.numel() * 4 + T_h.numel() * 8 + nb * 56)}
+               "d2h_bytes_per_step": int(perm_h.numel() * 4 + T_h.numel() * 8 + nb * 56),
+               "ms_h2d": float(split[0]), "ms_run": float(split[1]), "ms_d2h": float(split[2]),
+               "h2d_GBps": float(pack.numel() * 4 / split[0] / 1e6)}
         del host, perm_h, T_h
 
     cpu = None

@@ -20,6 +20,7 @@ Device memory and streams come from PyTorch; all arithmetic runs in the
 sm_103a kernels of ``librbrp_gb300.so``.
 """
 import ctypes
+from collections.abc import Sequence
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -252,8 +253,8 @@ class BatchIDResult:
     draws: np.ndarray
     alg_bytes: np.ndarray  # algorithmic HBM bytes per problem (minimum traffic)
     alg_flops: np.ndarray  # algorithmic flops per problem
-    perms: list          # (n_q,) int32 CUDA views: S = perm[:k], rd = perm[k:]
-    Ts: list             # (k_q, n_q - k_q) FP64 column-major CUDA views, or None
+    perms: Sequence      # (n_q,) int32 CUDA views: S = perm[:k], rd = perm[k:]
+    Ts: Sequence         # (k_q, n_q - k_q) FP64 column-major CUDA views, or None
     ms: float            # device time of the run (CUDA events), ms
 
 
@@ -328,26 +329,58 @@ class Batch:
         self.h._bind_stream(torch.cuda.current_stream(self.As[0].device) if stream is None else stream)
         check(self.h.lib.rbrp_batch_run(self.h.h), self.h.h)
 
+    def _perm_view(self, q):
+        return self.perm_buf[int(self.perm_off[q]): int(self.perm_off[q + 1])]
+
+    def _T_view(self, q, kq, status):
+        if not self.compute_T or status != 0:
+            return None
+        n = self.shapes[q][1]
+        if 0 < kq < n:
+            return self.T_buf[int(self.t_off[q]): int(self.t_off[q]) + kq * (n - kq)].view(n - kq, kq).t()
+        return torch.empty((kq, n - kq), dtype=torch.float64, device=self.T_buf.device)
+
     def results(self):
-        """Wait for the last run and return a :class:`BatchIDResult`."""
+        """Wait for the last run and return a :class:`BatchIDResult`.
+
+        The per-problem fields are numpy arrays read in one pass; ``perms`` and
+        ``Ts`` are sequences whose CUDA views are made when indexed.
+        """
         out = (_lib.BatchResult * self.n_prob)()
         check(self.h.lib.rbrp_batch_results(self.h.h, out, self.n_prob), self.h.h)
-        f = lambda name, dt: np.array([getattr(r, name) for r in out], dt)
-        k = f("k", np.int64)
-        status = f("status", np.int64)
-        perms, Ts = [], []
-        for q, (m, n) in enumerate(self.shapes):
-            perms.append(self.perm_buf[int(self.perm_off[q]): int(self.perm_off[q + 1])])
-            kq = int(k[q])
-            if self.compute_T and status[q] == 0:
-                Ts.append(self.T_buf[int(self.t_off[q]): int(self.t_off[q]) + kq * (n - kq)].view(n - kq, kq).t()
-                          if 0 < kq < n else torch.empty((kq, n - kq), dtype=torch.float64, device=self.T_buf.device))
-            else:
-                Ts.append(None)
-        return BatchIDResult(k=k, nblocks=f("nblocks", np.int64), status=status, attempts=f("attempts", np.int64),
-                             res0=f("res0", np.float64), err_est=f("err_est", np.float64),
-                             draws=f("draws", np.uint64), alg_bytes=f("alg_bytes", np.float64),
-                             alg_flops=f("alg_flops", np.float64), perms=perms, Ts=Ts, ms=self.info()["ms_last"])
+        arr = np.ctypeslib.as_array(out)
+        k = arr["k"].astype(np.int64)
+        status = arr["status"].astype(np.int64)
+        perms = _Views(self.n_prob, self._perm_view)
+        Ts = _Views(self.n_prob, lambda q: self._T_view(q, int(k[q]), int(status[q])))
+        return BatchIDResult(k=k, nblocks=arr["nblocks"].astype(np.int64), status=status,
+                             attempts=arr["attempts"].astype(np.int64), res0=arr["res0"].astype(np.float64),
+                             err_est=arr["err_est"].astype(np.float64), draws=arr["draws"].astype(np.uint64),
+                             alg_bytes=arr["alg_bytes"].astype(np.float64),
+                             alg_flops=arr["alg_flops"].astype(np.float64), perms=perms, Ts=Ts,
+                             ms=self.info()["ms_last"])
+
+
+class _Views(Sequence):
+    """Read-only sequence of per-problem views, each made on first access."""
+
+    def __init__(self, n, make):
+        self._n, self._make, self._cache = n, make, {}
+
+    def __len__(self):
+        return self._n
+
+    def __getitem__(self, q):
+        if isinstance(q, slice):
+            return [self[x] for x in range(*q.indices(self._n))]
+        q = int(q)
+        if q < 0:
+            q += self._n
+        if not 0 <= q < self._n:
+            raise IndexError(q)
+        if q not in self._cache:
+            self._cache[q] = self._make(q)
+        return self._cache[q]
 
 
 def batched_column_id(As, b=0, tol=1e-8, kmax=None, seed=0, sampler="np", tol_loc=None, compute_T=True,
