@@ -47,10 +47,15 @@ WORKLOADS = {
     "gmm65k": dict(kind="gmm", m=1024, n=65536, clusters=20, b=32, tol=1e-4),
     "adjoint8k": dict(kind="adjoint", n=8192, dim=8, lengthscale=1.5, b=64, tol=1e-6),
     "idcmp16k": dict(kind="idcmp", d=1000, n=16384, clusters=100, b=32, nb=6, tol=1e-12),
+    "cpqr16k": dict(kind="cpqr", d=1000, n=16384, clusters=100, k=192),
 }
 
 
 def describe(name, wl):
+    if wl["kind"] == "cpqr":
+        return (f"{name}: deterministic CPQR ID (greedy b=1, LAPACK dgeqp3's pivots) to rank {wl['k']} of the C++ "
+                f"driver's Gaussian-mixture matrix {wl['d']}x{wl['n']} ({wl['clusters']} clusters), FP64; a step is "
+                f"one ID (S, T)")
     if wl["kind"] == "idcmp":
         return (f"{name}: the C++ driver's Gaussian-mixture matrix {wl['d']}x{wl['n']} ({wl['clusters']} clusters, "
                 f"point i of cluster c shifted by 10(c+1) in coordinate c), FP64; a step is one RBRP (b={wl['b']}) "
@@ -759,6 +764,70 @@ def run_idcmp(args, wl, name, ctx):
     }
 
 
+def run_cpqr(args, wl, name, ctx):
+    """The deterministic CPQR ID (the driver's CPQR baseline) per step; returns the JSON line."""
+    torch = ctx.torch
+    from robust_blockwise_random_pivoting_gb300 import workloads as W
+    from robust_blockwise_random_pivoting_gb300.rbrp import Handle
+    from robust_blockwise_random_pivoting_gb300.sketch_ids import cpqr_id
+    seed = ctx.rank
+    A_host = W.driver_gmm(wl["n"], wl["d"], wl["clusters"], seed)
+    A = torch.from_numpy(A_host).to(ctx.device).t().contiguous().t()
+    m, n = A.shape
+    h = Handle(ctx.local)
+    for _ in range(args.warmup):
+        sk, rd, T = cpqr_id(A, wl["k"], handle=h)
+    h.set_profiling(True)
+    h.reset_phase_stats()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    ctx.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(ctx.uuid) as clk:
+        ev[0].record(ctx.stream)
+        for _ in range(args.steps):
+            sk, rd, T = cpqr_id(A, wl["k"], handle=h)
+        ev[1].record(ctx.stream)
+        torch.cuda.synchronize()
+    clocks = clk.summary()
+    stats = h.phase_stats()
+    h.set_profiling(False)
+    dt = ctx.max_over_ranks(ev[0].elapsed_time(ev[1]) * 1e-3)
+    E = A[:, rd.long()] - A[:, sk.long()] @ T
+    rel_err = float(torch.linalg.norm(E) / torch.linalg.norm(A))
+    st = stats["project"]
+    launches = max(1, st["launches"])
+    per_launch_s = st["ms"] * 1e-3 / launches
+    hbm_peak = ctx.peaks.get("hbm_gbs", 6800.0)
+    achieved = st["bytes"] / launches / per_launch_s / 1e9
+    cpu = None
+    if not args.no_cpu and ctx.rank == 0:
+        from oracle import rbrp_column_id
+        ks = 16
+        t0 = time.perf_counter()
+        rbrp_column_id(A_host, 1, tol=None, kmax=ks, seed=seed, mode="gp")
+        dtc = time.perf_counter() - t0
+        cpu = {"value": 1.0 / (dtc * wl["k"] / ks), "unit": "matrices/s", "cores": threads(), "kind": "port",
+               "sample": f"oracle port (numpy/scipy FP64) in greedy mode, b=1, first {ks} ranks of the same "
+                         f"matrix ({dtc:.2f} s), scaled to rank {wl['k']} by the rank count"}
+    h.close()
+    return {
+        "metric": METRIC, "value": ctx.world * args.steps / dt, "unit": "matrices/s", "n_gpus": ctx.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded Philox)",
+        "config": {"workload": describe(name, wl), "k": int(sk.numel()), "rel_err": rel_err,
+                   "l2": f"no flush: the {m * n * 8 / 2**20:.0f} MiB input is larger than L2",
+                   "phases": {q: {"ms_per_step": v["ms"] / args.steps, "launches_per_step": v["launches"] / args.steps}
+                              for q, v in stats.items()}},
+        "roofline": {"kernel": "k_project_skinny<double, 1>", "bound": "hbm", "achieved": achieved, "peak": hbm_peak,
+                     "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": None,
+                     "limiter": "the FP64 pipe (one FMA per element of A; GB300's FP64 rate)",
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if ctx.peaks else "fallback 6.8 TB/s"},
+        "cpu_baseline": cpu, "e2e": None, "clocks": clocks,
+        "gpu_launches": int(sum(v["launches"] for v in stats.values())),
+    }
+
+
 def run_reference_batched(args, wl, name):
     """Reference arm for the batched workload: the oracle port on a bounded sample of blocks per step."""
     if int(os.environ.get("RANK", "0")) != 0:
@@ -798,7 +867,7 @@ def main():
         if wl["kind"] == "adjoint":
             print(json.dumps({"impl": "reference", "unavailable": "the reference has no differentiable ID"}))
             return
-        if wl["kind"] == "idcmp":
+        if wl["kind"] in ("idcmp", "cpqr"):
             print(json.dumps({"impl": "reference", "unavailable": "the reference's comparison IDs are "
                               "cuSOLVER/MAGMA GPU code; its CPU RBRP is the reference arm of the other workloads"}))
             return
@@ -814,6 +883,8 @@ def main():
         line = run_adjoint(args, wl, args.workload, ctx)
     elif wl["kind"] == "idcmp":
         line = run_idcmp(args, wl, args.workload, ctx)
+    elif wl["kind"] == "cpqr":
+        line = run_cpqr(args, wl, args.workload, ctx)
     else:
         line = run_single(args, wl, args.workload, ctx)
     if ctx.rank == 0:

@@ -1182,10 +1182,13 @@ k_finish(State* st, const double* __restrict__ part_res, const int* __restrict__
     }
     return;
   }
+  // residual and nonzero count: strided partial sums, then a fixed-order block tree
+  double s = 0.0;
+  int c = 0;
+  for (int z = tid; z < nparts; z += blockDim.x) { s += part_res[z]; c += part_nnz[z]; }
+  s = block_sum(s, shd);
+  c = block_sum(c, shi);
   if (tid == 0) {
-    double s = 0.0;
-    int c = 0;
-    for (int z = 0; z < nparts; ++z) { s += part_res[z]; c += part_nnz[z]; }
     const int i = s_i + s_bs;
     const int nb = st->nblocks;
     st->i = i;

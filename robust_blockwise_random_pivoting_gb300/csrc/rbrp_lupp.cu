@@ -290,6 +290,8 @@ extern "C" rbrp_status rbrp_lupp_pivots_f64(rbrp_handle h, int k, int n, const d
   s = cuda_check(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lupp, LU_THREADS, smem), "occupancy");
   if (s != RBRP_OK) return s;
   if (per_sm < 1) return set_error(h, RBRP_ERR_INVALID_ARG, "k_lupp does not fit on an SM");
+  // all co-resident CTAs: the update's latency is hidden by warps, which matters more than
+  // the per-CTA candidate scan and barrier arrival (one CTA per SM measured slower)
   const int grid = std::min(ntiles, per_sm * sms);
   const int tpc = (ntiles + grid - 1) / grid;   // <= tpc_max
 
