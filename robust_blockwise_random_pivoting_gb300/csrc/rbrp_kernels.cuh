@@ -998,7 +998,18 @@ constexpr int P2_COLS = 64;
 constexpr int P2_ROWS = 128;
 constexpr int P2_MAX_SPLIT = 8;
 constexpr int P2_THREADS = 256;
-constexpr size_t P2_SMEM = sizeof(float) * (size_t)MAXB * (P2_COLS + P2_ROWS);
+constexpr size_t P2_SMEM = sizeof(float) * (size_t)MAXB * (P2_COLS + 2 * P2_ROWS);   // W + two basis stages
+
+// 16-byte asynchronous copy global -> shared; bytes beyond src_bytes are zero-filled
+__device__ __forceinline__ void upd_cp16(float* smem, const float* gmem, int src_bytes) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(sa), "l"(gmem), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void upd_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void upd_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
 
 __global__ void __launch_bounds__(P2_THREADS, 2)
 k_resid_update(const float* __restrict__ Qb, int64_t ldq, float* __restrict__ Ares, int64_t ld,
@@ -1006,7 +1017,7 @@ k_resid_update(const float* __restrict__ Qb, int64_t ldq, float* __restrict__ Ar
                int64_t ldr, const float2* __restrict__ Wpart, int wsplit, double* __restrict__ part_norm) {
   extern __shared__ __align__(16) float p2_smem[];
   float* Ws = p2_smem;                       // Ws[a * P2_COLS + c]
-  float* Qs = p2_smem + MAXB * P2_COLS;      // Qs[a * P2_ROWS + rr]
+  float* Qbuf = p2_smem + MAXB * P2_COLS;    // two stages of Qs[a * P2_ROWS + rr]
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   const int i = st->i, kept = st->bs;
   const int p0 = i + kept + blockIdx.x * P2_COLS;
@@ -1035,8 +1046,19 @@ k_resid_update(const float* __restrict__ Qb, int64_t ldq, float* __restrict__ Ar
   DF nrm[8];
 #pragma unroll
   for (int c = 0; c < 8; ++c) nrm[c].hi = nrm[c].lo = 0.f;
-  for (int r0 = rb; r0 < re; r0 += P2_ROWS) {
-    __syncthreads();
+  // basis stage of rows [r0, r0 + P2_ROWS) into dst by cp.async; rows at or past re read as zero
+  auto load_q = [&](int r0, float* dst) {
+    for (int idx = tid; idx < kept * (P2_ROWS / 4); idx += P2_THREADS) {
+      const int a = idx / (P2_ROWS / 4), j = idx % (P2_ROWS / 4), rq = r0 + 4 * j;
+      const int bytes = 4 * max(0, min(4, re - rq));
+      upd_cp16(dst + a * P2_ROWS + 4 * j, bytes > 0 ? Qb + rq + (int64_t)a * ldq : Qb, bytes);
+    }
+    upd_commit();
+  };
+  load_q(rb, Qbuf);
+  int stage = 0;
+  for (int r0 = rb; r0 < re; r0 += P2_ROWS, ++stage) {
+    const float* Qs = Qbuf + (stage & 1) * MAXB * P2_ROWS;
     // this thread's residual values, fetched before the products so the loads
     // are in flight during the stage's FMA work
     const int r = r0 + 4 * lane;
@@ -1048,17 +1070,13 @@ k_resid_update(const float* __restrict__ Qb, int64_t ldq, float* __restrict__ Ar
       xa[c] = (vec_ok && cc < ncol) ? *reinterpret_cast<const float4*>(Ares + (int64_t)(p0 + cc) * ld + r)
                                     : make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    for (int idx = tid; idx < kept * (P2_ROWS / 4); idx += P2_THREADS) {
-      const int a = idx / (P2_ROWS / 4), j = idx % (P2_ROWS / 4), rq = r0 + 4 * j;
-      float4 v;
-      if (rq + 3 < re) {
-        v = *reinterpret_cast<const float4*>(Qb + rq + (int64_t)a * ldq);
-      } else {
-        const float* qa = Qb + (int64_t)a * ldq;
-        v = make_float4(rq < re ? qa[rq] : 0.f, rq + 1 < re ? qa[rq + 1] : 0.f, rq + 2 < re ? qa[rq + 2] : 0.f,
-                        rq + 3 < re ? qa[rq + 3] : 0.f);
-      }
-      reinterpret_cast<float4*>(Qs + a * P2_ROWS)[j] = v;
+    // the next stage's basis goes into the other buffer, whose last readers passed the
+    // barrier that ended the previous stage
+    if (r0 + P2_ROWS < re) {
+      load_q(r0 + P2_ROWS, Qbuf + ((stage + 1) & 1) * MAXB * P2_ROWS);
+      upd_wait<1>();
+    } else {
+      upd_wait<0>();
     }
     __syncthreads();
     float acc[4][8];
@@ -1106,6 +1124,7 @@ k_resid_update(const float* __restrict__ Qb, int64_t ldq, float* __restrict__ Ar
         }
       }
     }
+    __syncthreads();   // every warp is done with this stage's basis before it is refilled
   }
   // warp sums of the double-float norms on the FP32 pipe; lane 0 converts once per column
 #pragma unroll
