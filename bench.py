@@ -366,6 +366,8 @@ def run_single(args, wl, name, ctx, light=False):
         pms = e0.elapsed_time(e1)
         plain = {"matrices_per_s": 1e3 / pms, "id_time_ms": pms, "k": rp.k,
                  "rel_err": float(np.sqrt(max(hp.id_error(A64), 0.0)))}
+        if coverage is not None:
+            plain["clusters_in_skeleton"] = len(set(labels[rp.perm[: rp.k].cpu().numpy()].tolist()))
         hp.close()
 
     hbm_peak = ctx.peaks.get("hbm_gbs", 6800.0)

@@ -974,7 +974,7 @@ __device__ void solve_problem(BatchSmem<BB>& sm, const rbrp_batch_problem& pr, i
     }
     const int i = st.i;
     const bool first = i == 0;
-    sample_block(&st, diags, perm, n, kcap, args.b, seed, args.sampler, pbuf,
+    sample_block<BT>(&st, diags, perm, n, kcap, args.b, seed, args.sampler, pbuf,
                  reinterpret_cast<unsigned long long*>(pbuf), sm.js, sm.cols);
     const int bss = st.bs_sampled;
     clk.mark(BPH_SAMPLE);

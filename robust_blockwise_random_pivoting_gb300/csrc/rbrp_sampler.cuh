@@ -24,8 +24,9 @@ namespace {
 // ===========================================================================
 constexpr int SAMPLE_THREADS = 1024;
 
-// Block-wide sampler body (any block size >= 64); k_sample runs it with 1024
-// threads, the batched kernel with its CTA.
+// Block-wide sampler body (any block size from 64 to MAXT); k_sample runs it with
+// 1024 threads, the batched kernel with its CTA.
+template <int MAXT = SAMPLE_THREADS>
 __device__ void sample_block(State* st, const double* __restrict__ diags, const int* __restrict__ perm, int n,
                              int kmax, int b, uint64_t seed, int sampler, double* __restrict__ pbuf,
                              unsigned long long* __restrict__ kbuf, int* __restrict__ js, int* __restrict__ cols,
@@ -70,7 +71,16 @@ __device__ void sample_block(State* st, const double* __restrict__ diags, const 
       s_size = min(req, npos);
       s_found = 0;
     }
-    double* cdf = pbuf + n;  // second half of the buffer
+    // The cdf is never stored.  Thread t's chunk [lo, hi) keeps its total `tot`; the
+    // block scan of the totals gives its offset; cdf(j) = (off + run(j)) * (1 / last),
+    // run(j) the chunk-local sequential sum, last = off + tot of the chunk holding
+    // index nrem - 1, whose cdf is exactly 1 (numpy's cdf /= cdf[-1]).  A draw
+    // binary-searches the chunks' last cdf entries in shared memory, then scans one
+    // chunk: the index searchsorted(side='right') returns on the stored cdf.
+    __shared__ double s_end[MAXT];
+    __shared__ double s_off[MAXT];
+    __shared__ double s_last;
+    double tot = 0.0;
     __syncthreads();
     // Rejection rounds.  Each round draws at least one new index unless every
     // remaining positive weight is absorbed by rounding in the cdf; the cap
@@ -79,31 +89,63 @@ __device__ void sample_block(State* st, const double* __restrict__ diags, const 
       const int found = s_found, need = s_size - s_found;
       if (tid < found) pbuf[s_rel[tid]] = 0.0;
       __syncthreads();
-      // inclusive cumsum: chunk-local sequential sums + block scan of chunk totals
-      double run = 0.0;
-      for (int j = lo; j < hi; ++j) {
-        run += pbuf[j];
-        cdf[j] = run;
+      // chunk totals: every chunk in the first round, afterwards the chunks holding a drawn index
+      bool dirty = round == 0;
+      for (int u = 0; u < found && !dirty; ++u) {
+        const int jr = s_rel[u];
+        dirty = jr >= lo && jr < hi;
       }
-      const double off = block_exclusive_scan(run, shd, (double*)nullptr);
-      for (int j = lo; j < hi; ++j) cdf[j] += off;
+      if (dirty) {
+        double run = 0.0;
+        int j = lo;
+        for (; j + 8 <= hi; j += 8) {
+          double v[8];
+#pragma unroll
+          for (int q = 0; q < 8; ++q) v[q] = pbuf[j + q];
+#pragma unroll
+          for (int q = 0; q < 8; ++q) run += v[q];
+        }
+        for (; j < hi; ++j) run += pbuf[j];
+        tot = run;
+      }
+      const double off = block_exclusive_scan(tot, shd, (double*)nullptr);
+      if (lo < hi && hi == nrem) s_last = off + tot;
+      s_off[tid] = off;
       __syncthreads();
-      // normalise by the last entry, as numpy's cdf /= cdf[-1]: the last entry is exactly 1
-      const double last = cdf[nrem - 1];
-      __syncthreads();
-      const double inv_last = 1.0 / last;
-      for (int j = lo; j < hi; ++j) cdf[j] *= inv_last;
-      __syncthreads();
-      if (tid == 0) cdf[nrem - 1] = 1.0;  // the last entry is exactly 1, as numpy's cdf /= cdf[-1]
+      const double inv_last = 1.0 / s_last;
+      s_end[tid] = lo < hi ? (hi == nrem ? 1.0 : (off + tot) * inv_last) : 2.0;
       __syncthreads();
       if (tid < need) {
         const double x = np_uniform(seed, s_draws + (unsigned long long)tid);
-        int a = 0, z = nrem;  // first index with cdf > x (searchsorted side='right')
+        int a = 0, z = (int)blockDim.x;  // first chunk whose last cdf entry is > x
         while (a < z) {
           const int mid = (a + z) >> 1;
-          if (cdf[mid] <= x) a = mid + 1; else z = mid;
+          if (s_end[mid] <= x) a = mid + 1; else z = mid;
         }
-        s_cand[tid] = a < nrem ? a : nrem - 1;
+        const int t = min(a, (int)blockDim.x - 1);
+        const int clo = min(nrem, t * chunk), chi = min(nrem, clo + chunk);
+        const double co = s_off[t];
+        int pick = chi - 1;
+        double run = 0.0;
+        bool hit = false;
+        for (int j0 = clo; j0 < chi && !hit; j0 += 8) {
+          double v[8];
+#pragma unroll
+          for (int q = 0; q < 8; ++q) v[q] = j0 + q < chi ? pbuf[j0 + q] : 0.0;
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const int j = j0 + q;
+            if (!hit && j < chi) {
+              run += v[q];
+              const double c = j == nrem - 1 ? 1.0 : (co + run) * inv_last;
+              if (c > x) {
+                pick = j;
+                hit = true;
+              }
+            }
+          }
+        }
+        s_cand[tid] = pick < nrem ? pick : nrem - 1;
       }
       __syncthreads();
       if (tid == 0) {

@@ -97,6 +97,16 @@ def test_gmm_small(handle):
     assert len(set(labels[S].tolist())) == 12
 
 
+def test_np_sampler_long_chunks_and_repeat_draws(handle):
+    """n = 20000 (20 positions per sampler thread) with 30 dominant columns, so draws
+    repeat and the rejection rounds recompute the chunks that lost an index."""
+    A = W.gaussian_exp(100, 20000, decay=8.0, seed=21)
+    heavy = np.random.default_rng(21).choice(20000, size=30, replace=False)
+    A[:, heavy] *= 50.0
+    r, o = check_against_oracle(handle, A, 32, 1e-10)
+    assert o["draws"] > r.k   # some draws were rejected as repeats
+
+
 def test_run_to_full_rank_and_kmax(handle):
     A = W.gaussian_exp(120, 150, decay=30.0, seed=4)
     check_against_oracle(handle, A, 16, None)
