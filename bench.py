@@ -444,13 +444,14 @@ def run_batched(args, wl, name, ctx):
     nb = wl["nblocks"]
     blocks = W.kernel_blocks_device(nb, wl["lo"], wl["hi"], wl["lengthscale"], seed, ctx.device)
     shapes = [tuple(A.shape) for A in blocks]
-    # all blocks packed in one device buffer (column major each), also the target of the e2e copy
-    sizes = np.array([m * n for m, n in shapes], np.int64)
-    offs = np.concatenate([[0], np.cumsum(sizes)])
-    pack = torch.empty(int(offs[-1]), dtype=torch.float32, device=ctx.device)
+    # all blocks packed in one device buffer (column major each, 16-byte aligned starts),
+    # also the layout of the e2e host buffer
+    from robust_blockwise_random_pivoting_gb300.rbrp import packed_offsets
+    offs, sizes = packed_offsets(shapes)
+    pack = torch.zeros(int(offs[-1]), dtype=torch.float32, device=ctx.device)
     As = []
     for q, ((m, n), A) in enumerate(zip(shapes, blocks)):
-        v = pack[int(offs[q]): int(offs[q + 1])].view(n, m).t()
+        v = pack[int(offs[q]): int(offs[q]) + int(sizes[q])].view(n, m).t()
         v.copy_(A)
         As.append(v)
     del blocks
@@ -572,12 +573,32 @@ def run_batched(args, wl, name, ctx):
         torch.cuda.synchronize()
         dt = ctx.max_over_ranks(time.perf_counter() - t0)
         split /= args.steps
+        sequential = {"value": ctx.world * args.steps * nb / dt, "unit": "matrices/s",
+                      "ms_h2d": float(split[0]), "ms_run": float(split[1]), "ms_d2h": float(split[2]),
+                      "h2d_GBps": float(pack.numel() * 4 / split[0] / 1e6)}
+        del perm_h, T_h
+        # the pipelined host API: groups of problems, copies overlapped with the IDs on two streams
+        from robust_blockwise_random_pivoting_gb300.rbrp import HostBatch
+        hb = HostBatch(host, shapes, parts=3, b=info["b"], tol=wl["tol"], seed=seed * nb, t_rank_cap=t_cap,
+                       device=ctx.local)
+
+        def hstep():
+            hb.run()
+            return hb.results()
+        hstep()
+        ctx.barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            hstep()
+        torch.cuda.synchronize()
+        dt = ctx.max_over_ranks(time.perf_counter() - t0)
         e2e = {"value": ctx.world * args.steps * nb / dt, "unit": "matrices/s",
-               "h2d_bytes_per_step": int(pack.numel() * 4),
-               "d2h_bytes_per_step": int(perm_h.numel() * 4 + T_h.numel() * 8 + nb * 56),
-               "ms_h2d": float(split[0]), "ms_run": float(split[1]), "ms_d2h": float(split[2]),
-               "h2d_GBps": float(pack.numel() * 4 / split[0] / 1e6)}
-        del host, perm_h, T_h
+               "h2d_bytes_per_step": hb.h2d_bytes, "d2h_bytes_per_step": int(hb.d2h_bytes + nb * 56),
+               "api": f"rbrp.HostBatch, {len(hb.groups)} groups on their own streams, copies overlapped with compute",
+               "sequential": sequential}
+        hb.close()
+        del host
 
     cpu = None
     if ctx.rank == 0 and ctx.world == 1 and not args.no_cpu:

@@ -383,6 +383,103 @@ class _Views(Sequence):
         return self._cache[q]
 
 
+def packed_offsets(shapes):
+    """Float offsets of matrices packed back to back, each column major and starting on a
+    16-byte boundary (offsets rounded up to 4 floats): the layout :class:`HostBatch` reads.
+    Aligned starts let the batched kernel load the first block with 16-byte vectors."""
+    sizes = np.array([int(m) * int(n) for m, n in shapes], np.int64)
+    padded = (sizes + 3) // 4 * 4
+    return np.concatenate([[0], np.cumsum(padded)]), sizes
+
+
+class HostBatch:
+    """Batched column IDs of FP32 matrices held in pinned host memory, with the
+    host-to-device copies overlapped with the IDs.
+
+    ``host_pack`` is one pinned FP32 CPU tensor holding the matrices back to
+    back (each column major, ``shapes[q] = (m_q, n_q)``, starting at
+    ``packed_offsets(shapes)[0][q]``).  The problems are cut
+    into ``parts`` consecutive groups of about equal size; each group has its
+    own handle, device buffer, plan and stream.  :meth:`run` enqueues, per
+    group, the copy of the group's matrices, its graph launch and the copies of
+    its perm and T back to pinned host buffers, so one group's copy runs while
+    the previous group computes.  The persistent kernel balances its load over
+    the problems it is given, largest first; a group holds fewer, so its kernel
+    runs less efficiently than one launch over all problems (on 4096 uneven
+    blocks three groups spend about 1.5x the compute of one batch, which the
+    overlap wins back).  Problem q keeps the Philox key
+    ``seed + q`` and every group uses the block size the first group's autotuner
+    chose, so the results are those of one batch over all problems with that b.
+    """
+
+    def __init__(self, host_pack, shapes, parts=3, b=0, tol=1e-8, kmax=None, seed=0, sampler="np", tol_loc=None,
+                 compute_T=True, t_rank_cap=None, device=None):
+        if host_pack.is_cuda or host_pack.dtype != torch.float32 or not host_pack.is_pinned():
+            raise TypeError("host_pack must be a pinned FP32 CPU tensor")
+        dev = torch.device("cuda", torch.cuda.current_device() if device is None else int(device))
+        offs, sizes = packed_offsets(shapes)
+        if offs[-1] != host_pack.numel():
+            raise ValueError("host_pack does not hold the listed shapes in the packed_offsets layout")
+        parts = max(1, min(int(parts), len(shapes)))
+        cuts = [0] + [int(np.searchsorted(offs, g * offs[-1] / parts)) for g in range(1, parts)] + [len(shapes)]
+        cuts = sorted(set(min(max(c, 0), len(shapes)) for c in cuts))
+        self.compute_T = compute_T
+        self.groups = []
+        b_used = b if b and b > 0 else 0
+        for q0, q1 in zip(cuts[:-1], cuts[1:]):
+            if q1 <= q0:
+                continue
+            base = int(offs[q0])
+            dpack = torch.empty(int(offs[q1]) - base, dtype=torch.float32, device=dev)
+            views = [dpack[int(offs[q]) - base: int(offs[q]) - base + int(sizes[q])]
+                     .view(int(shapes[q][1]), int(shapes[q][0])).t() for q in range(q0, q1)]
+            h = Handle(dev.index)
+            bt = Batch(h, views, b=b_used, tol=tol, kmax=kmax, seed=seed + q0, sampler=sampler, tol_loc=tol_loc,
+                       compute_T=compute_T, t_rank_cap=t_rank_cap)
+            if b_used <= 0:
+                b_used = bt.info()["b"]
+            self.groups.append(dict(
+                q0=q0, q1=q1, dpack=dpack, handle=h, batch=bt, host=host_pack[base: int(offs[q1])],
+                perm_h=torch.empty(bt.perm_buf.numel(), dtype=torch.int32, pin_memory=True),
+                T_h=torch.empty(bt.T_buf.numel() if compute_T else 0, dtype=torch.float64, pin_memory=True)))
+        self.b = b_used
+        self.streams = [torch.cuda.Stream(dev) for _ in self.groups]
+        self.h2d_bytes = int(host_pack.numel() * 4)
+        self.d2h_bytes = int(sum(G["perm_h"].numel() * 4 + G["T_h"].numel() * 8 for G in self.groups))
+
+    def run(self):
+        """Enqueue every group: copy in, graph launch, perm and T out (no host wait)."""
+        for G, s in zip(self.groups, self.streams):
+            with torch.cuda.stream(s):
+                G["dpack"].copy_(G["host"], non_blocking=True)
+                G["batch"].run(s)
+                G["perm_h"].copy_(G["batch"].perm_buf, non_blocking=True)
+                if self.compute_T:
+                    G["T_h"].copy_(G["batch"].T_buf, non_blocking=True)
+
+    def results(self):
+        """Wait for the last run; per group ``(first problem, BatchIDResult)`` with host perm and T buffers done."""
+        out = []
+        for G in self.groups:
+            out.append((G["q0"], G["batch"].results()))
+        for s in self.streams:
+            s.synchronize()
+        return out
+
+    def host_perm(self, q):
+        """perm of problem q from the pinned host buffer of the last run."""
+        for G in self.groups:
+            if G["q0"] <= q < G["q1"]:
+                bt = G["batch"]
+                j = q - G["q0"]
+                return G["perm_h"][int(bt.perm_off[j]): int(bt.perm_off[j + 1])]
+        raise IndexError(q)
+
+    def close(self):
+        for G in self.groups:
+            G["handle"].close()
+
+
 def batched_column_id(As, b=0, tol=1e-8, kmax=None, seed=0, sampler="np", tol_loc=None, compute_T=True,
                       t_rank_cap=None, handle=None):
     """Column IDs of many FP32 CUDA matrices in one persistent launch (plan, run, results)."""

@@ -198,3 +198,35 @@ def test_batched_invalid_inputs(handle):
         Batch(handle, [A], b=40)
     with pytest.raises(TypeError):
         Batch(handle, [A.double()])
+
+
+def test_host_batch_pipeline_equals_one_batch(handle):
+    """HostBatch (pinned host input, groups on alternating streams) returns what one batch returns."""
+    from robust_blockwise_random_pivoting_gb300.rbrp import Batch, HostBatch
+    shp = shapes(23, 40, 300, seed=31)
+    mats = [W.kernel_block_scaled(int(m), int(n), q, 0.5, seed=5) for q, (m, n) in enumerate(shp)]
+    from robust_blockwise_random_pivoting_gb300.rbrp import packed_offsets
+    offs, sizes = packed_offsets(shp)
+    host = torch.zeros(int(offs[-1]), dtype=torch.float32).pin_memory()
+    for q, A in enumerate(mats):
+        host[int(offs[q]): int(offs[q]) + int(sizes[q])] = \
+            torch.from_numpy(np.asfortranarray(A, dtype=np.float32)).t().reshape(-1)
+    hb = HostBatch(host, [tuple(int(v) for v in s) for s in shp], parts=3, b=0, tol=1e-8, seed=100,
+                   t_rank_cap=64)
+    try:
+        assert len(hb.groups) == 3
+        hb.run()
+        groups = hb.results()
+        ref = Batch(handle, [dev32(A) for A in mats], b=hb.b, tol=1e-8, seed=100, t_rank_cap=64)
+        ref.run()
+        rr = ref.results()
+        for q0, res in groups:
+            for j in range(len(res.k)):
+                q = q0 + j
+                assert res.k[j] == rr.k[q] and res.status[j] == rr.status[q]
+                assert res.err_est[j] == rr.err_est[q]
+                assert torch.equal(hb.host_perm(q), rr.perms[q].cpu())
+                if rr.Ts[q] is not None:
+                    assert torch.equal(res.Ts[j].cpu(), rr.Ts[q].cpu())
+    finally:
+        hb.close()
