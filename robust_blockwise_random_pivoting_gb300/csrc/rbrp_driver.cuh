@@ -36,16 +36,12 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
                                            (int)sizeof(PanelSmem)), "cudaFuncSetAttribute(k_panel2)");
     if (s != RBRP_OK) return s;
     if (RES) {
-      for (const void* fn : {(const void*)k_pchol_df, (const void*)k_chol2_df}) {
-        s = cuda_check(h, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)sizeof(PcholDfSmem)), "cudaFuncSetAttribute(panel df)");
-        if (s != RBRP_OK) return s;
-      }
-      for (const void* fn : {(const void*)k_panel1_df, (const void*)k_panel2_df, (const void*)k_panel_q_df}) {
-        s = cuda_check(h, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)sizeof(RowsDfSmem)), "cudaFuncSetAttribute(rows df)");
-        if (s != RBRP_OK) return s;
-      }
+      s = cuda_check(h, cudaFuncSetAttribute(k_pchol_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)sizeof(PcholDfSmem)), "cudaFuncSetAttribute(panel df)");
+      if (s != RBRP_OK) return s;
+      s = cuda_check(h, cudaFuncSetAttribute(k_panel_q_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)sizeof(RowsDfSmem)), "cudaFuncSetAttribute(rows df)");
+      if (s != RBRP_OK) return s;
       s = cuda_check(h, cudaFuncSetAttribute(k_resid_update, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)P2_SMEM), "cudaFuncSetAttribute(k_resid_update)");
       if (s != RBRP_OK) return s;
@@ -127,12 +123,14 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
     prof_end(h, RBRP_PHASE_CGS, ev, 0.0, 0.0, (!RES && i > 0) ? 4 : 2);
     ev = prof_begin(h);
     if (RES) {
-      k_pchol_df<<<1, 256, sizeof(PcholDfSmem), st>>>(h->G, m, h->st, tol_loc, h->js, h->perm, h->diags, h->R11,
+      // R11 as double-float pairs: the FP64 buffer of the same size, reinterpreted
+      float2* R11df = reinterpret_cast<float2*>(h->R11);
+      k_pchol_df<<<1, 256, sizeof(PcholDfSmem), st>>>(h->G, m, h->st, tol_loc, h->js, h->perm, h->diags, R11df,
                                                       h->ord, h->J, h->K1, h->K2);
-      k_panel_q_df<<<ttiles, DF_TROWS, sizeof(RowsDfSmem), st>>>((const float*)h->V, m, h->st, h->R11, h->ord,
+      k_panel_q_df<<<ttiles, DF_TROWS, sizeof(RowsDfSmem), st>>>((const float*)h->V, m, h->st, R11df, h->ord,
                                                                  (float*)Q, L.ld_res, use_tc ? h->Qh : nullptr,
                                                                  use_tc ? h->Ql : nullptr, L.ld_res);
-      k_write_r11<<<1, 256, 0, st>>>(h->st, h->R11, h->R, n);
+      k_write_r11<<<1, 256, 0, st>>>(h->st, R11df, h->R, n);
     } else {
       k_pchol<<<1, 256, panel_smem, st>>>(h->G, m, h->st, tol_loc, h->js, h->perm, h->diags, h->R11, h->ord,
                                           h->J, h->K1, h->K2);

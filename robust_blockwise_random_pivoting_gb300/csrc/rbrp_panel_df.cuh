@@ -67,10 +67,10 @@ using PcholDfSmem = PcholDfSmemT<MAXB>;
 
 // Pivoted Cholesky of the panel Gram matrix with the robust filter (same rule as
 // pivoted_chol_filter), 256 threads, no data movement for the swaps.  Publishes
-// R11 (slot order, FP64), ord, the kept count and performs the block swap.
+// R11 (slot order, double-float pairs), ord, the kept count and performs the block swap.
 __global__ void __launch_bounds__(256)
 k_pchol_df(const double* __restrict__ G, int m, State* st, double tol_loc, const int* __restrict__ js,
-           int* __restrict__ perm, double* __restrict__ diags, double* __restrict__ R11g, int* __restrict__ ordg,
+           int* __restrict__ perm, double* __restrict__ diags, float2* __restrict__ R11g, int* __restrict__ ordg,
            int* __restrict__ Jg, int* __restrict__ K1g, int* __restrict__ K2g) {
   extern __shared__ __align__(16) unsigned char dyn_smem[];
   PcholDfSmem& sm = *reinterpret_cast<PcholDfSmem*>(dyn_smem);
@@ -90,13 +90,14 @@ k_pchol_df(const double* __restrict__ G, int m, State* st, double tol_loc, const
   // R11 in slot order: R11[a][c] = R[a][ord[c]] for c >= a
   for (int idx = tid; idx < MAXB * MAXB; idx += 256) {
     const int a = idx / MAXB, c = idx % MAXB;
-    R11g[idx] = (a < kept && c < kept && c >= a) ? df_dbl(sm.R[a][sm.ord[c]]) : 0.0;
+    const dfl v = (a < kept && c < kept && c >= a) ? sm.R[a][sm.ord[c]] : dfl{0.f, 0.f};
+    R11g[idx] = make_float2(v.hi, v.lo);
   }
   if (tid < MAXB) ordg[tid] = sm.ord[tid];
   block_swap_parallel(sm, i, kept, js, perm, diags, Jg, K1g, K2g, st);
 }
 
-// Rows of X R^{-1} (R upper, kept x kept, FP64 in global) for 128 rows per CTA,
+// Rows of X R^{-1} (R upper, kept x kept, double-float pairs in global) for 128 rows per CTA,
 // one thread per row, in double-float; optionally the Gram partial of the result.
 struct RowsDfSmem {
   dfl R[MAXB][MAXB + 1];
@@ -116,55 +117,10 @@ __device__ __forceinline__ void rows_solve_df(RowsDfSmem& sm, int kept) {
   __syncthreads();
 }
 
-__device__ __forceinline__ void load_R_df(RowsDfSmem& sm, const double* __restrict__ Rg, int kept) {
-  for (int idx = threadIdx.x; idx < kept * kept; idx += blockDim.x)
-    sm.R[idx / kept][idx % kept] = df_of(Rg[(idx / kept) * MAXB + idx % kept]);
-}
-
-// Q1 = V(:, ord[:kept]) R11^{-1} (double-float, stored as float pairs) and Q1^T Q1 partials.
-__global__ void __launch_bounds__(DF_TROWS)
-k_panel1_df(const float* __restrict__ V, int m, const State* __restrict__ st, const double* __restrict__ R11g,
-            const int* __restrict__ ordg, float2* __restrict__ Q1, double* __restrict__ G2part) {
-  extern __shared__ __align__(16) unsigned char dyn_smem[];
-  RowsDfSmem& sm = *reinterpret_cast<RowsDfSmem*>(dyn_smem);
-  const int tid = threadIdx.x;
-  const int kept = st->bs;
-  if (kept == 0) return;
-  load_R_df(sm, R11g, kept);
-  if (tid < MAXB) sm.ord[tid] = ordg[tid];
-  __syncthreads();
-  const int r0 = blockIdx.x * DF_TROWS;
-  for (int idx = tid; idx < DF_TROWS * kept; idx += DF_TROWS) {
-    const int rr = idx % DF_TROWS, s = idx / DF_TROWS, r = r0 + rr;
-    sm.W[rr][s] = {r < m ? V[r + (int64_t)sm.ord[s] * m] : 0.f, 0.f};
-  }
-  __syncthreads();
-  rows_solve_df(sm, kept);
-  for (int idx = tid; idx < DF_TROWS * kept; idx += DF_TROWS) {
-    const int rr = idx % DF_TROWS, s = idx / DF_TROWS, r = r0 + rr;
-    if (r < m) Q1[r + (int64_t)s * m] = make_float2(sm.W[rr][s].hi, sm.W[rr][s].lo);
-  }
-  // Gram partial: thread -> column c1 = tid, all 64 columns c2 (64 independent chains
-  // would not fit; 16 at a time)
-  double* G = G2part + (int64_t)blockIdx.x * MAXB * MAXB;
-  const int rows_valid = max(0, min(DF_TROWS, m - r0));
-  const int c1 = tid;
-  for (int q0 = 0; q0 < MAXB; q0 += 16) {
-    dfl acc[16];
-#pragma unroll
-    for (int q = 0; q < 16; ++q) acc[q] = {0.f, 0.f};
-    if (c1 < kept) {
-      for (int rr = 0; rr < rows_valid; ++rr) {
-        const dfl x = sm.W[rr][c1];
-#pragma unroll
-        for (int q = 0; q < 16; ++q) acc[q] = df_fma2(acc[q], x, sm.W[rr][q0 + q]);
-      }
-    }
-#pragma unroll
-    for (int q = 0; q < 16; ++q) {
-      const int c2 = q0 + q;
-      G[c1 * MAXB + c2] = (c1 < kept && c2 < kept) ? df_dbl(acc[q]) : 0.0;
-    }
+__device__ __forceinline__ void load_R_df(RowsDfSmem& sm, const float2* __restrict__ Rg, int kept) {
+  for (int idx = threadIdx.x; idx < kept * kept; idx += blockDim.x) {
+    const float2 v = Rg[(idx / kept) * MAXB + idx % kept];
+    sm.R[idx / kept][idx % kept] = dfl{v.x, v.y};
   }
 }
 
@@ -174,7 +130,7 @@ k_panel1_df(const float* __restrict__ V, int m, const State* __restrict__ st, co
 // orthogonality, ~2^-48 cond(V_kept)^2, stays far below the FP32 rounding of
 // the stored basis for the conditioning the robust filter admits.
 __global__ void __launch_bounds__(DF_TROWS)
-k_panel_q_df(const float* __restrict__ V, int m, const State* __restrict__ st, const double* __restrict__ R11g,
+k_panel_q_df(const float* __restrict__ V, int m, const State* __restrict__ st, const float2* __restrict__ R11g,
              const int* __restrict__ ordg, float* __restrict__ Q, int64_t ldq, float* __restrict__ Qh,
              float* __restrict__ Ql, int64_t ldh) {
   extern __shared__ __align__(16) unsigned char dyn_smem[];
@@ -210,96 +166,13 @@ k_panel_q_df(const float* __restrict__ V, int m, const State* __restrict__ st, c
 }
 
 // R(I2, I2) = R11, the panel R of a single CholQR pass (upper triangle, slot order).
-__global__ void k_write_r11(const State* __restrict__ st, const double* __restrict__ R11g, double* __restrict__ R,
+__global__ void k_write_r11(const State* __restrict__ st, const float2* __restrict__ R11g, double* __restrict__ R,
                             int64_t ldr) {
   const int kept = st->bs, i = st->i;
   for (int idx = threadIdx.x; idx < kept * kept; idx += blockDim.x) {
     const int a = idx / kept, c = idx % kept;
-    R[(int64_t)(i + a) * ldr + (i + c)] = c >= a ? R11g[a * MAXB + c] : 0.0;
-  }
-}
-
-// R2 = chol(Q1^T Q1) (one CTA, double-float) and the panel R = R2 R11 into R(I2, I2).
-__global__ void __launch_bounds__(256)
-k_chol2_df(const double* __restrict__ G2, const State* __restrict__ st, const double* __restrict__ R11g,
-           double* __restrict__ R2g, double* __restrict__ R, int64_t ldr) {
-  extern __shared__ __align__(16) unsigned char dyn_smem[];
-  PcholDfSmem& sm = *reinterpret_cast<PcholDfSmem*>(dyn_smem);
-  const int tid = threadIdx.x;
-  const int kept = st->bs, i = st->i;
-  if (kept == 0) return;
-  for (int idx = tid; idx < kept * kept; idx += 256) sm.S[idx / kept][idx % kept] = df_of(G2[(idx / kept) * MAXB + idx % kept]);
-  __syncthreads();
-  const int ty = tid >> 4, tx = tid & 15;
-  for (int t = 0; t < kept; ++t) {
-    if (tid == 0) {
-      const dfl r = df_sqrt(sm.S[t][t]);
-      sm.R[t][t] = r;
-      sm.inv = df_recip(r);
-    }
-    __syncthreads();
-    const dfl inv = sm.inv;
-    if (tid > t && tid < kept) sm.R[t][tid] = df_mul(sm.S[t][tid], inv);
-    __syncthreads();
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int s1 = ty * 4 + u;
-      if (s1 <= t || s1 >= kept) continue;
-      const dfl r1 = sm.R[t][s1];
-#pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        const int s2 = tx * 4 + v;
-        if (s2 >= s1 && s2 < kept) sm.S[s1][s2] = df_fms(sm.S[s1][s2], r1, sm.R[t][s2]);
-      }
-    }
-    __syncthreads();
-  }
-  for (int idx = tid; idx < MAXB * MAXB; idx += 256) {
-    const int a = idx / MAXB, c = idx % MAXB;
-    R2g[idx] = (a < kept && c < kept && c >= a) ? df_dbl(sm.R[a][c]) : 0.0;
-  }
-  for (int idx = tid; idx < kept * kept; idx += 256) {
-    const int a = idx / kept, c = idx % kept;
-    dfl v = {0.f, 0.f};
-    if (c >= a)
-      for (int u = a; u <= c; ++u) v = df_add(v, df_mul(sm.R[a][u], df_of(R11g[u * MAXB + c])));
-    R[(int64_t)(i + a) * ldr + (i + c)] = df_dbl(v);
-  }
-}
-
-// Q_blk = Q1 R2^{-1}: FP32 basis for the residual update and its exact TF32
-// split (Qh = tf32(Q), Ql = fp32(Q - Qh), zero beyond the kept columns).
-__global__ void __launch_bounds__(DF_TROWS)
-k_panel2_df(const float2* __restrict__ Q1, int m, const State* __restrict__ st, const double* __restrict__ R2g,
-            float* __restrict__ Q, int64_t ldq, float* __restrict__ Qh, float* __restrict__ Ql, int64_t ldh) {
-  extern __shared__ __align__(16) unsigned char dyn_smem[];
-  RowsDfSmem& sm = *reinterpret_cast<RowsDfSmem*>(dyn_smem);
-  const int tid = threadIdx.x;
-  const int kept = st->bs;
-  if (kept == 0) return;
-  load_R_df(sm, R2g, kept);
-  const int r0 = blockIdx.x * DF_TROWS;
-  for (int idx = tid; idx < DF_TROWS * kept; idx += DF_TROWS) {
-    const int rr = idx % DF_TROWS, s = idx / DF_TROWS, r = r0 + rr;
-    const float2 v = r < m ? Q1[r + (int64_t)s * m] : make_float2(0.f, 0.f);
-    sm.W[rr][s] = {v.x, v.y};
-  }
-  __syncthreads();
-  rows_solve_df(sm, kept);
-  for (int idx = tid; idx < DF_TROWS * MAXB; idx += DF_TROWS) {
-    const int rr = idx % DF_TROWS, s = idx / DF_TROWS, r = r0 + rr;
-    if (r < m) {
-      // FP32 basis and its exact TF32 split, on the FP32 pipe: q = hi + lo (double-float),
-      // Q = rn(q), Qh = tf32(Q), Ql = rn(q - Qh) with hi - Qh exact (Sterbenz)
-      const dfl w = s < kept ? sm.W[rr][s] : dfl{0.f, 0.f};
-      const float qf = __fadd_rn(w.hi, w.lo);
-      if (s < kept) Q[r + (int64_t)s * ldq] = qf;
-      if (Qh) {
-        const float h = __uint_as_float(__float_as_uint(qf) & 0xFFFFE000u);
-        Qh[r + (int64_t)s * ldh] = h;
-        Ql[r + (int64_t)s * ldh] = __fadd_rn(w.hi - h, w.lo);
-      }
-    }
+    const float2 v = R11g[a * MAXB + c];
+    R[(int64_t)(i + a) * ldr + (i + c)] = c >= a ? (double)v.x + (double)v.y : 0.0;
   }
 }
 

@@ -90,11 +90,16 @@ __device__ int pchol_filter_df(PcholDfSmemT<BB>& sm, int nb, int rows, double to
   constexpr int U = BB / 16;  // U x U Schur entries per thread: rows ty*U+u, columns tx*U+v
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int ty = tid >> 4, tx = tid & 15;
-  double total = 0.0;  // trace(G), used by warp 0
+  // trace(G) and the stop threshold tol_loc * trace as a double-float, used by warp 0:
+  // the per-step test rem < thr stays on the FP32 pipe (rem / trace < tol_loc, no FP64 divide)
+  bool have_total = false;
+  dfl thr = {0.f, 0.f};
   if (wid == 0) {
     dfl t = {0.f, 0.f};
     for (int s2 = 0; s2 < nb; ++s2) t = df_add(t, sm.S[s2][s2]);
-    total = df_dbl(t);
+    const double total = df_dbl(t);
+    have_total = total > 0.0;
+    thr = df_of(tol_loc * total);
   }
   int kept = rows;
   for (int t = 0; t < rows; ++t) {
@@ -116,7 +121,7 @@ __device__ int pchol_filter_df(PcholDfSmemT<BB>& sm, int nb, int rows, double to
         if (df_gt(ob, best) || (df_eq(ob, best) && oi < bs)) { best = ob; bs = oi; }
       }
       if (lane == 0) {
-        const bool stop = !(total > 0.0) || (df_dbl(rem) / total < tol_loc) || !(best.hi > 0.f);
+        const bool stop = !have_total || df_gt(thr, rem) || !(best.hi > 0.f);
         sm.stop = stop;
         if (!stop) {
           const int o = sm.ord[t];
