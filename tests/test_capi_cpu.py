@@ -86,3 +86,15 @@ def test_batch_entry_points_reject_bad_arguments_without_gpu(rbrp_lib):
     info = _lib.BatchInfo()
     assert rbrp_lib.rbrp_batch_get_info(None, ctypes.byref(info)) == 1
     assert rbrp_lib.rbrp_batch_set_profiling(None, 1) == 1
+
+
+def test_sketch_lu_and_fixed_skeleton_entry_points_reject_null_handle(rbrp_lib):
+    """The comparison-ID and differentiable entry points check arguments before any CUDA call."""
+    r = _lib.Result()
+    loss = ctypes.c_double()
+    assert rbrp_lib.rbrp_sketch_gaussian_f32(None, 4, 8, 8, None, 8, 0, ctypes.c_float(1.0), None, 4) == 1
+    assert rbrp_lib.rbrp_lupp_pivots_f64(None, 2, 8, None, 2, None, None) == 1
+    assert rbrp_lib.rbrp_fixed_id_f64(None, 8, 8, None, 8, None, 2, 2, None, ctypes.byref(r)) == 1
+    assert rbrp_lib.rbrp_fixed_id_f32(None, 8, 8, None, 8, None, 2, 2, None, ctypes.byref(r)) == 1
+    assert rbrp_lib.rbrp_fixed_id_adjoint_f32(None, 8, 8, None, 8, None, ctypes.c_float(1.0), None, 8,
+                                              ctypes.byref(loss)) == 1
