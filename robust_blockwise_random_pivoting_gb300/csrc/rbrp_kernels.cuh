@@ -1108,10 +1108,13 @@ k_resid_update(const float* __restrict__ Qb, int64_t ldq, float* __restrict__ Ar
           x.z -= acc[2][c];
           x.w -= acc[3][c];
           *reinterpret_cast<float4*>(col + r) = x;
-          df_add_sq(nrm[c], x.x);
-          df_add_sq(nrm[c], x.y);
-          df_add_sq(nrm[c], x.z);
-          df_add_sq(nrm[c], x.w);
+          // FP32 sum of the 4 squares (positive terms, relative error < 3e-7), folded
+          // into the double-float norm by TwoSum
+          const float q4 = fmaf(x.w, x.w, fmaf(x.z, x.z, fmaf(x.y, x.y, x.x * x.x)));
+          const float t = nrm[c].hi + q4;
+          const float bb = t - nrm[c].hi;
+          nrm[c].lo += (nrm[c].hi - (t - bb)) + (q4 - bb);
+          nrm[c].hi = t;
         } else {
 #pragma unroll
           for (int u = 0; u < 4; ++u) {
