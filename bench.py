@@ -54,13 +54,13 @@ WORKLOADS = {
 def describe(name, wl):
     if wl["kind"] == "cpqr":
         return (f"{name}: deterministic CPQR ID (greedy b=1, LAPACK dgeqp3's pivots) to rank {wl['k']} of the C++ "
-                f"driver's Gaussian-mixture matrix {wl['d']}x{wl['n']} ({wl['clusters']} clusters), FP64; a step is "
+                f"Gaussian-mixture matrix of gpu/driver.cpp, {wl['d']}x{wl['n']} ({wl['clusters']} clusters), FP64; a step is "
                 f"one ID (S, T)")
     if wl["kind"] == "idcmp":
-        return (f"{name}: the C++ driver's Gaussian-mixture matrix {wl['d']}x{wl['n']} ({wl['clusters']} clusters, "
+        return (f"{name}: the Gaussian-mixture matrix of gpu/driver.cpp, {wl['d']}x{wl['n']} ({wl['clusters']} clusters, "
                 f"point i of cluster c shifted by 10(c+1) in coordinate c), FP64; a step is one RBRP (b={wl['b']}) "
                 f"to rank {wl['nb'] * wl['b']}; RandCPQR_OS, RandLUPP_OS and the CPQR ID are timed at the first "
-                f"{wl['nb']} RBRP ranks, as the driver does")
+                f"{wl['nb']} RBRP ranks, as gpu/driver.cpp does")
     if wl["kind"] == "adjoint":
         return (f"{name}: fixed-skeleton ID loss ||A - A(:,S) T||^2 + ||T w||^2 and its gradient, Gaussian kernel "
                 f"{wl['n']}^2 on N(0, I_{wl['dim']}) points, l={wl['lengthscale']}, S from FP32 RBRP at squared tol "
@@ -718,7 +718,7 @@ def run_adjoint(args, wl, name, ctx):
 
 
 def run_idcmp(args, wl, name, ctx):
-    """The driver's comparison: RBRP, then the comparison IDs at RBRP's first ranks; returns the JSON line."""
+    """The comparison of gpu/driver.cpp: RBRP, then the comparison IDs at RBRP's first ranks; returns the JSON line."""
     torch = ctx.torch
     from robust_blockwise_random_pivoting_gb300 import workloads as W
     from robust_blockwise_random_pivoting_gb300.rbrp import Handle
@@ -788,7 +788,7 @@ def run_idcmp(args, wl, name, ctx):
 
 
 def run_cpqr(args, wl, name, ctx):
-    """The deterministic CPQR ID (the driver's CPQR baseline) per step; returns the JSON line."""
+    """The deterministic CPQR ID (the CPQR baseline of gpu/driver.cpp) per step; returns the JSON line."""
     torch = ctx.torch
     from robust_blockwise_random_pivoting_gb300 import workloads as W
     from robust_blockwise_random_pivoting_gb300.rbrp import Handle

@@ -88,7 +88,7 @@ def gmm(d=1024, npts=65536, nclusters=20, seed=0):
 
 
 def driver_gmm(npts=1000, d=1000, nclusters=100, seed=0):
-    """The C++ driver's Gaussian-mixture test matrix (``gpu/driver.cpp:94-109``), d x npts.
+    """The Gaussian-mixture test matrix of ``gpu/driver.cpp:94-109``, d x npts.
 
     i.i.d. N(0, 1) entries; point i belongs to cluster c = i // (npts // nclusters)
     and has 10 (c + 1) added to coordinate c.
