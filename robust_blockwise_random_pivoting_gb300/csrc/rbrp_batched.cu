@@ -147,9 +147,10 @@ __device__ __forceinline__ int block_max_int(int v, int* sh) {
   return r;
 }
 
-// A warp's walk over one column, f(x) per entry: 16-byte loads (four in flight
-// per lane) when the column is 16-byte aligned.  Both norm passes use it, so a
-// lane sees the same entries in the same order in each.
+// A warp's walk over one column, f(x0, x1, x2, x3) per group of four entries
+// (zeros pad the scalar groups): 16-byte loads (four in flight per lane) when the
+// column is 16-byte aligned.  Both norm passes use it, so a lane sees the same
+// entries in the same groups and order in each.
 template <typename F>
 __device__ __forceinline__ void column_walk(const float* __restrict__ col, int m, int lane, bool vec, F&& f) {
   if (vec) {
@@ -158,19 +159,29 @@ __device__ __forceinline__ void column_walk(const float* __restrict__ col, int m
     int r = lane;
     for (; r + 96 < m4; r += 128) {
       const float4 a = c4[r], b = c4[r + 32], c = c4[r + 64], d = c4[r + 96];
-      f(a.x); f(a.y); f(a.z); f(a.w);
-      f(b.x); f(b.y); f(b.z); f(b.w);
-      f(c.x); f(c.y); f(c.z); f(c.w);
-      f(d.x); f(d.y); f(d.z); f(d.w);
+      f(a.x, a.y, a.z, a.w);
+      f(b.x, b.y, b.z, b.w);
+      f(c.x, c.y, c.z, c.w);
+      f(d.x, d.y, d.z, d.w);
     }
     for (; r < m4; r += 32) {
       const float4 a = c4[r];
-      f(a.x); f(a.y); f(a.z); f(a.w);
+      f(a.x, a.y, a.z, a.w);
     }
-    for (int t = 4 * m4 + lane; t < m; t += 32) f(col[t]);
+    for (int t = 4 * m4 + lane; t < m; t += 32) f(col[t], 0.f, 0.f, 0.f);
   } else {
-    for (int r = lane; r < m; r += 32) f(col[r]);
+    for (int r = lane; r < m; r += 32) f(col[r], 0.f, 0.f, 0.f);
   }
+}
+
+// acc += x0^2 + x1^2 + x2^2 + x3^2: an FP32 sum of the four squares (positive
+// terms, relative error < 3e-7) folded into the double-float sum by TwoSum
+__device__ __forceinline__ void df_add_sq4(DF& acc, float x0, float x1, float x2, float x3) {
+  const float q = fmaf(x3, x3, fmaf(x2, x2, fmaf(x1, x1, x0 * x0)));
+  const float t = acc.hi + q;
+  const float bb = t - acc.hi;
+  acc.lo += (acc.hi - (t - bb)) + (q - bb);
+  acc.hi = t;
 }
 
 // a1: column maxima, squared norms (double-float; a column whose maximum lies
@@ -190,11 +201,11 @@ __device__ int batch_norms(BatchSmem<BB>& sm, const float* __restrict__ A, int64
     unsigned mx = 0u;
     int nf = 0;
     DF raw{0.f, 0.f};
-    column_walk(col, m, lane, vec, [&](float x) {
-      const float v = fabsf(x);
-      nf |= !(v <= FLT_MAX);
-      mx = max(mx, __float_as_uint(v));
-      df_add_sq(raw, x);
+    column_walk(col, m, lane, vec, [&](float x0, float x1, float x2, float x3) {
+      const float v0 = fabsf(x0), v1 = fabsf(x1), v2 = fabsf(x2), v3 = fabsf(x3);
+      nf |= !(v0 <= FLT_MAX) | !(v1 <= FLT_MAX) | !(v2 <= FLT_MAX) | !(v3 <= FLT_MAX);
+      mx = max(max(mx, max(__float_as_uint(v0), __float_as_uint(v1))), max(__float_as_uint(v2), __float_as_uint(v3)));
+      df_add_sq4(raw, x0, x1, x2, x3);
     });
     mx = __reduce_max_sync(0xffffffffu, mx);
     nf = __any_sync(0xffffffffu, nf);
@@ -209,7 +220,9 @@ __device__ int batch_norms(BatchSmem<BB>& sm, const float* __restrict__ A, int64
       } else {
         const Pow2 sc = pow2_scale(-e);
         DF acc{0.f, 0.f};
-        column_walk(col, m, lane, vec, [&](float x) { df_add_sq(acc, sc.apply(x)); });
+        column_walk(col, m, lane, vec, [&](float x0, float x1, float x2, float x3) {
+          df_add_sq4(acc, sc.apply(x0), sc.apply(x1), sc.apply(x2), sc.apply(x3));
+        });
         d = warp_sum_df(acc.hi, acc.lo);
         ce = e;
       }
