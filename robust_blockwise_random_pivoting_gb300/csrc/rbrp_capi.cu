@@ -744,7 +744,8 @@ rbrp_status rbrp_create(rbrp_handle* out, int device) {
   if (!h) return RBRP_ERR_ALLOC;
   h->device = device;
   DeviceGuard g(device);
-  if (!g.ok || cudaEventCreate(&h->ev_start) != cudaSuccess || cudaEventCreate(&h->ev_loop) != cudaSuccess ||
+  if (!g.ok || cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+      cudaEventCreate(&h->ev_start) != cudaSuccess || cudaEventCreate(&h->ev_loop) != cudaSuccess ||
       cudaEventCreate(&h->ev_end) != cudaSuccess) {
     cudaGetLastError();
     delete h;

@@ -148,13 +148,27 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
     if (RES) {
       int wsplit = 0;
       if (use_tc) {
-        // split the rows so that about two CTAs per SM stream the remaining columns
+        // row split: one CTA per SM fits (shared memory), so the launch runs in
+        // ceil(ctiles * split / SMs) waves of sps stages each plus a fixed cost per CTA
+        // (TMEM allocation, pipeline fill and final drains: about 4 stages); take the
+        // split with the least wave time (the smallest on ties: fewer partials to sum)
         const int ctiles = (n - i + tc::BM - 1) / tc::BM;
         const int nstages = (m + tc::BK - 1) / tc::BK;
-        wsplit = std::min(std::min(P1_MAX_SPLIT, std::max(1, (2 * 152 + ctiles - 1) / ctiles)),
-                          std::max(1, nstages / tc::CHUNK));
-        const int sps = (nstages + wsplit - 1) / wsplit;
-        wsplit = (nstages + sps - 1) / sps;
+        const int maxsplit = std::min(P1_MAX_SPLIT, std::max(1, nstages / tc::CHUNK));
+        int sps = nstages;
+        wsplit = 1;
+        long best = -1;
+        for (int w = 1; w <= maxsplit; ++w) {
+          const int s_w = (nstages + w - 1) / w;
+          const int ws = (nstages + s_w - 1) / s_w;
+          const long waves = ((long)ctiles * ws + h->sms - 1) / h->sms;
+          const long cost = waves * (s_w + 4);
+          if (best < 0 || cost < best) {
+            best = cost;
+            wsplit = ws;
+            sps = s_w;
+          }
+        }
         tc::k_proj_w_tc<<<dim3(ctiles, wsplit), tc::NTHREADS, tc::P1_SMEM, st>>>(tmA, tmQh, tmQl, h->st, m, n, sps,
                                                                                 reinterpret_cast<float2*>(h->Wpart));
       } else {
@@ -164,9 +178,23 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
       prof_end(h, RBRP_PHASE_PROJECT, ev, 0.0, 0.0, 1);
       ev = prof_begin(h);
       const int ctiles = (n - i + P2_COLS - 1) / P2_COLS;
-      int nsplit = std::min(P2_MAX_SPLIT, std::max(1, (4 * 152 + ctiles - 1) / ctiles));
-      const int rps = ((m + nsplit - 1) / nsplit + P2_ROWS - 1) / P2_ROWS * P2_ROWS;
-      nsplit = (m + rps - 1) / rps;
+      // row split by the same wave rule, two CTAs per SM (registers and shared memory), with
+      // a fixed cost per CTA of about two stages (W partial sums and staging, norm partials)
+      int nsplit = 1, rps = (m + P2_ROWS - 1) / P2_ROWS * P2_ROWS;
+      {
+        long best = -1;
+        for (int w = 1; w <= P2_MAX_SPLIT; ++w) {
+          const int r_w = ((m + w - 1) / w + P2_ROWS - 1) / P2_ROWS * P2_ROWS;
+          const int ws = (m + r_w - 1) / r_w;
+          const long waves = ((long)ctiles * ws + 2 * h->sms - 1) / (2 * h->sms);
+          const long cost = waves * (r_w + 2 * P2_ROWS);
+          if (best < 0 || cost < best) {
+            best = cost;
+            nsplit = ws;
+            rps = r_w;
+          }
+        }
+      }
       k_resid_update<<<dim3(ctiles, nsplit), P2_THREADS, P2_SMEM, st>>>((const float*)Q, L.ld_res, h->Ares, L.ld_res,
                                                                        h->st, m, n, rps, h->R, n,
                                                                        use_tc ? reinterpret_cast<const float2*>(h->Wpart)

@@ -16,6 +16,7 @@ struct BatchState;                  // batched form (rbrp_batched.cu)
 
 struct rbrp_handle_st {
   int device = 0;
+  int sms = 152;   // SM count of the device (set at create)
   cudaStream_t stream = nullptr;
   std::string last_error;
 
