@@ -125,7 +125,7 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
     if (RES) {
       // R11 as double-float pairs: the FP64 buffer of the same size, reinterpreted
       float2* R11df = reinterpret_cast<float2*>(h->R11);
-      k_pchol_df<<<1, 256, sizeof(PcholDfSmem), st>>>(h->G, m, h->st, tol_loc, h->js, h->perm, h->diags, R11df,
+      k_pchol_df<<<1, LEAN_THREADS, sizeof(PcholDfSmem), st>>>(h->G, m, h->st, tol_loc, h->js, h->perm, h->diags, R11df,
                                                       h->ord, h->J, h->K1, h->K2);
       k_panel_q_df<<<ttiles, DF_TROWS, sizeof(RowsDfSmem), st>>>((const float*)h->V, m, h->st, R11df, h->ord,
                                                                  (float*)Q, L.ld_res, use_tc ? h->Qh : nullptr,

@@ -66,9 +66,9 @@ k_gram_df(const float* __restrict__ Ares, int64_t ld, const int* __restrict__ js
 using PcholDfSmem = PcholDfSmemT<MAXB>;
 
 // Pivoted Cholesky of the panel Gram matrix with the robust filter (same rule as
-// pivoted_chol_filter), 256 threads, no data movement for the swaps.  Publishes
+// pivoted_chol_filter), LEAN_THREADS threads, no data movement for the swaps.  Publishes
 // R11 (slot order, double-float pairs), ord, the kept count and performs the block swap.
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(LEAN_THREADS)
 k_pchol_df(const double* __restrict__ G, int m, State* st, double tol_loc, const int* __restrict__ js,
            int* __restrict__ perm, double* __restrict__ diags, float2* __restrict__ R11g, int* __restrict__ ordg,
            int* __restrict__ Jg, int* __restrict__ K1g, int* __restrict__ K2g) {
@@ -77,7 +77,7 @@ k_pchol_df(const double* __restrict__ G, int m, State* st, double tol_loc, const
   const int tid = threadIdx.x;
   const int nb = st->bs_sampled, i = st->i;
   const int rows = min(nb, m);
-  for (int idx = tid; idx < MAXB * MAXB; idx += 256) {
+  for (int idx = tid; idx < MAXB * MAXB; idx += blockDim.x) {
     const int a = idx / MAXB, c = idx % MAXB;
     sm.S[a][c] = (a < nb && c < nb) ? df_of(G[a * MAXB + c]) : dfl{0.f, 0.f};
   }
@@ -86,9 +86,10 @@ k_pchol_df(const double* __restrict__ G, int m, State* st, double tol_loc, const
     sm.alive[tid] = tid < nb;
   }
   __syncthreads();
-  const int kept = pchol_filter_df<MAXB>(sm, nb, rows, tol_loc);
+  static_assert(MAXB == 64, "the lean factorization is written for 64-column panels");
+  const int kept = pchol_filter_df_lean(sm, nb, rows, tol_loc);
   // R11 in slot order: R11[a][c] = R[a][ord[c]] for c >= a
-  for (int idx = tid; idx < MAXB * MAXB; idx += 256) {
+  for (int idx = tid; idx < MAXB * MAXB; idx += blockDim.x) {
     const int a = idx / MAXB, c = idx % MAXB;
     const dfl v = (a < kept && c < kept && c >= a) ? sm.R[a][sm.ord[c]] : dfl{0.f, 0.f};
     R11g[idx] = make_float2(v.hi, v.lo);
@@ -102,16 +103,29 @@ k_pchol_df(const double* __restrict__ G, int m, State* st, double tol_loc, const
 struct RowsDfSmem {
   dfl R[MAXB][MAXB + 1];
   dfl W[DF_TROWS][MAXB + 1];
+  dfl inv[MAXB];   // 1 / R(s, s)
   int ord[MAXB];
 };
 
+// Forward substitution of each row against R (one thread per row).  The sum over
+// the solved entries runs in four independent double-float chains, so the latency
+// chain of a row is a quarter as long; the diagonal reciprocals are computed once.
 __device__ __forceinline__ void rows_solve_df(RowsDfSmem& sm, int kept) {
   const int r = threadIdx.x;
+  if (r < kept) sm.inv[r] = df_recip(sm.R[r][r]);
+  __syncthreads();
   if (r < DF_TROWS) {
     for (int s = 0; s < kept; ++s) {
-      dfl x = sm.W[r][s];
-      for (int u = 0; u < s; ++u) x = df_fms(x, sm.W[r][u], sm.R[u][s]);
-      sm.W[r][s] = df_mul(x, df_recip(sm.R[s][s]));
+      dfl a0 = sm.W[r][s], a1 = {0.f, 0.f}, a2 = {0.f, 0.f}, a3 = {0.f, 0.f};
+      int u = 0;
+      for (; u + 4 <= s; u += 4) {
+        a0 = df_fms(a0, sm.W[r][u], sm.R[u][s]);
+        a1 = df_fms(a1, sm.W[r][u + 1], sm.R[u + 1][s]);
+        a2 = df_fms(a2, sm.W[r][u + 2], sm.R[u + 2][s]);
+        a3 = df_fms(a3, sm.W[r][u + 3], sm.R[u + 3][s]);
+      }
+      for (; u < s; ++u) a0 = df_fms(a0, sm.W[r][u], sm.R[u][s]);
+      sm.W[r][s] = df_mul(df_add(df_add(a0, a1), df_add(a2, a3)), sm.inv[s]);
     }
   }
   __syncthreads();

@@ -13,10 +13,13 @@ struct PcholDfSmemT {
   dfl S[BB][BB + 1];  // Schur complement, indexed by panel column
   dfl R[BB][BB + 1];  // R[t][j]: row t of the factor, by panel column j
   int ord[BB];        // slot -> panel column
+  int slot[BB];       // panel column -> slot (pchol_filter_df_lean)
   int alive[BB];
   int J[BB], K1[BB], K2[BB], inblk[BB], Tperm[BB];
   int stop, piv, nK;
   dfl inv;
+  dfl cval[32], crem[32];  // per diagonal owner: best live diagonal and live diagonal sum
+  int cslot[32], ccol[32];
 };
 
 // Block swap of perm and diags (matlab/RBRP.m:81-99), in parallel: K1 = block
@@ -158,6 +161,130 @@ __device__ int pchol_filter_df(PcholDfSmemT<BB>& sm, int nb, int rows, double to
 #pragma unroll
       for (int v = 0; v < U; ++v)
         if (au[u] && av[v]) sm.S[ty * U + u][tx * U + v] = df_fms(sm.S[ty * U + u][tx * U + v], ru[u], rv[v]);
+    __syncthreads();
+  }
+  return kept;
+}
+
+// The same factorization and filter as pchol_filter_df<64>, by 1024 threads
+// (LEAN_THREADS): thread (ty, tx) of a 32 x 32 grid owns the Schur entries of
+// rows ty + 32u and columns tx + 32v (u, v < 2), so a warp touches one row pair
+// of consecutive entries (no bank conflicts) and each thread's update is four
+// independent double-float chains.  Two barriers per step instead of three and
+// a 32-way pivot search: the 32 threads that own diagonal entries (ty == tx)
+// rank their live diagonals right after updating them, and every thread forms
+// its own factor-row values S(pv, j) / r from the pivot row, which no thread
+// writes during the update.  Each Schur entry gets the same double-float
+// operation on the same inputs and pivots tie to the first slot as before;
+// only the remaining-trace sum of the stop test is added in another order.
+// Square root and reciprocal start from the correctly rounded FP32 intrinsics.
+constexpr int LEAN_THREADS = 1024;
+
+__device__ __forceinline__ dfl df_sqrt_lean(dfl a) {
+  if (!(a.hi > 0.0f)) return {0.0f, 0.0f};
+  const float sq = __fsqrt_rn(a.hi);
+  const dfl e = df_add(a, df_neg(df_mul({sq, 0.0f}, {sq, 0.0f})));  // a - sq^2
+  return df_fast(sq, e.hi * (0.5f * __frcp_rn(sq)));
+}
+__device__ __forceinline__ dfl df_recip_lean(dfl b) {
+  const float q = __frcp_rn(b.hi);
+  const dfl r = df_add({1.0f, 0.0f}, df_neg(df_mul({q, 0.0f}, b)));  // 1 - q b
+  return df_fast(q, q * r.hi);
+}
+
+__device__ int pchol_filter_df_lean(PcholDfSmemT<64>& sm, int nb, int rows, double tol_loc) {
+  constexpr int BB = 64, U = 2, G = 32;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int ty = wid, tx = lane;
+  const bool owner = ty == tx;  // owns the diagonal entries ty + 32u
+  bool have_total = false;
+  dfl thr = {0.f, 0.f};
+  if (tid < BB) sm.slot[tid] = tid;
+  auto rank_diag = [&]() {
+    dfl best = {-1.f, 0.f}, rem = {0.f, 0.f};
+    int bs = BB, bc = -1;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int j = ty + G * u;
+      if (j < nb && sm.alive[j]) {
+        const dfl d = sm.S[j][j];
+        rem = df_add(rem, d);
+        const int sj = sm.slot[j];
+        if (df_gt(d, best) || (df_eq(d, best) && sj < bs)) { best = d; bs = sj; bc = j; }
+      }
+    }
+    sm.cval[ty] = best;
+    sm.crem[ty] = rem;
+    sm.cslot[ty] = bs;
+    sm.ccol[ty] = bc;
+  };
+  __syncthreads();
+  if (owner) rank_diag();
+  __syncthreads();
+  if (wid == 0) {
+    dfl t = sm.crem[lane];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+      t = df_add(t, {__shfl_down_sync(0xffffffffu, t.hi, o), __shfl_down_sync(0xffffffffu, t.lo, o)});
+    const double total = __shfl_sync(0xffffffffu, df_dbl(t), 0);
+    have_total = total > 0.0;
+    thr = df_of(tol_loc * total);
+  }
+  int kept = rows;
+  for (int t = 0; t < rows; ++t) {
+    if (wid == 0) {
+      dfl best = sm.cval[lane], rem = sm.crem[lane];
+      int bs = sm.cslot[lane], bc = sm.ccol[lane];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        rem = df_add(rem, {__shfl_down_sync(0xffffffffu, rem.hi, o), __shfl_down_sync(0xffffffffu, rem.lo, o)});
+        const dfl ob = {__shfl_down_sync(0xffffffffu, best.hi, o), __shfl_down_sync(0xffffffffu, best.lo, o)};
+        const int os = __shfl_down_sync(0xffffffffu, bs, o), oc = __shfl_down_sync(0xffffffffu, bc, o);
+        if (df_gt(ob, best) || (df_eq(ob, best) && os < bs)) { best = ob; bs = os; bc = oc; }
+      }
+      if (lane == 0) {
+        const bool stop = !have_total || df_gt(thr, rem) || !(best.hi > 0.f) || bc < 0;
+        sm.stop = stop;
+        if (!stop) {
+          // LAPACK order: the pivot column moves to slot t, slot t's column to the pivot's slot
+          const int o = sm.ord[t];
+          sm.ord[t] = bc;
+          sm.ord[bs] = o;
+          sm.slot[o] = bs;
+          sm.slot[bc] = t;
+          sm.alive[bc] = 0;
+          const dfl r = df_sqrt_lean(sm.S[bc][bc]);
+          sm.R[t][bc] = r;
+          sm.inv = df_recip_lean(r);
+          sm.piv = bc;
+        }
+      }
+    }
+    __syncthreads();
+    if (sm.stop) { kept = t; break; }
+    const int pv = sm.piv;
+    const dfl inv = sm.inv;
+    dfl ru[U], rv[U];
+    bool au[U], av[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int j = ty + G * u, c = tx + G * u;
+      au[u] = j < nb && sm.alive[j];
+      av[u] = c < nb && sm.alive[c];
+      ru[u] = au[u] ? df_mul(sm.S[pv][j], inv) : dfl{0.f, 0.f};
+      rv[u] = av[u] ? df_mul(sm.S[pv][c], inv) : dfl{0.f, 0.f};
+    }
+    if (ty == 0) {
+#pragma unroll
+      for (int v = 0; v < U; ++v)
+        if (av[v]) sm.R[t][tx + G * v] = rv[v];
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int v = 0; v < U; ++v)
+        if (au[u] && av[v]) sm.S[ty + G * u][tx + G * v] = df_fms(sm.S[ty + G * u][tx + G * v], ru[u], rv[v]);
+    if (owner) rank_diag();
     __syncthreads();
   }
   return kept;
