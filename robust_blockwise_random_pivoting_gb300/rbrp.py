@@ -400,19 +400,20 @@ class HostBatch:
     back (each column major, ``shapes[q] = (m_q, n_q)``, starting at
     ``packed_offsets(shapes)[0][q]``).  The problems are cut
     into ``parts`` consecutive groups of about equal size; each group has its
-    own handle, device buffer, plan and stream.  :meth:`run` enqueues, per
-    group, the copy of the group's matrices, its graph launch and the copies of
-    its perm and T back to pinned host buffers, so one group's copy runs while
-    the previous group computes.  The persistent kernel balances its load over
-    the problems it is given, largest first; a group holds fewer, so its kernel
-    runs less efficiently than one launch over all problems (on 4096 uneven
-    blocks three groups spend about 1.5x the compute of one batch, which the
-    overlap wins back).  Problem q keeps the Philox key
+    own handle, device buffer and plan.  :meth:`run` enqueues every group's
+    host-to-device copy on one copy stream and, on one compute stream, each
+    group's graph launch (after its copy's event) and the copies of its perm
+    and T back to pinned host buffers: group g + 1's copy runs while group g
+    computes, and the groups' persistent kernels never run at the same time
+    (concurrent ones take SMs from each other's largest problems).  A group
+    still balances its load over fewer problems than one launch over all of
+    them, so more groups hide more of the copy but lengthen the compute.
+    Problem q keeps the Philox key
     ``seed + q`` and every group uses the block size the first group's autotuner
     chose, so the results are those of one batch over all problems with that b.
     """
 
-    def __init__(self, host_pack, shapes, parts=3, b=0, tol=1e-8, kmax=None, seed=0, sampler="np", tol_loc=None,
+    def __init__(self, host_pack, shapes, parts=2, b=0, tol=1e-8, kmax=None, seed=0, sampler="np", tol_loc=None,
                  compute_T=True, t_rank_cap=None, device=None):
         if host_pack.is_cuda or host_pack.dtype != torch.float32 or not host_pack.is_pinned():
             raise TypeError("host_pack must be a pinned FP32 CPU tensor")
@@ -443,16 +444,29 @@ class HostBatch:
                 perm_h=torch.empty(bt.perm_buf.numel(), dtype=torch.int32, pin_memory=True),
                 T_h=torch.empty(bt.T_buf.numel() if compute_T else 0, dtype=torch.float64, pin_memory=True)))
         self.b = b_used
-        self.streams = [torch.cuda.Stream(dev) for _ in self.groups]
+        self.copy_stream = torch.cuda.Stream(dev)
+        self.compute_stream = torch.cuda.Stream(dev)
+        self.streams = [self.copy_stream, self.compute_stream]
         self.h2d_bytes = int(host_pack.numel() * 4)
         self.d2h_bytes = int(sum(G["perm_h"].numel() * 4 + G["T_h"].numel() * 8 for G in self.groups))
 
     def run(self):
         """Enqueue every group: copy in, graph launch, perm and T out (no host wait)."""
-        for G, s in zip(self.groups, self.streams):
-            with torch.cuda.stream(s):
+        cs, ks = self.copy_stream, self.compute_stream
+        # the copy stream must not overwrite a group's buffer before the previous run's
+        # graph has read it: start behind the compute stream's last work
+        cs.wait_stream(ks)
+        arrived = []
+        for G in self.groups:
+            with torch.cuda.stream(cs):
                 G["dpack"].copy_(G["host"], non_blocking=True)
-                G["batch"].run(s)
+                ev = torch.cuda.Event()
+                ev.record(cs)
+                arrived.append(ev)
+        for G, ev in zip(self.groups, arrived):
+            ks.wait_event(ev)
+            with torch.cuda.stream(ks):
+                G["batch"].run(ks)
                 G["perm_h"].copy_(G["batch"].perm_buf, non_blocking=True)
                 if self.compute_T:
                     G["T_h"].copy_(G["batch"].T_buf, non_blocking=True)

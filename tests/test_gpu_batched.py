@@ -214,7 +214,7 @@ def test_host_batch_pipeline_equals_one_batch(handle):
     hb = HostBatch(host, [tuple(int(v) for v in s) for s in shp], parts=3, b=0, tol=1e-8, seed=100,
                    t_rank_cap=64)
     try:
-        assert len(hb.groups) == 3
+        assert len(hb.groups) == 3   # parts=3 requested
         hb.run()
         groups = hb.results()
         ref = Batch(handle, [dev32(A) for A in mats], b=hb.b, tol=1e-8, seed=100, t_rank_cap=64)
