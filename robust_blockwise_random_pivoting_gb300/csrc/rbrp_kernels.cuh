@@ -9,7 +9,8 @@
 //   k_swap_R      R(:i, K2) = R(:i, K1), R(:i, I2) = R(:i, J)
 //   k_panel2      second CholQR pass: Q_blk = Q1 R2^{-1}, R(I2, I2) = R2 R11
 //   k_project     W = Q_blk^T A(:, perm[p]) for the remaining positions p,
-//                 R(I2, p) = W, diags(p) -= ||W(:, p)||^2 (clipped at 0)
+//                 R(I2, p) = W, diags(p) -= ||W(:, p)||^2 (clipped at 0);
+//                 k_project_skinny for blocks of b <= 8 (column streams)
 //   k_finish      residual, stop rule, per-block trace
 #pragma once
 #include <type_traits>

@@ -1,8 +1,9 @@
-// rbrp_panel_df.cuh - panel CPQR / CholQR2 of the FP32 residual form in
-// double-float arithmetic.
+// rbrp_panel_df.cuh - panel CPQR of the FP32 residual form in double-float
+// arithmetic (one CholQR pass: ~48-bit arithmetic keeps the basis orthogonal to
+// far below its FP32 rounding).
 //
 // GB300's FP64 pipe issues ~1/64 of the FP32 pipe's rate, and the panel work
-// (Gram matrices, two row solves, two small Cholesky factorisations per block)
+// (the Gram matrix, a pivoted Cholesky factorisation and a row solve per block)
 // is FP64-class arithmetic.  Here every FP64 quantity is a pair of floats
 // (hi + lo, ~48 significant bits) computed on the FP32 pipe with error-free
 // transformations: products by FMA splitting, sums by TwoSum.  The steps are
