@@ -51,6 +51,14 @@ __device__ __forceinline__ dfl df_fms(dfl s, dfl a, dfl b) {
   return df_fast(t.hi, t.lo + (s.lo - e));
 }
 // acc + a * b
+// acc + x * b for an FP32 x (an exact residual entry) and a double-float b
+__device__ __forceinline__ dfl df_fma_f(dfl acc, float x, dfl b) {
+  const float p = x * b.hi;
+  float e = fmaf(x, b.hi, -p);
+  e = fmaf(x, b.lo, e);
+  const dfl t = df_two_sum(acc.hi, p);
+  return df_fast(t.hi, t.lo + (acc.lo + e));
+}
 __device__ __forceinline__ dfl df_fma2(dfl acc, dfl a, dfl b) {
   const float p = a.hi * b.hi;
   float e = fmaf(a.hi, b.hi, -p);

@@ -40,7 +40,7 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
                                              (int)sizeof(PcholDfSmem)), "cudaFuncSetAttribute(panel df)");
       if (s != RBRP_OK) return s;
       s = cuda_check(h, cudaFuncSetAttribute(k_panel_q_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)sizeof(RowsDfSmem)), "cudaFuncSetAttribute(rows df)");
+                                             (int)sizeof(QSolveSmem)), "cudaFuncSetAttribute(basis df)");
       if (s != RBRP_OK) return s;
       s = cuda_check(h, cudaFuncSetAttribute(k_resid_update, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)P2_SMEM), "cudaFuncSetAttribute(k_resid_update)");
@@ -112,7 +112,6 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
       k_reduce_parts<T><<<(int)std::min<int64_t>(1024, (cnt + 255) / 256), 256, 0, st>>>(Cpart, splits, cnt, cnt, C);
     }
     const int dtiles = (m + DF_ROWS - 1) / DF_ROWS;   // row tiles of the double-float Gram kernel
-    const int ttiles = (m + DF_TROWS - 1) / DF_TROWS; // row tiles of the double-float row solves
     if (RES) {  // panel = residual columns at the sampled positions (FP32, exact), Gram in double-float
       k_gram_df<<<dtiles, 256, 0, st>>>(h->Ares, L.ld_res, h->js, h->st, m, (float*)h->V, h->Gpart);
       k_reduce_parts<double><<<16, 256, 0, st>>>(h->Gpart, dtiles, MAXB * MAXB, MAXB * MAXB, h->G);
@@ -123,13 +122,15 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
     prof_end(h, RBRP_PHASE_CGS, ev, 0.0, 0.0, (!RES && i > 0) ? 4 : 2);
     ev = prof_begin(h);
     if (RES) {
-      // R11 as double-float pairs: the FP64 buffer of the same size, reinterpreted
+      // R11 and its inverse as double-float pairs: the FP64 R11 / R2 buffers of the same
+      // size (R2 serves only the FP64 form's second CholQR pass), reinterpreted
       float2* R11df = reinterpret_cast<float2*>(h->R11);
-      k_pchol_df<<<1, LEAN_THREADS, sizeof(PcholDfSmem), st>>>(h->G, m, h->st, tol_loc, h->js, h->perm, h->diags, R11df,
-                                                      h->ord, h->J, h->K1, h->K2);
-      k_panel_q_df<<<ttiles, DF_TROWS, sizeof(RowsDfSmem), st>>>((const float*)h->V, m, h->st, R11df, h->ord,
-                                                                 (float*)Q, L.ld_res, use_tc ? h->Qh : nullptr,
-                                                                 use_tc ? h->Ql : nullptr, L.ld_res);
+      float2* Rinvdf = reinterpret_cast<float2*>(h->R2);
+      k_pchol_df<<<1, LEAN_THREADS, sizeof(PcholDfSmem), st>>>(h->G, m, h->st, tol_loc, h->js, h->perm, h->diags,
+                                                               R11df, Rinvdf, h->ord, h->J, h->K1, h->K2);
+      k_panel_q_df<<<(m + QS_ROWS - 1) / QS_ROWS, 256, sizeof(QSolveSmem), st>>>(
+          (const float*)h->V, m, h->st, Rinvdf, h->ord, (float*)Q, L.ld_res, use_tc ? h->Qh : nullptr,
+          use_tc ? h->Ql : nullptr, L.ld_res);
       k_write_r11<<<1, 256, 0, st>>>(h->st, R11df, h->R, n);
     } else {
       k_pchol<<<1, 256, panel_smem, st>>>(h->G, m, h->st, tol_loc, h->js, h->perm, h->diags, h->R11, h->ord,

@@ -23,7 +23,6 @@ namespace rbrp {
 namespace {
 
 constexpr int DF_ROWS = 128;  // panel rows per CTA of the Gram kernel
-constexpr int DF_TROWS = 64;  // panel rows per CTA of the row-solve kernels (one thread per row)
 
 // V = A_res(:, J) (FP32, exact) for 128 rows per CTA, and the tile's Gram partial V^T V
 // (upper triangle, mirrored) in double-float, stored as FP64.
@@ -71,8 +70,8 @@ using PcholDfSmem = PcholDfSmemT<MAXB>;
 // R11 (slot order, double-float pairs), ord, the kept count and performs the block swap.
 __global__ void __launch_bounds__(LEAN_THREADS)
 k_pchol_df(const double* __restrict__ G, int m, State* st, double tol_loc, const int* __restrict__ js,
-           int* __restrict__ perm, double* __restrict__ diags, float2* __restrict__ R11g, int* __restrict__ ordg,
-           int* __restrict__ Jg, int* __restrict__ K1g, int* __restrict__ K2g) {
+           int* __restrict__ perm, double* __restrict__ diags, float2* __restrict__ R11g, float2* __restrict__ Rinvg,
+           int* __restrict__ ordg, int* __restrict__ Jg, int* __restrict__ K1g, int* __restrict__ K2g) {
   extern __shared__ __align__(16) unsigned char dyn_smem[];
   PcholDfSmem& sm = *reinterpret_cast<PcholDfSmem*>(dyn_smem);
   const int tid = threadIdx.x;
@@ -95,86 +94,102 @@ k_pchol_df(const double* __restrict__ G, int m, State* st, double tol_loc, const
     const dfl v = (a < kept && c < kept && c >= a) ? sm.R[a][sm.ord[c]] : dfl{0.f, 0.f};
     R11g[idx] = make_float2(v.hi, v.lo);
   }
+  // R11^{-1} (upper triangular, slot order) by columns: 16 threads per column c solve
+  // R11 x = e_c from the bottom, the dot products split over the 16 lanes.  The Schur
+  // array is free now and holds x; the column groups of a warp are independent.
+  __shared__ dfl invd[MAXB];
+  if (tid < kept) invd[tid] = df_recip_lean(sm.R[tid][sm.ord[tid]]);
+  __syncthreads();
+  {
+    const int c = tid >> 4, l = tid & 15;
+    dfl(*X)[MAXB + 1] = sm.S;
+    if (c < kept) {
+      const unsigned mask = 0xFFFFu << (threadIdx.x & 16);
+      if (l == 0) X[c][c] = invd[c];
+      __syncwarp(mask);
+      for (int a = c - 1; a >= 0; --a) {
+        dfl acc = {0.f, 0.f};
+        for (int u = a + 1 + l; u <= c; u += 16) acc = df_fma2(acc, sm.R[a][sm.ord[u]], X[u][c]);
+#pragma unroll
+        for (int o = 8; o > 0; o >>= 1)
+          acc = df_add(acc, {__shfl_xor_sync(mask, acc.hi, o), __shfl_xor_sync(mask, acc.lo, o)});
+        if (l == 0) X[a][c] = df_mul(df_neg(acc), invd[a]);
+        __syncwarp(mask);
+      }
+    }
+    __syncthreads();
+    for (int idx = tid; idx < MAXB * MAXB; idx += blockDim.x) {
+      const int a = idx / MAXB, cc = idx % MAXB;
+      const dfl v = (a < kept && cc < kept && cc >= a) ? X[a][cc] : dfl{0.f, 0.f};
+      Rinvg[idx] = make_float2(v.hi, v.lo);
+    }
+  }
   if (tid < MAXB) ordg[tid] = sm.ord[tid];
   block_swap_parallel(sm, i, kept, js, perm, diags, Jg, K1g, K2g, st);
 }
 
-// Rows of X R^{-1} (R upper, kept x kept, double-float pairs in global) for 128 rows per CTA,
-// one thread per row, in double-float; optionally the Gram partial of the result.
-struct RowsDfSmem {
-  dfl R[MAXB][MAXB + 1];
-  dfl W[DF_TROWS][MAXB + 1];
-  dfl inv[MAXB];   // 1 / R(s, s)
+// Q_blk = V(:, ord[:kept]) R11^{-1} in double-float as the product with the explicit
+// inverse (k_pchol_df), written as the FP32 basis and its exact TF32 split (Qh =
+// tf32(Q), Ql = fp32(Q - Qh), zero beyond the kept columns).  Every output is an
+// independent dot product: a CTA takes 32 rows, warp w the outputs s = w + 8q of
+// every row (lane = row, so the stores coalesce), eight chains per thread.  One
+// CholQR pass suffices here: with ~48-bit arithmetic the loss of orthogonality,
+// ~2^-48 cond(V_kept)^2, stays far below the FP32 rounding of the stored basis for
+// the conditioning the robust filter admits.
+constexpr int QS_ROWS = 32;
+struct QSolveSmem {
+  dfl Ri[MAXB][MAXB + 1];
+  float W[MAXB][QS_ROWS + 1];
   int ord[MAXB];
 };
 
-// Forward substitution of each row against R (one thread per row).  The sum over
-// the solved entries runs in four independent double-float chains, so the latency
-// chain of a row is a quarter as long; the diagonal reciprocals are computed once.
-__device__ __forceinline__ void rows_solve_df(RowsDfSmem& sm, int kept) {
-  const int r = threadIdx.x;
-  if (r < kept) sm.inv[r] = df_recip(sm.R[r][r]);
-  __syncthreads();
-  if (r < DF_TROWS) {
-    for (int s = 0; s < kept; ++s) {
-      dfl a0 = sm.W[r][s], a1 = {0.f, 0.f}, a2 = {0.f, 0.f}, a3 = {0.f, 0.f};
-      int u = 0;
-      for (; u + 4 <= s; u += 4) {
-        a0 = df_fms(a0, sm.W[r][u], sm.R[u][s]);
-        a1 = df_fms(a1, sm.W[r][u + 1], sm.R[u + 1][s]);
-        a2 = df_fms(a2, sm.W[r][u + 2], sm.R[u + 2][s]);
-        a3 = df_fms(a3, sm.W[r][u + 3], sm.R[u + 3][s]);
-      }
-      for (; u < s; ++u) a0 = df_fms(a0, sm.W[r][u], sm.R[u][s]);
-      sm.W[r][s] = df_mul(df_add(df_add(a0, a1), df_add(a2, a3)), sm.inv[s]);
-    }
-  }
-  __syncthreads();
-}
-
-__device__ __forceinline__ void load_R_df(RowsDfSmem& sm, const float2* __restrict__ Rg, int kept) {
-  for (int idx = threadIdx.x; idx < kept * kept; idx += blockDim.x) {
-    const float2 v = Rg[(idx / kept) * MAXB + idx % kept];
-    sm.R[idx / kept][idx % kept] = dfl{v.x, v.y};
-  }
-}
-
-// Q_blk = V(:, ord[:kept]) R11^{-1} in double-float, written as the FP32 basis and
-// its exact TF32 split (Qh = tf32(Q), Ql = fp32(Q - Qh), zero beyond the kept
-// columns).  One CholQR pass suffices here: with ~48-bit arithmetic the loss of
-// orthogonality, ~2^-48 cond(V_kept)^2, stays far below the FP32 rounding of
-// the stored basis for the conditioning the robust filter admits.
-__global__ void __launch_bounds__(DF_TROWS)
-k_panel_q_df(const float* __restrict__ V, int m, const State* __restrict__ st, const float2* __restrict__ R11g,
+__global__ void __launch_bounds__(256)
+k_panel_q_df(const float* __restrict__ V, int m, const State* __restrict__ st, const float2* __restrict__ Rinvg,
              const int* __restrict__ ordg, float* __restrict__ Q, int64_t ldq, float* __restrict__ Qh,
              float* __restrict__ Ql, int64_t ldh) {
   extern __shared__ __align__(16) unsigned char dyn_smem[];
-  RowsDfSmem& sm = *reinterpret_cast<RowsDfSmem*>(dyn_smem);
-  const int tid = threadIdx.x;
+  QSolveSmem& sm = *reinterpret_cast<QSolveSmem*>(dyn_smem);
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   const int kept = st->bs;
   if (kept == 0) return;
-  load_R_df(sm, R11g, kept);
+  for (int idx = tid; idx < kept * kept; idx += 256) {
+    const int u = idx / kept, s = idx % kept;
+    const float2 v = Rinvg[u * MAXB + s];
+    sm.Ri[u][s] = dfl{v.x, v.y};
+  }
   if (tid < MAXB) sm.ord[tid] = ordg[tid];
   __syncthreads();
-  const int r0 = blockIdx.x * DF_TROWS;
-  for (int idx = tid; idx < DF_TROWS * kept; idx += DF_TROWS) {
-    const int rr = idx % DF_TROWS, s = idx / DF_TROWS, r = r0 + rr;
-    sm.W[rr][s] = {r < m ? V[r + (int64_t)sm.ord[s] * m] : 0.f, 0.f};
+  const int r0 = blockIdx.x * QS_ROWS;
+  for (int idx = tid; idx < QS_ROWS * kept; idx += 256) {
+    const int rr = idx % QS_ROWS, u = idx / QS_ROWS, r = r0 + rr;
+    sm.W[u][rr] = r < m ? V[r + (int64_t)sm.ord[u] * m] : 0.f;
   }
   __syncthreads();
-  rows_solve_df(sm, kept);
-  for (int idx = tid; idx < DF_TROWS * MAXB; idx += DF_TROWS) {
-    const int rr = idx % DF_TROWS, s = idx / DF_TROWS, r = r0 + rr;
-    if (r < m) {
+  dfl acc[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) acc[q] = dfl{0.f, 0.f};
+  for (int u = 0; u < kept; ++u) {
+    const float x = sm.W[u][lane];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int s = w + 8 * q;
+      if (s < kept && u <= s) acc[q] = df_fma_f(acc[q], x, sm.Ri[u][s]);
+    }
+  }
+  const int r = r0 + lane;
+  if (r < m) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int s = w + 8 * q;
       // FP32 basis and its exact TF32 split, on the FP32 pipe: q = hi + lo (double-float),
       // Q = rn(q), Qh = tf32(Q), Ql = rn(q - Qh) with hi - Qh exact (Sterbenz)
-      const dfl w = s < kept ? sm.W[rr][s] : dfl{0.f, 0.f};
-      const float qf = __fadd_rn(w.hi, w.lo);
+      const dfl v = s < kept ? acc[q] : dfl{0.f, 0.f};
+      const float qf = __fadd_rn(v.hi, v.lo);
       if (s < kept) Q[r + (int64_t)s * ldq] = qf;
       if (Qh) {
         const float h = __uint_as_float(__float_as_uint(qf) & 0xFFFFE000u);
         Qh[r + (int64_t)s * ldh] = h;
-        Ql[r + (int64_t)s * ldh] = __fadd_rn(w.hi - h, w.lo);
+        Ql[r + (int64_t)s * ldh] = __fadd_rn(v.hi - h, v.lo);
       }
     }
   }
