@@ -147,6 +147,30 @@ rbrp_status rbrp_sketch_gaussian_f32(rbrp_handle h, int l, int m, int n, const f
 rbrp_status rbrp_lupp_pivots_f64(rbrp_handle h, int k, int n, const double* dW, int64_t ldw, int* dPerm,
                                  int* dIpiv);
 
+/* The reference's comparison IDs (gpu/rid.hpp) on this library's kernels.  A is
+ * a device FP64 matrix, m x n, ld = m; k is the rank (1 <= k <= min(m, n)); the
+ * sketch Y = G A has 2k rows, G ~ N(0, 1/m) from Philox with key `seed` (the
+ * reference draws G from a process-wide counter, gpu/random.cu:43).  T is
+ * k x (n - k), ld = k, rows in sk order and columns in rd order, allocated here
+ * on the device (free with rbrp_free).  Synchronous; own temporary handle.
+ *  - RandLUPP_OS (gpu/randLUPP_OS.cu:14-119): sk (k) and rd (n - k) are device
+ *    arrays allocated here (free with rbrp_free); skeleton from the LU pivots
+ *    of Y(1:k, :)^T.
+ *  - RandCPQR_OS (gpu/randCPQR_OS.cu:20-111): h_sk (k) and h_rd (n - k) are
+ *    caller-owned host arrays; skeleton from the column-pivoted QR of Y(1:k, :).
+ * flops: the reference's operation count where it sets one. */
+rbrp_status rbrp_RandLUPP_OS(const double* dA, int m, int n, int k, int** sk, int** rd, double** T,
+                             double* flops, uint64_t seed);
+rbrp_status rbrp_RandCPQR_OS(const double* dA, int m, int n, int k, int* h_sk, int* h_rd, double** T,
+                             double* flops, uint64_t seed);
+/* The CPQR baseline (gpu/id_cpqr.hpp, gpu/id_cpqr.cu:30-172): column-pivoted QR
+ * of A (device FP64, m x n, ld = m; LAPACK dgeqp3's pivots, greedy b = 1) to the
+ * largest of ranks[0..nranks); err[q] receives the squared relative ID error at
+ * rank ranks[q], t_ranks[q] (may be NULL) the cumulative seconds to that rank,
+ * *t_cpqr the total seconds.  Synchronous; own temporary handle. */
+rbrp_status rbrp_CPQR(int m, int n, const double* dA, const int* ranks, int nranks, double* err,
+                      double* t_ranks, double* t_cpqr, double* flops);
+
 /* T (k x (n-k), column major) of the last run, into a device buffer with ldt >= k. */
 rbrp_status rbrp_copy_T(rbrp_handle h, double* dT, int64_t ldt);
 /* Device pointer of T of the last run (ld = k), valid until the next run. */

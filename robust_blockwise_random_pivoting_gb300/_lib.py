@@ -112,6 +112,9 @@ _SIGS = {
     "rbrp_sketch_gaussian_f32": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_int64, c_uint64,
                                          ctypes.c_float, c_void_p, c_int64]),
     "rbrp_lupp_pivots_f64": (c_int, [c_void_p, c_int, c_int, c_void_p, c_int64, c_void_p, c_void_p]),
+    "rbrp_RandLUPP_OS": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_uint64]),
+    "rbrp_RandCPQR_OS": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_uint64]),
+    "rbrp_CPQR": (c_int, [c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     "rbrp_batch_plan": (c_int, [c_void_p, c_int, ctypes.POINTER(BatchProblem), ctypes.POINTER(Params)]),
     "rbrp_batch_run": (c_int, [c_void_p]),
     "rbrp_batch_results": (c_int, [c_void_p, ctypes.POINTER(BatchResult), c_int]),

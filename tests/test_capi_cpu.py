@@ -98,3 +98,8 @@ def test_sketch_lu_and_fixed_skeleton_entry_points_reject_null_handle(rbrp_lib):
     assert rbrp_lib.rbrp_fixed_id_f32(None, 8, 8, None, 8, None, 2, 2, None, ctypes.byref(r)) == 1
     assert rbrp_lib.rbrp_fixed_id_adjoint_f32(None, 8, 8, None, 8, None, ctypes.c_float(1.0), None, 8,
                                               ctypes.byref(loss)) == 1
+    p, fl = ctypes.c_void_p(), ctypes.c_double()
+    assert rbrp_lib.rbrp_RandLUPP_OS(None, 8, 8, 2, ctypes.byref(p), ctypes.byref(p), ctypes.byref(p),
+                                     ctypes.byref(fl), 0) == 1
+    assert rbrp_lib.rbrp_RandCPQR_OS(None, 8, 8, 2, None, None, ctypes.byref(p), ctypes.byref(fl), 0) == 1
+    assert rbrp_lib.rbrp_CPQR(8, 8, None, None, 0, None, None, None, None) == 1

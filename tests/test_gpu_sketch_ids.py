@@ -187,3 +187,57 @@ def test_rand_lupp_os_matches_numpy_on_same_sketch(handle):
     s = np.linalg.svd(A, compute_uv=False)
     opt = np.sqrt((s[k:] ** 2).sum() / (s ** 2).sum())
     assert err < 30 * opt, (err, opt)
+
+
+class _DeviceArray:
+    """A raw device pointer seen by torch (``__cuda_array_interface__``)."""
+
+    def __init__(self, ptr, shape, typestr):
+        self.__cuda_array_interface__ = {"shape": shape, "typestr": typestr, "data": (ptr, False), "version": 3}
+
+
+def test_c_abi_comparison_ids_equal_the_python_ones(handle, rbrp_lib):
+    """rbrp_RandLUPP_OS / rbrp_RandCPQR_OS / rbrp_CPQR (the gpu/rid.hpp and gpu/id_cpqr.hpp
+    signatures) return what the Python comparison IDs return on the same sketch seed."""
+    import ctypes
+    from robust_blockwise_random_pivoting_gb300.sketch_ids import rand_cpqr_os, rand_lupp_os
+    m, n, k, seed = 300, 250, 30, 5
+    A = decaying(m, n, seed=12, rate=20.0)
+    At = torch.from_numpy(A).cuda().t().contiguous().t()
+    lib = rbrp_lib
+    dA = ctypes.c_void_p(At.data_ptr())
+    sk, rd, T, fl = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_double()
+    assert lib.rbrp_RandLUPP_OS(dA, m, n, k, ctypes.byref(sk), ctypes.byref(rd), ctypes.byref(T), ctypes.byref(fl),
+                                seed) == 0
+    try:
+        sk_t = torch.as_tensor(_DeviceArray(sk.value, (k,), "<i4"), device="cuda").clone()
+        rd_t = torch.as_tensor(_DeviceArray(rd.value, (n - k,), "<i4"), device="cuda").clone()
+        T_t = torch.as_tensor(_DeviceArray(T.value, (n - k, k), "<f8"), device="cuda").t().clone()
+    finally:
+        for p in (sk, rd, T):
+            lib.rbrp_free(p)
+    S_py, rd_py, T_py = rand_lupp_os(At, k, seed=seed, handle=handle)
+    assert torch.equal(sk_t, S_py) and torch.equal(rd_t, rd_py)
+    assert torch.equal(T_t, T_py)
+    assert fl.value > 0
+
+    h_sk = (ctypes.c_int * k)()
+    h_rd = (ctypes.c_int * (n - k))()
+    T = ctypes.c_void_p()
+    assert lib.rbrp_RandCPQR_OS(dA, m, n, k, h_sk, h_rd, ctypes.byref(T), ctypes.byref(fl), seed) == 0
+    try:
+        T_c = torch.as_tensor(_DeviceArray(T.value, (n - k, k), "<f8"), device="cuda").t().clone()
+    finally:
+        lib.rbrp_free(T)
+    S_py, rd_py, T_py = rand_cpqr_os(At, k, seed=seed, handle=handle)
+    assert list(h_sk) == S_py.cpu().tolist() and list(h_rd) == rd_py.cpu().tolist()
+    assert torch.equal(T_c, T_py)
+
+    ranks = (ctypes.c_int * 3)(5, 20, 40)
+    err, tr = (ctypes.c_double * 3)(), (ctypes.c_double * 3)()
+    tc, fl2 = ctypes.c_double(), ctypes.c_double()
+    assert lib.rbrp_CPQR(m, n, dA, ranks, 3, err, tr, ctypes.byref(tc), ctypes.byref(fl2)) == 0
+    r = handle.column_id(At, b=1, tol=None, kmax=40, sampler="greedy", compute_T=False)
+    for q, kq in enumerate((5, 20, 40)):
+        np.testing.assert_allclose(err[q], r.residuals[kq - 1], rtol=1e-12)
+    assert err[0] > err[1] > err[2] > 0 and tr[0] <= tr[1] <= tr[2] <= tc.value
