@@ -239,18 +239,26 @@ def run_reference(args, wl, name):
 class Ctx:
     """Process / device context shared by the bench legs."""
 
-    def __init__(self, args):
+    def __init__(self, args, device_type="cuda"):
+        """One rank: its GPU, NCCL for the timing all-reduce.  ``device_type="cpu"``
+        gives the same rank logic over gloo on host tensors (the multi-process tests)."""
         import torch
         import torch.distributed as dist
         self.torch, self.dist = torch, dist
         self.world = int(os.environ.get("WORLD_SIZE", "1"))
         self.rank = int(os.environ.get("RANK", "0"))
         self.local = int(os.environ.get("LOCAL_RANK", "0"))
-        torch.cuda.set_device(self.local)
-        self.device = torch.device("cuda", self.local)
-        if self.world > 1:
-            dist.init_process_group("nccl", device_id=self.device)
-        self.stream = torch.cuda.current_stream(self.device)
+        if device_type == "cpu":
+            self.device = torch.device("cpu")
+            if self.world > 1:
+                dist.init_process_group("gloo", rank=self.rank, world_size=self.world)
+            self.stream = None
+        else:
+            torch.cuda.set_device(self.local)
+            self.device = torch.device("cuda", self.local)
+            if self.world > 1:
+                dist.init_process_group("nccl", device_id=self.device)
+            self.stream = torch.cuda.current_stream(self.device)
         self.uuid = None
         try:
             self.uuid = "GPU-" + str(torch.cuda.get_device_properties(self.local).uuid)
@@ -271,6 +279,12 @@ class Ctx:
         if self.world > 1:
             self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
         return float(t.item())
+
+    def job_rate(self, units_per_rank, ms):
+        """Whole-job rate: the units of every rank over the slowest rank's time.
+        Returns (units/s, max ms)."""
+        ms_max = self.max_over_ranks(ms)
+        return self.world * units_per_rank / (ms_max * 1e-3), ms_max
 
     def close(self):
         if self.world > 1:
@@ -321,8 +335,7 @@ def run_single(args, wl, name, ctx, light=False):
     stats = h.phase_stats()
     h.set_profiling(False)
     clocks = clk.summary()
-    ms_max = ctx.max_over_ranks(ms)
-    value = ctx.world * steps / (ms_max * 1e-3)
+    value, ms_max = ctx.job_rate(steps, ms)
 
     k = r.k
     rel_err = h.id_error(A)             # squared, on the matrix the ID was computed for
@@ -478,8 +491,7 @@ def run_batched(args, wl, name, ctx):
     ms = ev0.elapsed_time(ev1)
     clocks = clk.summary()
     res = bt.results()
-    ms_max = ctx.max_over_ranks(ms)
-    value = ctx.world * args.steps * nb / (ms_max * 1e-3)
+    value, ms_max = ctx.job_rate(args.steps * nb, ms)
     ms_launch = ms / args.steps
 
     # quality: relative Frobenius error of every ID against the block in FP64 (device GEMMs)
