@@ -608,14 +608,48 @@ def run_batched(args, wl, name, ctx):
         pipelined = {"value": ctx.world * args.steps * nb / dt, "unit": "matrices/s",
                      "api": f"rbrp.HostBatch, {len(hb.groups)} groups: copies on one stream overlapped with "
                             f"the groups' launches on another"}
-        # headline: the one-batch form (a group balances its persistent kernel over fewer
-        # problems, which costs about what the overlap saves on this workload)
-        e2e = dict(sequential)
-        e2e.update({"h2d_bytes_per_step": int(pack.numel() * 4), "d2h_bytes_per_step": int(hb.d2h_bytes + nb * 56),
-                    "api": "one pinned H2D copy of the packed blocks, rbrp.Batch.run (one graph launch), "
-                           "perm and T copied to pinned host buffers, Batch.results()",
-                    "pipelined": pipelined})
         hb.close()
+        sequential.update({"h2d_bytes_per_step": int(pack.numel() * 4), "d2h_bytes_per_step": int(hb.d2h_bytes + nb * 56),
+                           "api": "one pinned H2D copy of the packed blocks, rbrp.Batch.run (one graph launch), "
+                                  "perm and T copied to pinned host buffers, Batch.results()"})
+        # host-resident form: rbrp.Batch over views of the pinned pack; the kernel reads each
+        # block once over the host link (its norms pass stages it in the CTA's workspace) and
+        # writes perm and T to pinned host memory, so the transfers overlap the other CTAs' IDs
+        hviews = [host[int(offs[q]): int(offs[q]) + int(sizes[q])].view(n, m).t() for q, (m, n) in enumerate(shapes)]
+        hz_handle = Handle(ctx.local)
+        hz = Batch(hz_handle, hviews, b=info["b"], tol=wl["tol"], seed=seed * nb, t_rank_cap=t_cap)
+
+        def zstep():
+            hz.run()
+            return hz.results()
+        for _ in range(max(1, args.warmup)):
+            zres = zstep()
+        same = bool(np.array_equal(zres.k, res.k) and np.array_equal(zres.err_est, res.err_est))
+        ctx.barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            zres = zstep()
+        torch.cuda.synchronize()
+        dt = ctx.max_over_ranks(time.perf_counter() - t0)
+        t_bytes = int(sum(int(k) * (n - int(k)) * 8 for k, (_, n) in zip(zres.k, shapes) if 0 < int(k) < n))
+        host_resident = {
+            "value": ctx.world * args.steps * nb / dt, "unit": "matrices/s", "ms_step": 1e3 * dt / args.steps,
+            "h2d_bytes_per_step": int(pack.numel() * 4),
+            "d2h_bytes_per_step": int(hz.perm_buf.numel() * 4 + t_bytes + nb * 56),
+            "results_equal_device_batch": same,
+            "api": "rbrp.Batch over views of the pinned host pack (one graph launch; the kernel reads each "
+                   "block in place once and writes perm and T to pinned host memory), Batch.results()"}
+        del hz, hviews
+        hz_handle.close()
+        # headline: the fastest of the host-buffer forms, the others beside it
+        forms = {"host_resident": host_resident, "sequential": sequential, "pipelined": pipelined}
+        best = max(forms, key=lambda f: forms[f]["value"])
+        e2e = dict(forms[best])
+        e2e["form"] = best
+        e2e.setdefault("h2d_bytes_per_step", int(pack.numel() * 4))
+        e2e.setdefault("d2h_bytes_per_step", int(hb.d2h_bytes + nb * 56))
+        e2e["other_forms"] = {f: forms[f] for f in forms if f != best}
         del host
 
     cpu = None

@@ -228,12 +228,16 @@ rbrp_status rbrp_id_f32_host(rbrp_handle h, int m, int n, const float* hA, int64
 typedef struct {
   int m, n;            /* shape, m, n >= 1 */
   int64_t lda;         /* leading dimension of A, >= m */
-  const float* A;      /* device, column major, FP32 */
-  int* perm;           /* device, n ints (output): perm[:k] = S, perm[k:] = rd */
-  double* T;           /* device (output) T = R11^{-1} R12, k x (n-k), column major, ld = k;
-                          NULL: not computed */
+  const float* A;      /* device or pinned host memory, column major, FP32 */
+  int* perm;           /* device or pinned host, n ints (output): perm[:k] = S, perm[k:] = rd */
+  double* T;           /* device or pinned host (output) T = R11^{-1} R12, k x (n-k), column
+                          major, ld = k; NULL: not computed */
   int64_t T_cap;       /* doubles available at T (k * (n-k) are written) */
 } rbrp_batch_problem;
+/* Pinned (page-locked) host buffers are used in place: a host A is read once by
+ * the kernel's first pass over its problem and staged in the CTA's workspace,
+ * perm and T are written to host memory by the kernel, so host-device traffic
+ * overlaps the IDs of other problems.  Pageable host memory is rejected. */
 
 typedef struct {
   int k;               /* rank found */
@@ -274,6 +278,10 @@ rbrp_status rbrp_batch_run(rbrp_handle h);
  * cap >= nprob entries, in the caller's problem order). */
 rbrp_status rbrp_batch_results(rbrp_handle h, rbrp_batch_result* out, int cap);
 rbrp_status rbrp_batch_get_info(rbrp_handle h, rbrp_batch_info* info);
+/* Replaces the planned queue order (problem indices in the order the persistent
+ * CTAs take them; the plan's default is largest m*n first).  order must list
+ * every problem once.  Results do not depend on the order. */
+rbrp_status rbrp_batch_set_order(rbrp_handle h, const int* order, int n);
 /* In-kernel phase profile of the batched kernel: when on, thread 0 of every CTA
  * adds the SM cycles of each phase (clock64 between the barriers that end the
  * phases) into device counters, accumulated over runs until switched on again.

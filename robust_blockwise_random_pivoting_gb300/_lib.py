@@ -119,6 +119,7 @@ _SIGS = {
     "rbrp_batch_run": (c_int, [c_void_p]),
     "rbrp_batch_results": (c_int, [c_void_p, ctypes.POINTER(BatchResult), c_int]),
     "rbrp_batch_get_info": (c_int, [c_void_p, ctypes.POINTER(BatchInfo)]),
+    "rbrp_batch_set_order": (c_int, [c_void_p, ctypes.POINTER(c_int), c_int]),
     "rbrp_batch_set_profiling": (c_int, [c_void_p, c_int]),
     "rbrp_batch_get_phase_cycles": (c_int, [c_void_p, ctypes.POINTER(c_double), c_int]),
     "rbrp_id_batched_f32": (c_int, [c_void_p, c_int, ctypes.POINTER(BatchProblem), ctypes.POINTER(Params),

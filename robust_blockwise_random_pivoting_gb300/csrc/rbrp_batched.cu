@@ -40,11 +40,18 @@ struct BatchArgs {
   unsigned char* slots;
   int64_t slot_bytes;
   int64_t off_R, off_V, off_Qc, off_Qr, off_diag, off_pbuf;
+  // host-resident problems (pinned host memory): with STAGE_A the norms pass copies
+  // A into the slot at off_stage, with STAGE_PERM perm is worked on in the slot at
+  // off_perm and copied out at the end
+  int64_t off_stage, off_perm;
+  int stage;  // STAGE_A | STAGE_PERM bits
   double tol, tol_loc;
   uint64_t seed;
   int b, sampler, kmax, compute_T;
   unsigned long long* prof;  // per-phase SM cycles summed over CTAs (NULL: off)
 };
+
+enum { STAGE_A = 1, STAGE_PERM = 2 };
 
 namespace {
 
@@ -151,14 +158,24 @@ __device__ __forceinline__ int block_max_int(int v, int* sh) {
 // (zeros pad the scalar groups): 16-byte loads (four in flight per lane) when the
 // column is 16-byte aligned.  Both norm passes use it, so a lane sees the same
 // entries in the same groups and order in each.
-template <typename F>
-__device__ __forceinline__ void column_walk(const float* __restrict__ col, int m, int lane, bool vec, F&& f) {
+// With STORE the walk also writes every entry it reads to dst (16-byte aligned):
+// the staging copy of a host-resident column, made by the same pass.
+template <bool STORE, typename F>
+__device__ __forceinline__ void column_walk(const float* __restrict__ col, float* __restrict__ dst, int m, int lane,
+                                            bool vec, F&& f) {
   if (vec) {
     const float4* c4 = reinterpret_cast<const float4*>(col);
+    float4* d4 = reinterpret_cast<float4*>(dst);
     const int m4 = m >> 2;
     int r = lane;
     for (; r + 96 < m4; r += 128) {
       const float4 a = c4[r], b = c4[r + 32], c = c4[r + 64], d = c4[r + 96];
+      if (STORE) {
+        d4[r] = a;
+        d4[r + 32] = b;
+        d4[r + 64] = c;
+        d4[r + 96] = d;
+      }
       f(a.x, a.y, a.z, a.w);
       f(b.x, b.y, b.z, b.w);
       f(c.x, c.y, c.z, c.w);
@@ -166,11 +183,20 @@ __device__ __forceinline__ void column_walk(const float* __restrict__ col, int m
     }
     for (; r < m4; r += 32) {
       const float4 a = c4[r];
+      if (STORE) d4[r] = a;
       f(a.x, a.y, a.z, a.w);
     }
-    for (int t = 4 * m4 + lane; t < m; t += 32) f(col[t], 0.f, 0.f, 0.f);
+    for (int t = 4 * m4 + lane; t < m; t += 32) {
+      const float x = col[t];
+      if (STORE) dst[t] = x;
+      f(x, 0.f, 0.f, 0.f);
+    }
   } else {
-    for (int r = lane; r < m; r += 32) f(col[r], 0.f, 0.f, 0.f);
+    for (int r = lane; r < m; r += 32) {
+      const float x = col[r];
+      if (STORE) dst[r] = x;
+      f(x, 0.f, 0.f, 0.f);
+    }
   }
 }
 
@@ -189,10 +215,12 @@ __device__ __forceinline__ void df_add_sq4(DF& acc, float x0, float x1, float x2
 // entries keep their resolution) and perm = identity.
 // Returns the problem's exponent emax (max |A| = f 2^emax, f in [0.5, 1)) and
 // rescales diags to the problem scale 2^-emax; *bad flags non-finite entries.
-template <int BB>
+// With STAGE the same pass copies A to stage (ld x n, 16-byte aligned): a
+// host-resident A crosses the host link once.
+template <int BB, bool STAGE>
 __device__ int batch_norms(BatchSmem<BB>& sm, const float* __restrict__ A, int64_t lda, int m, int n,
-                           int* __restrict__ perm, double* __restrict__ diags, int* __restrict__ colexp, int* bad,
-                           double* res0, int* nnz) {
+                           float* __restrict__ stage, int64_t ld, int* __restrict__ perm, double* __restrict__ diags,
+                           int* __restrict__ colexp, int* bad, double* res0, int* nnz) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const bool vec = (lda & 3) == 0 && (reinterpret_cast<uintptr_t>(A) & 15) == 0;
   int emax = INT_MIN, nonfinite = 0;
@@ -201,12 +229,19 @@ __device__ int batch_norms(BatchSmem<BB>& sm, const float* __restrict__ A, int64
     unsigned mx = 0u;
     int nf = 0;
     DF raw{0.f, 0.f};
-    column_walk(col, m, lane, vec, [&](float x0, float x1, float x2, float x3) {
+    auto visit = [&](float x0, float x1, float x2, float x3) {
       const float v0 = fabsf(x0), v1 = fabsf(x1), v2 = fabsf(x2), v3 = fabsf(x3);
       nf |= !(v0 <= FLT_MAX) | !(v1 <= FLT_MAX) | !(v2 <= FLT_MAX) | !(v3 <= FLT_MAX);
       mx = max(max(mx, max(__float_as_uint(v0), __float_as_uint(v1))), max(__float_as_uint(v2), __float_as_uint(v3)));
       df_add_sq4(raw, x0, x1, x2, x3);
-    });
+    };
+    if constexpr (STAGE) {
+      float* dst = stage + (int64_t)c * ld;
+      column_walk<true>(col, dst, m, lane, vec, visit);
+      col = dst;  // the rescaled walk below reads the device copy (same entries, same groups)
+    } else {
+      column_walk<false>(col, nullptr, m, lane, vec, visit);
+    }
     mx = __reduce_max_sync(0xffffffffu, mx);
     nf = __any_sync(0xffffffffu, nf);
     double d = 0.0;
@@ -220,7 +255,7 @@ __device__ int batch_norms(BatchSmem<BB>& sm, const float* __restrict__ A, int64
       } else {
         const Pow2 sc = pow2_scale(-e);
         DF acc{0.f, 0.f};
-        column_walk(col, m, lane, vec, [&](float x0, float x1, float x2, float x3) {
+        column_walk<false>(col, nullptr, m, lane, vec, [&](float x0, float x1, float x2, float x3) {
           df_add_sq4(acc, sc.apply(x0), sc.apply(x1), sc.apply(x2), sc.apply(x3));
         });
         d = warp_sum_df(acc.hi, acc.lo);
@@ -927,15 +962,18 @@ __device__ void batch_tsolve(float2* __restrict__ R, int n, int k, dfl* __restri
   }
 }
 
-template <int BB>
+template <int BB, bool HOST>
 __device__ void solve_problem(BatchSmem<BB>& sm, const rbrp_batch_problem& pr, int pid, unsigned char* slot,
                               const BatchArgs& args, rbrp_batch_result* res) {
   const int tid = threadIdx.x;
   const int m = pr.m, n = pr.n;
-  const int64_t lda = pr.lda;
+  int64_t lda = pr.lda;
   const float* A = pr.A;
-  int* perm = pr.perm;
   const int64_t ld = ((int64_t)m + 3) & ~(int64_t)3;
+  // host-resident batch: perm lives in the slot while the problem runs, A is read
+  // from the host once (norms pass) and from the slot's staged copy afterwards
+  float* stage = HOST ? reinterpret_cast<float*>(slot + args.off_stage) : nullptr;
+  int* perm = HOST ? reinterpret_cast<int*>(slot + args.off_perm) : pr.perm;
   float* Ares = reinterpret_cast<float*>(slot);
   float2* R = reinterpret_cast<float2*>(slot + args.off_R);
   float* V = reinterpret_cast<float*>(slot + args.off_V);
@@ -950,7 +988,12 @@ __device__ void solve_problem(BatchSmem<BB>& sm, const rbrp_batch_problem& pr, i
   clk.start(args.prof ? sm.pacc : nullptr);
   int bad = 0, nnz = 0;
   double res0 = 0.0;
-  const int emax = batch_norms<BB>(sm, A, lda, m, n, perm, diags, reinterpret_cast<int*>(pbuf), &bad, &res0, &nnz);
+  const int emax = batch_norms<BB, HOST>(sm, A, lda, m, n, stage, ld, perm, diags, reinterpret_cast<int*>(pbuf),
+                                         &bad, &res0, &nnz);
+  if (HOST) {
+    A = stage;
+    lda = ld;
+  }
   const Pow2 sc = pow2_scale(emax == INT_MIN ? 0 : -emax);
   State& st = sm.st;
   if (tid == 0) {
@@ -1047,6 +1090,8 @@ __device__ void solve_problem(BatchSmem<BB>& sm, const rbrp_batch_problem& pr, i
     clk.mark(BPH_FINISH);
   }
   const int k = st.i;
+  if (HOST)
+    for (int p = tid; p < n; p += BT) pr.perm[p] = perm[p];
   int status = st.status == 0 ? RBRP_OK : RBRP_ERR_NUMERIC;
   if (args.compute_T && pr.T && status == RBRP_OK && k > 0 && k < n) {
     if ((int64_t)k * (n - k) > pr.T_cap)
@@ -1069,7 +1114,7 @@ __device__ void solve_problem(BatchSmem<BB>& sm, const rbrp_batch_problem& pr, i
   clk.mark(BPH_TSOLVE);
 }
 
-template <int BB>
+template <int BB, bool HOST>
 __global__ void __launch_bounds__(BT, 2)
 k_rbrp_batched(const rbrp_batch_problem* __restrict__ probs, const int* __restrict__ order, int nprob,
                int* __restrict__ queue, BatchArgs args, rbrp_batch_result* __restrict__ results) {
@@ -1085,7 +1130,7 @@ k_rbrp_batched(const rbrp_batch_problem* __restrict__ probs, const int* __restri
     const int q = s_q;
     if (q >= nprob) break;
     const int pid = order[q];
-    solve_problem<BB>(sm, probs[pid], pid, slot, args, results + pid);
+    solve_problem<BB, HOST>(sm, probs[pid], pid, slot, args, results + pid);
   }
   if (args.prof && threadIdx.x < BPH_N) atomicAdd(args.prof + threadIdx.x, sm.pacc[threadIdx.x]);
 }
@@ -1123,11 +1168,11 @@ namespace {
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct SlotLayout {
-  int64_t off_R, off_V, off_Qc, off_Qr, off_diag, off_pbuf, bytes;
+  int64_t off_R, off_V, off_Qc, off_Qr, off_diag, off_pbuf, off_stage, off_perm, bytes;
 };
 
-SlotLayout slot_layout(const std::vector<rbrp_batch_problem>& P, int kmax, int BB) {
-  size_t a_res = 0, r = 0, v = 0, qr = 0, dg = 0;
+SlotLayout slot_layout(const std::vector<rbrp_batch_problem>& P, int kmax, int BB, int stage) {
+  size_t a_res = 0, r = 0, v = 0, qr = 0, dg = 0, pm = 0;
   for (const auto& q : P) {
     const size_t ld = ((size_t)q.m + 3) & ~(size_t)3;
     const int mn = std::min(q.m, q.n);
@@ -1137,6 +1182,7 @@ SlotLayout slot_layout(const std::vector<rbrp_batch_problem>& P, int kmax, int B
     v = std::max(v, ld * BB * sizeof(float));
     qr = std::max(qr, (size_t)q.m * BB * sizeof(float));
     dg = std::max(dg, (size_t)q.n * sizeof(double));
+    pm = std::max(pm, (size_t)q.n * sizeof(int));
   }
   SlotLayout L;
   size_t off = align256(a_res);
@@ -1152,6 +1198,15 @@ SlotLayout slot_layout(const std::vector<rbrp_batch_problem>& P, int kmax, int B
   off += align256(dg);
   L.off_pbuf = off;
   off += align256(2 * dg);
+  L.off_stage = L.off_perm = 0;
+  if (stage & STAGE_A) {
+    L.off_stage = off;
+    off += align256(a_res);
+  }
+  if (stage & STAGE_PERM) {
+    L.off_perm = off;
+    off += align256(pm);
+  }
   L.bytes = off;
   return L;
 }
@@ -1163,28 +1218,39 @@ size_t batch_smem_bytes() {
 
 template <int BB>
 cudaError_t set_batch_attr() {
-  return cudaFuncSetAttribute(k_rbrp_batched<BB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaError_t e = cudaFuncSetAttribute(k_rbrp_batched<BB, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)sizeof(BatchSmem<BB>));
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_rbrp_batched<BB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)sizeof(BatchSmem<BB>));
 }
 
 int occupancy(int BB) {
-  int nb = 0;
-  if (BB == 16)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_rbrp_batched<16>, BT, sizeof(BatchSmem<16>));
-  else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_rbrp_batched<32>, BT, sizeof(BatchSmem<32>));
-  return nb;
+  int nb = 0, nh = 0;
+  if (BB == 16) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_rbrp_batched<16, false>, BT, sizeof(BatchSmem<16>));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nh, k_rbrp_batched<16, true>, BT, sizeof(BatchSmem<16>));
+  } else {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_rbrp_batched<32, false>, BT, sizeof(BatchSmem<32>));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nh, k_rbrp_batched<32, true>, BT, sizeof(BatchSmem<32>));
+  }
+  return std::min(nb, nh);
+}
+
+template <int BB, bool HOST>
+void launch_variant(BatchState& B, cudaStream_t s) {
+  k_rbrp_batched<BB, HOST><<<B.grid, BT, sizeof(BatchSmem<BB>), s>>>(B.d_probs, B.d_order, B.nprob, B.d_queue,
+                                                                      B.args, B.d_res);
 }
 
 cudaError_t launch(BatchState& B, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(B.d_queue, 0, sizeof(int), s);
   if (e != cudaSuccess) return e;
+  const bool host = B.args.stage != 0;
   if (B.BB == 16)
-    k_rbrp_batched<16><<<B.grid, BT, sizeof(BatchSmem<16>), s>>>(B.d_probs, B.d_order, B.nprob, B.d_queue, B.args,
-                                                                 B.d_res);
+    host ? launch_variant<16, true>(B, s) : launch_variant<16, false>(B, s);
   else
-    k_rbrp_batched<32><<<B.grid, BT, sizeof(BatchSmem<32>), s>>>(B.d_probs, B.d_order, B.nprob, B.d_queue, B.args,
-                                                                 B.d_res);
+    host ? launch_variant<32, true>(B, s) : launch_variant<32, false>(B, s);
   return cudaGetLastError();
 }
 
@@ -1228,6 +1294,22 @@ void batch_release(rbrp_handle h) {
 using namespace rbrp;
 
 namespace {
+
+// Where a problem buffer lives: 0 device (or managed) memory, 1 pinned host memory
+// (*dev = the address kernels use for it), -1 memory CUDA does not know (pageable).
+int residency(const void* p, const void** dev) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return -1;
+  }
+  if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return 0;
+  if (a.type == cudaMemoryTypeHost && a.devicePointer) {
+    *dev = a.devicePointer;
+    return 1;
+  }
+  return -1;
+}
 
 rbrp_status batch_validate(rbrp_handle h, int nprob, const rbrp_batch_problem* problems, const rbrp_params* p) {
   if (!h) return RBRP_ERR_INVALID_ARG;
@@ -1314,8 +1396,35 @@ rbrp_status rbrp_batch_plan(rbrp_handle h, int nprob, const rbrp_batch_problem* 
   B.planned = false;
   B.ran = false;
   B.ms_autotune = 0.0;
-  B.nprob = nprob;
+  B.nprob = 0;
   B.probs.assign(problems, problems + nprob);
+  // pinned host buffers are read and written in place through their device
+  // addresses; a host A is staged into the workspace by the norms pass and a host
+  // perm is kept in the workspace while its problem runs
+  int stage = 0;
+  for (int q = 0; q < nprob; ++q) {
+    rbrp_batch_problem& r = B.probs[q];
+    const std::string at = " (problem " + std::to_string(q) + ")";
+    const void* dev = r.A;
+    int where = residency(r.A, &dev);
+    if (where < 0) return set_error(h, RBRP_ERR_INVALID_ARG, "A is neither device nor pinned host memory" + at);
+    if (where == 1) stage |= STAGE_A;
+    r.A = static_cast<const float*>(dev);
+    dev = r.perm;
+    where = residency(r.perm, &dev);
+    if (where < 0) return set_error(h, RBRP_ERR_INVALID_ARG, "perm is neither device nor pinned host memory" + at);
+    if (where == 1) stage |= STAGE_PERM;
+    r.perm = static_cast<int*>(const_cast<void*>(dev));
+    if (r.T) {
+      dev = r.T;
+      if (residency(r.T, &dev) < 0)
+        return set_error(h, RBRP_ERR_INVALID_ARG, "T is neither device nor pinned host memory" + at);
+      r.T = static_cast<double*>(const_cast<void*>(dev));
+    }
+  }
+  if (stage) stage = STAGE_A | STAGE_PERM;  // the host variant of the kernel stages both
+  B.nprob = nprob;
+  B.args.stage = stage;
 
   // largest problems first: the queue hands them out before the small ones
   std::vector<int> order(nprob);
@@ -1330,13 +1439,15 @@ rbrp_status rbrp_batch_plan(rbrp_handle h, int nprob, const rbrp_batch_problem* 
   B.args.kmax = p->kmax;
   B.args.compute_T = p->compute_T;
   B.args.prof = B.profiling ? B.d_prof : nullptr;
-  const SlotLayout L = slot_layout(B.probs, p->kmax, BATCH_MAXB);
+  const SlotLayout L = slot_layout(B.probs, p->kmax, BATCH_MAXB, stage);
   B.args.off_R = L.off_R;
   B.args.off_V = L.off_V;
   B.args.off_Qc = L.off_Qc;
   B.args.off_Qr = L.off_Qr;
   B.args.off_diag = L.off_diag;
   B.args.off_pbuf = L.off_pbuf;
+  B.args.off_stage = L.off_stage;
+  B.args.off_perm = L.off_perm;
   B.args.slot_bytes = L.bytes;
 
   // grid bounded by the memory the slots may take (80% of what is free)
@@ -1367,7 +1478,7 @@ rbrp_status rbrp_batch_plan(rbrp_handle h, int nprob, const rbrp_batch_problem* 
     int64_t tol_bits = 0, tol_loc_bits = 0;
     std::memcpy(&tol_bits, &p->tol, sizeof(double));
     std::memcpy(&tol_loc_bits, &p->tol_loc, sizeof(double));
-    std::vector<int64_t> sig = {nprob, p->kmax, p->sampler, tol_bits, tol_loc_bits, p->compute_T};
+    std::vector<int64_t> sig = {nprob, p->kmax, p->sampler, tol_bits, tol_loc_bits, p->compute_T, stage};
     int64_t sm = 0, sn = 0, smn = 0;
     for (const auto& q : B.probs) {
       sm += q.m;
@@ -1460,6 +1571,25 @@ rbrp_status rbrp_batch_results(rbrp_handle h, rbrp_batch_result* out, int cap) {
     s = cuda_check(h, cudaMemcpy(out, B.d_res, sizeof(rbrp_batch_result) * B.nprob, cudaMemcpyDeviceToHost),
                    "copy batch results");
   }
+  return s;
+}
+
+rbrp_status rbrp_batch_set_order(rbrp_handle h, const int* order, int n) {
+  if (!h) return RBRP_ERR_INVALID_ARG;
+  if (!h->batch || !h->batch->planned) return set_error(h, RBRP_ERR_NOT_COMPUTED, "no batch planned");
+  BatchState& B = *h->batch;
+  if (!order || n != B.nprob) return set_error(h, RBRP_ERR_INVALID_ARG, "order must list every problem once");
+  std::vector<char> seen(n, 0);
+  for (int q = 0; q < n; ++q) {
+    if (order[q] < 0 || order[q] >= n || seen[order[q]])
+      return set_error(h, RBRP_ERR_INVALID_ARG, "order must list every problem once");
+    seen[order[q]] = 1;
+  }
+  DeviceGuard g(h->device);
+  // the graph reads the order from device memory at run time: no new capture needed
+  rbrp_status s = cuda_check(h, cudaMemcpyAsync(B.d_order, order, sizeof(int) * n, cudaMemcpyHostToDevice, h->stream),
+                             "copy batch order");
+  if (s == RBRP_OK) s = cuda_check(h, cudaStreamSynchronize(h->stream), "copy batch order");
   return s;
 }
 

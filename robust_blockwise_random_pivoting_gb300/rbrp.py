@@ -261,36 +261,55 @@ class BatchIDResult:
 class Batch:
     """A planned batch of independent column IDs run in one persistent launch.
 
-    ``As`` is a sequence of FP32 CUDA matrices of any shapes.  ``b <= 0`` lets
-    the library's autotuner pick the block size on this batch.  ``tol`` bounds
-    the squared relative residual of every problem; problem q uses the Philox
-    key ``seed + q``.  T of problem q gets room for ``min(kcap_q, t_rank_cap)``
-    rows (kcap_q = min(m_q, n_q, kmax)); a larger rank reports status 6.
+    ``As`` is a sequence of FP32 matrices of any shapes, either all CUDA
+    tensors on one device or all column-major views of pinned host memory
+    (``pin_memory``).  Host-resident matrices are read in place by the kernel,
+    each once over the host link, while other problems compute; their perm
+    and T buffers are then pinned host memory too, so a run moves no data
+    through separate copies.  ``b <= 0`` lets the library's autotuner pick the
+    block size on this batch.  ``tol`` bounds the squared relative residual of
+    every problem; problem q uses the Philox key ``seed + q``.  T of problem q
+    gets room for ``min(kcap_q, t_rank_cap)`` rows (kcap_q = min(m_q, n_q,
+    kmax)); a larger rank reports status 6.
     """
 
     def __init__(self, handle, As, b=0, tol=1e-8, kmax=None, seed=0, sampler="np", tol_loc=None,
                  compute_T=True, t_rank_cap=None):
         self.h = handle
         lib = handle.lib
-        self.As = [_colmajor(A) for A in As]
-        if not self.As:
+        As = list(As)
+        if not As:
             raise ValueError("empty batch")
-        dev = self.As[0].device
-        for A in self.As:
-            if not A.is_cuda or A.dtype != torch.float32 or A.device != dev:
-                raise TypeError("the batched form takes FP32 CUDA matrices on one device")
+        self.host = not As[0].is_cuda
+        if self.host:
+            for A in As:
+                if A.is_cuda or A.dtype != torch.float32 or not A.is_pinned():
+                    raise TypeError("host-resident batches take FP32 views of pinned host memory")
+                if _colmajor(A) is not A:
+                    raise ValueError("host-resident matrices must be column-major views (no copies are made)")
+            dev = torch.device("cuda", handle.device)
+            out = dict(device="cpu", pin_memory=True)
+        else:
+            As = [_colmajor(A) for A in As]
+            dev = As[0].device
+            for A in As:
+                if not A.is_cuda or A.dtype != torch.float32 or A.device != dev:
+                    raise TypeError("the batched form takes FP32 CUDA matrices on one device")
+            out = dict(device=dev)
+        self.As = As
+        self.device = dev
         shapes = [tuple(A.shape) for A in self.As]
         self.shapes = shapes
         ns = np.array([n for _, n in shapes], np.int64)
         self.perm_off = np.concatenate([[0], np.cumsum(ns)])
-        self.perm_buf = torch.empty(int(self.perm_off[-1]), dtype=torch.int32, device=dev)
+        self.perm_buf = torch.empty(int(self.perm_off[-1]), dtype=torch.int32, **out)
         kc = [min(m, n, kmax or min(m, n)) for m, n in shapes]
         if t_rank_cap is not None:
             kc = [min(k, int(t_rank_cap)) for k in kc]
         tcap = np.array([k * n for k, (_, n) in zip(kc, shapes)], np.int64) if compute_T else np.zeros(len(shapes),
                                                                                                        np.int64)
         self.t_off = np.concatenate([[0], np.cumsum(tcap)])
-        self.T_buf = torch.empty(max(1, int(self.t_off[-1])), dtype=torch.float64, device=dev)
+        self.T_buf = torch.empty(max(1, int(self.t_off[-1])), dtype=torch.float64, **out)
         n_prob = len(self.As)
         self.probs = (_lib.BatchProblem * n_prob)()
         for q, A in enumerate(self.As):
@@ -306,12 +325,26 @@ class Batch:
         handle._bind_stream(torch.cuda.current_stream(dev))
         check(lib.rbrp_batch_plan(handle.h, n_prob, self.probs, ctypes.byref(p)), handle.h)
         self.n_prob = n_prob
+        # a handle holds one plan: a later Batch on the same handle replaces this one
+        self._token = object()
+        handle._batch_token = self._token
+
+    def _check_plan(self):
+        if getattr(self.h, "_batch_token", None) is not self._token:
+            raise RuntimeError("another Batch was planned on this handle since: use one handle per live Batch")
 
     def info(self):
         inf = _lib.BatchInfo()
         check(self.h.lib.rbrp_batch_get_info(self.h.h, ctypes.byref(inf)), self.h.h)
         return dict(b=inf.b, panel_cols=inf.panel_cols, ctas=inf.ctas, ctas_per_sm=inf.ctas_per_sm,
                     ms_last=inf.ms_last, ms_autotune=inf.ms_autotune, workspace_bytes=inf.workspace_bytes)
+
+    def set_order(self, order):
+        """Queue order of the persistent CTAs (problem indices, each once); results do not
+        depend on it.  The plan's default is largest m*n first."""
+        self._check_plan()
+        arr = (ctypes.c_int * self.n_prob)(*[int(q) for q in order])
+        check(self.h.lib.rbrp_batch_set_order(self.h.h, arr, len(order)), self.h.h)
 
     def set_profiling(self, on=True):
         """In-kernel phase cycle counters (reset when switched on)."""
@@ -326,7 +359,8 @@ class Batch:
 
     def run(self, stream=None):
         """Enqueue the batch (one CUDA graph launch) on the current torch stream."""
-        self.h._bind_stream(torch.cuda.current_stream(self.As[0].device) if stream is None else stream)
+        self._check_plan()
+        self.h._bind_stream(torch.cuda.current_stream(self.device) if stream is None else stream)
         check(self.h.lib.rbrp_batch_run(self.h.h), self.h.h)
 
     def _perm_view(self, q):
@@ -338,7 +372,8 @@ class Batch:
         n = self.shapes[q][1]
         if 0 < kq < n:
             return self.T_buf[int(self.t_off[q]): int(self.t_off[q]) + kq * (n - kq)].view(n - kq, kq).t()
-        return torch.empty((kq, n - kq), dtype=torch.float64, device=self.T_buf.device)
+        return torch.empty((kq, n - kq), dtype=torch.float64, device=self.T_buf.device,
+                           pin_memory=self.host)
 
     def results(self):
         """Wait for the last run and return a :class:`BatchIDResult`.
@@ -346,6 +381,7 @@ class Batch:
         The per-problem fields are numpy arrays read in one pass; ``perms`` and
         ``Ts`` are sequences whose CUDA views are made when indexed.
         """
+        self._check_plan()
         out = (_lib.BatchResult * self.n_prob)()
         check(self.h.lib.rbrp_batch_results(self.h.h, out, self.n_prob), self.h.h)
         arr = np.ctypeslib.as_array(out)
@@ -496,7 +532,8 @@ class HostBatch:
 
 def batched_column_id(As, b=0, tol=1e-8, kmax=None, seed=0, sampler="np", tol_loc=None, compute_T=True,
                       t_rank_cap=None, handle=None):
-    """Column IDs of many FP32 CUDA matrices in one persistent launch (plan, run, results)."""
+    """Column IDs of many FP32 matrices (CUDA tensors, or column-major views of pinned host
+    memory) in one persistent launch (plan, run, results)."""
     h = handle or Handle(As[0].device.index)
     bt = Batch(h, As, b=b, tol=tol, kmax=kmax, seed=seed, sampler=sampler, tol_loc=tol_loc, compute_T=compute_T,
                t_rank_cap=t_rank_cap)

@@ -86,6 +86,7 @@ def test_batch_entry_points_reject_bad_arguments_without_gpu(rbrp_lib):
     info = _lib.BatchInfo()
     assert rbrp_lib.rbrp_batch_get_info(None, ctypes.byref(info)) == 1
     assert rbrp_lib.rbrp_batch_set_profiling(None, 1) == 1
+    assert rbrp_lib.rbrp_batch_set_order(None, None, 0) == 1
 
 
 def test_sketch_lu_and_fixed_skeleton_entry_points_reject_null_handle(rbrp_lib):

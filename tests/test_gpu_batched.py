@@ -230,3 +230,74 @@ def test_host_batch_pipeline_equals_one_batch(handle):
                     assert torch.equal(res.Ts[j].cpu(), rr.Ts[q].cpu())
     finally:
         hb.close()
+
+
+@pytest.mark.parametrize("aligned", [True, False])
+def test_host_resident_batch_equals_device_batch(handle, aligned):
+    """Matrices in pinned host memory, read in place by the kernel (staged by its norms
+    pass), perm and T written to pinned host memory: every output equals the device
+    batch's bit for bit.  The unaligned pack takes the kernel's scalar load path."""
+    from robust_blockwise_random_pivoting_gb300.rbrp import Batch, packed_offsets
+    shp = [tuple(int(v) for v in s) for s in shapes(29, 20, 400, seed=41)] + [(1, 1), (3, 1), (1, 7)]
+    mats = [W.kernel_block_scaled(m, n, q, 0.5, seed=9) for q, (m, n) in enumerate(shp)]
+    mats[5] = mats[5] * np.float32(2.0 ** -70)          # rescaled norm walk (tiny entries)
+    mats[6][:, 2] = 0.0                                # a zero column
+    offs, sizes = packed_offsets(shp)
+    if not aligned:
+        offs = np.concatenate([[1], 1 + np.cumsum(sizes)])   # odd float offsets
+    host = torch.zeros(int(offs[-1]) + 4, dtype=torch.float32).pin_memory()
+    views = []
+    for q, ((m, n), A) in enumerate(zip(shp, mats)):
+        v = host[int(offs[q]): int(offs[q]) + m * n].view(n, m).t()
+        v.copy_(torch.from_numpy(np.asfortranarray(A, dtype=np.float32)))
+        views.append(v)
+    hb = Batch(handle, views, b=16, tol=1e-8, seed=7, t_rank_cap=64)
+    assert hb.host and not hb.perm_buf.is_cuda and not hb.T_buf.is_cuda
+    hb.run()
+    hr = hb.results()
+    from robust_blockwise_random_pivoting_gb300.rbrp import Handle
+    h2 = Handle(0)
+    dpack = host.cuda()     # same offsets on the device: same load path (vector or scalar) per matrix
+    dviews = [dpack[int(offs[q]): int(offs[q]) + m * n].view(n, m).t() for q, (m, n) in enumerate(shp)]
+    db = Batch(h2, dviews, b=16, tol=1e-8, seed=7, t_rank_cap=64)
+    db.run()
+    dr = db.results()
+    for q in range(len(shp)):
+        assert hr.k[q] == dr.k[q] and hr.status[q] == dr.status[q] == 0, q
+        assert hr.err_est[q] == dr.err_est[q] and hr.res0[q] == dr.res0[q], q
+        assert hr.draws[q] == dr.draws[q] and hr.nblocks[q] == dr.nblocks[q], q
+        assert torch.equal(hr.perms[q], dr.perms[q].cpu()), q
+        if dr.Ts[q] is not None:
+            assert not hr.Ts[q].is_cuda
+            assert torch.equal(hr.Ts[q], dr.Ts[q].cpu()), q
+    # a second run overwrites the host outputs with the same values
+    hb.perm_buf.fill_(-1)
+    hb.run()
+    hr2 = hb.results()
+    assert all(torch.equal(hr2.perms[q], dr.perms[q].cpu()) for q in range(len(shp)))
+    # a Batch whose handle was planned again refuses to run (it would run the other plan)
+    Batch(handle, [dev32(np.ones((4, 4)))], b=8)
+    with pytest.raises(RuntimeError):
+        hb.run()
+    h2.close()
+
+
+def test_host_resident_batch_rejects_pageable_memory(handle):
+    """Host matrices must be pinned; the C ABI also rejects pageable pointers itself."""
+    import ctypes
+    from robust_blockwise_random_pivoting_gb300 import _lib
+    from robust_blockwise_random_pivoting_gb300.rbrp import Batch
+    with pytest.raises(TypeError):
+        Batch(handle, [torch.zeros(4, 4).t()])
+    A = np.zeros((8, 8), np.float32, order="F")
+    perm = np.zeros(8, np.int32)
+    probs = (_lib.BatchProblem * 1)()
+    probs[0].m, probs[0].n, probs[0].lda = 8, 8, 8
+    probs[0].A = A.ctypes.data
+    probs[0].perm = perm.ctypes.data
+    probs[0].T = None
+    probs[0].T_cap = 0
+    p = handle._params(8, 1e-8, None, 0, "np", None, False, "f32_mixed", True)
+    st = handle.lib.rbrp_batch_plan(handle.h, 1, probs, ctypes.byref(p))
+    assert st != 0
+    assert b"pinned host memory" in handle.lib.rbrp_last_error(handle.h)

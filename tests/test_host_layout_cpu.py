@@ -1,4 +1,5 @@
-"""CPU: the packed host layout of the batched form and HostBatch's argument checks."""
+"""CPU: the packed host layout of the batched form and the host-side argument checks of
+HostBatch and of Batch over host-resident matrices."""
 import numpy as np
 import pytest
 
@@ -24,3 +25,16 @@ def test_host_batch_rejects_unpinned_or_misshaped_buffers():
         HostBatch(torch.zeros(int(offs[-1]), dtype=torch.float32), shapes)          # not pinned
     with pytest.raises(TypeError):
         HostBatch(torch.zeros(int(offs[-1]), dtype=torch.float64), shapes)          # not FP32
+
+
+def test_host_resident_batch_rejects_pageable_or_non_fp32_matrices():
+    """Batch over host matrices wants FP32 views of pinned memory (checked before any library call)."""
+    import types
+    from robust_blockwise_random_pivoting_gb300.rbrp import Batch
+    fake = types.SimpleNamespace(lib=None, device=0)
+    with pytest.raises(TypeError):
+        Batch(fake, [torch.zeros(4, 4).t()])                       # pageable
+    with pytest.raises(TypeError):
+        Batch(fake, [torch.zeros(4, 4, dtype=torch.float64).t()])  # not FP32
+    with pytest.raises(ValueError):
+        Batch(fake, [])
