@@ -155,9 +155,11 @@ __device__ __forceinline__ int block_max_int(int v, int* sh) {
 }
 
 // A warp's walk over one column, f(x0, x1, x2, x3) per group of four entries
-// (zeros pad the scalar groups): 16-byte loads (four in flight per lane) when the
-// column is 16-byte aligned.  Both norm passes use it, so a lane sees the same
-// entries in the same groups and order in each.
+// (zeros pad the scalar groups): 16-byte loads when the column is 16-byte
+// aligned.  A lane visits its groups lane, lane + 32, lane + 64, ... in order;
+// the loads of each 128-group chunk are all issued before any is used (four in
+// flight per lane however short the column).  Both norm passes use it, so a lane
+// sees the same entries in the same groups and order in each.
 // With STORE the walk also writes every entry it reads to dst (16-byte aligned):
 // the staging copy of a host-resident column, made by the same pass.
 template <bool STORE, typename F>
@@ -167,24 +169,16 @@ __device__ __forceinline__ void column_walk(const float* __restrict__ col, float
     const float4* c4 = reinterpret_cast<const float4*>(col);
     float4* d4 = reinterpret_cast<float4*>(dst);
     const int m4 = m >> 2;
-    int r = lane;
-    for (; r + 96 < m4; r += 128) {
-      const float4 a = c4[r], b = c4[r + 32], c = c4[r + 64], d = c4[r + 96];
-      if (STORE) {
-        d4[r] = a;
-        d4[r + 32] = b;
-        d4[r + 64] = c;
-        d4[r + 96] = d;
+    for (int r = lane; r < m4; r += 128) {
+      // groups past the end read as zeros: f adds nothing for them (exact)
+      float4 v[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) v[j] = r + 32 * j < m4 ? c4[r + 32 * j] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        if (STORE && r + 32 * j < m4) d4[r + 32 * j] = v[j];
+        f(v[j].x, v[j].y, v[j].z, v[j].w);
       }
-      f(a.x, a.y, a.z, a.w);
-      f(b.x, b.y, b.z, b.w);
-      f(c.x, c.y, c.z, c.w);
-      f(d.x, d.y, d.z, d.w);
-    }
-    for (; r < m4; r += 32) {
-      const float4 a = c4[r];
-      if (STORE) d4[r] = a;
-      f(a.x, a.y, a.z, a.w);
     }
     for (int t = 4 * m4 + lane; t < m; t += 32) {
       const float x = col[t];
@@ -309,13 +303,24 @@ __device__ void batch_gram(BatchSmem<BB>& sm, int m, int bss, bool first, Pow2 s
   float hi[NQ], lo[NQ];
 #pragma unroll
   for (int q = 0; q < NQ; ++q) hi[q] = lo[q] = 0.f;
+  constexpr int PER = BROWS * BB / BT;  // entries a thread gathers per chunk
+  static_assert(PER * BT == BROWS * BB, "gather split");
+  __syncthreads();  // the caller's sm.src (source column of each panel column) is published
   for (int r0 = 0; r0 < m; r0 += BROWS) {
+    // every load of the chunk is issued before the stores (the stores to V could
+    // alias the sources as far as the compiler knows, which would serialise them)
+    float x[PER];
+#pragma unroll
+    for (int u = 0; u < PER; ++u) {
+      const int idx = tid + u * BT, rr = idx % BROWS, c = idx / BROWS, r = r0 + rr;
+      x[u] = (r < m && c < bss) ? sm.src[c][r] : 0.f;
+    }
     __syncthreads();
-    for (int idx = tid; idx < BROWS * BB; idx += BT) {
-      const int rr = idx % BROWS, c = idx / BROWS, r = r0 + rr;
-      float v = 0.f;
+#pragma unroll
+    for (int u = 0; u < PER; ++u) {
+      const int idx = tid + u * BT, rr = idx % BROWS, c = idx / BROWS, r = r0 + rr;
+      float v = x[u];
       if (r < m && c < bss) {
-        v = sm.src[c][r];
         if (first) v = sc.apply(v);
         V[r + (int64_t)c * ld] = v;
       }
