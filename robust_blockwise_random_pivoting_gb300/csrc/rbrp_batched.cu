@@ -194,6 +194,57 @@ __device__ __forceinline__ void column_walk(const float* __restrict__ col, float
   }
 }
 
+// Two columns of one matrix walked in lockstep (col1 only when two): each
+// column's entries reach its own visitor in exactly the order column_walk gives,
+// with twice the loads in flight.
+template <bool STORE, typename F0, typename F1>
+__device__ __forceinline__ void column_walk2(const float* __restrict__ col0, float* __restrict__ dst0,
+                                             const float* __restrict__ col1, float* __restrict__ dst1, bool two,
+                                             int m, int lane, bool vec, F0&& f0, F1&& f1) {
+  if (vec) {
+    const float4* a4 = reinterpret_cast<const float4*>(col0);
+    const float4* b4 = reinterpret_cast<const float4*>(col1);
+    const int m4 = m >> 2;
+    for (int r = lane; r < m4; r += 128) {
+      float4 u[4], v[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const bool in = r + 32 * j < m4;
+        u[j] = in ? a4[r + 32 * j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        v[j] = in && two ? b4[r + 32 * j] : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        if (STORE && r + 32 * j < m4) {
+          reinterpret_cast<float4*>(dst0)[r + 32 * j] = u[j];
+          if (two) reinterpret_cast<float4*>(dst1)[r + 32 * j] = v[j];
+        }
+        f0(u[j].x, u[j].y, u[j].z, u[j].w);
+        f1(v[j].x, v[j].y, v[j].z, v[j].w);
+      }
+    }
+    for (int t = 4 * m4 + lane; t < m; t += 32) {
+      const float x = col0[t], y = two ? col1[t] : 0.f;
+      if (STORE) {
+        dst0[t] = x;
+        if (two) dst1[t] = y;
+      }
+      f0(x, 0.f, 0.f, 0.f);
+      f1(y, 0.f, 0.f, 0.f);
+    }
+  } else {
+    for (int r = lane; r < m; r += 32) {
+      const float x = col0[r], y = two ? col1[r] : 0.f;
+      if (STORE) {
+        dst0[r] = x;
+        if (two) dst1[r] = y;
+      }
+      f0(x, 0.f, 0.f, 0.f);
+      f1(y, 0.f, 0.f, 0.f);
+    }
+  }
+}
+
 // acc += x0^2 + x1^2 + x2^2 + x3^2: an FP32 sum of the four squares (positive
 // terms, relative error < 3e-7) folded into the double-float sum by TwoSum
 __device__ __forceinline__ void df_add_sq4(DF& acc, float x0, float x1, float x2, float x3) {
@@ -218,51 +269,65 @@ __device__ int batch_norms(BatchSmem<BB>& sm, const float* __restrict__ A, int64
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const bool vec = (lda & 3) == 0 && (reinterpret_cast<uintptr_t>(A) & 15) == 0;
   int emax = INT_MIN, nonfinite = 0;
-  for (int c = warp; c < n; c += BT / 32) {
-    const float* col = A + (int64_t)c * lda;
-    unsigned mx = 0u;
-    int nf = 0;
-    DF raw{0.f, 0.f};
-    auto visit = [&](float x0, float x1, float x2, float x3) {
-      const float v0 = fabsf(x0), v1 = fabsf(x1), v2 = fabsf(x2), v3 = fabsf(x3);
-      nf |= !(v0 <= FLT_MAX) | !(v1 <= FLT_MAX) | !(v2 <= FLT_MAX) | !(v3 <= FLT_MAX);
-      mx = max(max(mx, max(__float_as_uint(v0), __float_as_uint(v1))), max(__float_as_uint(v2), __float_as_uint(v3)));
-      df_add_sq4(raw, x0, x1, x2, x3);
+  // warp w takes columns w, w + 8, w + 16, ... two at a time
+  constexpr int NW = BT / 32;
+  for (int c0 = warp; c0 < n; c0 += 2 * NW) {
+    const int c1 = c0 + NW;
+    const bool two = c1 < n;
+    const float* col[2] = {A + (int64_t)c0 * lda, A + (int64_t)(two ? c1 : c0) * lda};
+    unsigned mx[2] = {0u, 0u};
+    int nf[2] = {0, 0};
+    DF raw[2] = {{0.f, 0.f}, {0.f, 0.f}};
+    auto visitor = [&](int k) {
+      return [&, k](float x0, float x1, float x2, float x3) {
+        const float v0 = fabsf(x0), v1 = fabsf(x1), v2 = fabsf(x2), v3 = fabsf(x3);
+        nf[k] |= !(v0 <= FLT_MAX) | !(v1 <= FLT_MAX) | !(v2 <= FLT_MAX) | !(v3 <= FLT_MAX);
+        mx[k] = max(max(mx[k], max(__float_as_uint(v0), __float_as_uint(v1))),
+                    max(__float_as_uint(v2), __float_as_uint(v3)));
+        df_add_sq4(raw[k], x0, x1, x2, x3);
+      };
     };
     if constexpr (STAGE) {
-      float* dst = stage + (int64_t)c * ld;
-      column_walk<true>(col, dst, m, lane, vec, visit);
-      col = dst;  // the rescaled walk below reads the device copy (same entries, same groups)
+      float* dst0 = stage + (int64_t)c0 * ld;
+      float* dst1 = stage + (int64_t)(two ? c1 : c0) * ld;
+      column_walk2<true>(col[0], dst0, col[1], dst1, two, m, lane, vec, visitor(0), visitor(1));
+      col[0] = dst0;  // the rescaled walk below reads the device copy (same entries, same groups)
+      col[1] = dst1;
     } else {
-      column_walk<false>(col, nullptr, m, lane, vec, visit);
+      column_walk2<false>(col[0], nullptr, col[1], nullptr, two, m, lane, vec, visitor(0), visitor(1));
     }
-    mx = __reduce_max_sync(0xffffffffu, mx);
-    nf = __any_sync(0xffffffffu, nf);
-    double d = 0.0;
-    int e = INT_MIN, ce = INT_MIN;  // column exponent; exponent of the scale d is expressed in
-    if (!nf && mx != 0u) {
-      frexpf(__uint_as_float(mx), &e);
-      if (e >= -40 && e <= 40) {
-        // squares of every entry that matters (>= max 2^-24) stay normal: the raw sum is exact enough
-        d = warp_sum_df(raw.hi, raw.lo);
-        ce = 0;
-      } else {
-        const Pow2 sc = pow2_scale(-e);
-        DF acc{0.f, 0.f};
-        column_walk<false>(col, nullptr, m, lane, vec, [&](float x0, float x1, float x2, float x3) {
-          df_add_sq4(acc, sc.apply(x0), sc.apply(x1), sc.apply(x2), sc.apply(x3));
-        });
-        d = warp_sum_df(acc.hi, acc.lo);
-        ce = e;
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      if (k == 1 && !two) break;
+      const int c = k ? c1 : c0;
+      const unsigned mxk = __reduce_max_sync(0xffffffffu, mx[k]);
+      const int nfk = __any_sync(0xffffffffu, nf[k]);
+      double d = 0.0;
+      int e = INT_MIN, ce = INT_MIN;  // column exponent; exponent of the scale d is expressed in
+      if (!nfk && mxk != 0u) {
+        frexpf(__uint_as_float(mxk), &e);
+        if (e >= -40 && e <= 40) {
+          // squares of every entry that matters (>= max 2^-24) stay normal: the raw sum is exact enough
+          d = warp_sum_df(raw[k].hi, raw[k].lo);
+          ce = 0;
+        } else {
+          const Pow2 sc = pow2_scale(-e);
+          DF acc{0.f, 0.f};
+          column_walk<false>(col[k], nullptr, m, lane, vec, [&](float x0, float x1, float x2, float x3) {
+            df_add_sq4(acc, sc.apply(x0), sc.apply(x1), sc.apply(x2), sc.apply(x3));
+          });
+          d = warp_sum_df(acc.hi, acc.lo);
+          ce = e;
+        }
       }
+      if (lane == 0) {
+        diags[c] = d;
+        colexp[c] = ce;
+        perm[c] = c;
+      }
+      emax = max(emax, e);
+      nonfinite |= nfk;
     }
-    if (lane == 0) {
-      diags[c] = d;
-      colexp[c] = ce;
-      perm[c] = c;
-    }
-    emax = max(emax, e);
-    nonfinite |= nf;
   }
   *bad = __syncthreads_or(nonfinite);
   emax = block_max_int(emax, sm.red_i);
