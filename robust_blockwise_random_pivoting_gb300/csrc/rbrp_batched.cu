@@ -158,16 +158,12 @@ __device__ __forceinline__ int block_max_int(int v, int* sh) {
 // (zeros pad the scalar groups): 16-byte loads when the column is 16-byte
 // aligned.  A lane visits its groups lane, lane + 32, lane + 64, ... in order;
 // the loads of each 128-group chunk are all issued before any is used (four in
-// flight per lane however short the column).  Both norm passes use it, so a lane
-// sees the same entries in the same groups and order in each.
-// With STORE the walk also writes every entry it reads to dst (16-byte aligned):
-// the staging copy of a host-resident column, made by the same pass.
-template <bool STORE, typename F>
-__device__ __forceinline__ void column_walk(const float* __restrict__ col, float* __restrict__ dst, int m, int lane,
-                                            bool vec, F&& f) {
+// flight per lane however short the column).  The norms pass (column_walk2) and
+// its rescaled second walk see the same entries in the same groups and order.
+template <typename F>
+__device__ __forceinline__ void column_walk(const float* __restrict__ col, int m, int lane, bool vec, F&& f) {
   if (vec) {
     const float4* c4 = reinterpret_cast<const float4*>(col);
-    float4* d4 = reinterpret_cast<float4*>(dst);
     const int m4 = m >> 2;
     for (int r = lane; r < m4; r += 128) {
       // groups past the end read as zeros: f adds nothing for them (exact)
@@ -175,28 +171,18 @@ __device__ __forceinline__ void column_walk(const float* __restrict__ col, float
 #pragma unroll
       for (int j = 0; j < 4; ++j) v[j] = r + 32 * j < m4 ? c4[r + 32 * j] : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        if (STORE && r + 32 * j < m4) d4[r + 32 * j] = v[j];
-        f(v[j].x, v[j].y, v[j].z, v[j].w);
-      }
+      for (int j = 0; j < 4; ++j) f(v[j].x, v[j].y, v[j].z, v[j].w);
     }
-    for (int t = 4 * m4 + lane; t < m; t += 32) {
-      const float x = col[t];
-      if (STORE) dst[t] = x;
-      f(x, 0.f, 0.f, 0.f);
-    }
+    for (int t = 4 * m4 + lane; t < m; t += 32) f(col[t], 0.f, 0.f, 0.f);
   } else {
-    for (int r = lane; r < m; r += 32) {
-      const float x = col[r];
-      if (STORE) dst[r] = x;
-      f(x, 0.f, 0.f, 0.f);
-    }
+    for (int r = lane; r < m; r += 32) f(col[r], 0.f, 0.f, 0.f);
   }
 }
 
 // Two columns of one matrix walked in lockstep (col1 only when two): each
 // column's entries reach its own visitor in exactly the order column_walk gives,
-// with twice the loads in flight.
+// with twice the loads in flight.  With STORE every entry read is also written
+// to dst0 / dst1 (16-byte aligned): the staging copy of a host-resident column.
 template <bool STORE, typename F0, typename F1>
 __device__ __forceinline__ void column_walk2(const float* __restrict__ col0, float* __restrict__ dst0,
                                              const float* __restrict__ col1, float* __restrict__ dst1, bool two,
@@ -313,7 +299,7 @@ __device__ int batch_norms(BatchSmem<BB>& sm, const float* __restrict__ A, int64
         } else {
           const Pow2 sc = pow2_scale(-e);
           DF acc{0.f, 0.f};
-          column_walk<false>(col[k], nullptr, m, lane, vec, [&](float x0, float x1, float x2, float x3) {
+          column_walk(col[k], m, lane, vec, [&](float x0, float x1, float x2, float x3) {
             df_add_sq4(acc, sc.apply(x0), sc.apply(x1), sc.apply(x2), sc.apply(x3));
           });
           d = warp_sum_df(acc.hi, acc.lo);

@@ -334,6 +334,7 @@ class Batch:
             raise RuntimeError("another Batch was planned on this handle since: use one handle per live Batch")
 
     def info(self):
+        self._check_plan()
         inf = _lib.BatchInfo()
         check(self.h.lib.rbrp_batch_get_info(self.h.h, ctypes.byref(inf)), self.h.h)
         return dict(b=inf.b, panel_cols=inf.panel_cols, ctas=inf.ctas, ctas_per_sm=inf.ctas_per_sm,
@@ -348,10 +349,12 @@ class Batch:
 
     def set_profiling(self, on=True):
         """In-kernel phase cycle counters (reset when switched on)."""
+        self._check_plan()
         check(self.h.lib.rbrp_batch_set_profiling(self.h.h, int(bool(on))), self.h.h)
 
     def phase_cycles(self):
         """{phase: SM cycles summed over CTAs} accumulated since profiling was switched on."""
+        self._check_plan()
         n = len(_lib.BATCH_PHASES)
         buf = (ctypes.c_double * n)()
         check(self.h.lib.rbrp_batch_get_phase_cycles(self.h.h, buf, n), self.h.h)
@@ -379,7 +382,8 @@ class Batch:
         """Wait for the last run and return a :class:`BatchIDResult`.
 
         The per-problem fields are numpy arrays read in one pass; ``perms`` and
-        ``Ts`` are sequences whose CUDA views are made when indexed.
+        ``Ts`` are sequences whose views (CUDA, or pinned CPU for a host-resident
+        batch) are made when indexed.
         """
         self._check_plan()
         out = (_lib.BatchResult * self.n_prob)()
