@@ -1351,15 +1351,17 @@ using namespace rbrp;
 
 namespace {
 
-// Where a problem buffer lives: 0 device (or managed) memory, 1 pinned host memory
-// (*dev = the address kernels use for it), -1 memory CUDA does not know (pageable).
-int residency(const void* p, const void** dev) {
+// Where a problem buffer lives: 0 memory of this device (or managed), 1 pinned host
+// memory (*dev = the address kernels use for it), -1 memory CUDA does not know
+// (pageable), -2 memory of another device.
+int residency(const void* p, const void** dev, int device) {
   cudaPointerAttributes a{};
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
     cudaGetLastError();
     return -1;
   }
-  if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return 0;
+  if (a.type == cudaMemoryTypeManaged) return 0;
+  if (a.type == cudaMemoryTypeDevice) return a.device == device ? 0 : -2;
   if (a.type == cudaMemoryTypeHost && a.devicePointer) {
     *dev = a.devicePointer;
     return 1;
@@ -1461,20 +1463,24 @@ rbrp_status rbrp_batch_plan(rbrp_handle h, int nprob, const rbrp_batch_problem* 
   for (int q = 0; q < nprob; ++q) {
     rbrp_batch_problem& r = B.probs[q];
     const std::string at = " (problem " + std::to_string(q) + ")";
+    auto where_msg = [&](int where, const char* what) {
+      return std::string(what) + (where == -2 ? " is memory of another device" :
+                                                " is neither device nor pinned host memory") + at;
+    };
     const void* dev = r.A;
-    int where = residency(r.A, &dev);
-    if (where < 0) return set_error(h, RBRP_ERR_INVALID_ARG, "A is neither device nor pinned host memory" + at);
+    int where = residency(r.A, &dev, h->device);
+    if (where < 0) return set_error(h, RBRP_ERR_INVALID_ARG, where_msg(where, "A"));
     if (where == 1) stage |= STAGE_A;
     r.A = static_cast<const float*>(dev);
     dev = r.perm;
-    where = residency(r.perm, &dev);
-    if (where < 0) return set_error(h, RBRP_ERR_INVALID_ARG, "perm is neither device nor pinned host memory" + at);
+    where = residency(r.perm, &dev, h->device);
+    if (where < 0) return set_error(h, RBRP_ERR_INVALID_ARG, where_msg(where, "perm"));
     if (where == 1) stage |= STAGE_PERM;
     r.perm = static_cast<int*>(const_cast<void*>(dev));
     if (r.T) {
       dev = r.T;
-      if (residency(r.T, &dev) < 0)
-        return set_error(h, RBRP_ERR_INVALID_ARG, "T is neither device nor pinned host memory" + at);
+      where = residency(r.T, &dev, h->device);
+      if (where < 0) return set_error(h, RBRP_ERR_INVALID_ARG, where_msg(where, "T"));
       r.T = static_cast<double*>(const_cast<void*>(dev));
     }
   }
