@@ -1,10 +1,10 @@
-"""Multi-process (gloo, world size 2, CPU) tests of bench.py's replica path.
+"""CPU tests of bench.py's replica path (gloo, world size 2) and of its reference arm.
 
 The column ID does not shard: every rank runs its own matrix or batch, and
 the only collective is the max of the ranks' times.  These tests run that
 rank logic over gloo on the host: the barrier, the max over ranks, the
-whole-job rate, per-rank seeding of the workloads, and the reference arm's
-rank-0-only rule.
+whole-job rate, per-rank seeding of the workloads, the reference arm's
+rank-0-only rule, and the reference arm's JSON line (one short step).
 """
 import json
 import os
@@ -74,8 +74,8 @@ def test_two_rank_replicas_over_gloo(tmp_path):
         np.testing.assert_allclose(res[rank]["sums"], ref, rtol=1e-5)
 
 
-def _bench(args, rank):
-    env = dict(os.environ, RANK=str(rank), WORLD_SIZE="2", LOCAL_RANK=str(rank))
+def _bench(args, rank, world=2):
+    env = dict(os.environ, RANK=str(rank), WORLD_SIZE=str(world), LOCAL_RANK=str(rank))
     return subprocess.run([sys.executable, os.path.join(ROOT, "bench.py")] + args, env=env,
                           capture_output=True, text=True, timeout=120)
 
@@ -94,3 +94,18 @@ def test_reference_arm_unavailable_lines(workload):
     assert p.returncode == 0, p.stderr
     line = json.loads(p.stdout.strip().splitlines()[-1])
     assert line["impl"] == "reference" and line["unavailable"]
+
+
+@pytest.mark.parametrize("workload", ["blocks4096", "gexp1000"])
+def test_reference_arm_line_on_cpu(workload):
+    """The reference arm (the oracle port on the host cores) prints one complete JSON line."""
+    p = _bench(["--impl", "reference", "--workload", workload, "--steps", "1", "--warmup", "0"], rank=0, world=1)
+    assert p.returncode == 0, p.stderr
+    line = json.loads(p.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["unit"] == "matrices/s" and line["value"] > 0
+    assert line["higher_is_better"] is True and line["steps"] == 1 and line["warmup"] == 0
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["value"] == line["value"]
+    assert line["cpu_baseline"]["cores"] >= 1 and line["cpu_baseline"]["sample"]
+    assert line["e2e"] == {"value": line["value"], "unit": "matrices/s", "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
+    assert line["config"]["workload"].startswith(workload)
