@@ -37,6 +37,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "RBRP matrices/s & ID time at equal rel err, mixed+batched vs plain FP64"
+L2_BYTES = 126 * 2**20        # GB300 L2
+L2_FLUSH_BYTES = 512 * 2**20  # written between timed steps when an input fits in L2
 
 WORKLOADS = {
     "blocks4096": dict(kind="blocks", nblocks=4096, lo=64, hi=2048, lengthscale=0.5, b=0, tol=1e-8),
@@ -68,7 +70,8 @@ def describe(name, wl):
     if wl["kind"] == "blocks":
         return (f"{name}: {wl['nblocks']} Gaussian-kernel blocks (l={wl['lengthscale']}, 3-D unit-cube clusters "
                 f"2-8 apart), m, n log-uniform in [{wl['lo']}, {wl['hi']}], FP32 storage scaled by each block's "
-                f"max, squared tol {wl['tol']:g} (rel. Frobenius {np.sqrt(wl['tol']):g}), b autotuned")
+                f"max, squared tol {wl['tol']:g} (rel. Frobenius {np.sqrt(wl['tol']):g}), "
+                + ("b autotuned" if wl["b"] <= 0 else f"b={wl['b']}"))
     if wl["kind"] == "gmm":
         return (f"{name}: Gaussian mixture, {wl['n']} points as columns in R^{wl['m']}, {wl['clusters']} clusters "
                 f"(weights 2^-c, means N(0, 4I), sigma U[0.1, 1]), FP32 storage, b={wl['b']}, squared tol "
@@ -78,6 +81,19 @@ def describe(name, wl):
                 f"b={wl['b']}, squared tol {wl['tol']:g} (rel. Frobenius {np.sqrt(wl['tol']):g})")
     return (f"{name}: U diag(exp(-i/20)) V^T {wl['m']}x{wl['n']} FP64, b={wl['b']}, "
             f"squared tol {wl['tol']:g}")
+
+
+def single_input_bytes(wl):
+    """Bytes of the matrix a single-matrix workload's timed step reads (FP32 for the mixed form)."""
+    return wl["m"] * wl["n"] * (4 if wl["kind"] in ("snn", "gmm") else 8)
+
+
+def single_config(name, wl):
+    """The ``config`` of both arms of a single-matrix workload (identical by construction)."""
+    b = single_input_bytes(wl)
+    l2 = (f"no flush: the {b / 2**20:.0f} MiB input is larger than L2" if b >= 2 * L2_BYTES
+          else f"L2 flushed before every timed step (the {b / 2**20:.0f} MiB input fits)")
+    return {"workload": describe(name, wl), "l2": l2}
 
 
 def make_matrix(wl, seed, torch, device):
@@ -226,7 +242,7 @@ def run_reference(args, wl, name):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Philox)",
-        "config": {"workload": describe(name, wl)},
+        "config": single_config(name, wl),
         "cpu_baseline": {"value": value, "unit": "matrices/s", "cores": threads(), "kind": "port",
                          "sample": f"oracle port (numpy/scipy FP64) of the reference's blocked_rpid on the first "
                                    f"{kmax_sample} ranks of the same matrix per step; matrices/s extrapolated by "
@@ -323,15 +339,29 @@ def run_single(args, wl, name, ctx, light=False):
     h.reset_phase_stats()
     ctx.barrier()
     torch.cuda.synchronize()
+    in_bytes = m * n * A.element_size()
+    # inputs that fit in L2 are evicted before every timed step by a write of a larger buffer
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=ctx.device) if in_bytes < 2 * L2_BYTES else None
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(ctx.uuid) as clk:
-        ev0.record(stream)
-        for _ in range(steps):
-            r = h.column_id(A, **kw)
-        ev1.record(stream)
-        torch.cuda.synchronize()
+        if flush is None:
+            ev0.record(stream)
+            for _ in range(steps):
+                r = h.column_id(A, **kw)
+            ev1.record(stream)
+            torch.cuda.synchronize()
+            ms = ev0.elapsed_time(ev1)
+        else:
+            ms = 0.0
+            for _ in range(steps):
+                flush.zero_()
+                ev0.record(stream)
+                r = h.column_id(A, **kw)
+                ev1.record(stream)
+                torch.cuda.synchronize()
+                ms += ev0.elapsed_time(ev1)
     ctx.barrier()
-    ms = ev0.elapsed_time(ev1)
+    del flush
     stats = h.phase_stats()
     h.set_profiling(False)
     clocks = clk.summary()
@@ -417,11 +447,12 @@ def run_single(args, wl, name, ctx, light=False):
         "warmup": warmup, "ms_per_step": ms_max / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if mixed else "f64",
         "data": "synthetic (seeded Philox), one independent matrix per rank",
-        "config": {"workload": describe(name, wl), "precision": "mixed" if mixed else "f64",
+        "config": single_config(name, wl),
+        "details": {"precision": "mixed" if mixed else "f64",
                    "k": k, "blocks": r.nblocks, "id_time_ms": ms_max / steps,
                    "rel_err": float(np.sqrt(max(rel_err, 0.0))), "err_est_sq": r.err_est,
                    "plain_f64": plain, "parallelism": f"replicas x{ctx.world}", "cluster_coverage": coverage,
-                   "l2": f"no flush: the {m * n * 4 / 2**20:.0f} MiB input is larger than L2", "phases": phases},
+                   "phases": phases},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
         "gpu_launches": gpu_launches,
     }
@@ -431,21 +462,135 @@ def block_sample_ids(nblocks, count, seed):
     return np.sort(np.random.default_rng(1000 + seed).choice(nblocks, size=min(count, nblocks), replace=False))
 
 
-def batched_cpu_sample(wl, seed, b, count):
-    """The oracle port on a seeded sample of the workload's blocks: (seconds, count, description)."""
-    from oracle import rbrp_column_id
+CPU_SAMPLE_BLOCKS = 256   # the seeded block sample both CPU legs time (cpu_baseline and --impl reference)
+
+
+def batched_cpu_sample(wl, seed, b, count=CPU_SAMPLE_BLOCKS, mats=None, keep=False):
+    """The oracle port on a seeded sample of the workload's blocks.
+
+    Each block is one complete ID as the GPU computes it: the adaptive RBRP
+    (``blocked_rpid``) and the interpolation matrix T (``interpolation(...,
+    mode='sid')``, the oracle's ``interp_sid``).  ``mats`` (FP64 host copies of
+    the sampled blocks) replaces the host-side generation; with ``keep`` the
+    oracle runs are returned for the parity check.  Returns ``(seconds, count,
+    description, ids, mats, runs)``."""
+    from oracle import interp_sid, rbrp_column_id
     from robust_blockwise_random_pivoting_gb300 import workloads as W
-    shapes = W.kernel_block_shapes(wl["nblocks"], wl["lo"], wl["hi"], seed)
     ids = block_sample_ids(wl["nblocks"], count, seed)
-    mats = [W.kernel_block_scaled(int(shapes[q][0]), int(shapes[q][1]), q, wl["lengthscale"], seed).astype(np.float64)
-            for q in ids]
+    if mats is None:
+        shapes = W.kernel_block_shapes(wl["nblocks"], wl["lo"], wl["hi"], seed)
+        mats = [W.kernel_block_scaled(int(shapes[q][0]), int(shapes[q][1]), q, wl["lengthscale"], seed)
+                .astype(np.float64) for q in ids]
+    runs = []
     t0 = time.perf_counter()
     for q, A in zip(ids, mats):
-        rbrp_column_id(A, b, tol=wl["tol"], seed=seed * wl["nblocks"] + int(q))
+        o = rbrp_column_id(A, b, tol=wl["tol"], seed=seed * wl["nblocks"] + int(q))
+        if 0 < o["k"] < A.shape[1]:
+            interp_sid(A, o["perm"], o["k"])
+        if keep:
+            runs.append(o)
     dt = time.perf_counter() - t0
-    return dt, len(ids), (f"oracle port (numpy/scipy FP64) of the reference's blocked_rpid on a seeded sample of "
-                          f"{len(ids)} of the {wl['nblocks']} blocks (same shape distribution), b={b}; "
-                          f"matrices/s = sample size / time")
+    return dt, len(ids), (f"oracle port (numpy/scipy FP64) of the reference's blocked_rpid plus interpolation "
+                          f"(mode='sid') for T, on a seeded sample of {len(ids)} of the {wl['nblocks']} blocks "
+                          f"(same shape distribution, same sample in both CPU legs), b={b}; "
+                          f"matrices/s = sample size / time"), ids, mats, runs
+
+
+def batched_config(name, wl):
+    """The ``config`` of both arms of a batched workload (identical by construction)."""
+    from robust_blockwise_random_pivoting_gb300 import workloads as W
+    sh = W.kernel_block_shapes(wl["nblocks"], wl["lo"], wl["hi"], 0)
+    gb = float((sh[:, 0] * sh[:, 1]).sum()) * 4 / 1e9
+    l2 = (f"no flush: the {gb:.1f} GB of inputs are larger than L2" if gb > 0.2 else
+          f"the {gb:.2f} GB of inputs may sit in L2 (a profiling subset)")
+    return {"workload": describe(name, wl), "l2": l2}
+
+
+def same_rank_parity(wl, seed, b, ids, mats, runs, res, rel):
+    """The GPU's IDs of the sampled blocks against the oracle's at the same rank.
+
+    For block q of rank k, the oracle's squared error at rank k comes from its
+    adaptive run with the same Philox key (``oracle.error_at_rank``: its
+    skeleton at the block boundary k, or a run capped at k when k is not a
+    boundary); the ratio is un-squared (relative Frobenius), GPU / oracle."""
+    from oracle import error_at_rank
+    ratios, same_k, same_S, capped = [], 0, 0, 0
+    for j, (q, A) in enumerate(zip(ids, mats)):
+        k = int(res.k[q])
+        perm = res.perms[q].cpu().numpy()
+        o = runs[j]
+        e_ref, how = error_at_rank(A, k, b, tol=wl["tol"], seed=seed * wl["nblocks"] + int(q), run=o)
+        e_gpu = float(rel[q]) ** 2
+        ratios.append(float(np.sqrt(max(e_gpu, 1e-24) / max(e_ref, 1e-24))))
+        same_k += k == o["k"]
+        same_S += k == o["k"] and bool(np.array_equal(perm[:k], o["perm"][:k]))
+        capped += how == "capped"
+    r = np.array(ratios)
+    return {"blocks": len(ids), "max_err_ratio_same_rank": float(r.max()), "median_err_ratio_same_rank":
+            float(np.median(r)), "blocks_same_rank": same_k, "blocks_same_ordered_skeleton": same_S,
+            "blocks_rank_not_an_oracle_boundary": capped,
+            "definition": "relative Frobenius ID error of the GPU's S and T over the oracle's (FP64, same FP32 "
+                          "values, same Philox key) at the GPU's rank"}
+
+
+def tight_tolerance_leg(args, wl, ctx, As, seed, b, t_cap, tol=1e-12, subset=64):
+    """The throughput target's tolerance: squared 1e-12 (relative Frobenius 1e-6).
+
+    The batched form over all blocks (own plan, CUDA-event timed launches) and
+    the plain FP64 one-launch-per-matrix form on a seeded subset of the same
+    blocks, each with its largest relative error checked in FP64 on the device."""
+    torch = ctx.torch
+    from robust_blockwise_random_pivoting_gb300.rbrp import Batch, Handle
+    nb = len(As)
+    h = Handle(ctx.local)
+    bt = Batch(h, As, b=b, tol=tol, seed=seed * nb, t_rank_cap=t_cap)
+    bt.run()
+    bt.results()
+    steps = max(1, min(args.steps, 5))
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(ctx.stream)
+    for _ in range(steps):
+        bt.run(ctx.stream)
+    ev1.record(ctx.stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / steps
+    res = bt.results()
+
+    def rel_err(A, perm, k, T):
+        n = A.shape[1]
+        if k == 0 or k == n:
+            return 0.0 if k == n else 1.0
+        p = perm.long()
+        A64 = A.double()
+        return float(torch.linalg.norm(A64[:, p[k:]] - A64[:, p[:k]] @ T) / torch.linalg.norm(A64))
+    rel = [rel_err(A, res.perms[q], int(res.k[q]), res.Ts[q]) if res.status[q] == 0 else float("nan")
+           for q, A in enumerate(As)]
+    batched = {"matrices_per_s": nb / (ms * 1e-3), "ms_per_launch": ms, "launches_timed": steps,
+               "k_mean": float(res.k.mean()), "k_max": int(res.k.max()), "status_ok": int((res.status == 0).sum()),
+               "rel_err_max": float(np.nanmax(rel))}
+    h.close()
+    ids = block_sample_ids(nb, subset, seed)
+    hs = Handle(ctx.local)
+    sub = [As[q].double().t().contiguous().t() for q in ids]
+    hs.column_id(sub[0], b=b, tol=tol, seed=0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ks = []
+    for q, A in zip(ids, sub):
+        ks.append(hs.column_id(A, b=b, tol=tol, seed=seed * nb + int(q)).k)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    errs = []
+    for q, A in zip(ids, sub):
+        hs.column_id(A, b=b, tol=tol, seed=seed * nb + int(q))
+        errs.append(float(np.sqrt(max(hs.id_error(A), 0.0))))
+    hs.close()
+    plain = {"subset": len(ids), "matrices_per_s": len(ids) / dt, "ms_per_matrix": 1e3 * dt / len(ids),
+             "k_mean": float(np.mean(ks)), "rel_err_max": float(np.max(errs))}
+    return {"tol_squared": tol, "rel_frobenius": float(np.sqrt(tol)), "b": b, "batched_mixed": batched,
+            "plain_f64_one_launch_per_matrix": plain,
+            "speedup_batched_vs_plain_f64": batched["matrices_per_s"] / plain["matrices_per_s"]}
 
 
 def run_batched(args, wl, name, ctx):
@@ -642,27 +787,33 @@ def run_batched(args, wl, name, ctx):
                    "block in place once and writes perm and T to pinned host memory), Batch.results()"}
         del hz, hviews
         hz_handle.close()
-        # headline: the fastest of the host-buffer forms, the others beside it
-        forms = {"host_resident": host_resident, "sequential": sequential, "pipelined": pipelined}
-        best = max(forms, key=lambda f: forms[f]["value"])
-        e2e = dict(forms[best])
-        e2e["form"] = best
-        e2e.setdefault("h2d_bytes_per_step", int(pack.numel() * 4))
-        e2e.setdefault("d2h_bytes_per_step", int(hb.d2h_bytes + nb * 56))
-        e2e["other_forms"] = {f: forms[f] for f in forms if f != best}
+        # headline: the host-resident form, declared in advance; the other host-buffer forms beside it
+        e2e = dict(host_resident)
+        e2e["form"] = "host_resident"
+        e2e["other_forms"] = {"sequential": sequential, "pipelined": pipelined}
         del host
 
-    cpu = None
+    cpu = parity = None
     if ctx.rank == 0 and ctx.world == 1 and not args.no_cpu:
-        dt, cnt, desc = batched_cpu_sample(wl, seed, info["b"], 256)
+        # the oracle on the GPU's own FP32 values of the sampled blocks: timed as the CPU
+        # baseline, then (outside the timing) the checker of the same-rank parity
+        ids = block_sample_ids(nb, CPU_SAMPLE_BLOCKS, seed)
+        mats = [As[q].double().cpu().numpy() for q in ids]
+        dt, cnt, desc, ids, mats, runs = batched_cpu_sample(wl, seed, info["b"], mats=mats, keep=True)
         cpu = {"value": cnt / dt, "unit": "matrices/s", "cores": threads(), "kind": "port", "sample": desc}
+        parity = same_rank_parity(wl, seed, info["b"], ids, mats, runs, res, rel)
+        del mats, runs
+
+    tight = None
+    if not args.no_plain:
+        tight = tight_tolerance_leg(args, wl, ctx, As, seed, info["b"], 256)
 
     single_matrix = None
     if not args.no_single and ctx.world == 1:
         sl = run_single(args, WORKLOADS["snn16k"], "snn16k", ctx, light=True)
-        single_matrix = {"workload": sl["config"]["workload"], "id_time_ms": sl["config"]["id_time_ms"],
-                         "k": sl["config"]["k"], "rel_err": sl["config"]["rel_err"],
-                         "plain_f64": sl["config"]["plain_f64"], "roofline": sl["roofline"],
+        single_matrix = {"workload": sl["config"]["workload"], "id_time_ms": sl["details"]["id_time_ms"],
+                         "k": sl["details"]["k"], "rel_err": sl["details"]["rel_err"],
+                         "plain_f64": sl["details"]["plain_f64"], "roofline": sl["roofline"],
                          "clocks": sl["clocks"], "timing": "2 warm-up + 2 timed IDs"}
     h.close()
     return {
@@ -670,14 +821,16 @@ def run_batched(args, wl, name, ctx):
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic (seeded Philox points), one independent batch per rank",
-        "config": {"workload": describe(name, wl), "precision": "mixed", "problems": nb,
+        "config": batched_config(name, wl),
+        "parity": parity, "tol_1e-12": tight,
+        "details": {"precision": "mixed", "problems": nb,
                    "elements": int(offs[-1]), "b": info["b"], "ctas": info["ctas"],
                    "ctas_per_sm": info["ctas_per_sm"], "plan_s": t_plan, "autotune_ms": info["ms_autotune"],
                    "k_mean": float(res.k.mean()), "k_max": int(res.k.max()), "blocks_mean": float(res.nblocks.mean()),
                    "status_ok": ok, "rel_err_max": float(np.nanmax(rel)), "rel_err_mean": float(np.nanmean(rel)),
                    "one_launch_per_matrix": single, "single_matrix_snn16k": single_matrix,
                    "parallelism": f"replicas x{ctx.world}", "launch": "one CUDA graph (queue reset + kernel)",
-                   "l2": "no flush: the 5.4 GB of inputs are larger than L2", "phase_cycle_share": phases},
+                   "phase_cycle_share": phases},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
         "gpu_launches": args.steps,
     }
@@ -910,7 +1063,7 @@ def run_reference_batched(args, wl, name):
     b = 16
     times, counts = [], []
     for s in range(args.warmup + args.steps):
-        dt, cnt, desc = batched_cpu_sample(wl, 0, b, 64)
+        dt, cnt, desc, _, _, _ = batched_cpu_sample(wl, 0, b)
         if s >= args.warmup:
             times.append(dt)
             counts.append(cnt)
@@ -919,7 +1072,7 @@ def run_reference_batched(args, wl, name):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "matrices/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded Philox points)", "config": {"workload": describe(name, wl)},
+        "data": "synthetic (seeded Philox points)", "config": batched_config(name, wl),
         "cpu_baseline": {"value": value, "unit": "matrices/s", "cores": threads(), "kind": "port", "sample": desc},
         "e2e": {"value": value, "unit": "matrices/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
@@ -936,8 +1089,19 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-single", action="store_true", help="skip the snn16k single-matrix figure")
+    ap.add_argument("--nblocks", type=int, default=0,
+                    help="batched workloads: a smaller problem count of the same shape distribution (profiling)")
+    ap.add_argument("--hi", type=int, default=0, help="batched workloads: a smaller largest m and n (profiling)")
+    ap.add_argument("--b", type=int, default=0, help="batched workloads: fixed block size instead of the autotuner")
     args = ap.parse_args()
-    wl = WORKLOADS[args.workload]
+    wl = dict(WORKLOADS[args.workload])
+    if wl["kind"] == "blocks":
+        if args.nblocks > 0:
+            wl["nblocks"] = args.nblocks
+        if args.hi > 0:
+            wl["hi"] = max(wl["lo"], args.hi)
+        if args.b > 0:
+            wl["b"] = args.b
     if args.impl == "reference":
         if wl["kind"] == "adjoint":
             print(json.dumps({"impl": "reference", "unavailable": "the reference has no differentiable ID"}))

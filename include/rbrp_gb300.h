@@ -55,7 +55,8 @@ typedef enum {
 
 typedef enum {
   RBRP_PREC_F64 = 0,        /* FP64 throughout: the plain form */
-  RBRP_PREC_F32_MIXED = 1   /* FP32 storage and projections, FP64 panels, sums and solve */
+  RBRP_PREC_F32_MIXED = 1   /* FP32 storage and projections; double-float (pairs of FP32,
+                               ~48-bit) panels, sums and T solve; FP64 sampler weights */
 } rbrp_precision;
 
 typedef struct {
@@ -195,12 +196,15 @@ rbrp_status rbrp_id_error_f32(rbrp_handle h, int m, int n, const float* dA, int6
  * squared relative ID error ||A(:,rd) - A(:,S) T||_F^2 / normA2 written to
  * *dErr on `stream` (cudaStream_t), computed without a handle and without any
  * allocation.  Inputs: A (m x n, FP64, lda), perm (n ints; S = perm[:k], rd =
- * perm[k:]), T (k x (n-k), ldt >= k); all device pointers on the current device.
- * Its scratch is a fixed 2 MiB device array in the library (held by every GPU
- * that loads it until exit), so sizes with ceil((n-k)/32) * ceil(m/64) > 262144
- * return RBRP_ERR_CAPACITY.  All calls on a device share that array: calls that
- * overlap on the GPU race and must be serialised.  The first call on a device
- * looks the array up (cudaGetSymbolAddress); make it before any stream capture. */
+ * perm[k:]), T (k x (n-k), ldt >= k); all device pointers in the current
+ * context.  k == 0 writes 1.0 and k == n writes 0.0 (A, perm and T may then be
+ * NULL), as rbrp_id_error_f64 reports them.  Its scratch is a fixed 2 MiB device
+ * array in the library (held by every GPU that loads it until exit), so sizes
+ * with ceil((n-k)/32) * ceil(m/64) > 262144 return RBRP_ERR_CAPACITY.  All calls
+ * on a device share that array: calls that overlap on the GPU race and must be
+ * serialised.  The first call in each CUDA context (primary or caller-created;
+ * a context made after cudaDeviceReset is a new one) looks the array up
+ * (cudaGetSymbolAddress); make that call before any stream capture. */
 rbrp_status rbrp_id_error_f64_noalloc(int m, int n, const double* dA, int64_t lda, const int* dPerm, int k,
                                       const double* dT, int64_t ldt, double normA2, double* dErr, void* stream);
 

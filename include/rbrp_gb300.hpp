@@ -39,6 +39,12 @@ inline rbrp_status RandAdapRBRP(const double* A, int m, int n, int*& sk, int*& r
                                 double& flops, double tol = 1e-8, int blk = 16) {
   return rbrp_RandAdapRBRP(A, m, n, &sk, &rd, &T, &rank, &flops, tol, blk);
 }
+/* The name gpu/rid.hpp:5-7 declares, so a caller written against it compiles
+ * unchanged; same arguments and results as RandAdapRBRP (RBRP pivoting). */
+inline rbrp_status RandAdapLUPP(const double* A, int m, int n, int*& sk, int*& rd, double*& T, int& rank,
+                                double& flops, double tol = 1e-8, int blk = 16) {
+  return RandAdapRBRP(A, m, n, sk, rd, T, rank, flops, tol, blk);
+}
 
 /* gpu/rid.hpp: RandLUPP_OS and RandCPQR_OS with the reference's arguments; each
  * call draws a new sketch (Philox key = call count, as the reference's RNG

@@ -19,6 +19,7 @@ from .rbrp_oracle import (
     interp_sid,
     interp_r11,
     id_error,
+    error_at_rank,
 )
 
 __all__ = [
@@ -33,4 +34,5 @@ __all__ = [
     "interp_sid",
     "interp_r11",
     "id_error",
+    "error_at_rank",
 ]

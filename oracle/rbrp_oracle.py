@@ -275,3 +275,33 @@ def id_error(A, perm, T, relative=True):
     if relative:
         e /= spla.norm(A, ord="fro") ** 2
     return e
+
+
+def error_at_rank(A, k, b, tol=None, seed=0, sampler="np", mode="rp", run=None):
+    """The oracle's squared relative ID error at rank ``k`` (SID interpolation).
+
+    Used to compare another implementation's ID of rank ``k`` with the
+    reference's "at the same rank".  The adaptive run (``rbrp_column_id`` with
+    ``tol``, or ``run`` when given) fixes the skeleton at every block
+    boundary: later block swaps never move positions below the current rank, so
+    its final ``perm[:k_t]`` is the skeleton after the block that reached
+    ``k_t``.  When ``k`` is such a boundary (or the final rank), the error is
+    that skeleton's; otherwise the run is repeated with ``kmax = k``, whose
+    last block samples only the columns still missing.
+
+    Returns ``(error, how)`` with ``how`` in ``{"boundary", "capped"}``.
+    """
+    A = np.asarray(A, dtype=np.float64)
+    n = A.shape[1]
+    if run is None:
+        run = rbrp_column_id(A, b, tol=tol, seed=seed, sampler=sampler, mode=mode)
+    if k <= 0:
+        return 1.0, "boundary"
+    if k >= n:
+        return 0.0, "boundary"
+    bounds = set(int(x) for x in run["ranks"]) | {int(run["k"])}
+    if k in bounds:
+        perm, how = run["perm"], "boundary"
+    else:
+        perm, how = rbrp_column_id(A, b, tol=None, kmax=k, seed=seed, sampler=sampler, mode=mode)["perm"], "capped"
+    return id_error(A, perm, interp_sid(A, perm, k)), how

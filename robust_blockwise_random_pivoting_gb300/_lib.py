@@ -101,6 +101,7 @@ _SIGS = {
     "rbrp_reset_phase_stats": (c_int, [c_void_p]),
     "rbrp_set_variant": (c_int, [c_void_p, c_int]),
     "rbrp_set_tsolve_fp64": (c_int, [c_void_p, c_int]),
+    "rbrp_set_wait_budget": (c_int, [c_void_p, ctypes.c_longlong]),
     "rbrp_id_error_f64_noalloc": (c_int, [c_int, c_int, c_void_p, c_int64, c_void_p, c_int, c_void_p, c_int64,
                                           c_double, c_void_p, c_void_p]),
     "rbrp_fixed_id_f32": (c_int, [c_void_p, c_int, c_int, c_void_p, c_int64, c_void_p, c_int, c_int, c_void_p,

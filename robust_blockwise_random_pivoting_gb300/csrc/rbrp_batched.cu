@@ -1362,7 +1362,8 @@ int residency(const void* p, const void** dev, int device) {
   }
   if (a.type == cudaMemoryTypeManaged) return 0;
   if (a.type == cudaMemoryTypeDevice) return a.device == device ? 0 : -2;
-  if (a.type == cudaMemoryTypeHost && a.devicePointer) {
+  if (a.type == cudaMemoryTypeHost) {
+    if (!a.devicePointer) return -3;  // pinned, but not mapped into the device's address space
     *dev = a.devicePointer;
     return 1;
   }
@@ -1464,8 +1465,12 @@ rbrp_status rbrp_batch_plan(rbrp_handle h, int nprob, const rbrp_batch_problem* 
     rbrp_batch_problem& r = B.probs[q];
     const std::string at = " (problem " + std::to_string(q) + ")";
     auto where_msg = [&](int where, const char* what) {
-      return std::string(what) + (where == -2 ? " is memory of another device" :
-                                                " is neither device nor pinned host memory") + at;
+      return std::string(what) +
+             (where == -2   ? " is memory of another device"
+              : where == -3 ? " is pinned host memory that is not mapped for device access (register it "
+                              "with cudaHostRegisterMapped, or allocate it with cudaHostAlloc)"
+                            : " is neither device nor pinned host memory") +
+             at;
     };
     const void* dev = r.A;
     int where = residency(r.A, &dev, h->device);

@@ -900,6 +900,12 @@ rbrp_status rbrp_set_variant(rbrp_handle h, int variant) {
   return RBRP_OK;
 }
 
+rbrp_status rbrp_set_wait_budget(rbrp_handle h, long long cycles) {
+  if (!h || cycles < 0) return RBRP_ERR_INVALID_ARG;
+  h->wait_budget = cycles;
+  return RBRP_OK;
+}
+
 rbrp_status rbrp_set_tsolve_fp64(rbrp_handle h, int on) {
   if (!h) return RBRP_ERR_INVALID_ARG;
   h->tsolve_fp64 = on != 0;

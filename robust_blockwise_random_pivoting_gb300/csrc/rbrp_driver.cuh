@@ -170,8 +170,9 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
             sps = s_w;
           }
         }
-        tc::k_proj_w_tc<<<dim3(ctiles, wsplit), tc::NTHREADS, tc::P1_SMEM, st>>>(tmA, tmQh, tmQl, h->st, m, n, sps,
-                                                                                reinterpret_cast<float2*>(h->Wpart));
+        tc::k_proj_w_tc<<<dim3(ctiles, wsplit), tc::NTHREADS, tc::P1_SMEM, st>>>(
+            tmA, tmQh, tmQl, h->st, m, n, sps, reinterpret_cast<float2*>(h->Wpart),
+            h->wait_budget > 0 ? h->wait_budget : kWaitBudgetDefault);
       } else {
         k_proj_w<<<(n - i + 63) / 64, 128, 0, st>>>((const float*)Q, L.ld_res, h->Ares, L.ld_res, h->st, m, n, h->R,
                                                     n);

@@ -1,5 +1,6 @@
 // FP32-storage instantiation of the RBRP block loop (the mixed-precision form:
-// FP32 A, Q and projections; FP64 weights, panel factorisation and sums).
+// FP32 A, Q and projections; double-float (pairs of FP32) panel factorisation,
+// sums and T solve; FP64 sampler weights).
 #include "rbrp_driver.cuh"
 
 namespace rbrp {

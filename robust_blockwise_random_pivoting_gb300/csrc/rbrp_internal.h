@@ -9,6 +9,10 @@
 #include "rbrp_common.cuh"
 
 namespace rbrp {
+
+// clock64 limit of a bounded device-side wait (~2 s at GB300's 2.07 GHz SM clock)
+constexpr long long kWaitBudgetDefault = 4ll << 30;
+
 constexpr int P2_MAX_SPLIT_WS = 8;  // row ranges of the residual update (workspace sizing)
 constexpr int P1_MAX_SPLIT = 8;     // row ranges of the tensor-core projection
 struct BatchState;                  // batched form (rbrp_batched.cu)
@@ -62,6 +66,7 @@ struct rbrp_handle_st {
   float* Ql = nullptr;
   int variant = 0;             // 0: tensor-core projection, 1: CUDA-core projection
   bool tsolve_fp64 = false;    // T solve on the FP64 pipe instead of double-float
+  long long wait_budget = 0;   // clock64 limit of bounded device waits (0: the default, ~2 s)
 
   // interpolation matrix of the last run
   double* T = nullptr;

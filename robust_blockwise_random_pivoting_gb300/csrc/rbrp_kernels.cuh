@@ -1222,7 +1222,7 @@ k_finish(State* st, const double* __restrict__ part_res, const int* __restrict__
     trace_samp[nb] = s_bss;
     st->nblocks = nb + 1;
     if ((tol > 0.0 && s < st->res0 * tol) || c == 0 || i >= kmax || !(s == s)) st->done = 1;
-    if (!(s == s)) st->status = ST_ERR_NUMERIC;
+    if (!(s == s) && st->status == 0) st->status = ST_ERR_NUMERIC;  // an earlier status (a timeout) stays
   }
 }
 

@@ -61,9 +61,10 @@ __device__ __forceinline__ void warp_argmax(double& v, int& pos, int& row) {
 
 // Sense-by-generation grid barrier.  Thread 0 of each CTA arrives; the last
 // arrival resets the count and advances the generation.  A wait longer than
-// ~2 s of SM clock sets `abort`; every later barrier then returns false at once.
-// Thread 0 decides the result for its whole CTA, so the CTA never splits.
-__device__ bool grid_sync(GridBar* b, unsigned nblocks) {
+// `budget` SM clocks (~2 s by default) sets `abort`; every later barrier then
+// returns false at once.  Thread 0 decides the result for its whole CTA, so the
+// CTA never splits.
+__device__ bool grid_sync(GridBar* b, unsigned nblocks, long long budget) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -79,7 +80,7 @@ __device__ bool grid_sync(GridBar* b, unsigned nblocks) {
       const long long t0 = clock64();
       while (*vgen == g) {
         if (*vabort) break;
-        if (clock64() - t0 > (4ll << 30)) {
+        if (clock64() - t0 > budget) {
           atomicExch(&b->abort, 1);
           atomicCAS(&b->status, 0, ST_TIMEOUT);
           break;
@@ -127,7 +128,7 @@ __host__ __device__ inline size_t lupp_smem(int k, int tpc) {
 __global__ void __launch_bounds__(LU_THREADS) k_lupp(double* __restrict__ Wt, int k, int n, int tpc,
                                                      int* __restrict__ rowAt, int* __restrict__ pivrow,
                                                      int* __restrict__ ipiv, LuKey* __restrict__ parts, GridBar* bar,
-                                                     int* __restrict__ perm) {
+                                                     int* __restrict__ perm, long long budget) {
   // shared: pivot row u (k) | current column, two steps (2 x tpc x 32) | next column prefetch
   // (tpc x 32) | positions of the owned rows (tpc x 32) | dead flags (tpc x 32)
   extern __shared__ __align__(16) unsigned char lsm[];
@@ -162,7 +163,7 @@ __global__ void __launch_bounds__(LU_THREADS) k_lupp(double* __restrict__ Wt, in
     warp_argmax(bv, bp, br);
     if (lane == 0) parts[blockIdx.x] = LuKey{bv, bp, br};
   }
-  if (!grid_sync(bar, nblocks)) return;
+  if (!grid_sync(bar, nblocks, budget)) return;
 
   for (int j = 0; j < k; ++j) {
     const LuKey* in = parts + (size_t)(j & 1) * nblocks;
@@ -253,7 +254,7 @@ __global__ void __launch_bounds__(LU_THREADS) k_lupp(double* __restrict__ Wt, in
       warp_argmax(kv, kp, kr);
       if (lane == 0) out[blockIdx.x] = LuKey{kv, kp, kr};
     }
-    if (!grid_sync(bar, nblocks)) return;
+    if (!grid_sync(bar, nblocks, budget)) return;
   }
 
   // perm[pos] = the original row at position pos after all swaps
@@ -324,7 +325,8 @@ extern "C" rbrp_status rbrp_lupp_pivots_f64(rbrp_handle h, int k, int n, const d
   s = cuda_check(h, cudaGetLastError(), "k_lupp_load");
   if (s != RBRP_OK) return s;
   int tpc_arg = tpc;
-  void* args[] = {&Wt, &k, &n, &tpc_arg, &rowAt, &pivrow, &dIpiv, &parts, &bar, &dPerm};
+  long long budget = h->wait_budget > 0 ? h->wait_budget : kWaitBudgetDefault;
+  void* args[] = {&Wt, &k, &n, &tpc_arg, &rowAt, &pivrow, &dIpiv, &parts, &bar, &dPerm, &budget};
   s = cuda_check(h, cudaLaunchCooperativeKernel((const void*)k_lupp, dim3(grid), dim3(LU_THREADS), args, smem, st),
                  "cooperative launch of k_lupp");
   if (s != RBRP_OK) return s;

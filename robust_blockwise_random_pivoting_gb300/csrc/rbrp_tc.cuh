@@ -63,6 +63,7 @@ struct __align__(1024) P1Smem {
   unsigned long long full[STAGES], split[STAGES], empty[STAGES];
   unsigned long long bigf[NBIG], bige[NBIG];  // large accumulators: full (MMA done) / empty (drained)
   unsigned long long smlf[2], smle[2];     // small accumulator
+  unsigned long long mmadone;             // abort path: every MMA this CTA issued has completed
   uint32_t tmem_base;
   int abort;
 };
@@ -90,14 +91,16 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* b, uint32_t pa
       : "memory");
   return ok != 0;
 }
-// Bounded wait for the phase of parity `parity`; false on timeout or abort.
-__device__ __forceinline__ bool mbar_wait(unsigned long long* b, uint32_t parity, volatile int* abort) {
+// Bounded wait for the phase of parity `parity`: false once `budget` SM clocks
+// have passed (setting *abort) or another warp has set *abort.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* b, uint32_t parity, volatile int* abort,
+                                          long long budget = kWaitBudgetDefault) {
   if (mbar_try_wait(b, parity)) return true;
   const long long t0 = clock64();
   for (;;) {
     if (mbar_try_wait(b, parity)) return true;
     if (*abort) return false;
-    if (clock64() - t0 > (4ll << 30)) {  // ~2 s at 2 GHz
+    if (clock64() - t0 > budget) {
       *abort = 1;
       return false;
     }
@@ -195,7 +198,7 @@ __device__ __forceinline__ void drain32(uint32_t taddr, float (&hi)[32], float (
 __global__ void __launch_bounds__(NTHREADS, 1)
 k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmQh,
             const __grid_constant__ CUtensorMap tmQl, State* st, int m, int n, int stages_per_split,
-            float2* __restrict__ Wpart) {
+            float2* __restrict__ Wpart, long long budget) {
   extern __shared__ uint8_t p1_raw[];
   P1Smem& sm = *reinterpret_cast<P1Smem*>((reinterpret_cast<uintptr_t>(p1_raw) + 1023) & ~(uintptr_t)1023);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -223,6 +226,7 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
       mbar_init(&sm.smlf[b], 1);
       mbar_init(&sm.smle[b], NDRAIN);
     }
+    mbar_init(&sm.mmadone, 1);
     sm.abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -243,7 +247,7 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
       for (int s = 0; s < nk; ++s) {
         const int slot = s % STAGES;
         const uint32_t use = (uint32_t)(s / STAGES);
-        if (s >= STAGES && !mbar_wait(&sm.empty[slot], (use & 1) ^ 1, abort)) break;
+        if (s >= STAGES && !mbar_wait(&sm.empty[slot], (use & 1) ^ 1, abort, budget)) break;
         uint8_t* base = sm.stage[slot];
         mbar_expect_tx(&sm.full[slot], A_BYTES + 2 * B_BYTES);
         tma_load_2d(base, &tmA, &sm.full[slot], (s0 + s) * BK, p0);
@@ -260,9 +264,9 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
         const int b = s % NBIG;                      // large accumulator of this stage
         const int chunk = s / CHUNK, sb = chunk & 1;  // small accumulator of this chunk
         const bool first = (s % CHUNK) == 0;
-        if (s >= NBIG && !mbar_wait(&sm.bige[b], (uint32_t)(s / NBIG - 1) & 1, abort)) break;
-        if (first && chunk >= 2 && !mbar_wait(&sm.smle[sb], (uint32_t)((chunk >> 1) - 1) & 1, abort)) break;
-        if (!mbar_wait(&sm.split[slot], use & 1, abort)) break;
+        if (s >= NBIG && !mbar_wait(&sm.bige[b], (uint32_t)(s / NBIG - 1) & 1, abort, budget)) break;
+        if (first && chunk >= 2 && !mbar_wait(&sm.smle[sb], (uint32_t)((chunk >> 1) - 1) & 1, abort, budget)) break;
+        if (!mbar_wait(&sm.split[slot], use & 1, abort, budget)) break;
         tc_fence_after();
         const uint8_t* base = sm.stage[slot];
         const uint64_t dah = sw128_desc(smem_u32(base));
@@ -287,7 +291,7 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
     const int et = threadIdx.x - 64;  // 0..NSPLIT-1
     for (int s = 0; s < nk; ++s) {
       const int slot = s % STAGES;
-      if (!mbar_wait(&sm.full[slot], (uint32_t)(s / STAGES) & 1, abort)) break;
+      if (!mbar_wait(&sm.full[slot], (uint32_t)(s / STAGES) & 1, abort, budget)) break;
       float4* a4 = reinterpret_cast<float4*>(sm.stage[slot]);
       float4* l4 = reinterpret_cast<float4*>(sm.stage[slot] + A_BYTES);
 #pragma unroll
@@ -312,14 +316,14 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
     bool ok = true;
     for (int d = 0; d < nk; ++d) {
       const int b = d % NBIG;
-      if (!mbar_wait(&sm.bigf[b], (uint32_t)(d / NBIG) & 1, abort)) { ok = false; break; }
+      if (!mbar_wait(&sm.bigf[b], (uint32_t)(d / NBIG) & 1, abort, budget)) { ok = false; break; }
       tc_fence_after();
       drain32(tbase + lane_off + (uint32_t)(b * BN), hi, lo);
       tc_fence_before();
       mbar_arrive(&sm.bige[b]);
       if ((d % CHUNK) == CHUNK - 1 || d == nk - 1) {
         const int chunk = d / CHUNK, sb = chunk & 1;
-        if (!mbar_wait(&sm.smlf[sb], (uint32_t)(chunk >> 1) & 1, abort)) { ok = false; break; }
+        if (!mbar_wait(&sm.smlf[sb], (uint32_t)(chunk >> 1) & 1, abort, budget)) { ok = false; break; }
         tc_fence_after();
         drain32(tbase + lane_off + (uint32_t)(NBIG * BN + sb * BN), hi, lo);
         tc_fence_before();
@@ -341,12 +345,21 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
   }
   __syncthreads();
   if (*abort) {
+    // Before tensor memory is freed and the CTA exits, everything this CTA started
+    // asynchronously must have finished: its TMA copies (their full barriers) and the
+    // MMAs the MMA thread issued (one last commit, from that thread, arrives on mmadone
+    // once all of them have completed).  Both always complete; these waits use the
+    // default budget whatever budget the main loop had.
+    int dummy = 0;
+    volatile int* never = &dummy;
     if (threadIdx.x == 0) atomicExch(&st->status, ST_ERR_TIMEOUT);
-    if (warp == 0 && lane == 0) {  // let this CTA's own TMA copies land before the CTA exits
-      int dummy = 0;
-      volatile int* never = &dummy;
+    if (warp == 0 && lane == 0) {
       for (int s = issued - STAGES > 0 ? issued - STAGES : 0; s < issued; ++s)
         mbar_wait(&sm.full[s % STAGES], (uint32_t)(s / STAGES) & 1, never);
+    }
+    if (warp == 1 && lane == 0) {
+      mma_commit(&sm.mmadone);
+      mbar_wait(&sm.mmadone, 0u, never);
     }
     __syncthreads();
   }

@@ -180,6 +180,12 @@ class Handle:
         """T solve on the FP64 pipe (True) or in double-float on the FP32 pipe (False, default)."""
         check(self.lib.rbrp_set_tsolve_fp64(self.h, int(bool(on))), self.h)
 
+    def set_wait_budget(self, cycles=0):
+        """Limit (SM clock cycles) of the bounded device-side waits launched through this
+        handle (the LU grid barrier, the tcgen05 projection's mbarriers); 0 = default (~2 s).
+        A few cycles makes them run out: calls then raise status 7 (device wait timed out)."""
+        check(self.lib.rbrp_set_wait_budget(self.h, int(cycles)), self.h)
+
     def reset_phase_stats(self):
         check(self.lib.rbrp_reset_phase_stats(self.h), self.h)
 

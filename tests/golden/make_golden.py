@@ -2,7 +2,7 @@
 
 Run in a container that has the reference checkout (read-only):
 
-    python tests/golden/make_golden.py [REFERENCE_ROOT]
+    python tests/golden/make_golden.py REFERENCE_ROOT
 
 It executes the reference's own Python RBRP (``python/RBRP.ipynb`` code cells
 2, 7 and 11) from REFERENCE_ROOT into a private namespace and records its
@@ -170,4 +170,6 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py REFERENCE_ROOT (the reference checkout, read-only)")
+    main(sys.argv[1])

@@ -1,21 +1,23 @@
 """GPU: the batched persistent form (rbrp_batch_* through the C ABI).
 
-Every problem of a batch runs the FP32 residual form inside one CTA, so the
-checks are those of the one-matrix FP32 form against the FP64 oracle on the
-same FP32-rounded matrix: the squared relative ID error (recomputed here in
-FP64 from the returned perm and T) stays within 1.05x of max(oracle error,
-tol); the rank stays within one block of the oracle's; the first block (whose
-sampling weights are the exact initial column norms in both) selects the same
-columns.  Runs are deterministic, so a replay of the captured graph must
-reproduce every output bit for bit, and scaling a matrix by a power of two
-must change nothing but res0.
+Every problem of a batch runs the FP32 residual form inside one CTA, and is
+compared with the FP64 oracle on the same FP32-rounded matrix, with the same
+Philox key, at the same rank: the relative Frobenius ID error (recomputed here
+in FP64 from the returned perm and T) stays within 1.05x of the oracle's error
+at the rank the GPU reached (``oracle.error_at_rank``), and the first block
+(whose sampling weights are the exact initial column norms in both) selects
+the same columns.  On the headline workload (4096 Gaussian-kernel blocks,
+squared tol 1e-8, b = 16) a seeded sample of its blocks must also give the
+oracle's rank and skeleton.  Runs are deterministic, so a replay of the
+captured graph must reproduce every output bit for bit, and scaling a matrix
+by a power of two must change nothing but res0.
 """
 import numpy as np
 import pytest
 
 torch = pytest.importorskip("torch")
 
-from oracle import id_error, interp_sid, rbrp_column_id  # noqa: E402
+from oracle import error_at_rank, id_error, interp_sid, rbrp_column_id  # noqa: E402
 from robust_blockwise_random_pivoting_gb300 import workloads as W  # noqa: E402
 
 pytestmark = pytest.mark.gpu
@@ -47,15 +49,25 @@ def run_batch(handle, mats, **kw):
     return bt, bt.results()
 
 
-def check_problem(A64, perm, T, k, err_est, tol, b, seed, kslack=None):
-    o = rbrp_column_id(A64, b, tol=tol, seed=seed)
-    e_ref = id_error(A64, o["perm"], interp_sid(A64, o["perm"], o["k"]))
+RATIO = 1.05  # relative Frobenius ID error at the same rank, GPU / oracle (un-squared)
+FLOOR = 1e-24  # squared errors below this are rounding noise of an exact-rank ID
+
+
+def same_rank_ratio(A64, perm, T, k, b, tol, seed, o=None):
+    """(GPU error / oracle error at the GPU's rank, un-squared; oracle run; how)."""
+    o = o or rbrp_column_id(A64, b, tol=tol, seed=seed)
+    n = A64.shape[1]
+    e = id_error(A64, perm, T) if 0 < k < n else (0.0 if k == n else 1.0)
+    e_ref, how = error_at_rank(A64, k, b, tol=tol, seed=seed, run=o)
+    return float(np.sqrt(max(e, FLOOR) / max(e_ref, FLOOR))), o, how
+
+
+def check_problem(A64, perm, T, k, err_est, tol, b, seed):
     n = A64.shape[1]
     assert sorted(perm.tolist()) == list(range(n))
-    e = id_error(A64, perm, T) if 0 < k < n else (0.0 if k == n else 1.0)
-    assert e <= 1.05 * max(e_ref, tol), (e, e_ref, k, o["k"])
+    ratio, o, how = same_rank_ratio(A64, perm, T, k, b, tol, seed)
+    assert ratio <= RATIO, (ratio, how, k, o["k"])
     assert err_est <= tol or k == min(A64.shape), (err_est, k)
-    assert abs(k - o["k"]) <= (kslack or b), (k, o["k"])
     k1 = int(o["ranks"][0]) if len(o["ranks"]) else 0
     assert np.array_equal(perm[:k1], o["perm"][:k1]), (perm[:k1], o["perm"][:k1])
     return o
@@ -105,6 +117,61 @@ def test_batched_uneven_shapes_to_2048(handle):
         e = id_error(A64, perm, res.Ts[q].cpu().numpy())
         assert e <= 1.05 * tol, (q, A.shape, k, e)
         np.testing.assert_allclose(res.res0[q], (A64 ** 2).sum(), rtol=1e-6)
+
+
+def headline_sample(count, seed=0):
+    """A seeded sample of the headline workload's blocks: (block ids, FP32 matrices)."""
+    shapes = W.kernel_block_shapes(4096, 64, 2048, seed)
+    ids = np.sort(np.random.default_rng(1000 + seed).choice(4096, size=count, replace=False))
+    return ids, [W.kernel_block_scaled(int(shapes[q][0]), int(shapes[q][1]), int(q), 0.5, seed) for q in ids]
+
+
+def test_headline_blocks_match_oracle_at_same_rank(handle):
+    """64 seeded blocks of the 4096-block workload (squared tol 1e-8, b = 16), each
+    against the oracle on the same FP32 values with the same Philox key: error
+    within 1.05x of the oracle's at the same rank for every block, the oracle's
+    rank and ordered skeleton for all but a few, and the first block always."""
+    tol, b = 1e-8, 16
+    ids, mats = headline_sample(64)
+    _, res = run_batch(handle, mats, b=b, tol=tol, seed=0)
+    assert (res.status == 0).all()
+    same_k = same_S = 0
+    worst = (0.0, None)
+    for j, A in enumerate(mats):
+        A64 = A.astype(np.float64)
+        k, perm = int(res.k[j]), res.perms[j].cpu().numpy()
+        ratio, o, how = same_rank_ratio(A64, perm, res.Ts[j].cpu().numpy(), k, b, tol, j)
+        worst = max(worst, (ratio, (int(ids[j]), A.shape, k, o["k"], how)))
+        same_k += k == o["k"]
+        same_S += k == o["k"] and np.array_equal(perm[:k], o["perm"][:k])
+        k1 = int(o["ranks"][0])
+        assert np.array_equal(perm[:k1], o["perm"][:k1]), (ids[j], perm[:k1], o["perm"][:k1])
+    assert worst[0] <= RATIO, worst
+    assert same_k >= 61 and same_S >= 58, (same_k, same_S)
+
+
+def test_headline_blocks_tol_1e12_same_rank(handle):
+    """The same sample at squared tol 1e-12 (relative Frobenius 1e-6), the
+    tolerance of the throughput target: every ID meets it, and where the FP32
+    residual still resolves the weights the trajectory is the oracle's.  At
+    this tolerance the trailing weights sit near FP32 resolution and a few
+    trajectories part late; those are compared by their own errors (below the
+    tolerance), the rest at the same rank."""
+    tol, b = 1e-12, 16
+    ids, mats = headline_sample(64)
+    _, res = run_batch(handle, mats, b=b, tol=tol, seed=0, t_rank_cap=256)
+    assert (res.status == 0).all()
+    same = []
+    for j, A in enumerate(mats):
+        A64 = A.astype(np.float64)
+        k, perm = int(res.k[j]), res.perms[j].cpu().numpy()
+        e = id_error(A64, perm, res.Ts[j].cpu().numpy())
+        assert e <= tol, (ids[j], k, e)
+        ratio, o, how = same_rank_ratio(A64, perm, res.Ts[j].cpu().numpy(), k, b, tol, j)
+        if k == o["k"] and np.array_equal(perm[:k], o["perm"][:k]):
+            same.append(ratio)
+    assert len(same) >= 54, len(same)
+    assert max(same) <= RATIO, max(same)
 
 
 def test_batched_replay_is_bit_exact(handle):

@@ -15,7 +15,7 @@ import pytest
 
 torch = pytest.importorskip("torch")
 
-from oracle import id_error, interp_sid, rbrp_column_id  # noqa: E402
+from oracle import error_at_rank, id_error, interp_sid, rbrp_column_id  # noqa: E402
 from robust_blockwise_random_pivoting_gb300 import workloads as W  # noqa: E402
 
 pytestmark = pytest.mark.gpu
@@ -140,17 +140,20 @@ def test_zero_matrix_and_tiny_shapes(handle):
 
 
 def _mixed_vs_fp64(handle, A, b, tol, kslack):
-    """FP32 residual-form run against the FP64 oracle on the same (FP32-rounded) matrix."""
+    """FP32 residual-form run against the FP64 oracle on the same (FP32-rounded)
+    matrix: the relative Frobenius error within 1.05x of the oracle's at the
+    GPU's rank (``oracle.error_at_rank``), the first block's columns equal."""
     A32 = A.astype(np.float32).astype(np.float64)
     o = rbrp_column_id(A32, b, tol=tol, seed=0)
-    e_ref = id_error(A32, o["perm"], interp_sid(A32, o["perm"], o["k"]))
     r = handle.column_id(dev(A, torch.float32), b=b, tol=tol, seed=0)
     perm = r.perm.cpu().numpy()
     assert sorted(perm.tolist()) == list(range(A.shape[1]))
     e_gpu = id_error(A32, perm, r.T.cpu().numpy())
-    # the stop rule sees exact residual norms, so the ID error sits at the tolerance
-    assert e_gpu <= 1.05 * max(e_ref, tol), (e_gpu, e_ref, r.k, o["k"])
+    e_same, how = error_at_rank(A32, r.k, b, tol=tol, seed=0, run=o)
+    assert np.sqrt(e_gpu) <= 1.05 * np.sqrt(e_same), (e_gpu, e_same, how, r.k, o["k"])
     assert r.err_est <= tol and abs(r.k - o["k"]) <= kslack, (r.k, o["k"])
+    k1 = int(o["ranks"][0])
+    assert np.array_equal(perm[:k1], o["perm"][:k1])
     np.testing.assert_allclose(handle.id_error(dev(A, torch.float32)), e_gpu, rtol=1e-4)
     return r, o
 
@@ -171,6 +174,30 @@ def test_fp32_mixed_gmm_clusters(handle):
     assert len(set(labels[r.perm[: r.k].cpu().numpy()].tolist())) == 12
 
 
+def test_gmm65k_full_size_coverage_matches_oracle(handle):
+    """The full imbalanced-mixture workload (1024 x 65536, 20 clusters of 2^-c weight,
+    b = 32, squared tol 1e-4) on its FP32 values.  The oracle itself covers 17 of
+    the 20 clusters at k = 1023: the five last clusters are single points, each
+    drawn with ~2e-4 of the weight per draw, and at rank 1023 of 1024 the span
+    already holds them.  The FP64 form reproduces the oracle's skeleton bit for
+    bit (so its coverage too); the mixed form covers as many clusters and meets
+    the same-rank error bound."""
+    A, labels = W.gmm(1024, 65536, 20, 0)
+    A32 = A.astype(np.float32).astype(np.float64)
+    o = rbrp_column_id(A32, 32, tol=1e-4, seed=0)
+    cover = lambda S: len(set(labels[S].tolist()))
+    r = handle.column_id(dev(A32), b=32, tol=1e-4, seed=0)
+    assert r.k == o["k"] and np.array_equal(r.ranks, o["ranks"])
+    assert np.array_equal(r.perm.cpu().numpy()[: r.k], o["perm"][: o["k"]])
+    assert cover(o["perm"][: o["k"]]) == 17
+    rm = handle.column_id(dev(A, torch.float32), b=32, tol=1e-4, seed=0)
+    pm = rm.perm.cpu().numpy()
+    assert cover(pm[: rm.k]) == cover(o["perm"][: o["k"]])
+    e_gpu = handle.id_error(dev(A, torch.float32))
+    e_same, how = error_at_rank(A32, rm.k, 32, tol=1e-4, seed=0, run=o)
+    assert np.sqrt(e_gpu) <= 1.05 * np.sqrt(e_same), (e_gpu, e_same, how, rm.k, o["k"])
+
+
 def test_tensor_core_projection_matches_cuda_core(handle):
     """The tcgen05 projection (3xTF32) against the CUDA-core one on the same FP32 matrix.
 
@@ -183,7 +210,6 @@ def test_tensor_core_projection_matches_cuda_core(handle):
     A32 = dev(A, torch.float32)
     A32h = A.astype(np.float32).astype(np.float64)
     o = rbrp_column_id(A32h, 64, tol=tol, seed=0)
-    e_ref = id_error(A32h, o["perm"], interp_sid(A32h, o["perm"], o["k"]))
     runs = {}
     for variant in (1, 0):
         handle.set_variant(variant)
@@ -193,7 +219,8 @@ def test_tensor_core_projection_matches_cuda_core(handle):
             handle.set_variant(0)
         runs[variant] = (r, handle.id_error(A32))
     for variant, (r, e) in runs.items():
-        assert r.err_est <= tol and e <= 1.05 * max(e_ref, tol), (variant, r.k, e, e_ref)
+        e_same, how = error_at_rank(A32h, r.k, 64, tol=tol, seed=0, run=o)
+        assert r.err_est <= tol and np.sqrt(e) <= 1.05 * np.sqrt(e_same), (variant, r.k, e, e_same, how)
         assert abs(r.k - o["k"]) <= 64, (variant, r.k, o["k"])
     assert abs(runs[0][0].k - runs[1][0].k) <= 64
     # the first block (before any accumulated difference) selects the same columns

@@ -49,6 +49,29 @@ def test_noalloc_id_error_matches_handle_entry_point(rbrp_lib):
                 np.testing.assert_allclose(out.item(), e_ref, rtol=RTOL, atol=1e-300)
 
 
+def test_noalloc_empty_and_full_skeletons(rbrp_lib):
+    """k == 0 and k == n are valid IDs: 1.0 and 0.0, as the handle's entry point reports them."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from robust_blockwise_random_pivoting_gb300.rbrp import Handle
+    stream = torch.cuda.current_stream()
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    A = torch.from_numpy(W.gaussian_exp(40, 30, decay=3.0, seed=5)).cuda().t().contiguous().t()
+    with Handle(0) as h:
+        r = h.column_id(A, b=8, tol=0.0, seed=0)          # full rank: k == n
+        assert r.k == A.shape[1]
+        e_full = h.id_error(A)
+    perm = r.perm
+    T = torch.zeros((0, 0), dtype=torch.float64, device="cuda")
+    for k, want in ((0, 1.0), (A.shape[1], e_full)):
+        for _ in range(2):
+            out.fill_(-1.0)
+            assert _noalloc(rbrp_lib, A, perm, k, T, r.res0, out, stream) == 0
+            torch.cuda.synchronize()
+            assert out.item() == want, (k, out.item(), want)
+    assert e_full == 0.0
+
+
 def test_noalloc_rejects_sizes_beyond_scratch(rbrp_lib):
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
