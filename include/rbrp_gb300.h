@@ -176,6 +176,22 @@ rbrp_status rbrp_CPQR(int m, int n, const double* dA, const int* ranks, int nran
 rbrp_status rbrp_copy_T(rbrp_handle h, double* dT, int64_t ldt);
 /* Device pointer of T of the last run (ld = k), valid until the next run. */
 rbrp_status rbrp_T_device(rbrp_handle h, const double** dT, int* ld);
+/* python/RBRP.ipynb cell 2 lines 111-126 (matdivide, A * pinv(B) from the SVD of
+ * B, singular values above the absolute cutoff tol kept; TOL_FP = 1e-12, cell 0
+ * line 26), which get_rpid_error uses for the interpolation matrix of blocked
+ * runs (cell 11 lines 226-232): X (q x nc, ldx >= q) = pinv_tol(B) C for B
+ * (p x q, ldb >= p) and C (p x nc, ldc >= p), FP64 device arrays.  The SVD is a
+ * one-sided Jacobi iteration in FP64; *rank (may be NULL) receives the number of
+ * singular values above tol.  The notebook's matdivide(A2, B2) is X^T for
+ * B = B2^T, C = A2^T.  Runs on the handle's stream and returns when done. */
+rbrp_status rbrp_matdivide_f64(rbrp_handle h, int p, int q, int nc, const double* dB, int64_t ldb,
+                               const double* dC, int64_t ldc, double tol, double* dX, int64_t ldx, int* rank);
+/* T of the last run replaced by pinv_tol(R11) R12 (rbrp_matdivide_f64 on the
+ * run's factor): the rank-revealing interpolation for a skeleton whose R11 is
+ * ill-conditioned or singular (a fixed skeleton given from outside).  Equal to
+ * R11^{-1} R12 when every singular value of R11 exceeds tol.  rbrp_copy_T /
+ * rbrp_T_device then return it. */
+rbrp_status rbrp_T_matdivide(rbrp_handle h, double tol, int* rank);
 /* Per-block trace of the last run: cumulative ranks and squared relative
  * residual estimates (gpu/rbrp.cu:467, 473-475) and cumulative device time per
  * block in ms.  Host arrays of capacity cap; *nblocks receives the count. */

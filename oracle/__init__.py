@@ -20,6 +20,7 @@ from .rbrp_oracle import (
     interp_r11,
     id_error,
     error_at_rank,
+    matdivide,
 )
 
 __all__ = [
@@ -35,4 +36,5 @@ __all__ = [
     "interp_r11",
     "id_error",
     "error_at_rank",
+    "matdivide",
 ]

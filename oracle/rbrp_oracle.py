@@ -147,6 +147,10 @@ def rbrp_column_id(A, b, tol=None, kmax=None, seed=0, sampler="np", mode="rp",
     ``'gp'`` (greedy top-b, cell 11 line 112).  ``sampler_impl='numpy'`` calls
     ``rng.choice`` itself instead of the restatement.
 
+    The per-block trace ``blocks`` holds, for each sampled panel, its positions
+    ``js``, the LAPACK pivots ``piv``, the kept count ``bs`` and ``cols_piv``, the
+    panel's original columns in pivot order.
+
     Returns a dict with ``perm`` (position -> original column), ``k``, ``ranks``
     (cumulative per block), ``residuals`` (relative squared residual per
     block), ``Q`` (m x k), ``R`` (k x n, indexed by original column, with the
@@ -205,7 +209,8 @@ def rbrp_column_id(A, b, tol=None, kmax=None, seed=0, sampler="np", mode="rp",
             V = AJ - Q[:, :i] @ (Q[:, :i].T @ AJ)
         QV, RV, pV = spla.qr(V, mode="economic", pivoting=True)
         bs = local_clip(RV, tol_loc)
-        blocks.append(dict(i=i, js=js.copy(), bs_sampled=bs_sampled, piv=pV.copy(), bs=bs))
+        blocks.append(dict(i=i, js=js.copy(), bs_sampled=bs_sampled, piv=pV.copy(), bs=bs,
+                           cols_piv=perm[js[pV]].copy()))
         t += 1
         if bs == 0:
             # numerically zero panel: these columns carry no residual
@@ -286,10 +291,14 @@ def error_at_rank(A, k, b, tol=None, seed=0, sampler="np", mode="rp", run=None):
     boundary: later block swaps never move positions below the current rank, so
     its final ``perm[:k_t]`` is the skeleton after the block that reached
     ``k_t``.  When ``k`` is such a boundary (or the final rank), the error is
-    that skeleton's; otherwise the run is repeated with ``kmax = k``, whose
-    last block samples only the columns still missing.
+    that skeleton's ("boundary").  When ``k`` falls inside a block's sampled
+    panel (``k_t < k <= k_t + sampled``), which is where a robust-filter
+    decision near its threshold keeps one pivot more or fewer, the skeleton is
+    ``perm[:k_t]`` plus the panel's first ``k - k_t`` pivots ("panel").
+    Otherwise the run is repeated with ``kmax = k``, whose last block samples
+    only the columns still missing ("capped").
 
-    Returns ``(error, how)`` with ``how`` in ``{"boundary", "capped"}``.
+    Returns ``(error, how)`` with ``how`` in ``{"boundary", "panel", "capped"}``.
     """
     A = np.asarray(A, dtype=np.float64)
     n = A.shape[1]
@@ -301,7 +310,28 @@ def error_at_rank(A, k, b, tol=None, seed=0, sampler="np", mode="rp", run=None):
         return 0.0, "boundary"
     bounds = set(int(x) for x in run["ranks"]) | {int(run["k"])}
     if k in bounds:
-        perm, how = run["perm"], "boundary"
-    else:
-        perm, how = rbrp_column_id(A, b, tol=None, kmax=k, seed=seed, sampler=sampler, mode=mode)["perm"], "capped"
-    return id_error(A, perm, interp_sid(A, perm, k)), how
+        return id_error(A, run["perm"], interp_sid(A, run["perm"], k)), "boundary"
+    # the block that started at the largest boundary below k (the one in progress at rank k)
+    starts = [blk for blk in run["blocks"] if int(blk["i"]) < k]
+    if starts:
+        blk = max(starts, key=lambda x: int(x["i"]))
+        i0, cols = int(blk["i"]), blk["cols_piv"]
+        if k <= i0 + len(cols):
+            S = np.concatenate([run["perm"][:i0], cols[: k - i0]])
+            perm = np.concatenate([S, np.setdiff1d(np.arange(n), S)])
+            return id_error(A, perm, interp_sid(A, perm, k)), "panel"
+    perm = rbrp_column_id(A, b, tol=None, kmax=k, seed=seed, sampler=sampler, mode=mode)["perm"]
+    return id_error(A, perm, interp_sid(A, perm, k)), "capped"
+
+
+def matdivide(A, B, tol=1e-12):
+    """``A * pinv(B)`` from the SVD of B, keeping singular values above the absolute
+    cutoff ``tol``: restates ``matdivide`` (``python/RBRP.ipynb`` cell 2 lines
+    111-126; ``TOL_FP = 1e-12``, cell 0 line 26).  A (m x n), B (k x n); returns
+    ``(X, r)`` with X (m x k) and r the number of singular values kept."""
+    A = np.asarray(A, dtype=np.float64)
+    B = np.asarray(B, dtype=np.float64)
+    U, s, Vh = spla.svd(B, full_matrices=False)
+    r = int(np.count_nonzero(s > tol))
+    aux = (A @ Vh[:r].T) / s[:r].reshape(1, -1)
+    return aux @ U[:, :r].T, r

@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "librbrp_gb300.so")
 SOURCES = ["rbrp_capi.cu", "rbrp_f64.cu", "rbrp_f32.cu", "rbrp_noalloc.cu", "rbrp_batched.cu",
-           "rbrp_adjoint.cu", "rbrp_sketch.cu", "rbrp_lupp.cu", "rbrp_compare.cu"]
+           "rbrp_adjoint.cu", "rbrp_sketch.cu", "rbrp_lupp.cu", "rbrp_compare.cu", "rbrp_matdivide.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr",
            "-Xptxas", "-warn-spills"]

@@ -767,6 +767,8 @@ rbrp_status rbrp_destroy(rbrp_handle h) {
     if (h->adj_ws) cudaFree(h->adj_ws);
     if (h->sketch_ws) cudaFree(h->sketch_ws);
     if (h->lupp_ws) cudaFree(h->lupp_ws);
+    if (h->md_ws) cudaFree(h->md_ws);
+    if (h->md_aux) cudaFree(h->md_aux);
     if (h->hst) cudaFreeHost(h->hst);
     for (auto e : h->block_events) cudaEventDestroy(e);
     for (auto e : h->prof_events) cudaEventDestroy(e);

@@ -81,6 +81,12 @@ struct rbrp_handle_st {
   void* lupp_ws = nullptr;
   size_t lupp_bytes = 0;
 
+  // truncated-SVD interpolation (rbrp_matdivide.cu): Jacobi workspace, R11 | R12 operands
+  void* md_ws = nullptr;
+  size_t md_bytes = 0;
+  void* md_aux = nullptr;
+  size_t md_aux_bytes = 0;
+
   // fixed-skeleton adjoint workspace (rbrp_adjoint.cu)
   void* adj_ws = nullptr;
   size_t adj_bytes = 0;

@@ -168,6 +168,15 @@ class Handle:
             check(self.lib.rbrp_copy_T(self.h, ctypes.c_void_p(out.data_ptr()), k), self.h)
         return out
 
+    def T_matdivide(self, tol=1e-12):
+        """T of the last run as pinv_tol(R11) R12 (the notebook's ``matdivide``, python/RBRP.ipynb
+        cell 2 lines 111-126): returns ``(T, rank)``, T a (k, n-k) column-major FP64 CUDA tensor
+        and rank the number of singular values of R11 above ``tol``.  Later ``T()`` calls
+        return the same matrix until the next run."""
+        rank = ctypes.c_int()
+        check(self.lib.rbrp_T_matdivide(self.h, float(tol), ctypes.byref(rank)), self.h)
+        return self.T(), rank.value
+
     def set_profiling(self, on=True):
         """Bracket every phase with CUDA events (accumulated until reset)."""
         check(self.lib.rbrp_set_profiling(self.h, int(bool(on))), self.h)

@@ -139,3 +139,24 @@ def interpolation(A, perm, k, mode="sid", oversampling=1.0, seed=0, handle=None)
         raise ValueError(f"mode {mode!r}: 'sid' or 'fsid' (the RBRP run's own T is 'id')")
     perm_run, T_run = fixed_skeleton(h, B, S, b=64)
     return _reorder(perm_run, T_run, S, rd)
+
+
+def matdivide(A, B, tol=1e-12, handle=None):
+    """``A * pinv(B)`` with the singular values of B above ``tol`` kept: the notebook's
+    ``matdivide(A, B, tol=TOL_FP)`` (``python/RBRP.ipynb`` cell 2 lines 111-126) on CUDA
+    tensors, A (m x n), B (k x n), result (m x k) FP64.  Returns ``(X, rank)``.  The SVD
+    is the library's FP64 one-sided Jacobi (``rbrp_matdivide_f64`` on B^T and A^T)."""
+    h = handle or Handle(A.device.index)
+    Bt = _cm(B.t(), torch.float64)          # (n x k): the matrix whose pseudo-inverse is taken
+    At = _cm(A.t(), torch.float64)          # (n x m)
+    n, k = Bt.shape
+    m = At.shape[1]
+    if At.shape[0] != n:
+        raise ValueError("A and B need the same number of columns")
+    X = torch.empty((m, k), dtype=torch.float64, device=A.device).t()   # (k x m) column major
+    rank = ctypes.c_int()
+    h._bind_stream(torch.cuda.current_stream(A.device))
+    check(h.lib.rbrp_matdivide_f64(h.h, n, k, m, ctypes.c_void_p(Bt.data_ptr()), _ld(Bt),
+                                   ctypes.c_void_p(At.data_ptr()), _ld(At), float(tol),
+                                   ctypes.c_void_p(X.data_ptr()), _ld(X), ctypes.byref(rank)), h.h)
+    return X.t(), rank.value

@@ -139,6 +139,12 @@ def test_zero_matrix_and_tiny_shapes(handle):
     check_against_oracle(handle, np.arange(1.0, 8.0).reshape(7, 1), 4, 1e-12)
 
 
+# FP32 resolution of an ID computed from FP32 data (u = 2^-24): squared errors of the
+# mixed form are compared as e <= 1.05^2 e_ref + (4u)^2; where the oracle's error at
+# that rank is below (4u)^2 (exact or full rank) the rank must match and e <= tol
+FP32_FLOOR_SQ = (4 * 2.0 ** -24) ** 2
+
+
 def _mixed_vs_fp64(handle, A, b, tol, kslack):
     """FP32 residual-form run against the FP64 oracle on the same (FP32-rounded)
     matrix: the relative Frobenius error within 1.05x of the oracle's at the
@@ -150,7 +156,12 @@ def _mixed_vs_fp64(handle, A, b, tol, kslack):
     assert sorted(perm.tolist()) == list(range(A.shape[1]))
     e_gpu = id_error(A32, perm, r.T.cpu().numpy())
     e_same, how = error_at_rank(A32, r.k, b, tol=tol, seed=0, run=o)
-    assert np.sqrt(e_gpu) <= 1.05 * np.sqrt(e_same), (e_gpu, e_same, how, r.k, o["k"])
+    if e_same <= FP32_FLOOR_SQ:
+        # exact (or full) rank in FP32 terms: the oracle's error is 0 to FP32 resolution and
+        # the GPU's is set by the FP32 data of T; the same rank and the tolerance must hold
+        assert r.k == o["k"] and e_gpu <= max(tol, FP32_FLOOR_SQ), (e_gpu, r.k, o["k"])
+    else:
+        assert e_gpu <= 1.05 ** 2 * e_same + FP32_FLOOR_SQ, (e_gpu, e_same, how, r.k, o["k"])
     assert r.err_est <= tol and abs(r.k - o["k"]) <= kslack, (r.k, o["k"])
     k1 = int(o["ranks"][0])
     assert np.array_equal(perm[:k1], o["perm"][:k1])
@@ -195,7 +206,7 @@ def test_gmm65k_full_size_coverage_matches_oracle(handle):
     assert cover(pm[: rm.k]) == cover(o["perm"][: o["k"]])
     e_gpu = handle.id_error(dev(A, torch.float32))
     e_same, how = error_at_rank(A32, rm.k, 32, tol=1e-4, seed=0, run=o)
-    assert np.sqrt(e_gpu) <= 1.05 * np.sqrt(e_same), (e_gpu, e_same, how, rm.k, o["k"])
+    assert e_gpu <= 1.05 ** 2 * e_same + FP32_FLOOR_SQ, (e_gpu, e_same, how, rm.k, o["k"])
 
 
 def test_tensor_core_projection_matches_cuda_core(handle):
@@ -220,7 +231,7 @@ def test_tensor_core_projection_matches_cuda_core(handle):
         runs[variant] = (r, handle.id_error(A32))
     for variant, (r, e) in runs.items():
         e_same, how = error_at_rank(A32h, r.k, 64, tol=tol, seed=0, run=o)
-        assert r.err_est <= tol and np.sqrt(e) <= 1.05 * np.sqrt(e_same), (variant, r.k, e, e_same, how)
+        assert r.err_est <= tol and e <= 1.05 ** 2 * e_same + FP32_FLOOR_SQ, (variant, r.k, e, e_same, how)
         assert abs(r.k - o["k"]) <= 64, (variant, r.k, o["k"])
     assert abs(runs[0][0].k - runs[1][0].k) <= 64
     # the first block (before any accumulated difference) selects the same columns
