@@ -812,7 +812,7 @@ __device__ void project_update_resident(BatchSmem<BB>& sm, int m, int n, int i, 
   for (int g = 0; g < ngroups; ++g) {
     const int p = p_first + g * stride, nc = min(CW, n - p);
     // projection: W(a, j) = sum_r q_a(r) x_j(r), FP32 stage sums folded into double-float
-    // (FP32 sums of a lane's 8 rows, two stages, are folded at a time)
+    // (FP32 sums of a lane's 16 rows, four stages, are folded at a time)
     float hi[16], lo[16], c[16];
 #pragma unroll
     for (int v = 0; v < 16; ++v) hi[v] = lo[v] = c[v] = 0.f;
@@ -822,7 +822,7 @@ __device__ void project_update_resident(BatchSmem<BB>& sm, int m, int n, int i, 
       float x[4][CW];
       fetch(t, x);
       const int r0 = s * BROWS + 4 * lane;
-      const bool fold = (s & 1) || s == nst - 1;
+      const bool fold = (s & 3) == 3 || s == nst - 1;
 #pragma unroll
       for (int a = 0; a < KA; ++a) {
         if (a < kept) {
@@ -853,11 +853,12 @@ __device__ void project_update_resident(BatchSmem<BB>& sm, int m, int n, int i, 
 #pragma unroll
       for (int j = 0; j < CW; ++j) w[a][j] = __shfl_sync(0xffffffffu, wsum.hi, 2 * (a * CW + j));
     // update X -= Q W into A_res; squared norms of the updated columns: FP32
-    // sums of each lane's 4 squares (positive terms, relative error < 3e-7),
-    // folded into double-float
+    // sums of each lane's 8 squares, two stages (positive terms, relative error
+    // < 5e-7), folded into double-float
     DF nrm[CW];
+    float sq[CW];
 #pragma unroll
-    for (int j = 0; j < CW; ++j) nrm[j].hi = nrm[j].lo = 0.f;
+    for (int j = 0; j < CW; ++j) nrm[j].hi = nrm[j].lo = sq[j] = 0.f;
     for (int s = 0; s < nst; ++s, ++t) {
       ring_issue<CW>(is, total, nst, p_first, stride, n, m, first, vec, A, lda, perm, Ares, ld, ring);
       cp_async_wait<RING_D - 1>();
@@ -896,7 +897,14 @@ __device__ void project_update_resident(BatchSmem<BB>& sm, int m, int n, int i, 
               if (u < valid) dst[u] = y[u];
           }
           // rows >= m give y = 0 (zero-filled x, zero basis rows)
-          fold_two_sum(nrm[j].hi, nrm[j].lo, fmaf(y[3], y[3], fmaf(y[2], y[2], fmaf(y[1], y[1], y[0] * y[0]))));
+          sq[j] = fmaf(y[3], y[3], fmaf(y[2], y[2], fmaf(y[1], y[1], fmaf(y[0], y[0], sq[j]))));
+        }
+      }
+      if ((s & 1) || s == nst - 1) {
+#pragma unroll
+        for (int j = 0; j < CW; ++j) {
+          fold_two_sum(nrm[j].hi, nrm[j].lo, sq[j]);
+          sq[j] = 0.f;
         }
       }
     }
