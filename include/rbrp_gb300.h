@@ -192,6 +192,20 @@ rbrp_status rbrp_matdivide_f64(rbrp_handle h, int p, int q, int nc, const double
  * R11^{-1} R12 when every singular value of R11 exceeds tol.  rbrp_copy_T /
  * rbrp_T_device then return it. */
 rbrp_status rbrp_T_matdivide(rbrp_handle h, double tol, int* rank);
+/* FP64 iterative refinement of the last run's T against the matrix A it was
+ * computed from (same m, n; device, column major, lda): each of `steps` steps
+ * is T += pinv(A_S) (A(:, rd) - A(:, S) T), in FP64 on the exact values of A
+ * (A_S and A(:, rd) gathered through perm, the pseudo-inverse by the Jacobi SVD
+ * of rbrp_matdivide_f64 with singular values below max(tol, max(m, k) eps
+ * |A_S|_F) dropped).  It recovers the least-squares T of the skeleton where the
+ * factor's R11 is ill-conditioned.  *change (may be NULL) receives |dT|_F/|T|_F
+ * of the last step.  The precision scheme of the mixed form (FP32 data) with
+ * "FP64 iterative refinement of T"; no counterpart in gpu/ (the reference's T
+ * is one triangular solve, gpu/id_cpqr.cu:133-136). */
+rbrp_status rbrp_refine_T_f64(rbrp_handle h, int m, int n, const double* dA, int64_t lda, int steps,
+                              double tol, double* change);
+rbrp_status rbrp_refine_T_f32(rbrp_handle h, int m, int n, const float* dA, int64_t lda, int steps,
+                              double tol, double* change);
 /* Per-block trace of the last run: cumulative ranks and squared relative
  * residual estimates (gpu/rbrp.cu:467, 473-475) and cumulative device time per
  * block in ms.  Host arrays of capacity cap; *nblocks receives the count. */

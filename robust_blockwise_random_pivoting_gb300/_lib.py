@@ -105,6 +105,10 @@ _SIGS = {
     "rbrp_matdivide_f64": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_int64, c_void_p, c_int64, c_double,
                                    c_void_p, c_int64, ctypes.POINTER(c_int)]),
     "rbrp_T_matdivide": (c_int, [c_void_p, c_double, ctypes.POINTER(c_int)]),
+    "rbrp_refine_T_f64": (c_int, [c_void_p, c_int, c_int, c_void_p, c_int64, c_int, c_double,
+                                  ctypes.POINTER(c_double)]),
+    "rbrp_refine_T_f32": (c_int, [c_void_p, c_int, c_int, c_void_p, c_int64, c_int, c_double,
+                                  ctypes.POINTER(c_double)]),
     "rbrp_id_error_f64_noalloc": (c_int, [c_int, c_int, c_void_p, c_int64, c_void_p, c_int, c_void_p, c_int64,
                                           c_double, c_void_p, c_void_p]),
     "rbrp_fixed_id_f32": (c_int, [c_void_p, c_int, c_int, c_void_p, c_int64, c_void_p, c_int, c_int, c_void_p,

@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <vector>
 
 #include "rbrp_internal.h"
 
@@ -205,6 +206,47 @@ __global__ void __launch_bounds__(256) k_md_gemm(const double* __restrict__ X, i
   }
 }
 
+// Columns perm[c0 + c] of A (m x ?, ld lda), c < nc, as an FP64 column-major
+// matrix (m x nc, ld m): exact for FP32 and FP64 A.
+template <typename T>
+__global__ void k_md_gather(const T* __restrict__ A, int64_t lda, const int* __restrict__ perm, int c0, int m,
+                            int nc, double* __restrict__ out) {
+  const int64_t total = (int64_t)m * nc;
+  for (int64_t z = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; z < total; z += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = z / m, r = z % m;
+    out[z] = (double)A[r + (int64_t)perm[c0 + c] * lda];
+  }
+}
+
+// y = x - y (elementwise, n entries)
+__global__ void k_md_xmy(const double* __restrict__ x, double* __restrict__ y, int64_t n) {
+  for (int64_t z = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; z < n; z += (int64_t)gridDim.x * blockDim.x)
+    y[z] = x[z] - y[z];
+}
+
+// T += D (k x nc, T with leading dimension ldt, D with k); partial sums of |D|^2 and |T|^2
+// per CTA into parts[2 * blockIdx.x + {0, 1}] (fixed order).
+__global__ void __launch_bounds__(256) k_md_add(double* __restrict__ T, int64_t ldt, const double* __restrict__ D,
+                                                int k, int nc, double* __restrict__ parts) {
+  __shared__ double red[32];
+  const int64_t total = (int64_t)k * nc;
+  double dd = 0.0, tt = 0.0;
+  for (int64_t z = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; z < total; z += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = z / k, r = z % k;
+    const double d = D[z];
+    const double t = T[r + c * ldt] + d;
+    T[r + c * ldt] = t;
+    dd = fma(d, d, dd);
+    tt = fma(t, t, tt);
+  }
+  dd = block_sum(dd, red);
+  tt = block_sum(tt, red);
+  if (threadIdx.x == 0) {
+    parts[2 * blockIdx.x] = dd;
+    parts[2 * blockIdx.x + 1] = tt;
+  }
+}
+
 }  // namespace
 }  // namespace rbrp
 
@@ -336,4 +378,83 @@ extern "C" rbrp_status rbrp_T_matdivide(rbrp_handle h, double tol, int* rank) {
   rbrp_status s = cuda_check(h, cudaGetLastError(), "matdivide gather");
   if (s != RBRP_OK) return s;
   return matdivide(h, k, k, nc, R11, k, R12, k, tol, h->T, k, rank);
+}
+
+namespace rbrp {
+
+// One or more refinement steps of the last run's T against the matrix A it was
+// computed from: T += pinv(A_S) (A_rd - A_S T), in FP64 on the exact values of A.
+template <typename T>
+rbrp_status refine_T(rbrp_handle h, int m, int n, const T* dA, int64_t lda, int steps, double tol, double* change) {
+  if (!h || !dA || lda < m || steps < 1 || !(tol >= 0.0) || !std::isfinite(tol)) return RBRP_ERR_INVALID_ARG;
+  if (!h->have_result) return set_error(h, RBRP_ERR_NOT_COMPUTED, "no successful run");
+  if (m != h->m || n != h->n) return set_error(h, RBRP_ERR_INVALID_ARG, "shape differs from the last run");
+  const int k = h->k, nc = n - k;
+  if (change) *change = 0.0;
+  if (k <= 0 || nc <= 0) return RBRP_OK;  // T is empty
+  if (!h->T) return set_error(h, RBRP_ERR_NOT_COMPUTED, "T was not computed");
+  DeviceGuard g(h->device);
+  // operands: A_S (m x k) | A_rd (m x nc) | E (m x nc) | D (k x nc) | CTA partials
+  constexpr int NP = 512;
+  const size_t bytes = ((size_t)m * k + 2 * (size_t)m * nc + (size_t)k * nc + 2 * NP) * sizeof(double);
+  if (h->md_aux_bytes < bytes) {
+    if (h->md_aux) cudaFree(h->md_aux);
+    h->md_aux = nullptr;
+    h->md_aux_bytes = 0;
+    rbrp_status s = cuda_check(h, cudaMalloc(&h->md_aux, bytes), "cudaMalloc(refinement operands)");
+    if (s != RBRP_OK) return s;
+    h->md_aux_bytes = bytes;
+  }
+  double* As = static_cast<double*>(h->md_aux);
+  double* Ard = As + (size_t)m * k;
+  double* E = Ard + (size_t)m * nc;
+  double* D = E + (size_t)m * nc;
+  double* parts = D + (size_t)k * nc;
+  cudaStream_t st = h->stream;
+  k_md_gather<T><<<1216, 256, 0, st>>>(dA, lda, h->perm, 0, m, k, As);
+  k_md_gather<T><<<1216, 256, 0, st>>>(dA, lda, h->perm, k, m, nc, Ard);
+  // numerical-rank cutoff of A_S: the caller's, or max(m, k) units of rounding of |A_S|_F
+  k_md_fro<<<1, MD_THREADS, 0, st>>>(As, (int64_t)m * k, parts);
+  double fro2 = 0.0;
+  rbrp_status s = cuda_check(h, cudaGetLastError(), "refinement gather");
+  if (s == RBRP_OK) s = cuda_check(h, cudaMemcpyAsync(&fro2, parts, 8, cudaMemcpyDeviceToHost, st), "norm");
+  if (s == RBRP_OK) s = cuda_check(h, cudaStreamSynchronize(st), "refinement gather");
+  if (s != RBRP_OK) return s;
+  if (!std::isfinite(fro2)) return set_error(h, RBRP_ERR_NUMERIC, "refinement: non-finite entries in A");
+  const double cut = std::max(tol, std::max(m, k) * 2.220446049250313e-16 * std::sqrt(fro2));
+  std::vector<double> hp(2 * NP);
+  for (int it = 0; it < steps; ++it) {
+    // E = A_rd - A_S T
+    k_md_gemm<false><<<dim3((nc + 31) / 32, (m + 31) / 32), 256, 0, st>>>(As, m, h->T, k, nullptr, m, nc, k, E, m);
+    k_md_xmy<<<1216, 256, 0, st>>>(Ard, E, (int64_t)m * nc);
+    s = cuda_check(h, cudaGetLastError(), "refinement residual");
+    if (s != RBRP_OK) return s;
+    // D = pinv(A_S) E, T += D
+    int rank = 0;
+    s = matdivide(h, m, k, nc, As, m, E, m, cut, D, k, &rank);
+    if (s != RBRP_OK) return s;
+    k_md_add<<<NP, 256, 0, st>>>(h->T, k, D, k, nc, parts);
+    s = cuda_check(h, cudaMemcpyAsync(hp.data(), parts, 2 * NP * sizeof(double), cudaMemcpyDeviceToHost, st), "refine");
+    if (s == RBRP_OK) s = cuda_check(h, cudaStreamSynchronize(st), "refinement step");
+    if (s != RBRP_OK) return s;
+    double dd = 0.0, tt = 0.0;
+    for (int z = 0; z < NP; ++z) {
+      dd += hp[2 * z];
+      tt += hp[2 * z + 1];
+    }
+    if (change) *change = tt > 0.0 ? std::sqrt(dd / tt) : 0.0;
+  }
+  return RBRP_OK;
+}
+
+}  // namespace rbrp
+
+extern "C" rbrp_status rbrp_refine_T_f64(rbrp_handle h, int m, int n, const double* dA, int64_t lda, int steps,
+                                         double tol, double* change) {
+  return rbrp::refine_T<double>(h, m, n, dA, lda, steps, tol, change);
+}
+
+extern "C" rbrp_status rbrp_refine_T_f32(rbrp_handle h, int m, int n, const float* dA, int64_t lda, int steps,
+                                         double tol, double* change) {
+  return rbrp::refine_T<float>(h, m, n, dA, lda, steps, tol, change);
 }

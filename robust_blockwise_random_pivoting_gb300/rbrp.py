@@ -177,6 +177,18 @@ class Handle:
         check(self.lib.rbrp_T_matdivide(self.h, float(tol), ctypes.byref(rank)), self.h)
         return self.T(), rank.value
 
+    def refine_T(self, A, steps=1, tol=0.0):
+        """FP64 iterative refinement of the last run's T against ``A`` (the CUDA matrix the run
+        used): each step adds pinv(A_S) (A_rd - A_S T), computed in FP64 on A's exact values.
+        Returns |dT|_F / |T|_F of the last step; ``T()`` then returns the refined T."""
+        A = _colmajor(A)
+        m, n = A.shape
+        ch = ctypes.c_double()
+        fn = self.lib.rbrp_refine_T_f64 if A.dtype == torch.float64 else self.lib.rbrp_refine_T_f32
+        check(fn(self.h, m, n, ctypes.c_void_p(A.data_ptr()), _ld(A), int(steps), float(tol), ctypes.byref(ch)),
+              self.h)
+        return ch.value
+
     def set_profiling(self, on=True):
         """Bracket every phase with CUDA events (accumulated until reset)."""
         check(self.lib.rbrp_set_profiling(self.h, int(bool(on))), self.h)

@@ -1,0 +1,74 @@
+"""GPU: FP64 iterative refinement of T (``rbrp_refine_T_f32`` / ``_f64``).
+
+One step T += pinv(A_S) (A_rd - A_S T), in FP64 on the exact values of A,
+recovers the least-squares T of the run's skeleton (the oracle's SID
+interpolation, python/RBRP.ipynb cell 7 lines 19-22, on the same skeleton)
+where the factor's R11 is ill-conditioned:
+
+* mixed form, FP32 data, a spectrum with a gap (20 singular values in
+  [1e-2, 1], 20 near 1e-5), squared tol 1e-12: kappa(A_S) ~ 1.6e6;
+* FP64 form to squared tol 1e-30 on a gap down to 1e-10: kappa(A_S) ~ 3e10;
+  on this matrix the oracle's own R11^{-1} R12 (one Gram-Schmidt pass, the
+  basis no longer orthogonal) reconstructs only to 1.3e-11 (squared) against
+  9.4e-20 for the least-squares T.
+
+The error at the run's rank is compared before and after the step, with the
+oracle's least-squares error on the same skeleton (the best any T can do),
+and a second step must change T by no more than rounding.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from oracle import id_error, interp_sid  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def handle(rbrp_lib):
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from robust_blockwise_random_pivoting_gb300.rbrp import Handle
+    h = Handle(0)
+    yield h
+    h.close()
+
+
+def with_spectrum(p, q, s, seed):
+    rng = np.random.default_rng(seed)
+    U, _ = np.linalg.qr(rng.standard_normal((p, len(s))))
+    V, _ = np.linalg.qr(rng.standard_normal((q, len(s))))
+    return (U * np.asarray(s)) @ V.T
+
+
+def _before_after(handle, A_dev, A64, b, tol):
+    r = handle.column_id(A_dev, b=b, tol=tol, seed=0)
+    k, perm = r.k, r.perm.cpu().numpy()
+    assert 0 < k < A64.shape[1]
+    e_before = id_error(A64, perm, r.T.cpu().numpy())
+    e_ls = id_error(A64, perm, interp_sid(A64, perm, k))   # least-squares T of this skeleton
+    change = handle.refine_T(A_dev, steps=1)
+    e_after = id_error(A64, perm, handle.T().cpu().numpy())
+    change2 = handle.refine_T(A_dev, steps=1)
+    return k, e_before, e_after, e_ls, change, change2
+
+
+def test_refine_mixed_form_ill_conditioned_skeleton(handle):
+    s = np.concatenate([np.logspace(0, -2, 20), np.logspace(-5, -5.5, 20)])
+    A32 = with_spectrum(300, 400, s, 5).astype(np.float32)
+    A64 = A32.astype(np.float64)
+    Ad = torch.from_numpy(np.asfortranarray(A32)).cuda()
+    k, e0, e1, e_ls, ch, ch2 = _before_after(handle, Ad, A64, 8, 1e-12)
+    assert e1 <= e0 * (1 + 1e-9) and e1 <= 1.01 * e_ls + 1e-30, (k, e0, e1, e_ls)
+    assert ch2 <= 1e-6, ch2
+
+
+def test_refine_fp64_form_one_gram_schmidt_pass_lost_orthogonality(handle):
+    s = np.concatenate([np.logspace(0, -3, 20), np.logspace(-10, -10.5, 20)])
+    A = with_spectrum(120, 160, s, 11)
+    Ad = torch.from_numpy(np.asfortranarray(A)).cuda()
+    k, e0, e1, e_ls, ch, ch2 = _before_after(handle, Ad, A, 8, 1e-30)
+    assert e1 <= e0 * (1 + 1e-9) and e1 <= 1.01 * e_ls + 1e-30, (k, e0, e1, e_ls)
+    assert ch2 <= 1e-6, ch2
