@@ -1067,17 +1067,40 @@ def run_cpqr(args, wl, name, ctx):
 
 
 def run_reference_batched(args, wl, name):
-    """Reference arm for the batched workload: the oracle port on a bounded sample of blocks per step."""
+    """Reference arm for the batched workload: the oracle port on the host cores.
+
+    The timed steps split the seeded 256-block sample of ``cpu_baseline`` between
+    them (step s takes its s-th share), so K steps time the whole sample once and
+    the run stays within seconds; each warm-up step runs the sample's first 4
+    blocks.  ``value`` = sampled blocks / the timed steps' total time."""
     if int(os.environ.get("RANK", "0")) != 0:
         return
+    from oracle import interp_sid, rbrp_column_id
+    from robust_blockwise_random_pivoting_gb300 import workloads as W
     b = 16
+    ids = block_sample_ids(wl["nblocks"], CPU_SAMPLE_BLOCKS, 0)
+    shapes = W.kernel_block_shapes(wl["nblocks"], wl["lo"], wl["hi"], 0)
+    mats = [W.kernel_block_scaled(int(shapes[q][0]), int(shapes[q][1]), q, wl["lengthscale"], 0).astype(np.float64)
+            for q in ids]
+
+    def one(j):
+        o = rbrp_column_id(mats[j], b, tol=wl["tol"], seed=int(ids[j]))
+        if 0 < o["k"] < mats[j].shape[1]:
+            interp_sid(mats[j], o["perm"], o["k"])
+    for _ in range(args.warmup):
+        for j in range(min(4, len(ids))):
+            one(j)
     times, counts = [], []
-    for s in range(args.warmup + args.steps):
-        dt, cnt, desc, _, _, _ = batched_cpu_sample(wl, 0, b)
-        if s >= args.warmup:
-            times.append(dt)
-            counts.append(cnt)
+    for part in np.array_split(np.arange(len(ids)), max(1, args.steps)):
+        t0 = time.perf_counter()
+        for j in part:
+            one(int(j))
+        times.append(time.perf_counter() - t0)
+        counts.append(len(part))
     value = sum(counts) / sum(times)
+    desc = (f"oracle port (numpy/scipy FP64) of the reference's blocked_rpid plus interpolation (mode='sid') for "
+            f"T, on a seeded sample of {len(ids)} of the {wl['nblocks']} blocks (the cpu_baseline sample), b={b}, "
+            f"split over the {max(1, args.steps)} timed steps; matrices/s = sample size / total time")
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": value, "unit": "matrices/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
