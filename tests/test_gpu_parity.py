@@ -231,7 +231,10 @@ def test_tensor_core_projection_matches_cuda_core(handle):
         runs[variant] = (r, handle.id_error(A32))
     for variant, (r, e) in runs.items():
         e_same, how = error_at_rank(A32h, r.k, 64, tol=tol, seed=0, run=o)
-        assert r.err_est <= tol and e <= 1.05 ** 2 * e_same + FP32_FLOOR_SQ, (variant, r.k, e, e_same, how)
+        if e_same <= FP32_FLOOR_SQ:   # past the exact rank (300): the oracle's error is FP32 noise
+            assert r.err_est <= tol and e <= max(tol, FP32_FLOOR_SQ), (variant, r.k, e, e_same, how)
+        else:
+            assert r.err_est <= tol and e <= 1.05 ** 2 * e_same + FP32_FLOOR_SQ, (variant, r.k, e, e_same, how)
         assert abs(r.k - o["k"]) <= 64, (variant, r.k, o["k"])
     assert abs(runs[0][0].k - runs[1][0].k) <= 64
     # the first block (before any accumulated difference) selects the same columns

@@ -13,8 +13,8 @@ where the factor's R11 is ill-conditioned:
   9.4e-20 for the least-squares T.
 
 The error at the run's rank is compared before and after the step, with the
-oracle's least-squares error on the same skeleton (the best any T can do),
-and a second step must change T by no more than rounding.
+oracle's least-squares error on the same skeleton (the best any T can do); a
+second step must keep it there (and, at kappa ~ 1e6, change T by < 1e-6).
 """
 import numpy as np
 import pytest
@@ -52,6 +52,8 @@ def _before_after(handle, A_dev, A64, b, tol):
     change = handle.refine_T(A_dev, steps=1)
     e_after = id_error(A64, perm, handle.T().cpu().numpy())
     change2 = handle.refine_T(A_dev, steps=1)
+    e_after2 = id_error(A64, perm, handle.T().cpu().numpy())
+    assert e_after2 <= 1.01 * e_ls + 1e-30, (k, e_after2, e_ls)   # a second step stays at least squares
     return k, e_before, e_after, e_ls, change, change2
 
 
@@ -71,4 +73,5 @@ def test_refine_fp64_form_one_gram_schmidt_pass_lost_orthogonality(handle):
     Ad = torch.from_numpy(np.asfortranarray(A)).cuda()
     k, e0, e1, e_ls, ch, ch2 = _before_after(handle, Ad, A, 8, 1e-30)
     assert e1 <= e0 * (1 + 1e-9) and e1 <= 1.01 * e_ls + 1e-30, (k, e0, e1, e_ls)
-    assert ch2 <= 1e-6, ch2
+    # kappa(A_S) ~ 3e10: along the smallest singular directions T itself is determined only to
+    # ~eps * kappa, so a second step may still move T; the reconstruction error does not move
