@@ -12,15 +12,26 @@
 //     dL/dC = -2 E T^T - 2 (C z) u^T + 2 (E w) z^T.
 // Nothing of the forward factorisation is stored: R11 and T come from the
 // handle's last run (the caller recomputes it for the backward), C and B are
-// read from A through perm.  The two products E = B - C T and E T^T are
-// 128 x 128-tiled FP32 GEMMs with the loss terms, E w and the rank-one terms
-// fused into their epilogues; z is a double-float triangular solve.
+// read from A through perm.  The two products E = B - C T and E T^T run on the
+// tensor cores (tcgen05, 3xTF32, rbrp_gemm_tc.cuh) with the loss terms, E w and
+// the rank-one terms fused into their epilogues (the handle's variant 1 keeps
+// them as 128 x 128-tiled FP32 FFMA GEMMs); z is a double-float triangular
+// solve.
+//
+// Tensor-core operand layouts (K-major, leading dimensions rounded up to 4
+// floats for TMA):
+//   E = B - C T:  M = rd columns c, N = rows r, K = skeleton index t
+//                 X = T (k x nc, ld kp), Y = C^T (k x m, ld kp, TF32 hi / lo)
+//                 written as E^T (nc x m, ld ncp): the drain lanes run along c
+//   E T^T:        M = rows r, N = skeleton index t, K = rd columns c
+//                 X = E^T, Y = T^T (nc x k, ld ncp, TF32 hi / lo)
 #include <algorithm>
 #include <cmath>
 
 #include "rbrp_internal.h"
 #include "rbrp_df.cuh"
 #include "rbrp_gemm.cuh"
+#include "rbrp_gemm_tc.cuh"
 
 namespace rbrp {
 namespace {
@@ -53,8 +64,9 @@ __global__ void k_adj_prep(const double* __restrict__ T, int k, int nc, const fl
     for (int c = c0 + threadIdx.x; c < min(nc, c0 + 32); c += blockDim.x) wr[c] = W[perm[k + c]];
 }
 
-// upart[p][t] = sum over columns c of part p of T[t, c] wr[c] (double-float, as float2)
-__global__ void k_adj_u(const float* __restrict__ Tc, int k, int nc, const float* __restrict__ wr,
+// upart[p][t] = sum over columns c of part p of T[t, c] wr[c] (double-float, as float2);
+// T is FP32, k x nc, column major with leading dimension ldt >= k
+__global__ void k_adj_u(const float* __restrict__ Tc, int64_t ldt, int k, int nc, const float* __restrict__ wr,
                         float2* __restrict__ upart) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int p = blockIdx.y, chunk = (nc + PARTS - 1) / PARTS;
@@ -62,8 +74,8 @@ __global__ void k_adj_u(const float* __restrict__ Tc, int k, int nc, const float
   if (t >= k) return;
   float hi = 0.f, lo = 0.f;
   for (int c = cb; c < ce; ++c) {
-    const float prod = Tc[t + (int64_t)c * k] * wr[c];
-    const float e = fmaf(Tc[t + (int64_t)c * k], wr[c], -prod);
+    const float prod = Tc[t + (int64_t)c * ldt] * wr[c];
+    const float e = fmaf(Tc[t + (int64_t)c * ldt], wr[c], -prod);
     const float s = hi + prod, z = s - hi;
     lo += ((hi - (s - z)) + (prod - z)) + e;
     hi = s;
@@ -291,7 +303,243 @@ __global__ void k_adj_loss(const float2* __restrict__ loss_part, int nparts, con
   }
 }
 
+// ---------------------------------------------------------------------------
+// tensor-core path
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float tf32_hi(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
+
+// Tx (k x nc, ld kp) = FP32 T; T^T hi / lo (nc x k, ld ncp) = tf32(t), fp32(t - tf32(t))
+// from the FP64 T; wr[c] = W[perm[k + c]].  32 x 32 tiles through shared memory.
+__global__ void k_adj_prep_tc(const double* __restrict__ T, int k, int nc, int kp, int ncp,
+                              const float* __restrict__ W, const int* __restrict__ perm, float* __restrict__ Tx,
+                              float* __restrict__ Trh, float* __restrict__ Trl, float* __restrict__ wr) {
+  __shared__ double tile[32][33];
+  const int t0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8 threads
+  for (int q = ty; q < 32; q += 8) {
+    const int t = t0 + tx, c = c0 + q;
+    double v = 0.0;
+    if (t < k && c < nc) {
+      v = T[t + (int64_t)c * k];
+      Tx[t + (int64_t)c * kp] = (float)v;
+    }
+    tile[q][tx] = v;
+  }
+  __syncthreads();
+  for (int q = ty; q < 32; q += 8) {
+    const int t = t0 + q, c = c0 + tx;
+    if (t < k && c < nc) {
+      const double v = tile[tx][q];
+      const float h = tf32_hi((float)v);
+      Trh[c + (int64_t)t * ncp] = h;
+      Trl[c + (int64_t)t * ncp] = (float)(v - (double)h);
+    }
+  }
+  if (blockIdx.x == 0)
+    for (int c = c0 + threadIdx.x; c < min(nc, c0 + 32); c += blockDim.x) wr[c] = W[perm[k + c]];
+}
+
+// C^T hi / lo (k x m, ld kp): element (t, r) = A[r, perm[t]] split into tf32 and the rest.
+__global__ void k_adj_gather_ct(const float* __restrict__ A, int64_t lda, const int* __restrict__ perm, int k,
+                                int m, int kp, float* __restrict__ Cth, float* __restrict__ Ctl) {
+  __shared__ float tile[32][33];
+  const int r0 = blockIdx.x * 32, t0 = blockIdx.y * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int q = ty; q < 32; q += 8) {
+    const int r = r0 + tx, t = t0 + q;
+    tile[q][tx] = (r < m && t < k) ? A[r + (int64_t)perm[t] * lda] : 0.f;
+  }
+  __syncthreads();
+  for (int q = ty; q < 32; q += 8) {
+    const int t = t0 + tx, r = r0 + q;
+    if (t < k && r < m) {
+      const float v = tile[tx][q];
+      const float h = tf32_hi(v);
+      Cth[t + (int64_t)r * kp] = h;
+      Ctl[t + (int64_t)r * kp] = v - h;
+    }
+  }
+}
+
+// Per-CTA reduction buffers of the E epilogue (one instance per CTA).
+__device__ __forceinline__ float* epi_ew_buf() {
+  __shared__ float buf[64 * 4];  // [row slot][lane quarter]
+  return buf;
+}
+__device__ __forceinline__ float2* epi_sq_buf() {
+  __shared__ float2 buf[8];      // [drain warp]
+  return buf;
+}
+
+// E = B - C T on a (128 rd columns) x (64 rows) tile: E^T stored (when Et), ||E||^2
+// and the row sums of E w as per-CTA partials, G(:, rd) = scale * 2 (E + (C z) w^T).
+struct EpiE {
+  const float* A;
+  int64_t lda;
+  const int* perm;
+  int k, m, nc;
+  const float* wr;
+  const float* cz;
+  float* Et;
+  int64_t ldet;
+  float* G;
+  int64_t ldg;
+  float scale;
+  float2* loss_part;
+  float2* ew_part;
+
+  __device__ void operator()(int c, int r0, const float (&hi)[32], const float (&lo)[32], int dw) const {
+    float* s_ew = epi_ew_buf();
+    float2* s_sq = epi_sq_buf();
+    const int lane = threadIdx.x & 31, quarter = (c & 127) >> 5, ch = dw >> 2;
+    const bool vc = c < nc;
+    const float w = vc ? wr[c] : 0.f;
+    const int64_t col = vc ? (int64_t)perm[k + c] : 0;
+    dfl sq = {0.f, 0.f};
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+      const int r = r0 + j;
+      float e = 0.f;
+      if (vc && r < m) {
+        e = (A[r + col * lda] - hi[j]) - lo[j];
+        df_acc_prod(sq, e, e);
+        if (Et) Et[c + (int64_t)r * ldet] = e;
+        if (G) G[r + col * ldg] = scale * 2.f * fmaf(cz[r], w, e);
+      }
+      float ew = e * w;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) ew += __shfl_xor_sync(0xffffffffu, ew, o);
+      if (lane == 0) s_ew[(ch * 32 + j) * 4 + quarter] = ew;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const dfl t = {__shfl_xor_sync(0xffffffffu, sq.hi, o), __shfl_xor_sync(0xffffffffu, sq.lo, o)};
+      sq = df_add(sq, t);
+    }
+    if (lane == 0) s_sq[dw] = make_float2(sq.hi, sq.lo);
+  }
+
+  // after the CTA barrier: fixed-order sums of the shared partials
+  __device__ void finish(bool ok) const {
+    if (!ok) return;
+    const float* s_ew = epi_ew_buf();
+    const float2* s_sq = epi_sq_buf();
+    const int t = threadIdx.x;
+    if (t < 64) {
+      const int r = blockIdx.y * 64 + t;
+      if (r < m) {
+        const float s = ((s_ew[t * 4] + s_ew[t * 4 + 1]) + s_ew[t * 4 + 2]) + s_ew[t * 4 + 3];
+        ew_part[(int64_t)blockIdx.x * m + r] = make_float2(s, 0.f);
+      }
+    } else if (t == 64) {
+      dfl a = {s_sq[0].x, s_sq[0].y};
+      for (int q = 1; q < 8; ++q) a = df_add(a, {s_sq[q].x, s_sq[q].y});
+      loss_part[(int64_t)blockIdx.y * gridDim.x + blockIdx.x] = make_float2(a.hi, a.lo);
+    }
+  }
+};
+
+// G(:, S) = scale * (-2 E T^T - 2 (C z) u^T + 2 (E w) z^T) on a (128 rows) x (64 skeleton) tile.
+struct EpiG {
+  const int* perm;
+  int m, k;
+  const float* cz;
+  const float* ew;
+  const float* u;
+  const float* z;
+  float* G;
+  int64_t ldg;
+  float scale;
+
+  __device__ void operator()(int r, int a0, const float (&hi)[32], const float (&lo)[32], int) const {
+    if (r >= m) return;
+    const float czr = cz[r], ewr = ew[r];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+      const int a = a0 + j;
+      if (a < k) {
+        const float g = -2.f * (hi[j] + lo[j]) - 2.f * czr * u[a] + 2.f * ewr * z[a];
+        G[r + (int64_t)perm[a] * ldg] = scale * g;
+      }
+    }
+  }
+  __device__ void finish(bool) const {}
+};
+
 size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
+
+}  // namespace
+}  // namespace rbrp
+
+namespace rbrp {
+namespace {
+
+// The tensor-core form of the loss and gradient (same outputs as the FFMA kernels).
+rbrp_status adjoint_tc(rbrp_handle h, int m, int k, int nc, int kp, int ncp, const float* dA, int64_t lda,
+                       const float* dW, float scale, float* dG, int64_t ldg, double* loss, float* Trh, float* Trl,
+                       float* Tx, float* wr, float2* up, float* u, float2* udf, float* z, float2* Rdf, float2* wk,
+                       float2* czp, float* cz, float* Et, float2* ewp, float* ew, float2* lp, double* lout,
+                       float* Cth, float* Ctl, int* dstatus) {
+  cudaStream_t st = h->stream;
+  const int n = h->n;
+  if (!h->smem_attr_gemm_tc) {
+    rbrp_status s = cuda_check(h, cudaFuncSetAttribute(tc::k_gemm_tc<EpiE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                       (int)tc::P1_SMEM), "cudaFuncSetAttribute(k_gemm_tc<E>)");
+    if (s == RBRP_OK)
+      s = cuda_check(h, cudaFuncSetAttribute(tc::k_gemm_tc<EpiG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)tc::P1_SMEM), "cudaFuncSetAttribute(k_gemm_tc<G>)");
+    if (s != RBRP_OK) return s;
+    h->smem_attr_gemm_tc = true;
+  }
+  const long long budget = h->wait_budget > 0 ? h->wait_budget : kWaitBudgetDefault;
+  CUtensorMap tmX1, tmY1h, tmY1l;
+  rbrp_status s = make_tmap_f32(h, &tmX1, Tx, k, nc, kp, tc::BK, tc::BM);
+  if (s == RBRP_OK) s = make_tmap_f32(h, &tmY1h, Cth, k, m, kp, tc::BK, tc::BN);
+  if (s == RBRP_OK) s = make_tmap_f32(h, &tmY1l, Ctl, k, m, kp, tc::BK, tc::BN);
+  if (s != RBRP_OK) return s;
+  s = cuda_check(h, cudaMemsetAsync(dstatus, 0, sizeof(int), st), "clear status");
+  if (s != RBRP_OK) return s;
+
+  k_adj_prep_tc<<<dim3((k + 31) / 32, (nc + 31) / 32), 256, 0, st>>>(h->T, k, nc, kp, ncp, dW, h->perm, Tx, Trh,
+                                                                     Trl, wr);
+  k_adj_gather_ct<<<dim3((m + 31) / 32, (k + 31) / 32), 256, 0, st>>>(dA, lda, h->perm, k, m, kp, Cth, Ctl);
+  k_adj_u<<<dim3((k + 255) / 256, PARTS), 256, 0, st>>>(Tx, kp, k, nc, wr, up);
+  k_adj_sum_parts<<<(k + 255) / 256, 256, 0, st>>>(up, k, u, udf);
+  if (dG) {
+    k_adj_split_r<<<1216, 256, 0, st>>>(h->R, n, k, Rdf);
+    k_adj_z<<<1, 1024, 0, st>>>(Rdf, k, udf, wk, z);
+    k_adj_cz<<<dim3((m + 255) / 256, PARTS), 256, 0, st>>>(dA, lda, m, k, h->perm, z, czp);
+    k_adj_sum_parts<<<(m + 255) / 256, 256, 0, st>>>(czp, m, cz, nullptr);
+  }
+  const int tx1 = (nc + tc::BM - 1) / tc::BM, ty1 = (m + tc::BN - 1) / tc::BN;
+  EpiE e1{dA, lda, h->perm, k, m, nc, wr, cz, dG ? Et : nullptr, ncp, dG, ldg, scale, lp, ewp};
+  tc::k_gemm_tc<EpiE><<<dim3(tx1, ty1), tc::NTHREADS, tc::P1_SMEM, st>>>(tmX1, tmY1h, tmY1l, nc, m, k, budget,
+                                                                       dstatus, e1);
+  if (dG) k_adj_sum_rows<<<(m + 255) / 256, 256, 0, st>>>(ewp, tx1, m, ew);
+  k_adj_loss<<<1, 256, 0, st>>>(lp, tx1 * ty1, udf, k, lout);
+  if (dG) {
+    CUtensorMap tmX2, tmY2h, tmY2l;
+    s = make_tmap_f32(h, &tmX2, Et, nc, m, ncp, tc::BK, tc::BM);
+    if (s == RBRP_OK) s = make_tmap_f32(h, &tmY2h, Trh, nc, k, ncp, tc::BK, tc::BN);
+    if (s == RBRP_OK) s = make_tmap_f32(h, &tmY2l, Trl, nc, k, ncp, tc::BK, tc::BN);
+    if (s != RBRP_OK) return s;
+    EpiG e2{h->perm, m, k, cz, ew, u, z, dG, ldg, scale};
+    tc::k_gemm_tc<EpiG><<<dim3((m + tc::BM - 1) / tc::BM, (k + tc::BN - 1) / tc::BN), tc::NTHREADS, tc::P1_SMEM, st>>>(
+        tmX2, tmY2h, tmY2l, m, k, nc, budget, dstatus, e2);
+  }
+  s = cuda_check(h, cudaGetLastError(), "adjoint kernels");
+  if (s != RBRP_OK) return s;
+  double hl[2] = {0.0, 0.0};
+  int hs = 0;
+  s = cuda_check(h, cudaMemcpyAsync(hl, lout, sizeof(hl), cudaMemcpyDeviceToHost, st), "copy loss");
+  if (s == RBRP_OK) s = cuda_check(h, cudaMemcpyAsync(&hs, dstatus, sizeof(int), cudaMemcpyDeviceToHost, st), "status");
+  if (s == RBRP_OK) s = cuda_check(h, cudaStreamSynchronize(st), "adjoint kernels");
+  if (s != RBRP_OK) return s;
+  if (hs == tc::ST_ERR_TIMEOUT)
+    return set_error(h, RBRP_ERR_DEVICE_TIMEOUT, "a device-side wait of the adjoint GEMMs timed out; they aborted cleanly");
+  if (loss) *loss = hl[0] + hl[1];
+  return RBRP_OK;
+}
 
 }  // namespace
 }  // namespace rbrp
@@ -313,16 +561,25 @@ extern "C" rbrp_status rbrp_fixed_id_adjoint_f32(rbrp_handle h, int m, int n, co
   cudaStream_t st = h->stream;
   // workspace: Tr, Tc (k x nc), wr (nc), u parts / u / udf, z, Rdf (k x k), work (k), cz parts / cz,
   // E (m x nc), E w parts / E w, loss parts, loss out
+  const bool use_tc = h->variant == 0;
   const int gx = (m + GTILE - 1) / GTILE, gy1 = (nc + GTILE - 1) / GTILE, gy2 = (k + GTILE - 1) / GTILE;
+  const int kp = (k + 3) & ~3, ncp = (nc + 3) & ~3;           // TMA leading dimensions (16-byte rows)
+  const int tx1 = (nc + tc::BM - 1) / tc::BM, ty1 = (m + tc::BN - 1) / tc::BN;   // E tiles
   const size_t kn = (size_t)k * nc;
   size_t off = 0;
   auto take = [&](size_t bytes) { const size_t o = off; off += al(bytes); return o; };
-  const size_t o_Tr = take(4 * kn), o_Tc = take(4 * kn), o_wr = take(4 * (size_t)nc);
+  const size_t o_Tr = take(4 * (use_tc ? (size_t)ncp * k : kn)), o_Tc = take(4 * (use_tc ? (size_t)kp * nc : kn));
+  const size_t o_wr = take(4 * (size_t)nc);
   const size_t o_up = take(8 * (size_t)PARTS * k), o_u = take(4 * (size_t)k), o_udf = take(8 * (size_t)k);
   const size_t o_z = take(4 * (size_t)k), o_R = take(8 * (size_t)k * k), o_wk = take(8 * (size_t)k);
   const size_t o_czp = take(8 * (size_t)PARTS * m), o_cz = take(4 * (size_t)m);
-  const size_t o_E = take(4 * (size_t)m * nc), o_ewp = take(8 * (size_t)gy1 * m), o_ew = take(4 * (size_t)m);
-  const size_t o_lp = take(8 * (size_t)gx * gy1), o_loss = take(16);
+  const size_t o_E = take(4 * (use_tc ? (size_t)ncp * m : (size_t)m * nc)), o_ewp = take(8 * (size_t)gy1 * m);
+  const size_t o_ew = take(4 * (size_t)m);
+  const size_t o_lp = take(8 * std::max((size_t)gx * gy1, (size_t)tx1 * ty1)), o_loss = take(16);
+  // tensor-core operands: T^T lo, C^T hi / lo, the timeout status
+  const size_t o_Trl = use_tc ? take(4 * (size_t)ncp * k) : 0;
+  const size_t o_Cth = use_tc ? take(4 * (size_t)kp * m) : 0, o_Ctl = use_tc ? take(4 * (size_t)kp * m) : 0;
+  const size_t o_st = take(16);
   if (h->adj_bytes < off) {
     if (h->adj_ws) cudaFree(h->adj_ws);
     h->adj_ws = nullptr;
@@ -348,9 +605,14 @@ extern "C" rbrp_status rbrp_fixed_id_adjoint_f32(rbrp_handle h, int m, int n, co
   float* ew = reinterpret_cast<float*>(w + o_ew);
   float2* lp = reinterpret_cast<float2*>(w + o_lp);
   double* lout = reinterpret_cast<double*>(w + o_loss);
+  int* dstatus = reinterpret_cast<int*>(w + o_st);
 
+  if (use_tc) return adjoint_tc(h, m, k, nc, kp, ncp, dA, lda, dW, scale, dG, ldg, loss, Tr /* T^T hi */,
+                                reinterpret_cast<float*>(w + o_Trl), Tc /* Tx */, wr, up, u, udf, z, Rdf, wk, czp,
+                                cz, E /* E^T */, ewp, ew, lp, lout, reinterpret_cast<float*>(w + o_Cth),
+                                reinterpret_cast<float*>(w + o_Ctl), dstatus);
   k_adj_prep<<<dim3((k + 31) / 32, (nc + 31) / 32), 256, 0, st>>>(h->T, k, nc, dW, h->perm, Tr, Tc, wr);
-  k_adj_u<<<dim3((k + 255) / 256, PARTS), 256, 0, st>>>(Tc, k, nc, wr, up);
+  k_adj_u<<<dim3((k + 255) / 256, PARTS), 256, 0, st>>>(Tc, k, k, nc, wr, up);
   k_adj_sum_parts<<<(k + 255) / 256, 256, 0, st>>>(up, k, u, udf);
   if (dG) {
     k_adj_split_r<<<1216, 256, 0, st>>>(h->R, n, k, Rdf);

@@ -1,0 +1,188 @@
+// rbrp_gemm_tc.cuh - a general tcgen05 / TMEM / TMA 3xTF32 GEMM with a
+// pluggable epilogue (sm_103a), on the pipeline of the residual projection
+// (rbrp_tc.cuh): D(p, c) = sum_k X(k, p) Y(k, c) for a tile of 128 values of p
+// (the MMA M dimension, TMEM lanes, one CTA along gridDim.x) and 64 values of
+// c (the MMA N dimension, one CTA along gridDim.y), reduced over all of k in
+// stages of 32 (MMA K).
+//
+// Both operands are K-major FP32 in global memory: X (K x M, column major, ld
+// a multiple of 4) and the hi and lo TF32 parts of Y (K x N each, same layout).
+//
+//   warp 0   TMA producer: the X tile (128 x 32) and the Y hi / lo tiles
+//            (64 x 32) into a 4-stage ring, 128-byte swizzled.
+//   warp 1   MMA issuer: X hi Y hi into a large accumulator, X hi Y lo and
+//            X lo Y hi into a small one (3xTF32: the FP32 product to ~2^-22).
+//   warps 2-5 split each staged X tile into exact TF32 hi + lo parts.
+//   warps 6-13 drain the large accumulator after every stage and the small one
+//            every CHUNK stages into double-float registers, then call the
+//            epilogue: thread (lane quarter q, column half ch) holds
+//            D(p0 + 32 q + lane, c0 + 32 ch + j) for j < 32.
+//
+// The tensor core rounds its FP32 accumulator once per MMA with a bias; the
+// per-stage drains keep the sum accurate to ~1e-7 however long K is.  Every
+// wait is bounded by `budget` clock64 cycles; on expiry the CTA sets an abort
+// flag and *status, waits (default budget) for its own TMA copies and for the
+// MMAs it issued, frees TMEM and returns without running the epilogue.
+#pragma once
+#include "rbrp_tc.cuh"
+
+namespace rbrp {
+namespace tc {
+namespace {
+
+template <typename Epi>
+__global__ void __launch_bounds__(NTHREADS, 1)
+k_gemm_tc(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmYh,
+          const __grid_constant__ CUtensorMap tmYl, int M, int N, int K, long long budget, int* status, Epi epi) {
+  extern __shared__ uint8_t gt_raw[];
+  P1Smem& sm = *reinterpret_cast<P1Smem*>((reinterpret_cast<uintptr_t>(gt_raw) + 1023) & ~(uintptr_t)1023);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int p0 = blockIdx.x * BM, c0 = blockIdx.y * BN;
+  const int nk = (K + BK - 1) / BK;
+  if (p0 >= M || c0 >= N || nk <= 0) return;
+  volatile int* abort = &sm.abort;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&sm.full[s], 1);
+      mbar_init(&sm.split[s], NSPLIT);
+      mbar_init(&sm.empty[s], 1);
+    }
+    for (int b = 0; b < NBIG; ++b) {
+      mbar_init(&sm.bigf[b], 1);
+      mbar_init(&sm.bige[b], NDRAIN);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&sm.smlf[b], 1);
+      mbar_init(&sm.smle[b], NDRAIN);
+    }
+    mbar_init(&sm.mmadone, 1);
+    sm.abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sm.tmem_base)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = sm.tmem_base;
+  int issued = 0;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      for (int s = 0; s < nk; ++s) {
+        const int slot = s % STAGES;
+        const uint32_t use = (uint32_t)(s / STAGES);
+        if (s >= STAGES && !mbar_wait(&sm.empty[slot], (use & 1) ^ 1, abort, budget)) break;
+        uint8_t* base = sm.stage[slot];
+        mbar_expect_tx(&sm.full[slot], A_BYTES + 2 * B_BYTES);
+        tma_load_2d(base, &tmX, &sm.full[slot], s * BK, p0);
+        tma_load_2d(base + 2 * A_BYTES, &tmYh, &sm.full[slot], s * BK, c0);
+        tma_load_2d(base + 2 * A_BYTES + B_BYTES, &tmYl, &sm.full[slot], s * BK, c0);
+        issued = s + 1;
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      for (int s = 0; s < nk; ++s) {
+        const int slot = s % STAGES;
+        const uint32_t use = (uint32_t)(s / STAGES);
+        const int b = s % NBIG;
+        const int chunk = s / CHUNK, sb = chunk & 1;
+        const bool first = (s % CHUNK) == 0;
+        if (s >= NBIG && !mbar_wait(&sm.bige[b], (uint32_t)(s / NBIG - 1) & 1, abort, budget)) break;
+        if (first && chunk >= 2 && !mbar_wait(&sm.smle[sb], (uint32_t)((chunk >> 1) - 1) & 1, abort, budget)) break;
+        if (!mbar_wait(&sm.split[slot], use & 1, abort, budget)) break;
+        tc_fence_after();
+        const uint8_t* base = sm.stage[slot];
+        const uint64_t dxh = sw128_desc(smem_u32(base));
+        const uint64_t dxl = sw128_desc(smem_u32(base + A_BYTES));
+        const uint64_t dyh = sw128_desc(smem_u32(base + 2 * A_BYTES));
+        const uint64_t dyl = sw128_desc(smem_u32(base + 2 * A_BYTES + B_BYTES));
+        const uint32_t dbig = tbase + (uint32_t)(b * BN);
+        const uint32_t dsml = tbase + (uint32_t)(NBIG * BN + sb * BN);
+#pragma unroll
+        for (int k = 0; k < BK / 8; ++k) {
+          mma_tf32(dbig, dxh + 2 * k, dyh + 2 * k, k == 0 ? 0u : 1u);
+          mma_tf32(dsml, dxh + 2 * k, dyl + 2 * k, (first && k == 0) ? 0u : 1u);
+          mma_tf32(dsml, dxl + 2 * k, dyh + 2 * k, 1u);
+        }
+        mma_commit(&sm.empty[slot]);
+        mma_commit(&sm.bigf[b]);
+        if ((s % CHUNK) == CHUNK - 1 || s == nk - 1) mma_commit(&sm.smlf[sb]);
+      }
+    }
+  } else if (warp < 2 + NSPLIT / 32) {
+    const int et = threadIdx.x - 64;
+    for (int s = 0; s < nk; ++s) {
+      const int slot = s % STAGES;
+      if (!mbar_wait(&sm.full[slot], (uint32_t)(s / STAGES) & 1, abort, budget)) break;
+      float4* a4 = reinterpret_cast<float4*>(sm.stage[slot]);
+      float4* l4 = reinterpret_cast<float4*>(sm.stage[slot] + A_BYTES);
+#pragma unroll
+      for (int e = et; e < A_BYTES / 16; e += NSPLIT) {
+        const float4 v = a4[e];
+        const float4 h = make_float4(tf32_trunc(v.x), tf32_trunc(v.y), tf32_trunc(v.z), tf32_trunc(v.w));
+        a4[e] = h;
+        l4[e] = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      mbar_arrive(&sm.split[slot]);
+    }
+  } else {
+    const int dw = warp - 2 - NSPLIT / 32;  // 0..7
+    const int q = warp & 3;                  // TMEM lane quarter of this warp
+    const int ch = dw >> 2;                  // column half of the accumulators
+    const uint32_t lane_off = ((uint32_t)(32 * q) << 16) + (uint32_t)(32 * ch);
+    float hi[32], lo[32];
+#pragma unroll
+    for (int a = 0; a < 32; ++a) hi[a] = lo[a] = 0.f;
+    bool ok = true;
+    for (int d = 0; d < nk; ++d) {
+      const int b = d % NBIG;
+      if (!mbar_wait(&sm.bigf[b], (uint32_t)(d / NBIG) & 1, abort, budget)) { ok = false; break; }
+      tc_fence_after();
+      drain32(tbase + lane_off + (uint32_t)(b * BN), hi, lo);
+      tc_fence_before();
+      mbar_arrive(&sm.bige[b]);
+      if ((d % CHUNK) == CHUNK - 1 || d == nk - 1) {
+        const int chunk = d / CHUNK, sb = chunk & 1;
+        if (!mbar_wait(&sm.smlf[sb], (uint32_t)(chunk >> 1) & 1, abort, budget)) { ok = false; break; }
+        tc_fence_after();
+        drain32(tbase + lane_off + (uint32_t)(NBIG * BN + sb * BN), hi, lo);
+        tc_fence_before();
+        mbar_arrive(&sm.smle[sb]);
+      }
+    }
+    if (ok && !*abort) epi(p0 + 32 * q + lane, c0 + 32 * ch, hi, lo, dw);
+  }
+  __syncthreads();
+  if (*abort) {
+    // as k_proj_w_tc: the CTA's own TMA copies and issued MMAs finish before TMEM is freed
+    int dummy = 0;
+    volatile int* never = &dummy;
+    if (threadIdx.x == 0) atomicExch(status, ST_ERR_TIMEOUT);
+    if (warp == 0 && lane == 0) {
+      for (int s = issued - STAGES > 0 ? issued - STAGES : 0; s < issued; ++s)
+        mbar_wait(&sm.full[s % STAGES], (uint32_t)(s / STAGES) & 1, never);
+    }
+    if (warp == 1 && lane == 0) {
+      mma_commit(&sm.mmadone);
+      mbar_wait(&sm.mmadone, 0u, never);
+    }
+    __syncthreads();
+  }
+  epi.finish(*abort == 0);
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(TMEM_COLS) : "memory");
+  }
+}
+
+}  // namespace
+}  // namespace tc
+}  // namespace rbrp

@@ -110,6 +110,7 @@ struct rbrp_handle_st {
   std::vector<cudaEvent_t> block_events;
   cudaEvent_t ev_start = nullptr, ev_loop = nullptr, ev_end = nullptr;
   bool smem_attr_set = false;
+  bool smem_attr_gemm_tc = false;  // the adjoint's tcgen05 GEMMs (rbrp_adjoint.cu)
 
   // per-phase profiling
   bool profiling = false;

@@ -164,3 +164,32 @@ def test_adjoint_requires_matching_run(handle):
         fixed_skeleton_id(handle, A, torch.tensor([3, 3], dtype=torch.int32, device="cuda"))
     with pytest.raises(RBRPError):
         fixed_skeleton_id(handle, A, torch.tensor([45], dtype=torch.int32, device="cuda"))
+
+
+def test_tensor_core_adjoint_matches_ffma(handle):
+    """The adjoint GEMMs on the tensor cores (tcgen05 3xTF32, variant 0, default) against
+    the FP32 FFMA kernels (variant 1) on the same problem, each against the FP64 autograd
+    gradient: the tensor-core loss and gradient no further from FP64 than the FFMA ones
+    (1.5x; the variants also differ in the forward's projection, 3xTF32 against CUDA-core
+    double-float)."""
+    from robust_blockwise_random_pivoting_gb300.adjoint import fixed_skeleton_loss_and_grad, gaussian_kernel_matrix
+    P, ls = kernel_problem(n=1500, dim=6, ls=1.2, seed=5)
+    A32 = colmajor(gaussian_kernel_matrix(P, ls).float())
+    S = skeleton(handle, A32, tol=1e-8)
+    w = torch.randn(1500, generator=torch.Generator(device="cpu").manual_seed(2)).cuda()
+    A64 = A32.double().requires_grad_(True)
+    lref, _, _ = ref_loss(A64, S, w.double())
+    lref.backward()
+    out = {}
+    for variant in (0, 1):
+        handle.set_variant(variant)
+        try:
+            loss, G = fixed_skeleton_loss_and_grad(handle, A32, S, w, b=64)
+        finally:
+            handle.set_variant(0)
+        out[variant] = (abs(loss - lref.item()) / abs(lref.item()),
+                        (torch.linalg.norm(G.double() - A64.grad) / torch.linalg.norm(A64.grad)).item())
+    # (measured: loss 1.3e-4 / 1.6e-4 and gradient 4.9e-3 / 4.3e-3 relative to FP64, tensor
+    # core / FFMA; at squared tol 1e-8 this skeleton is less well conditioned than the others)
+    assert out[0][0] <= 1.5 * out[1][0] + 1e-5 and out[0][0] <= 5e-4, out
+    assert out[0][1] <= 1.5 * out[1][1] + 1e-4 and out[0][1] <= 1e-2, out

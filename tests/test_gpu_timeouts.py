@@ -2,7 +2,7 @@
 
 The library's kernels that wait on other threads of the GPU - the grid barrier
 of the LU pivots (a cooperative launch) and the mbarrier waits of the tcgen05
-projection - give up after a clock64 limit, set an error status, let their own
+projection and of the adjoint's tcgen05 GEMMs - give up after a clock64 limit, set an error status, let their own
 asynchronous copies and MMAs finish, and exit.  The test-only limit of
 ``rbrp_set_wait_budget`` (a few cycles) makes the waits run out on purpose,
 without any fault or hang: the call must return RBRP_ERR_DEVICE_TIMEOUT (7),
@@ -66,3 +66,27 @@ def test_tcgen05_projection_timeout_is_clean(handle):
     assert r.k == want.k
     assert np.array_equal(r.perm.cpu().numpy(), want_perm)
     assert np.array_equal(r.T.cpu().numpy(), want_T)
+
+
+def test_tcgen05_adjoint_gemm_timeout_is_clean(handle):
+    """The adjoint's tensor-core GEMMs (the same bounded pipeline) run out cleanly too."""
+    import ctypes
+    from robust_blockwise_random_pivoting_gb300.adjoint import fixed_skeleton_id, fixed_skeleton_loss_and_grad
+    A = torch.from_numpy(W.gaussian_exp(400, 500, decay=20.0, seed=3)).float().cuda().t().contiguous().t()
+    S = torch.arange(0, 500, 5, dtype=torch.int32, device="cuda")
+    w = torch.randn(500, generator=torch.Generator(device="cpu").manual_seed(1)).cuda()
+    loss_ref, G_ref = fixed_skeleton_loss_and_grad(handle, A, S, w, b=32)
+    fixed_skeleton_id(handle, A, S, 32)                  # forward with the default budget
+    G = torch.empty((500, 400), dtype=torch.float32, device="cuda").t()
+    loss = ctypes.c_double()
+    handle.set_wait_budget(1)
+    try:
+        rc = handle.lib.rbrp_fixed_id_adjoint_f32(handle.h, 400, 500, ctypes.c_void_p(A.data_ptr()), 400,
+                                                  ctypes.c_void_p(w.data_ptr()), ctypes.c_float(1.0),
+                                                  ctypes.c_void_p(G.data_ptr()), 400, ctypes.byref(loss))
+        assert rc == DEVICE_TIMEOUT, rc
+    finally:
+        handle.set_wait_budget(0)
+    torch.cuda.synchronize()
+    loss2, G2 = fixed_skeleton_loss_and_grad(handle, A, S, w, b=32)
+    assert loss2 == loss_ref and torch.equal(G2, G_ref)
