@@ -123,58 +123,111 @@ __global__ void k_adj_split_r(const double* __restrict__ R, int64_t ldr, int k, 
   }
 }
 
-// z = R11^{-1} R11^{-T} u in double-float, one CTA: 32-wide diagonal blocks
-// solved by one thread, the remaining right-hand side updated by all threads.
-__global__ void __launch_bounds__(1024) k_adj_z(const float2* __restrict__ Rdf, int k, const float2* __restrict__ udf,
-                                                 float2* __restrict__ work, float* __restrict__ z) {
+// z = R11^{-1} R11^{-T} u in double-float, by 32-row blocks, one launch per block
+// and direction.  In every CTA warp 0 solves the block's 32 x 32 triangle from the
+// right-hand side rhs (lane-parallel: the lane of row i finishes x_i, every later
+// lane subtracts its term), CTA 0 stores it in sol, and all CTAs subtract the
+// block's contribution from their share of the remaining rows of rhs.  No CTA
+// writes what another reads in the same launch: the block's rhs rows are only
+// read, its solution goes to sol.
+__device__ __forceinline__ dfl r_df(const float2* __restrict__ R, int k, int a, int c) {
+  const float2 v = R[(int64_t)a * k + c];
+  return dfl{v.x, v.y};
+}
+
+// forward step: R11^T y = u for rows [j0, j0 + 32): y(j0..) into sol, rhs(j) for j >= j0 + 32
+__global__ void __launch_bounds__(256) k_adj_zf_step(const float2* __restrict__ R, int k, int j0,
+                                                     float2* __restrict__ rhs, float2* __restrict__ sol) {
   __shared__ dfl xb[32];
-  const int tid = threadIdx.x;
-  for (int i = tid; i < k; i += blockDim.x) work[i] = udf[i];
+  __shared__ dfl Rb[32][33];  // the block's diagonal 32 x 32 of R, staged once
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int jl = min(32, k - j0);
+  for (int e = tid; e < 32 * 32; e += blockDim.x) {
+    const int a = e >> 5, c = e & 31;
+    Rb[a][c] = (a < jl && c < jl) ? r_df(R, k, j0 + a, j0 + c) : dfl{1.f, 0.f};
+  }
   __syncthreads();
-  auto r_at = [&](int a, int c) { const float2 v = Rdf[(int64_t)a * k + c]; return dfl{v.x, v.y}; };
-  // forward: R11^T y = u (y overwrites work)
-  for (int j0 = 0; j0 < k; j0 += 32) {
-    const int jl = min(32, k - j0);
-    if (tid == 0) {
-      for (int jj = 0; jj < jl; ++jj) {
-        const float2 w0 = work[j0 + jj];
-        dfl v = {w0.x, w0.y};
-        for (int ii = 0; ii < jj; ++ii) v = df_fms(v, r_at(j0 + ii, j0 + jj), xb[ii]);
-        xb[jj] = df_mul(v, df_recip(r_at(j0 + jj, j0 + jj)));
-        work[j0 + jj] = make_float2(xb[jj].hi, xb[jj].lo);
-      }
+  if (tid < 32) {
+    dfl b = {0.f, 0.f};
+    if (lane < jl) {
+      const float2 v = rhs[j0 + lane];
+      b = {v.x, v.y};
     }
-    __syncthreads();
-    for (int j = j0 + jl + tid; j < k; j += blockDim.x) {
-      const float2 w0 = work[j];
-      dfl v = {w0.x, w0.y};
-      for (int ii = 0; ii < jl; ++ii) v = df_fms(v, r_at(j0 + ii, j), xb[ii]);
-      work[j] = make_float2(v.hi, v.lo);
+    dfl x = {0.f, 0.f};
+    for (int i = 0; i < jl; ++i) {
+      if (lane == i) x = df_mul(b, df_recip(Rb[i][i]));
+      const dfl xi = {__shfl_sync(0xffffffffu, x.hi, i), __shfl_sync(0xffffffffu, x.lo, i)};
+      if (lane > i && lane < jl) b = df_fms(b, Rb[i][lane], xi);
     }
-    __syncthreads();
+    xb[lane] = x;
   }
-  // backward: R11 z = y
+  __syncthreads();
+  if (blockIdx.x == 0 && tid < jl) sol[j0 + tid] = make_float2(xb[tid].hi, xb[tid].lo);
+  for (int j = j0 + jl + blockIdx.x * blockDim.x + tid; j < k; j += gridDim.x * blockDim.x) {
+    const float2 w0 = rhs[j];
+    dfl v = {w0.x, w0.y};
+    for (int ii = 0; ii < jl; ++ii) v = df_fms(v, r_df(R, k, j0 + ii, j), xb[ii]);
+    rhs[j] = make_float2(v.hi, v.lo);
+  }
+}
+
+// backward step: R11 z = y for rows [i0, i0 + il): z(i0..) into sol, rhs(i) for i < i0
+__global__ void __launch_bounds__(256) k_adj_zb_step(const float2* __restrict__ R, int k, int i0, int il,
+                                                     float2* __restrict__ rhs, float2* __restrict__ sol) {
+  __shared__ dfl xb[32];
+  __shared__ dfl Rb[32][33];  // the block's diagonal il x il of R, staged once
+  const int tid = threadIdx.x, lane = tid & 31;
+  for (int e = tid; e < 32 * 32; e += blockDim.x) {
+    const int a = e >> 5, c = e & 31;
+    Rb[a][c] = (a < il && c < il) ? r_df(R, k, i0 + a, i0 + c) : dfl{1.f, 0.f};
+  }
+  __syncthreads();
+  if (tid < 32) {
+    dfl b = {0.f, 0.f};
+    if (lane < il) {
+      const float2 v = rhs[i0 + lane];
+      b = {v.x, v.y};
+    }
+    dfl x = {0.f, 0.f};
+    for (int i = il - 1; i >= 0; --i) {
+      if (lane == i) x = df_mul(b, df_recip(Rb[i][i]));
+      const dfl xi = {__shfl_sync(0xffffffffu, x.hi, i), __shfl_sync(0xffffffffu, x.lo, i)};
+      if (lane < i) b = df_fms(b, Rb[lane][i], xi);
+    }
+    xb[lane] = x;
+  }
+  __syncthreads();
+  if (blockIdx.x == 0 && tid < il) sol[i0 + tid] = make_float2(xb[tid].hi, xb[tid].lo);
+  for (int i = blockIdx.x * blockDim.x + tid; i < i0; i += gridDim.x * blockDim.x) {
+    const float2 w0 = rhs[i];
+    dfl v = {w0.x, w0.y};
+    for (int jj = 0; jj < il; ++jj) v = df_fms(v, r_df(R, k, i, i0 + jj), xb[jj]);
+    rhs[i] = make_float2(v.hi, v.lo);
+  }
+}
+
+__global__ void k_adj_copy_df(const float2* __restrict__ in, float2* __restrict__ out, int k) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < k) out[i] = in[i];
+}
+
+__global__ void k_adj_z_out(const float2* __restrict__ zdf, float* __restrict__ z, int k) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < k) z[i] = zdf[i].x;
+}
+
+// z (FP32) = R11^{-1} R11^{-T} u; work and ys are k double-float scratch vectors each.
+void solve_z(cudaStream_t st, int sms, const float2* Rdf, int k, const float2* udf, float2* work, float2* ys,
+             float* z) {
+  const int grid = std::max(1, std::min((k + 255) / 256, 2 * sms));
+  k_adj_copy_df<<<(k + 255) / 256, 256, 0, st>>>(udf, work, k);
+  for (int j0 = 0; j0 < k; j0 += 32) k_adj_zf_step<<<grid, 256, 0, st>>>(Rdf, k, j0, work, ys);
+  // backward: the right-hand side is y (ys, updated in place), the solution goes to work
   for (int i1 = k; i1 > 0; i1 -= 32) {
-    const int i0 = max(0, i1 - 32), il = i1 - i0;
-    if (tid == 0) {
-      for (int ii = il - 1; ii >= 0; --ii) {
-        const float2 w0 = work[i0 + ii];
-        dfl v = {w0.x, w0.y};
-        for (int jj = ii + 1; jj < il; ++jj) v = df_fms(v, r_at(i0 + ii, i0 + jj), xb[jj]);
-        xb[ii] = df_mul(v, df_recip(r_at(i0 + ii, i0 + ii)));
-        work[i0 + ii] = make_float2(xb[ii].hi, xb[ii].lo);
-      }
-    }
-    __syncthreads();
-    for (int i = tid; i < i0; i += blockDim.x) {
-      const float2 w0 = work[i];
-      dfl v = {w0.x, w0.y};
-      for (int jj = 0; jj < il; ++jj) v = df_fms(v, r_at(i, i0 + jj), xb[jj]);
-      work[i] = make_float2(v.hi, v.lo);
-    }
-    __syncthreads();
+    const int i0 = std::max(0, i1 - 32);
+    k_adj_zb_step<<<grid, 256, 0, st>>>(Rdf, k, i0, i1 - i0, ys, work);
   }
-  for (int i = tid; i < k; i += blockDim.x) z[i] = work[i].x;
+  k_adj_z_out<<<(k + 255) / 256, 256, 0, st>>>(work, z, k);
 }
 
 // czpart[p][r] = sum over the part-p skeleton columns t of A[r, perm[t]] z[t]
@@ -478,7 +531,7 @@ namespace {
 rbrp_status adjoint_tc(rbrp_handle h, int m, int k, int nc, int kp, int ncp, const float* dA, int64_t lda,
                        const float* dW, float scale, float* dG, int64_t ldg, double* loss, float* Trh, float* Trl,
                        float* Tx, float* wr, float2* up, float* u, float2* udf, float* z, float2* Rdf, float2* wk,
-                       float2* czp, float* cz, float* Et, float2* ewp, float* ew, float2* lp, double* lout,
+                       float2* ys, float2* czp, float* cz, float* Et, float2* ewp, float* ew, float2* lp, double* lout,
                        float* Cth, float* Ctl, int* dstatus) {
   cudaStream_t st = h->stream;
   const int n = h->n;
@@ -507,7 +560,7 @@ rbrp_status adjoint_tc(rbrp_handle h, int m, int k, int nc, int kp, int ncp, con
   k_adj_sum_parts<<<(k + 255) / 256, 256, 0, st>>>(up, k, u, udf);
   if (dG) {
     k_adj_split_r<<<1216, 256, 0, st>>>(h->R, n, k, Rdf);
-    k_adj_z<<<1, 1024, 0, st>>>(Rdf, k, udf, wk, z);
+    solve_z(st, h->sms, Rdf, k, udf, wk, ys, z);
     k_adj_cz<<<dim3((m + 255) / 256, PARTS), 256, 0, st>>>(dA, lda, m, k, h->perm, z, czp);
     k_adj_sum_parts<<<(m + 255) / 256, 256, 0, st>>>(czp, m, cz, nullptr);
   }
@@ -572,6 +625,7 @@ extern "C" rbrp_status rbrp_fixed_id_adjoint_f32(rbrp_handle h, int m, int n, co
   const size_t o_wr = take(4 * (size_t)nc);
   const size_t o_up = take(8 * (size_t)PARTS * k), o_u = take(4 * (size_t)k), o_udf = take(8 * (size_t)k);
   const size_t o_z = take(4 * (size_t)k), o_R = take(8 * (size_t)k * k), o_wk = take(8 * (size_t)k);
+  const size_t o_ys = take(8 * (size_t)k);
   const size_t o_czp = take(8 * (size_t)PARTS * m), o_cz = take(4 * (size_t)m);
   const size_t o_E = take(4 * (use_tc ? (size_t)ncp * m : (size_t)m * nc)), o_ewp = take(8 * (size_t)gy1 * m);
   const size_t o_ew = take(4 * (size_t)m);
@@ -598,6 +652,7 @@ extern "C" rbrp_status rbrp_fixed_id_adjoint_f32(rbrp_handle h, int m, int n, co
   float* z = reinterpret_cast<float*>(w + o_z);
   float2* Rdf = reinterpret_cast<float2*>(w + o_R);
   float2* wk = reinterpret_cast<float2*>(w + o_wk);
+  float2* ys = reinterpret_cast<float2*>(w + o_ys);
   float2* czp = reinterpret_cast<float2*>(w + o_czp);
   float* cz = reinterpret_cast<float*>(w + o_cz);
   float* E = reinterpret_cast<float*>(w + o_E);
@@ -608,7 +663,7 @@ extern "C" rbrp_status rbrp_fixed_id_adjoint_f32(rbrp_handle h, int m, int n, co
   int* dstatus = reinterpret_cast<int*>(w + o_st);
 
   if (use_tc) return adjoint_tc(h, m, k, nc, kp, ncp, dA, lda, dW, scale, dG, ldg, loss, Tr /* T^T hi */,
-                                reinterpret_cast<float*>(w + o_Trl), Tc /* Tx */, wr, up, u, udf, z, Rdf, wk, czp,
+                                reinterpret_cast<float*>(w + o_Trl), Tc /* Tx */, wr, up, u, udf, z, Rdf, wk, ys, czp,
                                 cz, E /* E^T */, ewp, ew, lp, lout, reinterpret_cast<float*>(w + o_Cth),
                                 reinterpret_cast<float*>(w + o_Ctl), dstatus);
   k_adj_prep<<<dim3((k + 31) / 32, (nc + 31) / 32), 256, 0, st>>>(h->T, k, nc, dW, h->perm, Tr, Tc, wr);
@@ -616,7 +671,7 @@ extern "C" rbrp_status rbrp_fixed_id_adjoint_f32(rbrp_handle h, int m, int n, co
   k_adj_sum_parts<<<(k + 255) / 256, 256, 0, st>>>(up, k, u, udf);
   if (dG) {
     k_adj_split_r<<<1216, 256, 0, st>>>(h->R, n, k, Rdf);
-    k_adj_z<<<1, 1024, 0, st>>>(Rdf, k, udf, wk, z);
+    solve_z(st, h->sms, Rdf, k, udf, wk, ys, z);
     k_adj_cz<<<dim3((m + 255) / 256, PARTS), 256, 0, st>>>(dA, lda, m, k, h->perm, z, czp);
     k_adj_sum_parts<<<(m + 255) / 256, 256, 0, st>>>(czp, m, cz, nullptr);
   }
