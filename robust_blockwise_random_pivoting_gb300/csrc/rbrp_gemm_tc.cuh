@@ -13,22 +13,35 @@
 //   warp 1   MMA issuer: X hi Y hi into a large accumulator, X hi Y lo and
 //            X lo Y hi into a small one (3xTF32: the FP32 product to ~2^-22).
 //   warps 2-5 split each staged X tile into exact TF32 hi + lo parts.
-//   warps 6-13 drain the large accumulator after every stage and the small one
-//            every CHUNK stages into double-float registers, then call the
+//   warps 6-13 drain the large accumulator after every RBRP_GEMM_DRAIN stages
+//            and the small one every CHUNK stages into double-float registers, then call the
 //            epilogue: thread (lane quarter q, column half ch) holds
 //            D(p0 + 32 q + lane, c0 + 32 ch + j) for j < 32.
 //
-// The tensor core rounds its FP32 accumulator once per MMA with a bias; the
-// per-stage drains keep the sum accurate to ~1e-7 however long K is.  Every
+// The tensor core rounds its FP32 accumulator once per MMA with a bias; draining
+// every RBRP_GEMM_DRAIN stages keeps the rounding from growing with K: the sum
+// stays FP32-accurate however long K is.  Every
 // wait is bounded by `budget` clock64 cycles; on expiry the CTA sets an abort
 // flag and *status, waits (default budget) for its own TMA copies and for the
 // MMAs it issued, frees TMEM and returns without running the epilogue.
 #pragma once
 #include "rbrp_tc.cuh"
 
+// Stages accumulated in the large accumulator between two drains (1, 2 or 4; CHUNK
+// is a multiple): more MMAs per drain halve the drain work at twice the rounding
+// growth between drains.  2 (8 MMAs per drain): the adjoint's E GEMM at 8192^2,
+// k = 4370 took 3.86 ms with 1 and ~3.4 ms with 2, its gradients unchanged against
+// FP64 within the tests' bounds.
+#ifndef RBRP_GEMM_DRAIN
+#define RBRP_GEMM_DRAIN 2
+#endif
+
 namespace rbrp {
 namespace tc {
 namespace {
+
+constexpr int GEMM_DRAIN = RBRP_GEMM_DRAIN;
+static_assert(GEMM_DRAIN >= 1 && CHUNK % GEMM_DRAIN == 0, "drain interval");
 
 template <typename Epi>
 __global__ void __launch_bounds__(NTHREADS, 1)
@@ -91,10 +104,12 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUten
       for (int s = 0; s < nk; ++s) {
         const int slot = s % STAGES;
         const uint32_t use = (uint32_t)(s / STAGES);
-        const int b = s % NBIG;
+        const int g = s / GEMM_DRAIN;                 // drain group of the large accumulator
+        const int b = g % NBIG;
+        const bool gfirst = (s % GEMM_DRAIN) == 0, glast = (s % GEMM_DRAIN) == GEMM_DRAIN - 1 || s == nk - 1;
         const int chunk = s / CHUNK, sb = chunk & 1;
         const bool first = (s % CHUNK) == 0;
-        if (s >= NBIG && !mbar_wait(&sm.bige[b], (uint32_t)(s / NBIG - 1) & 1, abort, budget)) break;
+        if (gfirst && g >= NBIG && !mbar_wait(&sm.bige[b], (uint32_t)(g / NBIG - 1) & 1, abort, budget)) break;
         if (first && chunk >= 2 && !mbar_wait(&sm.smle[sb], (uint32_t)((chunk >> 1) - 1) & 1, abort, budget)) break;
         if (!mbar_wait(&sm.split[slot], use & 1, abort, budget)) break;
         tc_fence_after();
@@ -107,12 +122,12 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUten
         const uint32_t dsml = tbase + (uint32_t)(NBIG * BN + sb * BN);
 #pragma unroll
         for (int k = 0; k < BK / 8; ++k) {
-          mma_tf32(dbig, dxh + 2 * k, dyh + 2 * k, k == 0 ? 0u : 1u);
+          mma_tf32(dbig, dxh + 2 * k, dyh + 2 * k, (gfirst && k == 0) ? 0u : 1u);
           mma_tf32(dsml, dxh + 2 * k, dyl + 2 * k, (first && k == 0) ? 0u : 1u);
           mma_tf32(dsml, dxl + 2 * k, dyh + 2 * k, 1u);
         }
         mma_commit(&sm.empty[slot]);
-        mma_commit(&sm.bigf[b]);
+        if (glast) mma_commit(&sm.bigf[b]);
         if ((s % CHUNK) == CHUNK - 1 || s == nk - 1) mma_commit(&sm.smlf[sb]);
       }
     }
@@ -142,9 +157,11 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUten
 #pragma unroll
     for (int a = 0; a < 32; ++a) hi[a] = lo[a] = 0.f;
     bool ok = true;
-    for (int d = 0; d < nk; ++d) {
-      const int b = d % NBIG;
-      if (!mbar_wait(&sm.bigf[b], (uint32_t)(d / NBIG) & 1, abort, budget)) { ok = false; break; }
+    const int ngroups = (nk + GEMM_DRAIN - 1) / GEMM_DRAIN;
+    for (int g = 0; g < ngroups; ++g) {
+      const int b = g % NBIG;
+      const int d = min(nk - 1, g * GEMM_DRAIN + GEMM_DRAIN - 1);  // last stage of the group
+      if (!mbar_wait(&sm.bigf[b], (uint32_t)(g / NBIG) & 1, abort, budget)) { ok = false; break; }
       tc_fence_after();
       drain32(tbase + lane_off + (uint32_t)(b * BN), hi, lo);
       tc_fence_before();
