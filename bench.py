@@ -800,6 +800,13 @@ def run_batched(args, wl, name, ctx):
         # headline: the host-resident form, declared in advance; the other host-buffer forms beside it
         e2e = dict(host_resident)
         e2e["form"] = "host_resident"
+        # the host link's own rate on this machine (the sequential form's pinned H2D copy of the same
+        # bytes): the time the inputs alone need, against the step
+        link = float(sequential["h2d_GBps"])
+        ms_inputs = pack.numel() * 4 / (link * 1e6)
+        e2e["host_link"] = {"GBps": link, "ms_for_inputs": ms_inputs,
+                            "frac_of_step": ms_inputs / host_resident["ms_step"],
+                            "note": "pinned H2D rate measured by cudaMemcpyAsync of the same 5.4 GB in this run"}
         e2e["other_forms"] = {"sequential": sequential, "pipelined": pipelined}
         del host
 
