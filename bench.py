@@ -806,7 +806,9 @@ def run_batched(args, wl, name, ctx):
         ms_inputs = pack.numel() * 4 / (link * 1e6)
         e2e["host_link"] = {"GBps": link, "ms_for_inputs": ms_inputs,
                             "frac_of_step": ms_inputs / host_resident["ms_step"],
-                            "note": "pinned H2D rate measured by cudaMemcpyAsync of the same 5.4 GB in this run"}
+                            "note": ("pinned H2D rate of one cudaMemcpyAsync of the same inputs in this run; the "
+                                     "host-resident kernel reads them in place at about this rate, so "
+                                     "frac_of_step near 1 means the link bounds the step")}
         e2e["other_forms"] = {"sequential": sequential, "pipelined": pipelined}
         del host
 

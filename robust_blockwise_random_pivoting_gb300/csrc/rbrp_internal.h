@@ -111,6 +111,7 @@ struct rbrp_handle_st {
   cudaEvent_t ev_start = nullptr, ev_loop = nullptr, ev_end = nullptr;
   bool smem_attr_set = false;
   bool smem_attr_gemm_tc = false;  // the adjoint's tcgen05 GEMMs (rbrp_adjoint.cu)
+  bool smem_attr_sketch_tc = false;  // the sketch's tcgen05 GEMM (rbrp_sketch.cu)
 
   // per-phase profiling
   bool profiling = false;

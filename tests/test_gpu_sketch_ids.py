@@ -50,6 +50,29 @@ def test_sketch_is_linear_map_with_scale(handle):
     assert not np.array_equal(Y, Y3)
 
 
+def test_tensor_core_sketch_matches_cuda_core_and_fp64(handle):
+    """A with a 16-byte leading dimension takes the tcgen05 3xTF32 GEMM, any other the CUDA-core one: on the same
+    seed both equal the FP64 product G B to FP32 accuracy (G read back through an identity block)."""
+    from robust_blockwise_random_pivoting_gb300.sketch_ids import gaussian_sketch
+    m, l, nb = 1500, 200, 700          # several tiles in every dimension, partial last tiles
+    rng = np.random.default_rng(7)
+    B = rng.standard_normal((m, nb)).astype(np.float32)
+    A = np.concatenate([np.eye(m, dtype=np.float32), B], axis=1)
+    n = A.shape[1]
+    At = torch.from_numpy(A).cuda().t().contiguous().t()             # ld m = 1500: tensor cores
+    Au = torch.zeros((n, m + 1), dtype=torch.float32, device="cuda").t()[:m, :]
+    Au.copy_(At)                                                      # ld 1501: CUDA cores
+    Yt = gaussian_sketch(At, l, seed=9, handle=handle).double().cpu().numpy()
+    Yu = gaussian_sketch(Au, l, seed=9, handle=handle).double().cpu().numpy()
+    G = Yu[:, :m]                      # FP32 FMA against the identity is exact
+    ref = G @ B.astype(np.float64)
+    tol = 2e-5 * np.abs(ref).max()
+    np.testing.assert_allclose(Yu[:, m:], ref, rtol=0, atol=tol)
+    np.testing.assert_allclose(Yt[:, m:], ref, rtol=0, atol=tol)
+    np.testing.assert_allclose(Yt[:, :m], G, rtol=0, atol=1e-6 * np.abs(G).max())
+    assert np.array_equal(Yt, gaussian_sketch(At, l, seed=9, handle=handle).double().cpu().numpy())
+
+
 def test_cpqr_id_matches_lapack_pivots(handle):
     from robust_blockwise_random_pivoting_gb300.sketch_ids import cpqr_id
     A = decaying(300, 220, seed=1)

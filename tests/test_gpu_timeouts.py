@@ -2,7 +2,7 @@
 
 The library's kernels that wait on other threads of the GPU - the grid barrier
 of the LU pivots (a cooperative launch) and the mbarrier waits of the tcgen05
-projection and of the adjoint's tcgen05 GEMMs - give up after a clock64 limit, set an error status, let their own
+projection, of the adjoint's tcgen05 GEMMs and of the sketch GEMM - give up after a clock64 limit, set an error status, let their own
 asynchronous copies and MMAs finish, and exit.  The test-only limit of
 ``rbrp_set_wait_budget`` (a few cycles) makes the waits run out on purpose,
 without any fault or hang: the call must return RBRP_ERR_DEVICE_TIMEOUT (7),
@@ -90,3 +90,20 @@ def test_tcgen05_adjoint_gemm_timeout_is_clean(handle):
     torch.cuda.synchronize()
     loss2, G2 = fixed_skeleton_loss_and_grad(handle, A, S, w, b=32)
     assert loss2 == loss_ref and torch.equal(G2, G_ref)
+
+
+def test_tcgen05_sketch_gemm_timeout_is_clean(handle):
+    """The sketch's tensor-core GEMM (the same bounded pipeline) runs out cleanly."""
+    from robust_blockwise_random_pivoting_gb300._lib import RBRPError
+    from robust_blockwise_random_pivoting_gb300.sketch_ids import gaussian_sketch
+    A = torch.from_numpy(np.random.default_rng(4).standard_normal((800, 900))).float().cuda().t().contiguous().t()
+    want = gaussian_sketch(A, 96, seed=2, handle=handle)
+    handle.set_wait_budget(1)
+    try:
+        with pytest.raises(RBRPError) as e:
+            gaussian_sketch(A, 96, seed=2, handle=handle)
+        assert e.value.status == DEVICE_TIMEOUT
+    finally:
+        handle.set_wait_budget(0)
+    torch.cuda.synchronize()
+    assert torch.equal(gaussian_sketch(A, 96, seed=2, handle=handle), want)
