@@ -16,8 +16,9 @@
 extern "C" {
 #endif
 
-/* Projection kernel of the FP32 residual form: 0 = tcgen05 / TMEM / TMA
- * (default), 1 = CUDA-core FFMA.  Both accumulate to ~1e-8 relative. */
+/* Projection and update kernels of the FP32 residual form: 0 = tcgen05 /
+ * TMEM / TMA 3xTF32 (default), 1 = CUDA-core FFMA.  Both accumulate to
+ * ~1e-8 relative. */
 rbrp_status rbrp_set_variant(rbrp_handle h, int variant);
 
 /* T = R11^{-1} R12 block updates: 0 = double-float on the FP32 pipe (default,
@@ -26,7 +27,8 @@ rbrp_status rbrp_set_tsolve_fp64(rbrp_handle h, int on);
 
 /* Limit, in SM clock cycles, of the bounded device-side waits of kernels launched
  * through this handle: the grid barrier of the LU pivots (rbrp_lupp_pivots_f64)
- * and the mbarrier waits of the tcgen05 projection.  0 restores the default
+ * and the mbarrier waits of the tcgen05 kernels (projection, update, the
+ * adjoint's and the sketch's GEMMs).  0 restores the default
  * (~2 s).  A limit of a few cycles makes a wait run out: the kernel then exits
  * cleanly and the call returns RBRP_ERR_DEVICE_TIMEOUT, which is how the tests
  * exercise that path without faulting or hanging a GPU.  The waits that let an

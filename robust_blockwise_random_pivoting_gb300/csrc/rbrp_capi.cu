@@ -382,6 +382,10 @@ rbrp_status ensure_workspace(rbrp_handle h, const Layout& L) {
       {(void**)&h->Ares, L.residual ? (size_t)L.ld_res * n * sizeof(float) : 0},
       {(void**)&h->Qh, L.residual ? (size_t)L.ld_res * MAXB * sizeof(float) : 0},
       {(void**)&h->Ql, L.residual ? (size_t)L.ld_res * MAXB * sizeof(float) : 0},
+      {(void**)&h->Qrh, L.residual ? m * MAXB * sizeof(float) : 0},
+      {(void**)&h->Qrl, L.residual ? m * MAXB * sizeof(float) : 0},
+      {(void**)&h->Wth, L.residual ? n * MAXB * sizeof(float) : 0},
+      {(void**)&h->Wtl, L.residual ? n * MAXB * sizeof(float) : 0},
       {(void**)&h->R, kmax * n * 8},
       {(void**)&h->V, m * MAXB * 8},
       {(void**)&h->Q1, m * MAXB * 8},

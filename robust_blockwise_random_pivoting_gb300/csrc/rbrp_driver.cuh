@@ -13,6 +13,7 @@
 #include "rbrp_kernels.cuh"
 #include "rbrp_panel_df.cuh"
 #include "rbrp_tc.cuh"
+#include "rbrp_update_tc.cuh"
 
 namespace rbrp {
 
@@ -48,15 +49,23 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
       s = cuda_check(h, cudaFuncSetAttribute(tc::k_proj_w_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)tc::P1_SMEM), "cudaFuncSetAttribute(k_proj_w_tc)");
       if (s != RBRP_OK) return s;
+      s = cuda_check(h, cudaFuncSetAttribute(tc::k_resid_update_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)tc::U_SMEM), "cudaFuncSetAttribute(k_resid_update_tc)");
+      if (s != RBRP_OK) return s;
     }
   }
   cudaStream_t st = h->stream;
   const bool use_tc = RES && h->variant == 0;
-  CUtensorMap tmA, tmQh, tmQl;
-  if (use_tc) {  // TMA views: A_res (m x n) and the split basis (m x 64), boxes of 32 rows
+  CUtensorMap tmA, tmQh, tmQl, tmWth, tmWtl, tmQrh, tmQrl;
+  if (use_tc) {  // TMA views: A_res (m x n) and the split basis (m x 64), boxes of 32 rows; for the
+                 // update, W^T (64 per position, boxes of 128 positions) and the basis by rows (boxes of 64)
     s = make_tmap_f32(h, &tmA, h->Ares, m, n, L.ld_res, tc::BK, tc::BM);
     if (s == RBRP_OK) s = make_tmap_f32(h, &tmQh, h->Qh, m, MAXB, L.ld_res, tc::BK, tc::BN);
     if (s == RBRP_OK) s = make_tmap_f32(h, &tmQl, h->Ql, m, MAXB, L.ld_res, tc::BK, tc::BN);
+    if (s == RBRP_OK) s = make_tmap_f32(h, &tmWth, h->Wth, MAXB, n, MAXB, tc::BK, tc::BM);
+    if (s == RBRP_OK) s = make_tmap_f32(h, &tmWtl, h->Wtl, MAXB, n, MAXB, tc::BK, tc::BM);
+    if (s == RBRP_OK) s = make_tmap_f32(h, &tmQrh, h->Qrh, MAXB, m, MAXB, tc::BK, tc::U_CH);
+    if (s == RBRP_OK) s = make_tmap_f32(h, &tmQrl, h->Qrl, MAXB, m, MAXB, tc::BK, tc::U_CH);
     if (s != RBRP_OK) return s;
     cudaMemsetAsync(h->Qh, 0, (size_t)L.ld_res * MAXB * sizeof(float), st);
     cudaMemsetAsync(h->Ql, 0, (size_t)L.ld_res * MAXB * sizeof(float), st);
@@ -130,7 +139,7 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
                                                                R11df, Rinvdf, h->ord, h->J, h->K1, h->K2);
       k_panel_q_df<<<(m + QS_ROWS - 1) / QS_ROWS, 256, sizeof(QSolveSmem), st>>>(
           (const float*)h->V, m, h->st, Rinvdf, h->ord, (float*)Q, L.ld_res, use_tc ? h->Qh : nullptr,
-          use_tc ? h->Ql : nullptr, L.ld_res);
+          use_tc ? h->Ql : nullptr, L.ld_res, use_tc ? h->Qrh : nullptr, use_tc ? h->Qrl : nullptr);
       k_write_r11<<<1, 256, 0, st>>>(h->st, R11df, h->R, n);
     } else {
       k_pchol<<<1, 256, panel_smem, st>>>(h->G, m, h->st, tol_loc, h->js, h->perm, h->diags, h->R11, h->ord,
@@ -179,11 +188,35 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
       }
       prof_end(h, RBRP_PHASE_PROJECT, ev, 0.0, 0.0, 1);
       ev = prof_begin(h);
-      const int ctiles = (n - i + P2_COLS - 1) / P2_COLS;
-      // row split by the same wave rule, two CTAs per SM (registers and shared memory), with
-      // a fixed cost per CTA of about two stages (W partial sums and staging, norm partials)
-      int nsplit = 1, rps = (m + P2_ROWS - 1) / P2_ROWS * P2_ROWS;
-      {
+      int nsplit = 1;
+      if (use_tc) {
+        // W^T parts (and R(I2, p)), then the tensor-core update.  Row split by the wave rule
+        // with one CTA per SM (shared memory) and a fixed cost per CTA of about four chunks
+        // (TMEM allocation, the W^T tile, pipeline fill and drain)
+        tc::k_upd_w_prep<<<(n - i + 31) / 32, 256, 0, st>>>(h->st, n, reinterpret_cast<const float2*>(h->Wpart),
+                                                            wsplit, h->R, n, h->Wth, h->Wtl);
+        const int ctiles = (n - i + tc::BM - 1) / tc::BM;
+        int rps = (m + tc::U_CH - 1) / tc::U_CH * tc::U_CH;
+        long best = -1;
+        for (int w = 1; w <= P2_MAX_SPLIT_WS; ++w) {
+          const int r_w = ((m + w - 1) / w + tc::U_CH - 1) / tc::U_CH * tc::U_CH;
+          const int ws = (m + r_w - 1) / r_w;
+          const long waves = ((long)ctiles * ws + h->sms - 1) / h->sms;
+          const long cost = waves * (r_w / tc::U_CH + 4);
+          if (best < 0 || cost < best) {
+            best = cost;
+            nsplit = ws;
+            rps = r_w;
+          }
+        }
+        tc::k_resid_update_tc<<<dim3(ctiles, nsplit), tc::U_THREADS, tc::U_SMEM, st>>>(
+            tmWth, tmWtl, tmQrh, tmQrl, h->st, h->Ares, L.ld_res, m, n, rps, h->part_norm,
+            h->wait_budget > 0 ? h->wait_budget : kWaitBudgetDefault);
+      } else {
+        const int ctiles = (n - i + P2_COLS - 1) / P2_COLS;
+        // row split by the same wave rule, two CTAs per SM (registers and shared memory), with
+        // a fixed cost per CTA of about two stages (W staging, norm partials)
+        int rps = (m + P2_ROWS - 1) / P2_ROWS * P2_ROWS;
         long best = -1;
         for (int w = 1; w <= P2_MAX_SPLIT; ++w) {
           const int r_w = ((m + w - 1) / w + P2_ROWS - 1) / P2_ROWS * P2_ROWS;
@@ -196,15 +229,13 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
             rps = r_w;
           }
         }
+        k_resid_update<<<dim3(ctiles, nsplit), P2_THREADS, P2_SMEM, st>>>((const float*)Q, L.ld_res, h->Ares,
+                                                                         L.ld_res, h->st, m, n, rps, h->R, n,
+                                                                         h->part_norm);
       }
-      k_resid_update<<<dim3(ctiles, nsplit), P2_THREADS, P2_SMEM, st>>>((const float*)Q, L.ld_res, h->Ares, L.ld_res,
-                                                                       h->st, m, n, rps, h->R, n,
-                                                                       use_tc ? reinterpret_cast<const float2*>(h->Wpart)
-                                                                              : nullptr, wsplit,
-                                                                       h->part_norm);
       nproj = (n - i + 255) / 256;
       k_norm_reduce<<<nproj, 256, 0, st>>>(h->part_norm, nsplit, n, h->st, h->diags, h->part_res, h->part_nnz);
-      prof_end(h, RBRP_PHASE_UPDATE, ev, 0.0, 0.0, 2);
+      prof_end(h, RBRP_PHASE_UPDATE, ev, 0.0, 0.0, use_tc ? 3 : 2);
     } else {
       // basis tile height: the smallest KB >= b (kept <= b); b <= 8 takes the column-streaming form
       auto project = [&](auto kb) {

@@ -64,7 +64,11 @@ struct rbrp_handle_st {
                                // double-float pairs (float2, 8 bytes each)
   float* Qh = nullptr;         // residual form: TF32 hi / lo parts of the block basis, ld_res x 64
   float* Ql = nullptr;
-  int variant = 0;             // 0: tensor-core projection, 1: CUDA-core projection
+  float* Qrh = nullptr;        // the same parts by rows (m x 64, row major) for the tensor-core update
+  float* Qrl = nullptr;
+  float* Wth = nullptr;        // TF32 hi / lo parts of W^T (n x 64, position major) for the same
+  float* Wtl = nullptr;
+  int variant = 0;             // 0: tensor-core projection and update, 1: CUDA-core ones
   bool tsolve_fp64 = false;    // T solve on the FP64 pipe instead of double-float
   long long wait_budget = 0;   // clock64 limit of bounded device waits (0: the default, ~2 s)
 

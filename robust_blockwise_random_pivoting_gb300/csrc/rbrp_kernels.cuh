@@ -988,13 +988,12 @@ k_proj_w(const float* __restrict__ Qb, int64_t ldq, const float* __restrict__ Ar
   }
 }
 
-// P2: A_res(:, p) -= Q_blk W(:, p) and the partial squared norms of the updated
+// P2 on the CUDA cores (the CUDA-core variant; the default is k_resid_update_tc):
+// A_res(:, p) -= Q_blk W(:, p) and the partial squared norms of the updated
 // columns (double-float sums), for 64 positions x one row range per CTA.  Warp w
 // owns 8 columns, lane l four consecutive rows of every 128-row stage (16-byte
 // loads and stores, coalesced along the column).  Row ranges of the same columns
-// are summed by k_norm_reduce.  W comes either from R (one projection per
-// column) or from the row-split partials of the tensor-core projection, summed
-// here in split order; CTAs of the first row range then also write R(I2, p).
+// are summed by k_norm_reduce.  W comes from R (written by k_proj_w).
 constexpr int P2_COLS = 64;
 constexpr int P2_ROWS = 128;
 constexpr int P2_MAX_SPLIT = 8;
@@ -1014,8 +1013,8 @@ __device__ __forceinline__ void upd_wait() {
 
 __global__ void __launch_bounds__(P2_THREADS, 2)
 k_resid_update(const float* __restrict__ Qb, int64_t ldq, float* __restrict__ Ares, int64_t ld,
-               const State* __restrict__ st, int m, int n, int rows_per_split, double* __restrict__ R,
-               int64_t ldr, const float2* __restrict__ Wpart, int wsplit, double* __restrict__ part_norm) {
+               const State* __restrict__ st, int m, int n, int rows_per_split, const double* __restrict__ R,
+               int64_t ldr, double* __restrict__ part_norm) {
   extern __shared__ __align__(16) float p2_smem[];
   float* Ws = p2_smem;                       // Ws[a * P2_COLS + c]
   float* Qbuf = p2_smem + MAXB * P2_COLS;    // two stages of Qs[a * P2_ROWS + rr]
@@ -1027,22 +1026,7 @@ k_resid_update(const float* __restrict__ Qb, int64_t ldq, float* __restrict__ Ar
   const int rb = blockIdx.y * rows_per_split, re = min(m, rb + rows_per_split);
   for (int idx = tid; idx < kept * P2_COLS; idx += P2_THREADS) {
     const int a = idx / P2_COLS, c = idx % P2_COLS;
-    float wv = 0.f;
-    if (c < ncol) {
-      if (Wpart) {
-        // double-float sum of the row-split partials on the FP32 pipe; one row range writes R
-        dfl v = {0.f, 0.f};
-        for (int z = 0; z < wsplit; ++z) {
-          const float2 t = Wpart[((int64_t)z * MAXB + a) * n + p0 + c];
-          v = df_add(v, {t.x, t.y});
-        }
-        if (blockIdx.y == 0) R[(int64_t)(i + a) * ldr + p0 + c] = (double)v.hi + (double)v.lo;
-        wv = v.hi;
-      } else {
-        wv = (float)R[(int64_t)(i + a) * ldr + p0 + c];
-      }
-    }
-    Ws[idx] = wv;
+    Ws[idx] = c < ncol ? (float)R[(int64_t)(i + a) * ldr + p0 + c] : 0.f;
   }
   DF nrm[8];
 #pragma unroll

@@ -140,13 +140,15 @@ constexpr int QS_ROWS = 32;
 struct QSolveSmem {
   dfl Ri[MAXB][MAXB + 1];
   float W[MAXB][QS_ROWS + 1];
+  float Hr[QS_ROWS][MAXB + 1];  // the tile's hi / lo parts by rows, for the row-major copies
+  float Lr[QS_ROWS][MAXB + 1];
   int ord[MAXB];
 };
 
 __global__ void __launch_bounds__(256)
 k_panel_q_df(const float* __restrict__ V, int m, const State* __restrict__ st, const float2* __restrict__ Rinvg,
              const int* __restrict__ ordg, float* __restrict__ Q, int64_t ldq, float* __restrict__ Qh,
-             float* __restrict__ Ql, int64_t ldh) {
+             float* __restrict__ Ql, int64_t ldh, float* __restrict__ Qrh, float* __restrict__ Qrl) {
   extern __shared__ __align__(16) unsigned char dyn_smem[];
   QSolveSmem& sm = *reinterpret_cast<QSolveSmem*>(dyn_smem);
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
@@ -177,19 +179,32 @@ k_panel_q_df(const float* __restrict__ V, int m, const State* __restrict__ st, c
     }
   }
   const int r = r0 + lane;
-  if (r < m) {
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      const int s = w + 8 * q;
-      // FP32 basis and its exact TF32 split, on the FP32 pipe: q = hi + lo (double-float),
-      // Q = rn(q), Qh = tf32(Q), Ql = rn(q - Qh) with hi - Qh exact (Sterbenz)
-      const dfl v = s < kept ? acc[q] : dfl{0.f, 0.f};
-      const float qf = __fadd_rn(v.hi, v.lo);
+  for (int q = 0; q < 8; ++q) {
+    const int s = w + 8 * q;
+    // FP32 basis and its exact TF32 split, on the FP32 pipe: q = hi + lo (double-float),
+    // Q = rn(q), Qh = tf32(Q), Ql = rn(q - Qh) with hi - Qh exact (Sterbenz)
+    const dfl v = s < kept ? acc[q] : dfl{0.f, 0.f};
+    const float qf = __fadd_rn(v.hi, v.lo);
+    const float h = __uint_as_float(__float_as_uint(qf) & 0xFFFFE000u);
+    const float l = __fadd_rn(v.hi - h, v.lo);
+    if (r < m) {
       if (s < kept) Q[r + (int64_t)s * ldq] = qf;
       if (Qh) {
-        const float h = __uint_as_float(__float_as_uint(qf) & 0xFFFFE000u);
         Qh[r + (int64_t)s * ldh] = h;
-        Ql[r + (int64_t)s * ldh] = __fadd_rn(v.hi - h, v.lo);
+        Ql[r + (int64_t)s * ldh] = l;
+      }
+    }
+    sm.Hr[lane][s] = h;
+    sm.Lr[lane][s] = l;
+  }
+  if (Qrh) {  // the same parts by rows (64 per row), for the tensor-core update
+    __syncthreads();
+    for (int idx = tid; idx < QS_ROWS * MAXB; idx += 256) {
+      const int rr = idx / MAXB, s = idx % MAXB, rw = r0 + rr;
+      if (rw < m) {
+        Qrh[(int64_t)rw * MAXB + s] = sm.Hr[rr][s];
+        Qrl[(int64_t)rw * MAXB + s] = sm.Lr[rr][s];
       }
     }
   }

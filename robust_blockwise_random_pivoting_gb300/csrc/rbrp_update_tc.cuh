@@ -1,0 +1,284 @@
+// rbrp_update_tc.cuh - tcgen05 / TMEM / TMA residual update of the residual form (sm_103a).
+//
+// P2: A_res(r, p) -= sum_a Q_blk(r, a) W(a, p) for a tile of 128 trailing
+// positions p (the MMA M dimension, TMEM lanes) and the rows of one row range
+// in chunks of 64 (MMA N), with K = the kept basis vectors (<= 64, one or two
+// 32-wide halves).  Both operands come pre-split into exact TF32 hi / lo
+// parts, K-major: W^T from k_upd_w_prep (which also sums the projection's
+// row-split partials and writes R(I2, p)) and the basis by rows from
+// k_panel_q_df.  The CUDA-core form of the same step is k_resid_update.
+//
+//   warp 0   TMA: the W^T tile once (hi and lo, up to 64 KB), then the basis rows
+//            of every chunk (hi and lo, up to 32 KB) into a 4-stage ring.
+//   warp 1   MMA issuer: per chunk and K half, W_hi Q_hi into that half's large
+//            accumulator and W_hi Q_lo + W_lo Q_hi into the small one; 3 x 64 TMEM
+//            columns per chunk, double buffered.
+//   warps 2-9 the update: a thread owns one position and 32 rows of the chunk.  It
+//            loads those 32 residual entries (the next chunk's loads are in flight
+//            while it works on the current one), subtracts the three accumulators
+//            (tcgen05.ld), stores the result and adds its squares to the column's
+//            norm partial.
+//
+// Accuracy: each large accumulator takes the 4 MMAs of one K half (exact TF32
+// products), so its rounding - once per MMA, biased - stays at the level of an
+// FP32 FMA chain over the same terms; the small products are 2^-11 smaller.
+// Norm partials are FP32 sums of 32 squares (positive terms) folded into
+// double-float, one per row range and position, summed by k_norm_reduce.
+//
+// Every wait is bounded as in rbrp_tc.cuh; on a timeout the CTA sets an abort
+// flag and st->status, waits (bounded) for its own TMA copies and MMAs, frees
+// TMEM and returns.
+#pragma once
+#include "rbrp_df.cuh"
+#include "rbrp_tc.cuh"
+
+namespace rbrp {
+namespace tc {
+namespace {
+
+constexpr int U_CH = BN;                    // rows per chunk (MMA N = 64)
+constexpr int U_STAGES = 4;
+constexpr int U_NUPD = 256;                 // 8 update warps
+constexpr int U_THREADS = 64 + U_NUPD;
+constexpr int U_ACC = 3 * U_CH;             // TMEM columns per chunk: large (K half 0), large (half 1), small
+
+struct __align__(1024) UpdSmem {
+  uint8_t wt[2][2][A_BYTES];                // [K half][hi, lo]: W^T, 128 positions x 32
+  uint8_t qs[U_STAGES][2][2][B_BYTES];      // [stage][K half][hi, lo]: basis rows, 64 x 32
+  unsigned long long wfull, qfull[U_STAGES], qempty[U_STAGES], accf[2], acce[2], mmadone;
+  float2 nrm[BM];                           // norm partials of the second row half, by tile position
+  uint32_t tmem_base;
+  int abort;
+};
+constexpr size_t U_SMEM = sizeof(UpdSmem) + 1024;  // + alignment slack of the dynamic window
+
+// 32 residual entries of one column from row r0 (zeros at and past re); 16-byte
+// loads when all 32 are in range (columns and r0 are 128-byte aligned).
+__device__ __forceinline__ void upd_load32(float (&x)[32], const float* __restrict__ col, int r0, int re, bool pv) {
+  if (pv && r0 + 32 <= re) {
+#pragma unroll
+    for (int j = 0; j < 32; j += 4) {
+      const float4 v = *reinterpret_cast<const float4*>(col + r0 + j);
+      x[j] = v.x;
+      x[j + 1] = v.y;
+      x[j + 2] = v.z;
+      x[j + 3] = v.w;
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < 32; ++j) x[j] = (pv && r0 + j < re) ? col[r0 + j] : 0.f;
+  }
+}
+
+__global__ void __launch_bounds__(U_THREADS, 1)
+k_resid_update_tc(const __grid_constant__ CUtensorMap tmWh, const __grid_constant__ CUtensorMap tmWl,
+                  const __grid_constant__ CUtensorMap tmQh, const __grid_constant__ CUtensorMap tmQl, State* st,
+                  float* __restrict__ Ares, int64_t ld, int m, int n, int rows_per_split,
+                  double* __restrict__ part_norm, long long budget) {
+  extern __shared__ uint8_t u_raw[];
+  UpdSmem& sm = *reinterpret_cast<UpdSmem*>((reinterpret_cast<uintptr_t>(u_raw) + 1023) & ~(uintptr_t)1023);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = st->i, kept = st->bs;
+  const int p0 = i + kept + blockIdx.x * BM;
+  if (kept == 0 || p0 >= n) return;
+  const int rb = blockIdx.y * rows_per_split, re = min(m, rb + rows_per_split);
+  if (rb >= re) return;
+  const int nch = (re - rb + U_CH - 1) / U_CH;
+  const int nkc = kept > BK ? 2 : 1;
+  volatile int* abort = &sm.abort;
+
+  if (threadIdx.x == 0) {
+    mbar_init(&sm.wfull, 1);
+    for (int s = 0; s < U_STAGES; ++s) {
+      mbar_init(&sm.qfull[s], 1);
+      mbar_init(&sm.qempty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&sm.accf[b], 1);
+      mbar_init(&sm.acce[b], U_NUPD);
+    }
+    mbar_init(&sm.mmadone, 1);
+    sm.abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sm.tmem_base)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = sm.tmem_base;
+  int issued = 0;  // producer: chunks whose basis loads were issued
+  DF nrm;
+  nrm.hi = nrm.lo = 0.f;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      mbar_expect_tx(&sm.wfull, (uint32_t)(nkc * 2 * A_BYTES));
+      for (int kc = 0; kc < nkc; ++kc) {
+        tma_load_2d(sm.wt[kc][0], &tmWh, &sm.wfull, kc * BK, p0);
+        tma_load_2d(sm.wt[kc][1], &tmWl, &sm.wfull, kc * BK, p0);
+      }
+      for (int c = 0; c < nch; ++c) {
+        const int slot = c % U_STAGES;
+        const uint32_t use = (uint32_t)(c / U_STAGES);
+        if (c >= U_STAGES && !mbar_wait(&sm.qempty[slot], (use & 1) ^ 1, abort, budget)) break;
+        mbar_expect_tx(&sm.qfull[slot], (uint32_t)(nkc * 2 * B_BYTES));
+        for (int kc = 0; kc < nkc; ++kc) {
+          tma_load_2d(sm.qs[slot][kc][0], &tmQh, &sm.qfull[slot], kc * BK, rb + c * U_CH);
+          tma_load_2d(sm.qs[slot][kc][1], &tmQl, &sm.qfull[slot], kc * BK, rb + c * U_CH);
+        }
+        issued = c + 1;
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0 && mbar_wait(&sm.wfull, 0u, abort, budget)) {
+      for (int c = 0; c < nch; ++c) {
+        const int slot = c % U_STAGES, buf = c & 1;
+        const uint32_t use = (uint32_t)(c / U_STAGES);
+        if (c >= 2 && !mbar_wait(&sm.acce[buf], (uint32_t)((c >> 1) - 1) & 1, abort, budget)) break;
+        if (!mbar_wait(&sm.qfull[slot], use & 1, abort, budget)) break;
+        tc_fence_after();
+        const uint32_t dacc = tbase + (uint32_t)(buf * U_ACC);
+        for (int kc = 0; kc < nkc; ++kc) {
+          const uint64_t dwh = sw128_desc(smem_u32(sm.wt[kc][0]));
+          const uint64_t dwl = sw128_desc(smem_u32(sm.wt[kc][1]));
+          const uint64_t dqh = sw128_desc(smem_u32(sm.qs[slot][kc][0]));
+          const uint64_t dql = sw128_desc(smem_u32(sm.qs[slot][kc][1]));
+#pragma unroll
+          for (int k = 0; k < BK / 8; ++k) {
+            mma_tf32(dacc + (uint32_t)(kc * U_CH), dwh + 2 * k, dqh + 2 * k, k == 0 ? 0u : 1u);
+            mma_tf32(dacc + (uint32_t)(2 * U_CH), dwh + 2 * k, dql + 2 * k, (kc == 0 && k == 0) ? 0u : 1u);
+            mma_tf32(dacc + (uint32_t)(2 * U_CH), dwl + 2 * k, dqh + 2 * k, 1u);
+          }
+        }
+        mma_commit(&sm.qempty[slot]);
+        mma_commit(&sm.accf[buf]);
+      }
+    }
+  } else {
+    const int q = warp & 3;               // TMEM lane quarter of this warp
+    const int ch = (warp - 2) >> 2;       // row half of each chunk
+    const int tp = 32 * q + lane;         // tile position
+    const int p = p0 + tp;
+    const bool pv = p < n;
+    float* __restrict__ col = Ares + (int64_t)(pv ? p : p0) * ld;
+    const uint32_t toff = ((uint32_t)(32 * q) << 16) + (uint32_t)(32 * ch);
+    float x[32], xn[32];
+    upd_load32(x, col, rb + 32 * ch, re, pv);
+    for (int c = 0; c < nch; ++c) {
+      const int r0 = rb + c * U_CH + 32 * ch;
+      if (c + 1 < nch) upd_load32(xn, col, r0 + U_CH, re, pv);
+      const int buf = c & 1;
+      if (!mbar_wait(&sm.accf[buf], (uint32_t)(c >> 1) & 1, abort, budget)) break;
+      tc_fence_after();
+      const uint32_t ta = tbase + toff + (uint32_t)(buf * U_ACC);
+      float v[32];
+      tmem_ld32(ta, v);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) x[j] -= v[j];
+      if (nkc > 1) {
+        tmem_ld32(ta + U_CH, v);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) x[j] -= v[j];
+      }
+      tmem_ld32(ta + 2 * U_CH, v);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) x[j] -= v[j];
+      tc_fence_before();
+      mbar_arrive(&sm.acce[buf]);
+      float s = 0.f;
+      if (pv && r0 + 32 <= re) {
+#pragma unroll
+        for (int j = 0; j < 32; j += 4) {
+          *reinterpret_cast<float4*>(col + r0 + j) = make_float4(x[j], x[j + 1], x[j + 2], x[j + 3]);
+          s = fmaf(x[j + 3], x[j + 3], fmaf(x[j + 2], x[j + 2], fmaf(x[j + 1], x[j + 1], fmaf(x[j], x[j], s))));
+        }
+      } else if (pv) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+          if (r0 + j < re) {
+            col[r0 + j] = x[j];
+            s = fmaf(x[j], x[j], s);
+          }
+      }
+      df_acc(nrm.hi, nrm.lo, s);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) x[j] = xn[j];
+    }
+    if (ch == 1) sm.nrm[tp] = make_float2(nrm.hi, nrm.lo);
+  }
+  __syncthreads();
+  if (!*abort && warp >= 2 && ((warp - 2) >> 2) == 0) {
+    // the two row halves of each position, in a fixed order
+    const int tp = 32 * (warp & 3) + lane, p = p0 + tp;
+    const float2 o = sm.nrm[tp];
+    const dfl a = df_add(df_two_sum(nrm.hi, nrm.lo), dfl{o.x, o.y});
+    if (p < n) part_norm[(int64_t)blockIdx.y * n + p] = (double)a.hi + (double)a.lo;
+  }
+  if (*abort) {
+    // as k_proj_w_tc: the CTA's own TMA copies and issued MMAs finish before TMEM is freed
+    int dummy = 0;
+    volatile int* never = &dummy;
+    if (threadIdx.x == 0) atomicExch(&st->status, ST_ERR_TIMEOUT);
+    if (warp == 0 && lane == 0) {
+      mbar_wait(&sm.wfull, 0u, never);
+      for (int c = issued - U_STAGES > 0 ? issued - U_STAGES : 0; c < issued; ++c)
+        mbar_wait(&sm.qfull[c % U_STAGES], (uint32_t)(c / U_STAGES) & 1, never);
+    }
+    if (warp == 1 && lane == 0) {
+      mma_commit(&sm.mmadone);
+      mbar_wait(&sm.mmadone, 0u, never);
+    }
+    __syncthreads();
+  }
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(TMEM_COLS) : "memory");
+  }
+}
+
+// W^T for k_resid_update_tc, 32 trailing positions per CTA: W(a, p) = the
+// double-float sum of the projection's row-split partials in split order (as
+// k_resid_update sums them), R(i + a, p) = W in FP64, and the TF32 hi / lo parts
+// of rn(W) into Wth / Wtl (position-major, 64 per position, zero for a >= kept).
+__global__ void __launch_bounds__(256)
+k_upd_w_prep(const State* __restrict__ st, int n, const float2* __restrict__ Wpart, int wsplit,
+             double* __restrict__ R, int64_t ldr, float* __restrict__ Wth, float* __restrict__ Wtl) {
+  __shared__ float tile[32][MAXB + 1];
+  const int i = st->i, kept = st->bs;
+  const int pb = i + kept + blockIdx.x * 32;
+  if (kept == 0 || pb >= n) return;
+  const int tid = threadIdx.x;
+  for (int idx = tid; idx < 32 * MAXB; idx += 256) {
+    const int pp = idx & 31, a = idx >> 5, p = pb + pp;
+    float w = 0.f;
+    if (a < kept && p < n) {
+      dfl v = {0.f, 0.f};
+      for (int z = 0; z < wsplit; ++z) {
+        const float2 t = Wpart[((int64_t)z * MAXB + a) * n + p];
+        v = df_add(v, {t.x, t.y});
+      }
+      R[(int64_t)(i + a) * ldr + p] = (double)v.hi + (double)v.lo;
+      w = v.hi;
+    }
+    tile[pp][a] = w;
+  }
+  __syncthreads();
+  for (int idx = tid; idx < 32 * MAXB; idx += 256) {
+    const int a = idx & (MAXB - 1), pp = idx / MAXB, p = pb + pp;
+    if (p < n) {
+      const float w = tile[pp][a];
+      const float h = tf32_trunc(w);
+      Wth[(int64_t)p * MAXB + a] = h;
+      Wtl[(int64_t)p * MAXB + a] = w - h;
+    }
+  }
+}
+
+}  // namespace
+}  // namespace tc
+}  // namespace rbrp

@@ -194,7 +194,7 @@ class Handle:
         check(self.lib.rbrp_set_profiling(self.h, int(bool(on))), self.h)
 
     def set_variant(self, variant):
-        """Projection kernel of the FP32 form: 0 = tcgen05 (default), 1 = CUDA-core FFMA."""
+        """Projection and update kernels of the FP32 form: 0 = tcgen05 (default), 1 = CUDA-core FFMA."""
         check(self.lib.rbrp_set_variant(self.h, int(variant)), self.h)
 
     def set_tsolve_fp64(self, on=True):
