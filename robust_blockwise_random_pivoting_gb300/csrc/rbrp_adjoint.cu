@@ -359,9 +359,7 @@ __global__ void k_adj_loss(const float2* __restrict__ loss_part, int nparts, con
 // ---------------------------------------------------------------------------
 // tensor-core path
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ float tf32_hi(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
-
-// Tx (k x nc, ld kp) = FP32 T; T^T hi / lo (nc x k, ld ncp) = tf32(t), fp32(t - tf32(t))
+// Tx (k x nc, ld kp) = FP32 T; T^T hi / lo (nc x k, ld ncp) = tf32_rn(t), tf32_rn(t - hi)
 // from the FP64 T; wr[c] = W[perm[k + c]].  32 x 32 tiles through shared memory.
 __global__ void k_adj_prep_tc(const double* __restrict__ T, int k, int nc, int kp, int ncp,
                               const float* __restrict__ W, const int* __restrict__ perm, float* __restrict__ Tx,
@@ -383,16 +381,16 @@ __global__ void k_adj_prep_tc(const double* __restrict__ T, int k, int nc, int k
     const int t = t0 + q, c = c0 + tx;
     if (t < k && c < nc) {
       const double v = tile[tx][q];
-      const float h = tf32_hi((float)v);
+      const float h = tf32_rn((float)v);
       Trh[c + (int64_t)t * ncp] = h;
-      Trl[c + (int64_t)t * ncp] = (float)(v - (double)h);
+      Trl[c + (int64_t)t * ncp] = tf32_rn((float)(v - (double)h));
     }
   }
   if (blockIdx.x == 0)
     for (int c = c0 + threadIdx.x; c < min(nc, c0 + 32); c += blockDim.x) wr[c] = W[perm[k + c]];
 }
 
-// C^T hi / lo (k x m, ld kp): element (t, r) = A[r, perm[t]] split into tf32 and the rest.
+// C^T hi / lo (k x m, ld kp): element (t, r) = A[r, perm[t]] split by tf32_split.
 __global__ void k_adj_gather_ct(const float* __restrict__ A, int64_t lda, const int* __restrict__ perm, int k,
                                 int m, int kp, float* __restrict__ Cth, float* __restrict__ Ctl) {
   __shared__ float tile[32][33];
@@ -406,10 +404,10 @@ __global__ void k_adj_gather_ct(const float* __restrict__ A, int64_t lda, const 
   for (int q = ty; q < 32; q += 8) {
     const int t = t0 + tx, r = r0 + q;
     if (t < k && r < m) {
-      const float v = tile[tx][q];
-      const float h = tf32_hi(v);
+      float h, l;
+      tf32_split(tile[tx][q], h, l);
       Cth[t + (int64_t)r * kp] = h;
-      Ctl[t + (int64_t)r * kp] = v - h;
+      Ctl[t + (int64_t)r * kp] = l;
     }
   }
 }

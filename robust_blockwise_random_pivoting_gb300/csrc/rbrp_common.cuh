@@ -159,4 +159,19 @@ __device__ __forceinline__ void df_add_sq(DF& s, float x) {
   s.lo += e + pe;
 }
 
+// x rounded to the nearest TF32 value (ties away from zero) for finite x below
+// 2^127: adding half a TF32 ulp to the bit pattern carries into the kept bits
+// exactly when the dropped part is at least half an ulp.
+__device__ __forceinline__ float tf32_rn(float x) {
+  return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
+}
+// The operand split of the tensor cores' 3xTF32 / 4xTF32 products: hi =
+// tf32_rn(x) and lo = tf32_rn(x - hi) (x - hi is exact), both TF32 values, so the
+// tensor core reads them without loss and |x - hi - lo| <= 2^-23 |x|: a product
+// of split operands is good to about an FP32 product's error.
+__device__ __forceinline__ void tf32_split(float x, float& hi, float& lo) {
+  hi = tf32_rn(x);
+  lo = tf32_rn(x - hi);
+}
+
 }  // namespace rbrp

@@ -151,7 +151,7 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
     if (i > 0) k_swap_R<<<(i + 127) / 128, 128, 0, st>>>(h->R, n, h->st, h->J, h->K1, h->K2);
     if (RES)
       k_swap_cols<<<dim3((m + 1023) / 1024, MAXB), 256, 0, st>>>(h->Ares, L.ld_res, h->st, m, h->K1, h->K2);
-    if (!RES) k_panel2<T><<<ntiles, 256, panel_smem, st>>>(h->Q1, m, h->st, h->R2, Q, m, 1, nullptr, nullptr, 0);
+    if (!RES) k_panel2<T><<<ntiles, 256, panel_smem, st>>>(h->Q1, m, h->st, h->R2, Q, m, 1);
     prof_end(h, RBRP_PHASE_PANEL, ev, 0.0, 0.0, RES ? (i > 0 ? 5 : 4) : (i > 0 ? 6 : 5));
     int nproj;
     ev = prof_begin(h);

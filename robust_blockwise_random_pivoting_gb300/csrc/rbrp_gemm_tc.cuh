@@ -12,7 +12,8 @@
 //            (64 x 32) into a 4-stage ring, 128-byte swizzled.
 //   warp 1   MMA issuer: X hi Y hi into a large accumulator, X hi Y lo and
 //            X lo Y hi into a small one (3xTF32: the FP32 product to ~2^-22).
-//   warps 2-5 split each staged X tile into exact TF32 hi + lo parts.
+//   warps 2-5 split each staged X tile into hi (rounded to the nearest TF32
+//            value) + lo parts, exact in FP32.
 //   warps 6-13 drain the large accumulator after every RBRP_GEMM_DRAIN stages
 //            and the small one every CHUNK stages into double-float registers, then call the
 //            epilogue: thread (lane quarter q, column half ch) holds
@@ -141,9 +142,13 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUten
 #pragma unroll
       for (int e = et; e < A_BYTES / 16; e += NSPLIT) {
         const float4 v = a4[e];
-        const float4 h = make_float4(tf32_trunc(v.x), tf32_trunc(v.y), tf32_trunc(v.z), tf32_trunc(v.w));
+        float4 h, l;
+        tf32_split(v.x, h.x, l.x);
+        tf32_split(v.y, h.y, l.y);
+        tf32_split(v.z, h.z, l.z);
+        tf32_split(v.w, h.w, l.w);
         a4[e] = h;
-        l4[e] = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+        l4[e] = l;
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       mbar_arrive(&sm.split[slot]);

@@ -619,12 +619,10 @@ __global__ void k_swap_R(double* __restrict__ R, int64_t ldr, const State* __res
 }
 
 // Second CholQR pass: Q_blk = Q1 R2^{-1}, 64 rows per CTA.
-// With Qh != nullptr also the exact TF32 split of the basis for the tensor-core
-// projection: Qh = tf32(Q), Ql = fp32(Q - Qh) (ld = ldh), zero beyond the kept columns.
 template <typename T>
 __global__ void __launch_bounds__(256)
 k_panel2(const double* __restrict__ Q1, int m, const State* __restrict__ st, const double* __restrict__ R2g,
-         T* __restrict__ Q, int64_t ldq, int q_at_i, float* __restrict__ Qh, float* __restrict__ Ql, int64_t ldh) {
+         T* __restrict__ Q, int64_t ldq, int q_at_i) {
   extern __shared__ __align__(16) unsigned char dyn_smem[];
   PanelSmem& sm = *reinterpret_cast<PanelSmem*>(dyn_smem);
   const int tid = threadIdx.x;
@@ -641,17 +639,6 @@ k_panel2(const double* __restrict__ Q1, int m, const State* __restrict__ st, con
   for (int idx = tid; idx < 64 * kept; idx += blockDim.x) {
     const int rr = idx & 63, s = idx >> 6, r = r0 + rr;
     if (r < m) Q[r + (int64_t)((q_at_i ? i : 0) + s) * ldq] = (T)sm.W[rr][s];
-  }
-  if (Qh) {
-    for (int idx = tid; idx < 64 * MAXB; idx += blockDim.x) {
-      const int rr = idx & 63, s = idx >> 6, r = r0 + rr;
-      if (r < m) {
-        const double q = s < kept ? sm.W[rr][s] : 0.0;
-        const float h = __uint_as_float(__float_as_uint((float)q) & 0xFFFFE000u);
-        Qh[r + (int64_t)s * ldh] = h;
-        Ql[r + (int64_t)s * ldh] = (float)(q - (double)h);
-      }
-    }
   }
 }
 

@@ -129,8 +129,9 @@ k_pchol_df(const double* __restrict__ G, int m, State* st, double tol_loc, const
 }
 
 // Q_blk = V(:, ord[:kept]) R11^{-1} in double-float as the product with the explicit
-// inverse (k_pchol_df), written as the FP32 basis and its exact TF32 split (Qh =
-// tf32(Q), Ql = fp32(Q - Qh), zero beyond the kept columns).  Every output is an
+// inverse (k_pchol_df), written as the FP32 basis and its TF32 split (Qh = Q
+// rounded to the nearest TF32 value, Ql = fp32(q - Qh); zero beyond the kept
+// columns), by columns for the projection and by rows for the update.  Every output is an
 // independent dot product: a CTA takes 32 rows, warp w the outputs s = w + 8q of
 // every row (lane = row, so the stores coalesce), eight chains per thread.  One
 // CholQR pass suffices here: with ~48-bit arithmetic the loss of orthogonality,
@@ -182,12 +183,13 @@ k_panel_q_df(const float* __restrict__ V, int m, const State* __restrict__ st, c
 #pragma unroll
   for (int q = 0; q < 8; ++q) {
     const int s = w + 8 * q;
-    // FP32 basis and its exact TF32 split, on the FP32 pipe: q = hi + lo (double-float),
-    // Q = rn(q), Qh = tf32(Q), Ql = rn(q - Qh) with hi - Qh exact (Sterbenz)
+    // FP32 basis and its TF32 split, on the FP32 pipe: q = hi + lo (double-float),
+    // Q = rn(q), Qh = Q rounded to the nearest TF32 value, Ql = q - Qh (hi - Qh
+    // exact by Sterbenz) rounded to the nearest TF32 value: q - Qh - Ql <= 2^-23 |q|
     const dfl v = s < kept ? acc[q] : dfl{0.f, 0.f};
     const float qf = __fadd_rn(v.hi, v.lo);
-    const float h = __uint_as_float(__float_as_uint(qf) & 0xFFFFE000u);
-    const float l = __fadd_rn(v.hi - h, v.lo);
+    const float h = tf32_rn(qf);
+    const float l = tf32_rn(__fadd_rn(v.hi - h, v.lo));
     if (r < m) {
       if (s < kept) Q[r + (int64_t)s * ldq] = qf;
       if (Qh) {

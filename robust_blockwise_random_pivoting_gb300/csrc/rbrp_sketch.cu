@@ -63,8 +63,8 @@ __global__ void __launch_bounds__(GT) k_sketch_gemm(const float* __restrict__ G,
   }
 }
 
-// Gt (m x l, ld mp) hi and lo TF32 parts of G^T (hi = G truncated to TF32,
-// lo = G - hi), through a 32 x 32 shared tile so both sides are coalesced.
+// Gt (m x l, ld mp) hi and lo TF32 parts of G^T (tf32_split), through a 32 x 32
+// shared tile so both sides are coalesced.
 __global__ void k_gt_split(const float* __restrict__ G, int l, int m, int64_t mp, float* __restrict__ Gth,
                            float* __restrict__ Gtl) {
   __shared__ float tile[32][33];
@@ -78,10 +78,10 @@ __global__ void k_gt_split(const float* __restrict__ G, int l, int m, int64_t mp
   for (int y = ty; y < 32; y += 8) {
     const int kc = k0 + tx, r = r0 + y;
     if (r < l && kc < m) {
-      const float g = tile[tx][y];
-      const float hi = tc::tf32_trunc(g);
+      float hi, lo;
+      tf32_split(tile[tx][y], hi, lo);
       Gth[kc + (int64_t)r * mp] = hi;
-      Gtl[kc + (int64_t)r * mp] = g - hi;
+      Gtl[kc + (int64_t)r * mp] = lo;
     }
   }
 }

@@ -7,8 +7,8 @@
 //   warp 0   TMA producer: A_res tile (128 columns x 32 rows, FP32) and the hi
 //            and lo parts of the Q tile (64 x 32) into a 4-stage ring, 128-byte
 //            swizzled, completion on an mbarrier with a transaction count.
-//   warp 1   MMA issuer: tcgen05.mma kind::tf32.  The FP32 data is split exactly
-//            into TF32 hi + lo parts; per K step the large product Ahi Qhi goes
+//   warp 1   MMA issuer: tcgen05.mma kind::tf32.  The FP32 data is split into
+//            hi (rounded to the nearest TF32 value) + lo parts, exact in FP32; per K step the large product Ahi Qhi goes
 //            to one TMEM accumulator and the two small ones (Ahi Qlo, Alo Qhi)
 //            to another.
 //   warps 2-5 split each staged A tile into its hi / lo parts (in shared
@@ -162,7 +162,6 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
   for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
 }
 
-__device__ __forceinline__ float tf32_trunc(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
 
 __device__ __forceinline__ void df_acc(float& hi, float& lo, float x) {
   const float t = hi + x;
@@ -297,9 +296,13 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
 #pragma unroll
       for (int e = et; e < A_BYTES / 16; e += NSPLIT) {
         const float4 v = a4[e];
-        const float4 h = make_float4(tf32_trunc(v.x), tf32_trunc(v.y), tf32_trunc(v.z), tf32_trunc(v.w));
+        float4 h, l;
+        tf32_split(v.x, h.x, l.x);
+        tf32_split(v.y, h.y, l.y);
+        tf32_split(v.z, h.z, l.z);
+        tf32_split(v.w, h.w, l.w);
         a4[e] = h;
-        l4[e] = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+        l4[e] = l;
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       mbar_arrive(&sm.split[slot]);

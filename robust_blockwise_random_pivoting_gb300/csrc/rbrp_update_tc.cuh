@@ -3,25 +3,29 @@
 // P2: A_res(r, p) -= sum_a Q_blk(r, a) W(a, p) for a tile of 128 trailing
 // positions p (the MMA M dimension, TMEM lanes) and the rows of one row range
 // in chunks of 64 (MMA N), with K = the kept basis vectors (<= 64, one or two
-// 32-wide halves).  Both operands come pre-split into exact TF32 hi / lo
-// parts, K-major: W^T from k_upd_w_prep (which also sums the projection's
+// 32-wide halves).  Both operands come pre-split into TF32 hi / lo parts
+// (hi + lo = the FP32 value), K-major: W^T from k_upd_w_prep (which also sums the projection's
 // row-split partials and writes R(I2, p)) and the basis by rows from
 // k_panel_q_df.  The CUDA-core form of the same step is k_resid_update.
 //
 //   warp 0   TMA: the W^T tile once (hi and lo, up to 64 KB), then the basis rows
 //            of every chunk (hi and lo, up to 32 KB) into a 4-stage ring.
 //   warp 1   MMA issuer: per chunk and K half, W_hi Q_hi into that half's large
-//            accumulator and W_hi Q_lo + W_lo Q_hi into the small one; 3 x 64 TMEM
-//            columns per chunk, double buffered.
+//            accumulator and W_hi Q_lo + W_lo Q_hi + W_lo Q_lo into the small one;
+//            3 x 64 TMEM columns per chunk, double buffered.
 //   warps 2-9 the update: a thread owns one position and 32 rows of the chunk.  It
 //            loads those 32 residual entries (the next chunk's loads are in flight
 //            while it works on the current one), subtracts the three accumulators
 //            (tcgen05.ld), stores the result and adds its squares to the column's
 //            norm partial.
 //
-// Accuracy: each large accumulator takes the 4 MMAs of one K half (exact TF32
-// products), so its rounding - once per MMA, biased - stays at the level of an
-// FP32 FMA chain over the same terms; the small products are 2^-11 smaller.
+// Accuracy: both operands are split by tf32_split (hi and lo rounded to the
+// nearest TF32 values, the pair within 2^-23 of the value) and all four products
+// are taken - the kernel is bound by memory, not by the MMAs - so each product is
+// good to ~2^-22, about an FP32 product's error.  Each large accumulator takes the 4
+// MMAs of one K half (exact TF32 products), so its rounding - once per MMA,
+// biased - stays at the level of an FP32 FMA chain over the same terms; the
+// small products are 2^-11 smaller.
 // Norm partials are FP32 sums of 32 squares (positive terms) folded into
 // double-float, one per row range and position, summed by k_norm_reduce.
 //
@@ -153,6 +157,7 @@ k_resid_update_tc(const __grid_constant__ CUtensorMap tmWh, const __grid_constan
             mma_tf32(dacc + (uint32_t)(kc * U_CH), dwh + 2 * k, dqh + 2 * k, k == 0 ? 0u : 1u);
             mma_tf32(dacc + (uint32_t)(2 * U_CH), dwh + 2 * k, dql + 2 * k, (kc == 0 && k == 0) ? 0u : 1u);
             mma_tf32(dacc + (uint32_t)(2 * U_CH), dwl + 2 * k, dqh + 2 * k, 1u);
+            mma_tf32(dacc + (uint32_t)(2 * U_CH), dwl + 2 * k, dql + 2 * k, 1u);
           }
         }
         mma_commit(&sm.qempty[slot]);
@@ -244,7 +249,8 @@ k_resid_update_tc(const __grid_constant__ CUtensorMap tmWh, const __grid_constan
 // W^T for k_resid_update_tc, 32 trailing positions per CTA: W(a, p) = the
 // double-float sum of the projection's row-split partials in split order (as
 // k_resid_update sums them), R(i + a, p) = W in FP64, and the TF32 hi / lo parts
-// of rn(W) into Wth / Wtl (position-major, 64 per position, zero for a >= kept).
+// of rn(W) (tf32_split) into Wth / Wtl (position-major, 64 per position, zero
+// for a >= kept).
 __global__ void __launch_bounds__(256)
 k_upd_w_prep(const State* __restrict__ st, int n, const float2* __restrict__ Wpart, int wsplit,
              double* __restrict__ R, int64_t ldr, float* __restrict__ Wth, float* __restrict__ Wtl) {
@@ -271,10 +277,10 @@ k_upd_w_prep(const State* __restrict__ st, int n, const float2* __restrict__ Wpa
   for (int idx = tid; idx < 32 * MAXB; idx += 256) {
     const int a = idx & (MAXB - 1), pp = idx / MAXB, p = pb + pp;
     if (p < n) {
-      const float w = tile[pp][a];
-      const float h = tf32_trunc(w);
+      float h, l;
+      tf32_split(tile[pp][a], h, l);
       Wth[(int64_t)p * MAXB + a] = h;
-      Wtl[(int64_t)p * MAXB + a] = w - h;
+      Wtl[(int64_t)p * MAXB + a] = l;
     }
   }
 }
