@@ -14,8 +14,8 @@
 //            accumulator and W_hi Q_lo + W_lo Q_hi + W_lo Q_lo into the small one;
 //            3 x 64 TMEM columns per chunk, double buffered.
 //   warps 2-9 the update: a thread owns one position and 32 rows of the chunk.  It
-//            loads those 32 residual entries (the next chunk's loads are in flight
-//            while it works on the current one), subtracts the three accumulators
+//            loads those 32 residual entries (the next two chunks' loads are in
+//            flight while it works on the current one), subtracts the three accumulators
 //            (tcgen05.ld), stores the result and adds its squares to the column's
 //            norm partial.
 //
@@ -172,13 +172,18 @@ k_resid_update_tc(const __grid_constant__ CUtensorMap tmWh, const __grid_constan
     const bool pv = p < n;
     float* __restrict__ col = Ares + (int64_t)(pv ? p : p0) * ld;
     const uint32_t toff = ((uint32_t)(32 * q) << 16) + (uint32_t)(32 * ch);
-    float x[32], xn[32];
-    upd_load32(x, col, rb + 32 * ch, re, pv);
-    for (int c = 0; c < nch; ++c) {
+    // a ring of three register chunks: while chunk c is updated, the loads of chunks
+    // c + 1 and c + 2 are in flight (64 KB per SM)
+    bool ok = true;
+    auto step = [&](float (&x)[32], float (&xf)[32], int c) {
+      if (!ok || c >= nch) return;
       const int r0 = rb + c * U_CH + 32 * ch;
-      if (c + 1 < nch) upd_load32(xn, col, r0 + U_CH, re, pv);
+      if (c + 2 < nch) upd_load32(xf, col, r0 + 2 * U_CH, re, pv);
       const int buf = c & 1;
-      if (!mbar_wait(&sm.accf[buf], (uint32_t)(c >> 1) & 1, abort, budget)) break;
+      if (!mbar_wait(&sm.accf[buf], (uint32_t)(c >> 1) & 1, abort, budget)) {
+        ok = false;
+        return;
+      }
       tc_fence_after();
       const uint32_t ta = tbase + toff + (uint32_t)(buf * U_ACC);
       float v[32];
@@ -211,8 +216,14 @@ k_resid_update_tc(const __grid_constant__ CUtensorMap tmWh, const __grid_constan
           }
       }
       df_acc(nrm.hi, nrm.lo, s);
-#pragma unroll
-      for (int j = 0; j < 32; ++j) x[j] = xn[j];
+    };
+    float x0[32], x1[32], x2[32];
+    upd_load32(x0, col, rb + 32 * ch, re, pv);
+    if (nch > 1) upd_load32(x1, col, rb + U_CH + 32 * ch, re, pv);
+    for (int c = 0; c < nch && ok; c += 3) {
+      step(x0, x2, c);
+      step(x1, x0, c + 1);
+      step(x2, x1, c + 2);
     }
     if (ch == 1) sm.nrm[tp] = make_float2(nrm.hi, nrm.lo);
   }
