@@ -47,7 +47,7 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
                                              (int)P2_SMEM), "cudaFuncSetAttribute(k_resid_update)");
       if (s != RBRP_OK) return s;
       s = cuda_check(h, cudaFuncSetAttribute(tc::k_proj_w_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)tc::P1_SMEM), "cudaFuncSetAttribute(k_proj_w_tc)");
+                                             (int)tc::PROJ_SMEM), "cudaFuncSetAttribute(k_proj_w_tc)");
       if (s != RBRP_OK) return s;
       s = cuda_check(h, cudaFuncSetAttribute(tc::k_resid_update_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)tc::U_SMEM), "cudaFuncSetAttribute(k_resid_update_tc)");
@@ -179,7 +179,7 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
             sps = s_w;
           }
         }
-        tc::k_proj_w_tc<<<dim3(ctiles, wsplit), tc::NTHREADS, tc::P1_SMEM, st>>>(
+        tc::k_proj_w_tc<<<dim3(ctiles, wsplit), tc::NTHREADS, tc::PROJ_SMEM, st>>>(
             tmA, tmQh, tmQl, h->st, m, n, sps, reinterpret_cast<float2*>(h->Wpart),
             h->wait_budget > 0 ? h->wait_budget : kWaitBudgetDefault);
       } else {

@@ -194,28 +194,50 @@ __device__ __forceinline__ void drain32(uint32_t taddr, float (&hi)[32], float (
   }
 }
 
+// Shared memory of k_proj_w_tc: the TMA ring holds raw A tiles only (16 KB a
+// stage, so 112 KB of A are in flight per SM); the split warps turn each into
+// its hi / lo parts in one of two operand slots, which also receive that
+// stage's Q hi / lo tiles, and free the raw slot at once.
+constexpr int RAW = 7;                                   // raw A stages in flight
+struct __align__(1024) ProjSmem {
+  uint8_t raw[RAW][A_BYTES];
+  uint8_t op[2][STAGE_BYTES];                            // A hi, A lo, Q hi, Q lo
+  unsigned long long rfull[RAW], rempty[RAW];            // raw ring: TMA done / split done
+  unsigned long long ofree[2], osplit[2], oq[2];         // operand slots: MMAs done / split done / Q landed
+  unsigned long long bigf[NBIG], bige[NBIG];             // large accumulators: full (MMA done) / empty (drained)
+  unsigned long long smlf[2], smle[2];                   // small accumulator
+  unsigned long long mmadone;                            // abort path: every MMA this CTA issued has completed
+  uint32_t tmem_base;
+  int abort;
+};
+constexpr size_t PROJ_SMEM = sizeof(ProjSmem) + 1024;    // + alignment slack of the dynamic window
+
 __global__ void __launch_bounds__(NTHREADS, 1)
 k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmQh,
             const __grid_constant__ CUtensorMap tmQl, State* st, int m, int n, int stages_per_split,
             float2* __restrict__ Wpart, long long budget) {
   extern __shared__ uint8_t p1_raw[];
-  P1Smem& sm = *reinterpret_cast<P1Smem*>((reinterpret_cast<uintptr_t>(p1_raw) + 1023) & ~(uintptr_t)1023);
+  ProjSmem& sm = *reinterpret_cast<ProjSmem*>((reinterpret_cast<uintptr_t>(p1_raw) + 1023) & ~(uintptr_t)1023);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int i = st->i, kept = st->bs;
   const int p0 = i + kept + blockIdx.x * BM;
   if (kept == 0 || p0 >= n) return;
   // this CTA's row range: stages [s0, s0 + nk) of 32 rows (CTAs along y split the rows;
-  // their partial W are summed, in split order, by the residual update)
+  // their partial W are summed, in split order, by the update)
   const int s0 = blockIdx.y * stages_per_split;
   const int nk = min(stages_per_split, (m + BK - 1) / BK - s0);
   if (nk <= 0) return;
   volatile int* abort = &sm.abort;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < STAGES; ++s) {
-      mbar_init(&sm.full[s], 1);
-      mbar_init(&sm.split[s], NSPLIT);
-      mbar_init(&sm.empty[s], 1);
+    for (int s = 0; s < RAW; ++s) {
+      mbar_init(&sm.rfull[s], 1);
+      mbar_init(&sm.rempty[s], NSPLIT);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&sm.ofree[b], 1);
+      mbar_init(&sm.osplit[b], NSPLIT);
+      mbar_init(&sm.oq[b], 1);
     }
     for (int b = 0; b < NBIG; ++b) {
       mbar_init(&sm.bigf[b], 1);
@@ -239,35 +261,33 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
   __syncthreads();
   tc_fence_after();
   const uint32_t tbase = sm.tmem_base;
-  int issued = 0;  // producer: stages whose TMA loads were issued
+  int issued = 0;   // producer: stages whose A loads were issued
+  int qissued = 0;  // first split thread: stages whose Q loads were issued
 
   if (warp == 0) {
     if (lane == 0) {
       for (int s = 0; s < nk; ++s) {
-        const int slot = s % STAGES;
-        const uint32_t use = (uint32_t)(s / STAGES);
-        if (s >= STAGES && !mbar_wait(&sm.empty[slot], (use & 1) ^ 1, abort, budget)) break;
-        uint8_t* base = sm.stage[slot];
-        mbar_expect_tx(&sm.full[slot], A_BYTES + 2 * B_BYTES);
-        tma_load_2d(base, &tmA, &sm.full[slot], (s0 + s) * BK, p0);
-        tma_load_2d(base + 2 * A_BYTES, &tmQh, &sm.full[slot], (s0 + s) * BK, 0);
-        tma_load_2d(base + 2 * A_BYTES + B_BYTES, &tmQl, &sm.full[slot], (s0 + s) * BK, 0);
+        const int rs = s % RAW;
+        if (s >= RAW && !mbar_wait(&sm.rempty[rs], (uint32_t)((s / RAW) & 1) ^ 1, abort, budget)) break;
+        mbar_expect_tx(&sm.rfull[rs], A_BYTES);
+        tma_load_2d(sm.raw[rs], &tmA, &sm.rfull[rs], (s0 + s) * BK, p0);
         issued = s + 1;
       }
     }
   } else if (warp == 1) {
     if (lane == 0) {
       for (int s = 0; s < nk; ++s) {
-        const int slot = s % STAGES;
-        const uint32_t use = (uint32_t)(s / STAGES);
+        const int os = s & 1;
+        const uint32_t ouse = (uint32_t)(s >> 1);
         const int b = s % NBIG;                      // large accumulator of this stage
         const int chunk = s / CHUNK, sb = chunk & 1;  // small accumulator of this chunk
         const bool first = (s % CHUNK) == 0;
         if (s >= NBIG && !mbar_wait(&sm.bige[b], (uint32_t)(s / NBIG - 1) & 1, abort, budget)) break;
         if (first && chunk >= 2 && !mbar_wait(&sm.smle[sb], (uint32_t)((chunk >> 1) - 1) & 1, abort, budget)) break;
-        if (!mbar_wait(&sm.split[slot], use & 1, abort, budget)) break;
+        if (!mbar_wait(&sm.osplit[os], ouse & 1, abort, budget)) break;
+        if (!mbar_wait(&sm.oq[os], ouse & 1, abort, budget)) break;
         tc_fence_after();
-        const uint8_t* base = sm.stage[slot];
+        const uint8_t* base = sm.op[os];
         const uint64_t dah = sw128_desc(smem_u32(base));
         const uint64_t dal = sw128_desc(smem_u32(base + A_BYTES));
         const uint64_t dqh = sw128_desc(smem_u32(base + 2 * A_BYTES));
@@ -280,32 +300,43 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
           mma_tf32(dsml, dah + 2 * k, dql + 2 * k, (first && k == 0) ? 0u : 1u);
           mma_tf32(dsml, dal + 2 * k, dqh + 2 * k, 1u);
         }
-        mma_commit(&sm.empty[slot]);
+        mma_commit(&sm.ofree[os]);
         mma_commit(&sm.bigf[b]);
         if ((s % CHUNK) == CHUNK - 1 || s == nk - 1) mma_commit(&sm.smlf[sb]);
       }
     }
   } else if (warp < 2 + NSPLIT / 32) {
-    // split warps: A tile of stage s -> hi / lo parts, then hand it to the MMA warp
+    // split warps: raw A tile of stage s -> hi / lo parts in operand slot s % 2 (the
+    // same swizzled positions), whose Q tiles the first split thread requests once
+    // the slot is free; then the raw slot goes back to the producer
     const int et = threadIdx.x - 64;  // 0..NSPLIT-1
     for (int s = 0; s < nk; ++s) {
-      const int slot = s % STAGES;
-      if (!mbar_wait(&sm.full[slot], (uint32_t)(s / STAGES) & 1, abort, budget)) break;
-      float4* a4 = reinterpret_cast<float4*>(sm.stage[slot]);
-      float4* l4 = reinterpret_cast<float4*>(sm.stage[slot] + A_BYTES);
+      const int rs = s % RAW, os = s & 1;
+      if (s >= 2 && !mbar_wait(&sm.ofree[os], (uint32_t)((s >> 1) - 1) & 1, abort, budget)) break;
+      if (et == 0) {
+        mbar_expect_tx(&sm.oq[os], 2 * B_BYTES);
+        tma_load_2d(sm.op[os] + 2 * A_BYTES, &tmQh, &sm.oq[os], (s0 + s) * BK, 0);
+        tma_load_2d(sm.op[os] + 2 * A_BYTES + B_BYTES, &tmQl, &sm.oq[os], (s0 + s) * BK, 0);
+        qissued = s + 1;
+      }
+      if (!mbar_wait(&sm.rfull[rs], (uint32_t)(s / RAW) & 1, abort, budget)) break;
+      const float4* r4 = reinterpret_cast<const float4*>(sm.raw[rs]);
+      float4* h4 = reinterpret_cast<float4*>(sm.op[os]);
+      float4* l4 = reinterpret_cast<float4*>(sm.op[os] + A_BYTES);
 #pragma unroll
       for (int e = et; e < A_BYTES / 16; e += NSPLIT) {
-        const float4 v = a4[e];
+        const float4 v = r4[e];
         float4 h, l;
         tf32_split(v.x, h.x, l.x);
         tf32_split(v.y, h.y, l.y);
         tf32_split(v.z, h.z, l.z);
         tf32_split(v.w, h.w, l.w);
-        a4[e] = h;
+        h4[e] = h;
         l4[e] = l;
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      mbar_arrive(&sm.split[slot]);
+      mbar_arrive(&sm.rempty[rs]);
+      mbar_arrive(&sm.osplit[os]);
     }
   } else {
     // drain warps
@@ -349,16 +380,20 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
   __syncthreads();
   if (*abort) {
     // Before tensor memory is freed and the CTA exits, everything this CTA started
-    // asynchronously must have finished: its TMA copies (their full barriers) and the
-    // MMAs the MMA thread issued (one last commit, from that thread, arrives on mmadone
-    // once all of them have completed).  Both always complete; these waits use the
-    // default budget whatever budget the main loop had.
+    // asynchronously must have finished: its TMA copies (their barriers) and the MMAs
+    // the MMA thread issued (one last commit, from that thread, arrives on mmadone once
+    // all of them have completed).  Both always complete; these waits use the default
+    // budget whatever budget the main loop had.
     int dummy = 0;
     volatile int* never = &dummy;
     if (threadIdx.x == 0) atomicExch(&st->status, ST_ERR_TIMEOUT);
     if (warp == 0 && lane == 0) {
-      for (int s = issued - STAGES > 0 ? issued - STAGES : 0; s < issued; ++s)
-        mbar_wait(&sm.full[s % STAGES], (uint32_t)(s / STAGES) & 1, never);
+      for (int s = issued - RAW > 0 ? issued - RAW : 0; s < issued; ++s)
+        mbar_wait(&sm.rfull[s % RAW], (uint32_t)(s / RAW) & 1, never);
+    }
+    if (threadIdx.x == 64) {
+      for (int s = qissued - 2 > 0 ? qissued - 2 : 0; s < qissued; ++s)
+        mbar_wait(&sm.oq[s & 1], (uint32_t)(s >> 1) & 1, never);
     }
     if (warp == 1 && lane == 0) {
       mma_commit(&sm.mmadone);
