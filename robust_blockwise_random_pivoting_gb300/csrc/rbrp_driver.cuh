@@ -58,14 +58,14 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
   const bool use_tc = RES && h->variant == 0;
   CUtensorMap tmA, tmQh, tmQl, tmWth, tmWtl, tmQrh, tmQrl;
   if (use_tc) {  // TMA views: A_res (m x n) and the split basis (m x 64), boxes of 32 rows; for the
-                 // update, W^T (64 per position, boxes of 128 positions) and the basis by rows (boxes of 64)
+                 // update, W^T (64 per position, boxes of 64 positions) and the basis by rows (boxes of 128)
     s = make_tmap_f32(h, &tmA, h->Ares, m, n, L.ld_res, tc::BK, tc::BM);
     if (s == RBRP_OK) s = make_tmap_f32(h, &tmQh, h->Qh, m, MAXB, L.ld_res, tc::BK, tc::BN);
     if (s == RBRP_OK) s = make_tmap_f32(h, &tmQl, h->Ql, m, MAXB, L.ld_res, tc::BK, tc::BN);
-    if (s == RBRP_OK) s = make_tmap_f32(h, &tmWth, h->Wth, MAXB, n, MAXB, tc::BK, tc::BM);
-    if (s == RBRP_OK) s = make_tmap_f32(h, &tmWtl, h->Wtl, MAXB, n, MAXB, tc::BK, tc::BM);
-    if (s == RBRP_OK) s = make_tmap_f32(h, &tmQrh, h->Qrh, MAXB, m, MAXB, tc::BK, tc::U_CH);
-    if (s == RBRP_OK) s = make_tmap_f32(h, &tmQrl, h->Qrl, MAXB, m, MAXB, tc::BK, tc::U_CH);
+    if (s == RBRP_OK) s = make_tmap_f32(h, &tmWth, h->Wth, MAXB, n, MAXB, tc::BK, tc::U_POS);
+    if (s == RBRP_OK) s = make_tmap_f32(h, &tmWtl, h->Wtl, MAXB, n, MAXB, tc::BK, tc::U_POS);
+    if (s == RBRP_OK) s = make_tmap_f32(h, &tmQrh, h->Qrh, MAXB, m, MAXB, tc::BK, tc::U_ROWS);
+    if (s == RBRP_OK) s = make_tmap_f32(h, &tmQrl, h->Qrl, MAXB, m, MAXB, tc::BK, tc::U_ROWS);
     if (s != RBRP_OK) return s;
     cudaMemsetAsync(h->Qh, 0, (size_t)L.ld_res * MAXB * sizeof(float), st);
     cudaMemsetAsync(h->Ql, 0, (size_t)L.ld_res * MAXB * sizeof(float), st);
@@ -191,18 +191,18 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
       int nsplit = 1;
       if (use_tc) {
         // W^T parts (and R(I2, p)), then the tensor-core update.  Row split by the wave rule
-        // with one CTA per SM (shared memory) and a fixed cost per CTA of about four chunks
+        // with one CTA per SM (shared memory) and a fixed cost per CTA of about two chunks
         // (TMEM allocation, the W^T tile, pipeline fill and drain)
         tc::k_upd_w_prep<<<(n - i + 31) / 32, 256, 0, st>>>(h->st, n, reinterpret_cast<const float2*>(h->Wpart),
                                                             wsplit, h->R, n, h->Wth, h->Wtl);
-        const int ctiles = (n - i + tc::BM - 1) / tc::BM;
-        int rps = (m + tc::U_CH - 1) / tc::U_CH * tc::U_CH;
+        const int ctiles = (n - i + tc::U_POS - 1) / tc::U_POS;
+        int rps = (m + tc::U_ROWS - 1) / tc::U_ROWS * tc::U_ROWS;
         long best = -1;
         for (int w = 1; w <= P2_MAX_SPLIT_WS; ++w) {
-          const int r_w = ((m + w - 1) / w + tc::U_CH - 1) / tc::U_CH * tc::U_CH;
+          const int r_w = ((m + w - 1) / w + tc::U_ROWS - 1) / tc::U_ROWS * tc::U_ROWS;
           const int ws = (m + r_w - 1) / r_w;
           const long waves = ((long)ctiles * ws + h->sms - 1) / h->sms;
-          const long cost = waves * (r_w / tc::U_CH + 4);
+          const long cost = waves * (r_w / tc::U_ROWS + 2);
           if (best < 0 || cost < best) {
             best = cost;
             nsplit = ws;

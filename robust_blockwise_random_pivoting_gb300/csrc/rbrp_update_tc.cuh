@@ -1,33 +1,36 @@
 // rbrp_update_tc.cuh - tcgen05 / TMEM / TMA residual update of the residual form (sm_103a).
 //
-// P2: A_res(r, p) -= sum_a Q_blk(r, a) W(a, p) for a tile of 128 trailing
-// positions p (the MMA M dimension, TMEM lanes) and the rows of one row range
-// in chunks of 64 (MMA N), with K = the kept basis vectors (<= 64, one or two
-// 32-wide halves).  Both operands come pre-split into TF32 hi / lo parts
-// (hi + lo = the FP32 value), K-major: W^T from k_upd_w_prep (which also sums the projection's
-// row-split partials and writes R(I2, p)) and the basis by rows from
-// k_panel_q_df.  The CUDA-core form of the same step is k_resid_update.
+// P2: A_res(r, p) -= sum_a Q_blk(r, a) W(a, p) for a tile of 64 trailing
+// positions p (the MMA N dimension) and the rows of one row range in chunks of
+// 128 (MMA M, TMEM lanes), with K = the kept basis vectors (<= 64, one or two
+// 32-wide halves).  Both operands come pre-split into TF32 hi / lo parts (hi +
+// lo = the FP32 value), K-major: the basis by rows from k_panel_q_df and W^T
+// from k_upd_w_prep (which also sums the projection's row-split partials and
+// writes R(I2, p)).  The CUDA-core form of the same step is k_resid_update.
 //
-//   warp 0   TMA: the W^T tile once (hi and lo, up to 64 KB), then the basis rows
-//            of every chunk (hi and lo, up to 32 KB) into a 4-stage ring.
-//   warp 1   MMA issuer: per chunk and K half, W_hi Q_hi into that half's large
-//            accumulator and W_hi Q_lo + W_lo Q_hi + W_lo Q_lo into the small one;
+//   warp 0   TMA: the W^T tile once (hi and lo, up to 32 KB), then the basis rows
+//            of every chunk (hi and lo, up to 64 KB) into a 2-stage ring.
+//   warp 1   MMA issuer: per chunk and K half, Q_hi W_hi into that half's large
+//            accumulator and Q_hi W_lo + Q_lo W_hi + Q_lo W_lo into the small one;
 //            3 x 64 TMEM columns per chunk, double buffered.
-//   warps 2-9 the update: a thread owns one position and 32 rows of the chunk.  It
-//            loads those 32 residual entries (the next two chunks' loads are in
-//            flight while it works on the current one), subtracts the three accumulators
-//            (tcgen05.ld), stores the result and adds its squares to the column's
-//            norm partial.
+//   warps 2-9 the update: TMEM lane = row, so a thread owns one row of the chunk
+//            and 32 of the tile's positions, and every load and store instruction
+//            of a warp covers 128 contiguous bytes of one column.  The thread loads
+//            its 32 residual entries (the next chunk's are in flight meanwhile),
+//            subtracts the three accumulators (tcgen05.ld), stores the result, and
+//            a reduce-scatter over the warp's 32 rows leaves each lane the chunk's
+//            sum of squares of one position, folded into its double-float partial.
 //
 // Accuracy: both operands are split by tf32_split (hi and lo rounded to the
 // nearest TF32 values, the pair within 2^-23 of the value) and all four products
 // are taken - the kernel is bound by memory, not by the MMAs - so each product is
-// good to ~2^-22, about an FP32 product's error.  Each large accumulator takes the 4
-// MMAs of one K half (exact TF32 products), so its rounding - once per MMA,
-// biased - stays at the level of an FP32 FMA chain over the same terms; the
-// small products are 2^-11 smaller.
-// Norm partials are FP32 sums of 32 squares (positive terms) folded into
-// double-float, one per row range and position, summed by k_norm_reduce.
+// good to ~2^-22, about an FP32 product's error.  Each large accumulator takes the
+// 4 MMAs of one K half (exact TF32 products), so its rounding - once per MMA,
+// biased - stays at the level of an FP32 FMA chain over the same terms; the small
+// products are 2^-11 smaller.  Norm partials: pairwise FP32 sums of 32 squares
+// (positive terms) folded into double-float per chunk; the four row quarters of
+// a position are added in a fixed order, one partial per row range and
+// position, summed by k_norm_reduce.
 //
 // Every wait is bounded as in rbrp_tc.cuh; on a timeout the CTA sets an abort
 // flag and st->status, waits (bounded) for its own TMA copies and MMAs, frees
@@ -40,38 +43,41 @@ namespace rbrp {
 namespace tc {
 namespace {
 
-constexpr int U_CH = BN;                    // rows per chunk (MMA N = 64)
-constexpr int U_STAGES = 4;
+constexpr int U_ROWS = BM;                  // rows per chunk (MMA M = 128)
+constexpr int U_POS = BN;                   // positions per CTA (MMA N = 64)
+constexpr int U_STAGES = 2;
 constexpr int U_NUPD = 256;                 // 8 update warps
 constexpr int U_THREADS = 64 + U_NUPD;
-constexpr int U_ACC = 3 * U_CH;             // TMEM columns per chunk: large (K half 0), large (half 1), small
+constexpr int U_ACC = 3 * U_POS;            // TMEM columns per chunk: large (K half 0), large (half 1), small
 
 struct __align__(1024) UpdSmem {
-  uint8_t wt[2][2][A_BYTES];                // [K half][hi, lo]: W^T, 128 positions x 32
-  uint8_t qs[U_STAGES][2][2][B_BYTES];      // [stage][K half][hi, lo]: basis rows, 64 x 32
+  uint8_t wt[2][2][B_BYTES];                // [K half][hi, lo]: W^T, 64 positions x 32
+  uint8_t qs[U_STAGES][2][2][A_BYTES];      // [stage][K half][hi, lo]: basis rows, 128 x 32
   unsigned long long wfull, qfull[U_STAGES], qempty[U_STAGES], accf[2], acce[2], mmadone;
-  float2 nrm[BM];                           // norm partials of the second row half, by tile position
+  float2 nrm[4][U_POS];                     // norm partials by row quarter and tile position
   uint32_t tmem_base;
   int abort;
 };
 constexpr size_t U_SMEM = sizeof(UpdSmem) + 1024;  // + alignment slack of the dynamic window
 
-// 32 residual entries of one column from row r0 (zeros at and past re); 16-byte
-// loads when all 32 are in range (columns and r0 are 128-byte aligned).
-__device__ __forceinline__ void upd_load32(float (&x)[32], const float* __restrict__ col, int r0, int re, bool pv) {
-  if (pv && r0 + 32 <= re) {
+// Sum over the warp's 32 lanes of 32 values per lane, scattered: afterwards lane l
+// holds the sum of value l (rounds at offsets 16, 8, 4, 2, 1 halve the values a
+// lane holds; a fixed pairwise order).
+__device__ __forceinline__ float warp_reduce_scatter32(float (&v)[32]) {
+  const int lane = threadIdx.x & 31;
 #pragma unroll
-    for (int j = 0; j < 32; j += 4) {
-      const float4 v = *reinterpret_cast<const float4*>(col + r0 + j);
-      x[j] = v.x;
-      x[j + 1] = v.y;
-      x[j + 2] = v.z;
-      x[j + 3] = v.w;
+  for (int o = 16; o >= 1; o >>= 1) {
+    const bool upper = (lane & o) != 0;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      if (k < o) {
+        const float send = upper ? v[k] : v[k + o];
+        const float keep = upper ? v[k + o] : v[k];
+        v[k] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+      }
     }
-  } else {
-#pragma unroll
-    for (int j = 0; j < 32; ++j) x[j] = (pv && r0 + j < re) ? col[r0 + j] : 0.f;
   }
+  return v[0];
 }
 
 __global__ void __launch_bounds__(U_THREADS, 1)
@@ -83,11 +89,11 @@ k_resid_update_tc(const __grid_constant__ CUtensorMap tmWh, const __grid_constan
   UpdSmem& sm = *reinterpret_cast<UpdSmem*>((reinterpret_cast<uintptr_t>(u_raw) + 1023) & ~(uintptr_t)1023);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int i = st->i, kept = st->bs;
-  const int p0 = i + kept + blockIdx.x * BM;
+  const int p0 = i + kept + blockIdx.x * U_POS;
   if (kept == 0 || p0 >= n) return;
   const int rb = blockIdx.y * rows_per_split, re = min(m, rb + rows_per_split);
   if (rb >= re) return;
-  const int nch = (re - rb + U_CH - 1) / U_CH;
+  const int nch = (re - rb + U_ROWS - 1) / U_ROWS;
   const int nkc = kept > BK ? 2 : 1;
   volatile int* abort = &sm.abort;
 
@@ -121,7 +127,7 @@ k_resid_update_tc(const __grid_constant__ CUtensorMap tmWh, const __grid_constan
 
   if (warp == 0) {
     if (lane == 0) {
-      mbar_expect_tx(&sm.wfull, (uint32_t)(nkc * 2 * A_BYTES));
+      mbar_expect_tx(&sm.wfull, (uint32_t)(nkc * 2 * B_BYTES));
       for (int kc = 0; kc < nkc; ++kc) {
         tma_load_2d(sm.wt[kc][0], &tmWh, &sm.wfull, kc * BK, p0);
         tma_load_2d(sm.wt[kc][1], &tmWl, &sm.wfull, kc * BK, p0);
@@ -130,10 +136,10 @@ k_resid_update_tc(const __grid_constant__ CUtensorMap tmWh, const __grid_constan
         const int slot = c % U_STAGES;
         const uint32_t use = (uint32_t)(c / U_STAGES);
         if (c >= U_STAGES && !mbar_wait(&sm.qempty[slot], (use & 1) ^ 1, abort, budget)) break;
-        mbar_expect_tx(&sm.qfull[slot], (uint32_t)(nkc * 2 * B_BYTES));
+        mbar_expect_tx(&sm.qfull[slot], (uint32_t)(nkc * 2 * A_BYTES));
         for (int kc = 0; kc < nkc; ++kc) {
-          tma_load_2d(sm.qs[slot][kc][0], &tmQh, &sm.qfull[slot], kc * BK, rb + c * U_CH);
-          tma_load_2d(sm.qs[slot][kc][1], &tmQl, &sm.qfull[slot], kc * BK, rb + c * U_CH);
+          tma_load_2d(sm.qs[slot][kc][0], &tmQh, &sm.qfull[slot], kc * BK, rb + c * U_ROWS);
+          tma_load_2d(sm.qs[slot][kc][1], &tmQl, &sm.qfull[slot], kc * BK, rb + c * U_ROWS);
         }
         issued = c + 1;
       }
@@ -148,16 +154,16 @@ k_resid_update_tc(const __grid_constant__ CUtensorMap tmWh, const __grid_constan
         tc_fence_after();
         const uint32_t dacc = tbase + (uint32_t)(buf * U_ACC);
         for (int kc = 0; kc < nkc; ++kc) {
-          const uint64_t dwh = sw128_desc(smem_u32(sm.wt[kc][0]));
-          const uint64_t dwl = sw128_desc(smem_u32(sm.wt[kc][1]));
           const uint64_t dqh = sw128_desc(smem_u32(sm.qs[slot][kc][0]));
           const uint64_t dql = sw128_desc(smem_u32(sm.qs[slot][kc][1]));
+          const uint64_t dwh = sw128_desc(smem_u32(sm.wt[kc][0]));
+          const uint64_t dwl = sw128_desc(smem_u32(sm.wt[kc][1]));
 #pragma unroll
           for (int k = 0; k < BK / 8; ++k) {
-            mma_tf32(dacc + (uint32_t)(kc * U_CH), dwh + 2 * k, dqh + 2 * k, k == 0 ? 0u : 1u);
-            mma_tf32(dacc + (uint32_t)(2 * U_CH), dwh + 2 * k, dql + 2 * k, (kc == 0 && k == 0) ? 0u : 1u);
-            mma_tf32(dacc + (uint32_t)(2 * U_CH), dwl + 2 * k, dqh + 2 * k, 1u);
-            mma_tf32(dacc + (uint32_t)(2 * U_CH), dwl + 2 * k, dql + 2 * k, 1u);
+            mma_tf32(dacc + (uint32_t)(kc * U_POS), dqh + 2 * k, dwh + 2 * k, k == 0 ? 0u : 1u);
+            mma_tf32(dacc + (uint32_t)(2 * U_POS), dqh + 2 * k, dwl + 2 * k, (kc == 0 && k == 0) ? 0u : 1u);
+            mma_tf32(dacc + (uint32_t)(2 * U_POS), dql + 2 * k, dwh + 2 * k, 1u);
+            mma_tf32(dacc + (uint32_t)(2 * U_POS), dql + 2 * k, dwl + 2 * k, 1u);
           }
         }
         mma_commit(&sm.qempty[slot]);
@@ -165,20 +171,24 @@ k_resid_update_tc(const __grid_constant__ CUtensorMap tmWh, const __grid_constan
       }
     }
   } else {
-    const int q = warp & 3;               // TMEM lane quarter of this warp
-    const int ch = (warp - 2) >> 2;       // row half of each chunk
-    const int tp = 32 * q + lane;         // tile position
-    const int p = p0 + tp;
-    const bool pv = p < n;
-    float* __restrict__ col = Ares + (int64_t)(pv ? p : p0) * ld;
+    const int q = warp & 3;               // TMEM lane quarter: rows 32q .. 32q + 31 of each chunk
+    const int ch = (warp - 2) >> 2;       // position half of the tile
+    const int pb = p0 + 32 * ch;          // this thread's positions pb .. pb + 31
+    const int np = max(0, min(32, n - pb));
+    float* __restrict__ base = Ares + (int64_t)pb * ld;
     const uint32_t toff = ((uint32_t)(32 * q) << 16) + (uint32_t)(32 * ch);
-    // a ring of three register chunks: while chunk c is updated, the loads of chunks
-    // c + 1 and c + 2 are in flight (64 KB per SM)
+    // a running pointer down the positions keeps one 64-bit address live, not 32
+    auto load = [&](float (&x)[32], int r) {
+      const float* pj = base + r;
+      const bool rv = r < re;
+#pragma unroll
+      for (int j = 0; j < 32; ++j, pj += ld) x[j] = (j < np && rv) ? *pj : 0.f;
+    };
     bool ok = true;
     auto step = [&](float (&x)[32], float (&xf)[32], int c) {
       if (!ok || c >= nch) return;
-      const int r0 = rb + c * U_CH + 32 * ch;
-      if (c + 2 < nch) upd_load32(xf, col, r0 + 2 * U_CH, re, pv);
+      const int r = rb + c * U_ROWS + 32 * q + lane;
+      if (c + 1 < nch) load(xf, r + U_ROWS);
       const int buf = c & 1;
       if (!mbar_wait(&sm.accf[buf], (uint32_t)(c >> 1) & 1, abort, budget)) {
         ok = false;
@@ -186,53 +196,47 @@ k_resid_update_tc(const __grid_constant__ CUtensorMap tmWh, const __grid_constan
       }
       tc_fence_after();
       const uint32_t ta = tbase + toff + (uint32_t)(buf * U_ACC);
-      float v[32];
-      tmem_ld32(ta, v);
 #pragma unroll
-      for (int j = 0; j < 32; ++j) x[j] -= v[j];
-      if (nkc > 1) {
-        tmem_ld32(ta + U_CH, v);
+      for (int hf = 0; hf < 2; ++hf) {  // 16 columns at a time keeps the register count down
+        float v[16];
+        tmem_ld16(ta + 16 * hf, v);
 #pragma unroll
-        for (int j = 0; j < 32; ++j) x[j] -= v[j];
+        for (int j = 0; j < 16; ++j) x[16 * hf + j] -= v[j];
+        if (nkc > 1) {
+          tmem_ld16(ta + U_POS + 16 * hf, v);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) x[16 * hf + j] -= v[j];
+        }
+        tmem_ld16(ta + 2 * U_POS + 16 * hf, v);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) x[16 * hf + j] -= v[j];
       }
-      tmem_ld32(ta + 2 * U_CH, v);
-#pragma unroll
-      for (int j = 0; j < 32; ++j) x[j] -= v[j];
       tc_fence_before();
       mbar_arrive(&sm.acce[buf]);
-      float s = 0.f;
-      if (pv && r0 + 32 <= re) {
+      const bool rv = r < re;
+      float* pj = base + r;
 #pragma unroll
-        for (int j = 0; j < 32; j += 4) {
-          *reinterpret_cast<float4*>(col + r0 + j) = make_float4(x[j], x[j + 1], x[j + 2], x[j + 3]);
-          s = fmaf(x[j + 3], x[j + 3], fmaf(x[j + 2], x[j + 2], fmaf(x[j + 1], x[j + 1], fmaf(x[j], x[j], s))));
-        }
-      } else if (pv) {
-#pragma unroll
-        for (int j = 0; j < 32; ++j)
-          if (r0 + j < re) {
-            col[r0 + j] = x[j];
-            s = fmaf(x[j], x[j], s);
-          }
+      for (int j = 0; j < 32; ++j, pj += ld) {
+        if (j < np && rv) *pj = x[j];
+        x[j] = (j < np && rv) ? x[j] * x[j] : 0.f;  // x is spent: its squares
       }
-      df_acc(nrm.hi, nrm.lo, s);
+      df_acc(nrm.hi, nrm.lo, warp_reduce_scatter32(x));
     };
-    float x0[32], x1[32], x2[32];
-    upd_load32(x0, col, rb + 32 * ch, re, pv);
-    if (nch > 1) upd_load32(x1, col, rb + U_CH + 32 * ch, re, pv);
-    for (int c = 0; c < nch && ok; c += 3) {
-      step(x0, x2, c);
+    float x0[32], x1[32];
+    load(x0, rb + 32 * q + lane);
+    for (int c = 0; c < nch && ok; c += 2) {
+      step(x0, x1, c);
       step(x1, x0, c + 1);
-      step(x2, x1, c + 2);
     }
-    if (ch == 1) sm.nrm[tp] = make_float2(nrm.hi, nrm.lo);
+    sm.nrm[q][32 * ch + lane] = make_float2(nrm.hi, nrm.lo);
   }
   __syncthreads();
-  if (!*abort && warp >= 2 && ((warp - 2) >> 2) == 0) {
-    // the two row halves of each position, in a fixed order
-    const int tp = 32 * (warp & 3) + lane, p = p0 + tp;
-    const float2 o = sm.nrm[tp];
-    const dfl a = df_add(df_two_sum(nrm.hi, nrm.lo), dfl{o.x, o.y});
+  if (!*abort && threadIdx.x < U_POS) {
+    // the four row quarters of each position, in a fixed order
+    const int t = threadIdx.x, p = p0 + t;
+    dfl a = {sm.nrm[0][t].x, sm.nrm[0][t].y};
+#pragma unroll
+    for (int qq = 1; qq < 4; ++qq) a = df_add(a, dfl{sm.nrm[qq][t].x, sm.nrm[qq][t].y});
     if (p < n) part_norm[(int64_t)blockIdx.y * n + p] = (double)a.hi + (double)a.lo;
   }
   if (*abort) {
