@@ -10,6 +10,8 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <type_traits>
+
 #include "rbrp_internal.h"
 #include "../../include/rbrp_gb300_testing.h"
 
@@ -184,26 +186,32 @@ __device__ __forceinline__ float2 df2_recip(float2 b) {
   return df2_fast(q, q * r.x);
 }
 
+// One CTA solves a tile of 4 NQ columns of T (NQ per thread: columns (tid & 3) + 4q).
+// The host picks NQ so that the tiles fill whole waves of CTAs: a CTA is bound by
+// its own latency chains, so it runs about as fast alone on an SM as beside a
+// second one, and a partial last wave costs a whole one.
+template <int NQ>
 __global__ void __launch_bounds__(256) k_trsm_T_df(const float2* __restrict__ R11, int k, int ncols,
                                                    float2* __restrict__ T) {
+  constexpr int W = 4 * NQ;
   extern __shared__ __align__(16) unsigned char dyn_smem[];
   TrsmDfSmem& sm = *reinterpret_cast<TrsmDfSmem*>(dyn_smem);
   const int tid = threadIdx.x;
-  const int c0 = blockIdx.x * 32;
-  const int nc = min(32, ncols - c0);
+  const int c0 = blockIdx.x * W;
+  const int nc = min(W, ncols - c0);
   const int nbk = (k + 63) / 64;
   const int x = tid >> 2;
   for (int bi = nbk - 1; bi >= 0; --bi) {
     const int b0 = bi * 64, bl = min(64, k - b0);
-    for (int idx = tid; idx < 64 * 32; idx += 256) {
+    for (int idx = tid; idx < 64 * W; idx += 256) {
       const int xr = idx & 63, c = idx >> 6;
       sm.Acc[xr][c] = (xr < bl && c < nc) ? T[(b0 + xr) + (int64_t)(c0 + c) * k] : make_float2(0.f, 0.f);
     }
-    float sh[8], sl[8];
+    float sh[NQ], sl[NQ];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) sh[q] = sl[q] = 0.f;
+    for (int q = 0; q < NQ; ++q) sh[q] = sl[q] = 0.f;
     // the tiles of step bj are fetched into registers during step bj - 1
-    float2 rpre[16], xpre[8];
+    float2 rpre[16], xpre[NQ];
     auto fetch = [&](int bj) {
       const int cr = bj * 64, cl = min(64, k - cr);
 #pragma unroll
@@ -213,7 +221,7 @@ __global__ void __launch_bounds__(256) k_trsm_T_df(const float2* __restrict__ R1
         rpre[u] = make_float2(-v.x, -v.y);
       }
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
+      for (int u = 0; u < NQ; ++u) {
         const int idx = tid + 256 * u, y = idx & 63, c = idx >> 6;
         xpre[u] = (y < cl && c < nc) ? T[(cr + y) + (int64_t)(c0 + c) * k] : make_float2(0.f, 0.f);
       }
@@ -227,7 +235,7 @@ __global__ void __launch_bounds__(256) k_trsm_T_df(const float2* __restrict__ R1
         sm.Rs[idx >> 6][idx & 63] = rpre[u];
       }
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
+      for (int u = 0; u < NQ; ++u) {
         const int idx = tid + 256 * u;
         sm.Xs[idx & 63][idx >> 6] = xpre[u];
       }
@@ -237,10 +245,10 @@ __global__ void __launch_bounds__(256) k_trsm_T_df(const float2* __restrict__ R1
       for (int y = 0; y < 64; ++y) {
         const float2 r = sm.Rs[x][y];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) df_mac(sh[q], sl[q], r, sm.Xs[y][(tid & 3) + 4 * q]);
+        for (int q = 0; q < NQ; ++q) df_mac(sh[q], sl[q], r, sm.Xs[y][(tid & 3) + 4 * q]);
       }
 #pragma unroll
-      for (int q = 0; q < 8; ++q) {  // renormalise so the low part stays small
+      for (int q = 0; q < NQ; ++q) {  // renormalise so the low part stays small
         const float t = sh[q] + sl[q];
         sl[q] = sl[q] - (t - sh[q]);
         sh[q] = t;
@@ -248,7 +256,7 @@ __global__ void __launch_bounds__(256) k_trsm_T_df(const float2* __restrict__ R1
     }
     __syncthreads();
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
+    for (int q = 0; q < NQ; ++q) {
       float2& a = sm.Acc[x][(tid & 3) + 4 * q];
       a = df2_add(a, make_float2(sh[q], sl[q]));
     }
@@ -268,7 +276,7 @@ __global__ void __launch_bounds__(256) k_trsm_T_df(const float2* __restrict__ R1
       }
     }
     __syncthreads();
-    for (int idx = tid; idx < 64 * 32; idx += 256) {
+    for (int idx = tid; idx < 64 * W; idx += 256) {
       const int xr = idx & 63, c = idx >> 6;
       if (xr < bl && c < nc) T[(b0 + xr) + (int64_t)(c0 + c) * k] = sm.Acc[xr][c];
     }
@@ -496,10 +504,43 @@ rbrp_status solve_T(rbrp_handle h, int k, int n) {
     float2* R11df = static_cast<float2*>(h->df_buf);
     float2* Tdf = R11df + (size_t)k * k;
     k_split_df<<<1216, 256, 0, h->stream>>>(h->R, n, k, ncols, R11df, Tdf);
-    s = cuda_check(h, cudaFuncSetAttribute(k_trsm_T_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)sizeof(TrsmDfSmem)), "cudaFuncSetAttribute(k_trsm_T_df)");
-    if (s != RBRP_OK) return s;
-    k_trsm_T_df<<<(ncols + 31) / 32, 256, sizeof(TrsmDfSmem), h->stream>>>(R11df, k, ncols, Tdf);
+    // tile width 4 NQ columns: the fewest waves of co-resident CTAs times the per-CTA work
+    // (NQ + 1 units: the NQ products per R entry and its shared load), larger tiles on ties
+    auto tsolve = [&](auto nq) -> rbrp_status {
+      constexpr int NQ = decltype(nq)::value;
+      return cuda_check(h, cudaFuncSetAttribute(k_trsm_T_df<NQ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)sizeof(TrsmDfSmem)), "cudaFuncSetAttribute(k_trsm_T_df)");
+    };
+    auto slots = [&](auto nq) -> long {
+      constexpr int NQ = decltype(nq)::value;
+      int per_sm = 0;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trsm_T_df<NQ>, 256, sizeof(TrsmDfSmem));
+      return (long)std::max(1, per_sm) * h->sms;
+    };
+    const std::integral_constant<int, 8> q8;
+    const std::integral_constant<int, 6> q6;
+    const std::integral_constant<int, 4> q4;
+    for (rbrp_status e : {tsolve(q8), tsolve(q6), tsolve(q4)})
+      if (e != RBRP_OK) return e;
+    int best_nq = 8;
+    long best = -1;
+    const long sl[3] = {slots(q8), slots(q6), slots(q4)};
+    const int nqs[3] = {8, 6, 4};
+    for (int v = 0; v < 3; ++v) {
+      const long tiles = (ncols + 4 * nqs[v] - 1) / (4 * nqs[v]);
+      const long cost = (tiles + sl[v] - 1) / sl[v] * (nqs[v] + 1);
+      if (best < 0 || cost < best) {
+        best = cost;
+        best_nq = nqs[v];
+      }
+    }
+    const int grid = (ncols + 4 * best_nq - 1) / (4 * best_nq);
+    if (best_nq == 8)
+      k_trsm_T_df<8><<<grid, 256, sizeof(TrsmDfSmem), h->stream>>>(R11df, k, ncols, Tdf);
+    else if (best_nq == 6)
+      k_trsm_T_df<6><<<grid, 256, sizeof(TrsmDfSmem), h->stream>>>(R11df, k, ncols, Tdf);
+    else
+      k_trsm_T_df<4><<<grid, 256, sizeof(TrsmDfSmem), h->stream>>>(R11df, k, ncols, Tdf);
     k_join_df<<<1216, 256, 0, h->stream>>>(Tdf, (int64_t)k * ncols, h->T);
   }
   return cuda_check(h, cudaGetLastError(), "T solve launch");
