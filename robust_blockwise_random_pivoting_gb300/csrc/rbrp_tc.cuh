@@ -140,6 +140,31 @@ __device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t adesc, uint64
       : "memory");
 }
 
+// The same MMA with A (M x 8 TF32, row = TMEM lane, the 8 K values in consecutive
+// 32-bit columns) read from tensor memory at a_tmem instead of shared memory.
+__device__ __forceinline__ void mma_tf32_ta(uint32_t d_tmem, uint32_t a_tmem, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "r"(a_tmem), "l"(bdesc), "r"(IDESC), "r"(accumulate)
+      : "memory");
+}
+
+// 32 registers into 32 consecutive TMEM columns of this warp's 32 lanes (completion
+// is awaited by the caller with tcgen05.wait::st).
+__device__ __forceinline__ void tmem_st32(uint32_t taddr, const float (&v)[32]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], "
+      "{%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, "
+      "%17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31, %32};" ::"r"(taddr),
+      "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7]), "f"(v[8]), "f"(v[9]),
+      "f"(v[10]), "f"(v[11]), "f"(v[12]), "f"(v[13]), "f"(v[14]), "f"(v[15]), "f"(v[16]), "f"(v[17]), "f"(v[18]),
+      "f"(v[19]), "f"(v[20]), "f"(v[21]), "f"(v[22]), "f"(v[23]), "f"(v[24]), "f"(v[25]), "f"(v[26]), "f"(v[27]),
+      "f"(v[28]), "f"(v[29]), "f"(v[30]), "f"(v[31])
+      : "memory");
+}
+
 __device__ __forceinline__ void mma_commit(unsigned long long* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
                : "memory");
@@ -194,16 +219,21 @@ __device__ __forceinline__ void drain32(uint32_t taddr, float (&hi)[32], float (
   }
 }
 
-// Shared memory of k_proj_w_tc: the TMA ring holds raw A tiles only (16 KB a
-// stage, so 112 KB of A are in flight per SM); the split warps turn each into
-// its hi / lo parts in one of two operand slots, which also receive that
-// stage's Q hi / lo tiles, and free the raw slot at once.
-constexpr int RAW = 7;                                   // raw A stages in flight
+// Shared memory of k_proj_w_tc.  The TMA ring holds raw A tiles only (16 KB a
+// stage: 160 KB of A in flight per SM).  The split warps write each tile's hi /
+// lo parts straight into tensor memory (the MMAs read A from there), so shared
+// memory carries only the raw tiles and, per operand slot, that stage's Q hi / lo.
+// An MMA whose A comes from shared memory re-reads its 4 KB per instruction at
+// about 128 bytes per clock (a probe: 51 clocks per M128 N64 K8 TF32 MMA); from
+// tensor memory only the 2 KB Q operand is read.
+constexpr int RAW = 10;                                  // raw A stages in flight
+constexpr uint32_t TA_COL = NBIG * BN + 2 * BN;          // TMEM columns of the A slots (after the accumulators)
+static_assert(TA_COL + 2 * 2 * BK <= TMEM_COLS, "TMEM budget: accumulators + two A slots of hi, lo");
 struct __align__(1024) ProjSmem {
   uint8_t raw[RAW][A_BYTES];
-  uint8_t op[2][STAGE_BYTES];                            // A hi, A lo, Q hi, Q lo
+  uint8_t qs[2][2 * B_BYTES];                            // per operand slot: Q hi, Q lo
   unsigned long long rfull[RAW], rempty[RAW];            // raw ring: TMA done / split done
-  unsigned long long ofree[2], osplit[2], oq[2];         // operand slots: MMAs done / split done / Q landed
+  unsigned long long ofree[2], osplit[2], oq[2];         // operand slots: MMAs done / A in TMEM / Q landed
   unsigned long long bigf[NBIG], bige[NBIG];             // large accumulators: full (MMA done) / empty (drained)
   unsigned long long smlf[2], smle[2];                   // small accumulator
   unsigned long long mmadone;                            // abort path: every MMA this CTA issued has completed
@@ -287,18 +317,16 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
         if (!mbar_wait(&sm.osplit[os], ouse & 1, abort, budget)) break;
         if (!mbar_wait(&sm.oq[os], ouse & 1, abort, budget)) break;
         tc_fence_after();
-        const uint8_t* base = sm.op[os];
-        const uint64_t dah = sw128_desc(smem_u32(base));
-        const uint64_t dal = sw128_desc(smem_u32(base + A_BYTES));
-        const uint64_t dqh = sw128_desc(smem_u32(base + 2 * A_BYTES));
-        const uint64_t dql = sw128_desc(smem_u32(base + 2 * A_BYTES + B_BYTES));
+        const uint32_t tah = tbase + TA_COL + (uint32_t)(os * 2 * BK);   // A hi: 32 columns, then A lo
+        const uint64_t dqh = sw128_desc(smem_u32(sm.qs[os]));
+        const uint64_t dql = sw128_desc(smem_u32(sm.qs[os] + B_BYTES));
         const uint32_t dbig = tbase + (uint32_t)(b * BN);
         const uint32_t dsml = tbase + (uint32_t)(NBIG * BN + sb * BN);
 #pragma unroll
-        for (int k = 0; k < BK / 8; ++k) {  // K = 8 TF32 = 32 bytes: +2 in the 16-byte address field
-          mma_tf32(dbig, dah + 2 * k, dqh + 2 * k, k == 0 ? 0u : 1u);
-          mma_tf32(dsml, dah + 2 * k, dql + 2 * k, (first && k == 0) ? 0u : 1u);
-          mma_tf32(dsml, dal + 2 * k, dqh + 2 * k, 1u);
+        for (int k = 0; k < BK / 8; ++k) {  // K = 8 TF32: 8 TMEM columns of A, 32 bytes of Q
+          mma_tf32_ta(dbig, tah + 8 * k, dqh + 2 * k, k == 0 ? 0u : 1u);
+          mma_tf32_ta(dsml, tah + 8 * k, dql + 2 * k, (first && k == 0) ? 0u : 1u);
+          mma_tf32_ta(dsml, tah + BK + 8 * k, dqh + 2 * k, 1u);
         }
         mma_commit(&sm.ofree[os]);
         mma_commit(&sm.bigf[b]);
@@ -306,35 +334,39 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
       }
     }
   } else if (warp < 2 + NSPLIT / 32) {
-    // split warps: raw A tile of stage s -> hi / lo parts in operand slot s % 2 (the
-    // same swizzled positions), whose Q tiles the first split thread requests once
-    // the slot is free; then the raw slot goes back to the producer
+    // split warps: TMEM lane quarter warp % 4; a thread takes one position (a 128-byte
+    // row of the swizzled raw tile: 16-byte chunk c of row r sits at chunk c ^ (r % 8)),
+    // splits its 32 values and stores hi / lo into the A slot of stage s; the first split
+    // thread requests that stage's Q tiles once the slot is free
     const int et = threadIdx.x - 64;  // 0..NSPLIT-1
+    const int row = 32 * (warp & 3) + lane;
+    const uint32_t lane_off = (uint32_t)(32 * (warp & 3)) << 16;
     for (int s = 0; s < nk; ++s) {
       const int rs = s % RAW, os = s & 1;
       if (s >= 2 && !mbar_wait(&sm.ofree[os], (uint32_t)((s >> 1) - 1) & 1, abort, budget)) break;
       if (et == 0) {
         mbar_expect_tx(&sm.oq[os], 2 * B_BYTES);
-        tma_load_2d(sm.op[os] + 2 * A_BYTES, &tmQh, &sm.oq[os], (s0 + s) * BK, 0);
-        tma_load_2d(sm.op[os] + 2 * A_BYTES + B_BYTES, &tmQl, &sm.oq[os], (s0 + s) * BK, 0);
+        tma_load_2d(sm.qs[os], &tmQh, &sm.oq[os], (s0 + s) * BK, 0);
+        tma_load_2d(sm.qs[os] + B_BYTES, &tmQl, &sm.oq[os], (s0 + s) * BK, 0);
         qissued = s + 1;
       }
       if (!mbar_wait(&sm.rfull[rs], (uint32_t)(s / RAW) & 1, abort, budget)) break;
-      const float4* r4 = reinterpret_cast<const float4*>(sm.raw[rs]);
-      float4* h4 = reinterpret_cast<float4*>(sm.op[os]);
-      float4* l4 = reinterpret_cast<float4*>(sm.op[os] + A_BYTES);
+      tc_fence_after();
+      const uint8_t* rrow = sm.raw[rs] + row * 128;
+      float hi[32], lo[32];
 #pragma unroll
-      for (int e = et; e < A_BYTES / 16; e += NSPLIT) {
-        const float4 v = r4[e];
-        float4 h, l;
-        tf32_split(v.x, h.x, l.x);
-        tf32_split(v.y, h.y, l.y);
-        tf32_split(v.z, h.z, l.z);
-        tf32_split(v.w, h.w, l.w);
-        h4[e] = h;
-        l4[e] = l;
+      for (int c = 0; c < 8; ++c) {
+        const float4 v = *reinterpret_cast<const float4*>(rrow + ((c ^ (row & 7)) << 4));
+        tf32_split(v.x, hi[4 * c], lo[4 * c]);
+        tf32_split(v.y, hi[4 * c + 1], lo[4 * c + 1]);
+        tf32_split(v.z, hi[4 * c + 2], lo[4 * c + 2]);
+        tf32_split(v.w, hi[4 * c + 3], lo[4 * c + 3]);
       }
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      const uint32_t ta = tbase + lane_off + TA_COL + (uint32_t)(os * 2 * BK);
+      tmem_st32(ta, hi);
+      tmem_st32(ta + BK, lo);
+      asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+      tc_fence_before();
       mbar_arrive(&sm.rempty[rs]);
       mbar_arrive(&sm.osplit[os]);
     }
