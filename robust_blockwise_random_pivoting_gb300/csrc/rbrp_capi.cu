@@ -504,18 +504,21 @@ rbrp_status solve_T(rbrp_handle h, int k, int n) {
     float2* R11df = static_cast<float2*>(h->df_buf);
     float2* Tdf = R11df + (size_t)k * k;
     k_split_df<<<1216, 256, 0, h->stream>>>(h->R, n, k, ncols, R11df, Tdf);
-    // tile width 4 NQ columns: the fewest waves of co-resident CTAs times the per-CTA work
-    // (NQ + 1 units: the NQ products per R entry and its shared load), larger tiles on ties
+    // tile width 4 NQ columns by a measured model: a CTA beside another one on its SM takes
+    // Tp ~ NQ + 2.5 (units), alone about 0.55 Tp (it is latency-bound; two CTAs per SM are
+    // issue-bound).  Full waves of two CTAs per SM cost Tp each; a remainder that fits one
+    // CTA per SM costs 0.55 Tp, a larger one Tp.  (16384 columns, k = 2030: 32 columns per
+    // tile 16.3 ms, 24 columns 16.9; 8192: 10.5 and 8.5.)
     auto tsolve = [&](auto nq) -> rbrp_status {
       constexpr int NQ = decltype(nq)::value;
       return cuda_check(h, cudaFuncSetAttribute(k_trsm_T_df<NQ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                 (int)sizeof(TrsmDfSmem)), "cudaFuncSetAttribute(k_trsm_T_df)");
     };
-    auto slots = [&](auto nq) -> long {
+    auto per_sm = [&](auto nq) -> int {
       constexpr int NQ = decltype(nq)::value;
-      int per_sm = 0;
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trsm_T_df<NQ>, 256, sizeof(TrsmDfSmem));
-      return (long)std::max(1, per_sm) * h->sms;
+      int c = 0;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_trsm_T_df<NQ>, 256, sizeof(TrsmDfSmem));
+      return std::max(1, c);
     };
     const std::integral_constant<int, 8> q8;
     const std::integral_constant<int, 6> q6;
@@ -523,13 +526,16 @@ rbrp_status solve_T(rbrp_handle h, int k, int n) {
     for (rbrp_status e : {tsolve(q8), tsolve(q6), tsolve(q4)})
       if (e != RBRP_OK) return e;
     int best_nq = 8;
-    long best = -1;
-    const long sl[3] = {slots(q8), slots(q6), slots(q4)};
+    double best = -1.0;
+    const int occ[3] = {per_sm(q8), per_sm(q6), per_sm(q4)};
     const int nqs[3] = {8, 6, 4};
     for (int v = 0; v < 3; ++v) {
       const long tiles = (ncols + 4 * nqs[v] - 1) / (4 * nqs[v]);
-      const long cost = (tiles + sl[v] - 1) / sl[v] * (nqs[v] + 1);
-      if (best < 0 || cost < best) {
+      const long full = (long)occ[v] * h->sms;
+      const long waves = tiles / full, rest = tiles - waves * full;
+      const double tail = rest == 0 ? 0.0 : (occ[v] > 1 && rest <= h->sms ? 0.55 : 1.0);
+      const double cost = ((double)waves + tail) * (nqs[v] + 2.5);
+      if (best < 0.0 || cost < best) {
         best = cost;
         best_nq = nqs[v];
       }
