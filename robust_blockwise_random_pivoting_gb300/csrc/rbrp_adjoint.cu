@@ -535,10 +535,10 @@ rbrp_status adjoint_tc(rbrp_handle h, int m, int k, int nc, int kp, int ncp, con
   const int n = h->n;
   if (!h->smem_attr_gemm_tc) {
     rbrp_status s = cuda_check(h, cudaFuncSetAttribute(tc::k_gemm_tc<EpiE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                       (int)tc::P1_SMEM), "cudaFuncSetAttribute(k_gemm_tc<E>)");
+                                                       (int)tc::GEMM_SMEM), "cudaFuncSetAttribute(k_gemm_tc<E>)");
     if (s == RBRP_OK)
       s = cuda_check(h, cudaFuncSetAttribute(tc::k_gemm_tc<EpiG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)tc::P1_SMEM), "cudaFuncSetAttribute(k_gemm_tc<G>)");
+                                             (int)tc::GEMM_SMEM), "cudaFuncSetAttribute(k_gemm_tc<G>)");
     if (s != RBRP_OK) return s;
     h->smem_attr_gemm_tc = true;
   }
@@ -564,7 +564,7 @@ rbrp_status adjoint_tc(rbrp_handle h, int m, int k, int nc, int kp, int ncp, con
   }
   const int tx1 = (nc + tc::BM - 1) / tc::BM, ty1 = (m + tc::BN - 1) / tc::BN;
   EpiE e1{dA, lda, h->perm, k, m, nc, wr, cz, dG ? Et : nullptr, ncp, dG, ldg, scale, lp, ewp};
-  tc::k_gemm_tc<EpiE><<<dim3(tx1, ty1), tc::NTHREADS, tc::P1_SMEM, st>>>(tmX1, tmY1h, tmY1l, nc, m, k, budget,
+  tc::k_gemm_tc<EpiE><<<dim3(tx1, ty1), tc::NTHREADS, tc::GEMM_SMEM, st>>>(tmX1, tmY1h, tmY1l, nc, m, k, budget,
                                                                        dstatus, e1);
   if (dG) k_adj_sum_rows<<<(m + 255) / 256, 256, 0, st>>>(ewp, tx1, m, ew);
   k_adj_loss<<<1, 256, 0, st>>>(lp, tx1 * ty1, udf, k, lout);
@@ -575,7 +575,7 @@ rbrp_status adjoint_tc(rbrp_handle h, int m, int k, int nc, int kp, int ncp, con
     if (s == RBRP_OK) s = make_tmap_f32(h, &tmY2l, Trl, nc, k, ncp, tc::BK, tc::BN);
     if (s != RBRP_OK) return s;
     EpiG e2{h->perm, m, k, cz, ew, u, z, dG, ldg, scale};
-    tc::k_gemm_tc<EpiG><<<dim3((m + tc::BM - 1) / tc::BM, (k + tc::BN - 1) / tc::BN), tc::NTHREADS, tc::P1_SMEM, st>>>(
+    tc::k_gemm_tc<EpiG><<<dim3((m + tc::BM - 1) / tc::BM, (k + tc::BN - 1) / tc::BN), tc::NTHREADS, tc::GEMM_SMEM, st>>>(
         tmX2, tmY2h, tmY2l, m, k, nc, budget, dstatus, e2);
   }
   s = cuda_check(h, cudaGetLastError(), "adjoint kernels");

@@ -8,12 +8,14 @@
 // Both operands are K-major FP32 in global memory: X (K x M, column major, ld
 // a multiple of 4) and the hi and lo TF32 parts of Y (K x N each, same layout).
 //
-//   warp 0   TMA producer: the X tile (128 x 32) and the Y hi / lo tiles
-//            (64 x 32) into a 4-stage ring, 128-byte swizzled.
+//   warp 0   TMA producer: the raw X tiles (128 x 32, 128-byte swizzled) into a
+//            10-stage ring.
 //   warp 1   MMA issuer: X hi Y hi into a large accumulator, X hi Y lo and
-//            X lo Y hi into a small one (3xTF32: the FP32 product to ~2^-22).
-//   warps 2-5 split each staged X tile into hi (rounded to the nearest TF32
-//            value) + lo parts, exact in FP32.
+//            X lo Y hi into a small one (3xTF32: the FP32 product to ~2^-22); X is
+//            read from tensor memory, Y from shared memory.
+//   warps 2-5 split each X tile by tf32_split into tensor memory (one row per
+//            thread), with two operand slots; the first split thread loads the
+//            slot's Y hi / lo tiles (64 x 32).
 //   warps 6-13 drain the large accumulator after every RBRP_GEMM_DRAIN stages
 //            and the small one every CHUNK stages into double-float registers, then call the
 //            epilogue: thread (lane quarter q, column half ch) holds
@@ -44,12 +46,29 @@ namespace {
 constexpr int GEMM_DRAIN = RBRP_GEMM_DRAIN;
 static_assert(GEMM_DRAIN >= 1 && CHUNK % GEMM_DRAIN == 0, "drain interval");
 
+// Shared memory of k_gemm_tc: raw X tiles in a TMA ring, and per operand slot the
+// Y hi / lo tiles; the split warps write X's hi / lo parts into tensor memory (A slots
+// after the accumulators), so the MMAs read only Y from shared memory (as k_proj_w_tc).
+constexpr int GRAW = 10;
+struct __align__(1024) GemmSmem {
+  uint8_t raw[GRAW][A_BYTES];
+  uint8_t ys[2][2 * B_BYTES];                            // per operand slot: Y hi, Y lo
+  unsigned long long rfull[GRAW], rempty[GRAW];
+  unsigned long long ofree[2], osplit[2], oy[2];
+  unsigned long long bigf[NBIG], bige[NBIG];
+  unsigned long long smlf[2], smle[2];
+  unsigned long long mmadone;
+  uint32_t tmem_base;
+  int abort;
+};
+constexpr size_t GEMM_SMEM = sizeof(GemmSmem) + 1024;
+
 template <typename Epi>
 __global__ void __launch_bounds__(NTHREADS, 1)
 k_gemm_tc(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmYh,
           const __grid_constant__ CUtensorMap tmYl, int M, int N, int K, long long budget, int* status, Epi epi) {
   extern __shared__ uint8_t gt_raw[];
-  P1Smem& sm = *reinterpret_cast<P1Smem*>((reinterpret_cast<uintptr_t>(gt_raw) + 1023) & ~(uintptr_t)1023);
+  GemmSmem& sm = *reinterpret_cast<GemmSmem*>((reinterpret_cast<uintptr_t>(gt_raw) + 1023) & ~(uintptr_t)1023);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int p0 = blockIdx.x * BM, c0 = blockIdx.y * BN;
   const int nk = (K + BK - 1) / BK;
@@ -57,10 +76,14 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUten
   volatile int* abort = &sm.abort;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < STAGES; ++s) {
-      mbar_init(&sm.full[s], 1);
-      mbar_init(&sm.split[s], NSPLIT);
-      mbar_init(&sm.empty[s], 1);
+    for (int s = 0; s < GRAW; ++s) {
+      mbar_init(&sm.rfull[s], 1);
+      mbar_init(&sm.rempty[s], NSPLIT);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&sm.ofree[b], 1);
+      mbar_init(&sm.osplit[b], NSPLIT);
+      mbar_init(&sm.oy[b], 1);
     }
     for (int b = 0; b < NBIG; ++b) {
       mbar_init(&sm.bigf[b], 1);
@@ -84,27 +107,23 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUten
   __syncthreads();
   tc_fence_after();
   const uint32_t tbase = sm.tmem_base;
-  int issued = 0;
+  int issued = 0, yissued = 0;
 
   if (warp == 0) {
     if (lane == 0) {
       for (int s = 0; s < nk; ++s) {
-        const int slot = s % STAGES;
-        const uint32_t use = (uint32_t)(s / STAGES);
-        if (s >= STAGES && !mbar_wait(&sm.empty[slot], (use & 1) ^ 1, abort, budget)) break;
-        uint8_t* base = sm.stage[slot];
-        mbar_expect_tx(&sm.full[slot], A_BYTES + 2 * B_BYTES);
-        tma_load_2d(base, &tmX, &sm.full[slot], s * BK, p0);
-        tma_load_2d(base + 2 * A_BYTES, &tmYh, &sm.full[slot], s * BK, c0);
-        tma_load_2d(base + 2 * A_BYTES + B_BYTES, &tmYl, &sm.full[slot], s * BK, c0);
+        const int rs = s % GRAW;
+        if (s >= GRAW && !mbar_wait(&sm.rempty[rs], (uint32_t)((s / GRAW) & 1) ^ 1, abort, budget)) break;
+        mbar_expect_tx(&sm.rfull[rs], A_BYTES);
+        tma_load_2d(sm.raw[rs], &tmX, &sm.rfull[rs], s * BK, p0);
         issued = s + 1;
       }
     }
   } else if (warp == 1) {
     if (lane == 0) {
       for (int s = 0; s < nk; ++s) {
-        const int slot = s % STAGES;
-        const uint32_t use = (uint32_t)(s / STAGES);
+        const int os = s & 1;
+        const uint32_t ouse = (uint32_t)(s >> 1);
         const int g = s / GEMM_DRAIN;                 // drain group of the large accumulator
         const int b = g % NBIG;
         const bool gfirst = (s % GEMM_DRAIN) == 0, glast = (s % GEMM_DRAIN) == GEMM_DRAIN - 1 || s == nk - 1;
@@ -112,46 +131,59 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUten
         const bool first = (s % CHUNK) == 0;
         if (gfirst && g >= NBIG && !mbar_wait(&sm.bige[b], (uint32_t)(g / NBIG - 1) & 1, abort, budget)) break;
         if (first && chunk >= 2 && !mbar_wait(&sm.smle[sb], (uint32_t)((chunk >> 1) - 1) & 1, abort, budget)) break;
-        if (!mbar_wait(&sm.split[slot], use & 1, abort, budget)) break;
+        if (!mbar_wait(&sm.osplit[os], ouse & 1, abort, budget)) break;
+        if (!mbar_wait(&sm.oy[os], ouse & 1, abort, budget)) break;
         tc_fence_after();
-        const uint8_t* base = sm.stage[slot];
-        const uint64_t dxh = sw128_desc(smem_u32(base));
-        const uint64_t dxl = sw128_desc(smem_u32(base + A_BYTES));
-        const uint64_t dyh = sw128_desc(smem_u32(base + 2 * A_BYTES));
-        const uint64_t dyl = sw128_desc(smem_u32(base + 2 * A_BYTES + B_BYTES));
+        const uint32_t txh = tbase + TA_COL + (uint32_t)(os * 2 * BK);   // X hi: 32 columns, then X lo
+        const uint64_t dyh = sw128_desc(smem_u32(sm.ys[os]));
+        const uint64_t dyl = sw128_desc(smem_u32(sm.ys[os] + B_BYTES));
         const uint32_t dbig = tbase + (uint32_t)(b * BN);
         const uint32_t dsml = tbase + (uint32_t)(NBIG * BN + sb * BN);
 #pragma unroll
         for (int k = 0; k < BK / 8; ++k) {
-          mma_tf32(dbig, dxh + 2 * k, dyh + 2 * k, (gfirst && k == 0) ? 0u : 1u);
-          mma_tf32(dsml, dxh + 2 * k, dyl + 2 * k, (first && k == 0) ? 0u : 1u);
-          mma_tf32(dsml, dxl + 2 * k, dyh + 2 * k, 1u);
+          mma_tf32_ta(dbig, txh + 8 * k, dyh + 2 * k, (gfirst && k == 0) ? 0u : 1u);
+          mma_tf32_ta(dsml, txh + 8 * k, dyl + 2 * k, (first && k == 0) ? 0u : 1u);
+          mma_tf32_ta(dsml, txh + BK + 8 * k, dyh + 2 * k, 1u);
         }
-        mma_commit(&sm.empty[slot]);
+        mma_commit(&sm.ofree[os]);
         if (glast) mma_commit(&sm.bigf[b]);
         if ((s % CHUNK) == CHUNK - 1 || s == nk - 1) mma_commit(&sm.smlf[sb]);
       }
     }
   } else if (warp < 2 + NSPLIT / 32) {
+    // split warps: one X row (a 128-byte swizzled row of the raw tile) per thread into
+    // TMEM lane 32 (warp % 4) + lane; the first split thread requests the Y tiles
     const int et = threadIdx.x - 64;
+    const int row = 32 * (warp & 3) + lane;
+    const uint32_t lane_off = (uint32_t)(32 * (warp & 3)) << 16;
     for (int s = 0; s < nk; ++s) {
-      const int slot = s % STAGES;
-      if (!mbar_wait(&sm.full[slot], (uint32_t)(s / STAGES) & 1, abort, budget)) break;
-      float4* a4 = reinterpret_cast<float4*>(sm.stage[slot]);
-      float4* l4 = reinterpret_cast<float4*>(sm.stage[slot] + A_BYTES);
-#pragma unroll
-      for (int e = et; e < A_BYTES / 16; e += NSPLIT) {
-        const float4 v = a4[e];
-        float4 h, l;
-        tf32_split(v.x, h.x, l.x);
-        tf32_split(v.y, h.y, l.y);
-        tf32_split(v.z, h.z, l.z);
-        tf32_split(v.w, h.w, l.w);
-        a4[e] = h;
-        l4[e] = l;
+      const int rs = s % GRAW, os = s & 1;
+      if (s >= 2 && !mbar_wait(&sm.ofree[os], (uint32_t)((s >> 1) - 1) & 1, abort, budget)) break;
+      if (et == 0) {
+        mbar_expect_tx(&sm.oy[os], 2 * B_BYTES);
+        tma_load_2d(sm.ys[os], &tmYh, &sm.oy[os], s * BK, c0);
+        tma_load_2d(sm.ys[os] + B_BYTES, &tmYl, &sm.oy[os], s * BK, c0);
+        yissued = s + 1;
       }
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      mbar_arrive(&sm.split[slot]);
+      if (!mbar_wait(&sm.rfull[rs], (uint32_t)(s / GRAW) & 1, abort, budget)) break;
+      tc_fence_after();
+      const uint8_t* rrow = sm.raw[rs] + row * 128;
+      float hi[32], lo[32];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        const float4 v = *reinterpret_cast<const float4*>(rrow + ((c ^ (row & 7)) << 4));
+        tf32_split(v.x, hi[4 * c], lo[4 * c]);
+        tf32_split(v.y, hi[4 * c + 1], lo[4 * c + 1]);
+        tf32_split(v.z, hi[4 * c + 2], lo[4 * c + 2]);
+        tf32_split(v.w, hi[4 * c + 3], lo[4 * c + 3]);
+      }
+      const uint32_t ta = tbase + lane_off + TA_COL + (uint32_t)(os * 2 * BK);
+      tmem_st32(ta, hi);
+      tmem_st32(ta + BK, lo);
+      asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+      tc_fence_before();
+      mbar_arrive(&sm.rempty[rs]);
+      mbar_arrive(&sm.osplit[os]);
     }
   } else {
     const int dw = warp - 2 - NSPLIT / 32;  // 0..7
@@ -189,8 +221,12 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUten
     volatile int* never = &dummy;
     if (threadIdx.x == 0) atomicExch(status, ST_ERR_TIMEOUT);
     if (warp == 0 && lane == 0) {
-      for (int s = issued - STAGES > 0 ? issued - STAGES : 0; s < issued; ++s)
-        mbar_wait(&sm.full[s % STAGES], (uint32_t)(s / STAGES) & 1, never);
+      for (int s = issued - GRAW > 0 ? issued - GRAW : 0; s < issued; ++s)
+        mbar_wait(&sm.rfull[s % GRAW], (uint32_t)(s / GRAW) & 1, never);
+    }
+    if (threadIdx.x == 64) {
+      for (int s = yissued - 2 > 0 ? yissued - 2 : 0; s < yissued; ++s)
+        mbar_wait(&sm.oy[s & 1], (uint32_t)(s >> 1) & 1, never);
     }
     if (warp == 1 && lane == 0) {
       mma_commit(&sm.mmadone);

@@ -150,7 +150,7 @@ extern "C" rbrp_status rbrp_sketch_gaussian_f32(rbrp_handle h, int l, int m, int
   int* dstatus = reinterpret_cast<int*>(base + 2 * tbytes);
   if (!h->smem_attr_sketch_tc) {
     rbrp_status s = cuda_check(h, cudaFuncSetAttribute(tc::k_gemm_tc<EpiY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                       (int)tc::P1_SMEM), "cudaFuncSetAttribute(k_gemm_tc<Y>)");
+                                                       (int)tc::GEMM_SMEM), "cudaFuncSetAttribute(k_gemm_tc<Y>)");
     if (s != RBRP_OK) return s;
     h->smem_attr_sketch_tc = true;
   }
@@ -164,7 +164,7 @@ extern "C" rbrp_status rbrp_sketch_gaussian_f32(rbrp_handle h, int l, int m, int
   const bool vec = (ldy % 4) == 0 && (reinterpret_cast<uintptr_t>(dY) & 15) == 0;
   EpiY epi{dY, ldy, l, n, vec};
   const long long budget = h->wait_budget > 0 ? h->wait_budget : kWaitBudgetDefault;
-  tc::k_gemm_tc<EpiY><<<dim3((n + tc::BM - 1) / tc::BM, (l + tc::BN - 1) / tc::BN), tc::NTHREADS, tc::P1_SMEM,
+  tc::k_gemm_tc<EpiY><<<dim3((n + tc::BM - 1) / tc::BM, (l + tc::BN - 1) / tc::BN), tc::NTHREADS, tc::GEMM_SMEM,
                         h->stream>>>(tmA, tmGh, tmGl, n, l, m, budget, dstatus, epi);
   s = cuda_check(h, cudaGetLastError(), "sketch kernels");
   if (s != RBRP_OK) return s;
