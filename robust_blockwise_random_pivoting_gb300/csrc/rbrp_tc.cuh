@@ -4,30 +4,31 @@
 // columns p (the MMA M dimension, TMEM lanes) and the <= 64 basis vectors a of
 // the block (MMA N), reduced over the m rows (MMA K) in stages of 32 rows.
 //
-//   warp 0   TMA producer: A_res tile (128 columns x 32 rows, FP32) and the hi
-//            and lo parts of the Q tile (64 x 32) into a 4-stage ring, 128-byte
-//            swizzled, completion on an mbarrier with a transaction count.
-//   warp 1   MMA issuer: tcgen05.mma kind::tf32.  The FP32 data is split into
-//            hi (rounded to the nearest TF32 value) + lo parts, exact in FP32; per K step the large product Ahi Qhi goes
-//            to one TMEM accumulator and the two small ones (Ahi Qlo, Alo Qhi)
-//            to another.
-//   warps 2-5 split each staged A tile into its hi / lo parts (in shared
-//            memory, same swizzled layout) ahead of the MMAs.
+//   warp 0   TMA producer: raw A_res tiles (128 columns x 32 rows, FP32,
+//            128-byte swizzled) into a 10-stage ring, completion on an mbarrier
+//            with a transaction count.
+//   warp 1   MMA issuer: tcgen05.mma kind::tf32 with A read from tensor memory and
+//            Q from shared memory; per K step the large product Ahi Qhi goes to
+//            one TMEM accumulator and the two small ones (Ahi Qlo, Alo Qhi) to
+//            another.
+//   warps 2-5 split each raw tile (one column per thread) by tf32_split and store
+//            the hi / lo parts into one of two A slots in tensor memory; the first
+//            of them loads that stage's Q hi / lo tiles (64 x 32) into the slot's
+//            shared memory.
 //   warps 6-13 drain the large accumulator after every stage and the small one
 //            every 512 rows with tcgen05.ld into double-float registers; two
 //            warps share each TMEM lane quarter, one per half of the 64 columns.
-//            Splitting and draining are independent chains, so neither waits
-//            for the other's latency.
 //
 // Why the drains: the tensor core rounds its FP32 accumulator once per MMA and
 // the rounding is biased, so the error grows linearly with the number of MMAs
 // between drains; 4 MMAs per drain keep W accurate to ~2e-7, which the
 // residual form needs (the part of A_res left along Q_blk by an error in W is
-// never removed by later blocks).  Both accumulators are double buffered.
+// never removed by later blocks).  The large accumulator has four buffers, the
+// small one two.
 //
 // Every wait is bounded (about 2 s of clock64 time); on a timeout the CTA sets
-// an abort flag, raises st->status, waits (bounded) for its own TMA copies,
-// frees its TMEM and returns.
+// an abort flag, raises st->status, waits (bounded) for its own TMA copies and
+// MMAs, frees its TMEM and returns.
 #pragma once
 #include <cuda.h>
 
@@ -40,16 +41,14 @@ namespace {  // internal linkage: included by each element-type translation unit
 constexpr int BM = 128;                  // residual columns per CTA (MMA M)
 constexpr int BN = 64;                   // basis vectors (MMA N)
 constexpr int BK = 32;                   // rows per stage = one 128-byte swizzle row of FP32
-constexpr int STAGES = 4;
 constexpr int CHUNK = 16;                // stages per drain of the small-product accumulator
 constexpr int A_BYTES = BM * BK * 4;     // 16 KB
 constexpr int B_BYTES = BN * BK * 4;     // 8 KB
-constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;  // A hi, A lo, Q hi, Q lo
 constexpr int NSPLIT = 128;              // 4 split warps
 constexpr int NDRAIN = 256;              // 8 drain warps
 constexpr int NTHREADS = 64 + NSPLIT + NDRAIN;  // TMA warp, MMA warp, split warps, drain warps
 constexpr int NBIG = 4;                   // large-product accumulators in the TMEM ring
-constexpr int TMEM_COLS = 512;            // large x4 + small x2 = 384 columns, rounded to a power of 2
+constexpr int TMEM_COLS = 512;            // large x4 + small x2 = 384 columns, + two A slots of 64
 constexpr int ST_ERR_TIMEOUT = 7;
 
 // tcgen05 instruction descriptor: D = F32 (bits 4-5 = 1), A = B = TF32 (bits 7-9,
@@ -57,17 +56,6 @@ constexpr int ST_ERR_TIMEOUT = 7;
 // bits 24-28.
 constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) |
                            ((uint32_t)(BM >> 4) << 24);
-
-struct __align__(1024) P1Smem {
-  uint8_t stage[STAGES][STAGE_BYTES];
-  unsigned long long full[STAGES], split[STAGES], empty[STAGES];
-  unsigned long long bigf[NBIG], bige[NBIG];  // large accumulators: full (MMA done) / empty (drained)
-  unsigned long long smlf[2], smle[2];     // small accumulator
-  unsigned long long mmadone;             // abort path: every MMA this CTA issued has completed
-  uint32_t tmem_base;
-  int abort;
-};
-constexpr size_t P1_SMEM = sizeof(P1Smem) + 1024;  // + alignment slack of the dynamic window
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
