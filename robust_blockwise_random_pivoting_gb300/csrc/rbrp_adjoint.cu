@@ -543,8 +543,10 @@ rbrp_status adjoint_tc(rbrp_handle h, int m, int k, int nc, int kp, int ncp, con
     h->smem_attr_gemm_tc = true;
   }
   const long long budget = h->wait_budget > 0 ? h->wait_budget : kWaitBudgetDefault;
-  CUtensorMap tmX1;
+  CUtensorMap tmX1, tmY1h, tmY1l;
   rbrp_status s = make_tmap_f32(h, &tmX1, Tx, k, nc, kp, tc::BK, tc::BM);
+  if (s == RBRP_OK) s = make_tmap_f32(h, &tmY1h, Cth, k, m, kp, tc::BK, tc::BN);
+  if (s == RBRP_OK) s = make_tmap_f32(h, &tmY1l, Ctl, k, m, kp, tc::BK, tc::BN);
   if (s != RBRP_OK) return s;
   s = cuda_check(h, cudaMemsetAsync(dstatus, 0, sizeof(int), st), "clear status");
   if (s != RBRP_OK) return s;
@@ -562,17 +564,19 @@ rbrp_status adjoint_tc(rbrp_handle h, int m, int k, int nc, int kp, int ncp, con
   }
   const int tx1 = (nc + tc::BM - 1) / tc::BM, ty1 = (m + tc::BN - 1) / tc::BN;
   EpiE e1{dA, lda, h->perm, k, m, nc, wr, cz, dG ? Et : nullptr, ncp, dG, ldg, scale, lp, ewp};
-  tc::k_gemm_tc<EpiE><<<dim3(tx1, ty1), tc::NTHREADS, tc::GEMM_SMEM, st>>>(tmX1, Cth, Ctl, kp, nc, m, k, budget,
+  tc::k_gemm_tc<EpiE><<<dim3(tx1, ty1), tc::NTHREADS, tc::GEMM_SMEM, st>>>(tmX1, tmY1h, tmY1l, nc, m, k, budget,
                                                                        dstatus, e1);
   if (dG) k_adj_sum_rows<<<(m + 255) / 256, 256, 0, st>>>(ewp, tx1, m, ew);
   k_adj_loss<<<1, 256, 0, st>>>(lp, tx1 * ty1, udf, k, lout);
   if (dG) {
-    CUtensorMap tmX2;
+    CUtensorMap tmX2, tmY2h, tmY2l;
     s = make_tmap_f32(h, &tmX2, Et, nc, m, ncp, tc::BK, tc::BM);
+    if (s == RBRP_OK) s = make_tmap_f32(h, &tmY2h, Trh, nc, k, ncp, tc::BK, tc::BN);
+    if (s == RBRP_OK) s = make_tmap_f32(h, &tmY2l, Trl, nc, k, ncp, tc::BK, tc::BN);
     if (s != RBRP_OK) return s;
     EpiG e2{h->perm, m, k, cz, ew, u, z, dG, ldg, scale};
     tc::k_gemm_tc<EpiG><<<dim3((m + tc::BM - 1) / tc::BM, (k + tc::BN - 1) / tc::BN), tc::NTHREADS, tc::GEMM_SMEM, st>>>(
-        tmX2, Trh, Trl, ncp, m, k, nc, budget, dstatus, e2);
+        tmX2, tmY2h, tmY2l, m, k, nc, budget, dstatus, e2);
   }
   s = cuda_check(h, cudaGetLastError(), "adjoint kernels");
   if (s != RBRP_OK) return s;

@@ -56,10 +56,12 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
   }
   cudaStream_t st = h->stream;
   const bool use_tc = RES && h->variant == 0;
-  CUtensorMap tmA, tmWth, tmWtl, tmQrh, tmQrl;
-  if (use_tc) {  // TMA views: A_res (m x n), boxes of 32 rows; for the update, W^T (64 per position,
-                 // boxes of 64 positions) and the basis by rows (boxes of 128)
+  CUtensorMap tmA, tmQh, tmQl, tmWth, tmWtl, tmQrh, tmQrl;
+  if (use_tc) {  // TMA views: A_res (m x n) and the split basis (m x 64), boxes of 32 rows; for the
+                 // update, W^T (64 per position, boxes of 64 positions) and the basis by rows (boxes of 128)
     s = make_tmap_f32(h, &tmA, h->Ares, m, n, L.ld_res, tc::BK, tc::BM);
+    if (s == RBRP_OK) s = make_tmap_f32(h, &tmQh, h->Qh, m, MAXB, L.ld_res, tc::BK, tc::BN);
+    if (s == RBRP_OK) s = make_tmap_f32(h, &tmQl, h->Ql, m, MAXB, L.ld_res, tc::BK, tc::BN);
     if (s == RBRP_OK) s = make_tmap_f32(h, &tmWth, h->Wth, MAXB, n, MAXB, tc::BK, tc::U_POS);
     if (s == RBRP_OK) s = make_tmap_f32(h, &tmWtl, h->Wtl, MAXB, n, MAXB, tc::BK, tc::U_POS);
     if (s == RBRP_OK) s = make_tmap_f32(h, &tmQrh, h->Qrh, MAXB, m, MAXB, tc::BK, tc::U_ROWS);
@@ -178,7 +180,7 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
           }
         }
         tc::k_proj_w_tc<<<dim3(ctiles, wsplit), tc::NTHREADS, tc::PROJ_SMEM, st>>>(
-            tmA, h->Qh, h->Ql, L.ld_res, h->st, m, n, sps, reinterpret_cast<float2*>(h->Wpart),
+            tmA, tmQh, tmQl, h->st, m, n, sps, reinterpret_cast<float2*>(h->Wpart),
             h->wait_budget > 0 ? h->wait_budget : kWaitBudgetDefault);
       } else {
         k_proj_w<<<(n - i + 63) / 64, 128, 0, st>>>((const float*)Q, L.ld_res, h->Ares, L.ld_res, h->st, m, n, h->R,

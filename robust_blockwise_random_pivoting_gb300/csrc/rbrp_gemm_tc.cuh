@@ -6,8 +6,7 @@
 // stages of 32 (MMA K).
 //
 // Both operands are K-major FP32 in global memory: X (K x M, column major, ld
-// a multiple of 4, read through a tensor map) and the hi and lo TF32 parts of Y
-// (K x N each, same layout, ld a multiple of 4, 16-byte aligned).
+// a multiple of 4) and the hi and lo TF32 parts of Y (K x N each, same layout).
 //
 //   warp 0   TMA producer: the raw X tiles (128 x 32, 128-byte swizzled) into a
 //            10-stage ring.
@@ -15,9 +14,8 @@
 //            X lo Y hi into a small one (3xTF32: the FP32 product to ~2^-22); X is
 //            read from tensor memory, Y from shared memory.
 //   warps 2-5 split each X tile by tf32_split into tensor memory (one row per
-//            thread), with two operand slots.
-//   warp 14  loads the Y hi / lo tiles (64 x 32) of each stage into a 4-slot ring
-//            by cp.async (load_b_stage).
+//            thread), with two operand slots; the first split thread loads the
+//            slot's Y hi / lo tiles (64 x 32).
 //   warps 6-13 drain the large accumulator after every RBRP_GEMM_DRAIN stages
 //            and the small one every CHUNK stages into double-float registers, then call the
 //            epilogue: thread (lane quarter q, column half ch) holds
@@ -48,16 +46,15 @@ namespace {
 constexpr int GEMM_DRAIN = RBRP_GEMM_DRAIN;
 static_assert(GEMM_DRAIN >= 1 && CHUNK % GEMM_DRAIN == 0, "drain interval");
 
-// Shared memory of k_gemm_tc: raw X tiles in a TMA ring and the loader warp's ring of
+// Shared memory of k_gemm_tc: raw X tiles in a TMA ring, and per operand slot the
 // Y hi / lo tiles; the split warps write X's hi / lo parts into tensor memory (A slots
 // after the accumulators), so the MMAs read only Y from shared memory (as k_proj_w_tc).
-constexpr int GRAW = 8;
+constexpr int GRAW = 10;
 struct __align__(1024) GemmSmem {
   uint8_t raw[GRAW][A_BYTES];
-  uint8_t ys[QST][2 * B_BYTES];                          // B slots: Y hi, Y lo (the loader warp's ring)
+  uint8_t ys[2][2 * B_BYTES];                            // per operand slot: Y hi, Y lo
   unsigned long long rfull[GRAW], rempty[GRAW];
-  unsigned long long ofree[2], osplit[2];                // X slots in TMEM: MMAs done / split done
-  unsigned long long qfull[QST], qfree[QST];             // Y slots: landed / MMAs done
+  unsigned long long ofree[2], osplit[2], oy[2];
   unsigned long long bigf[NBIG], bige[NBIG];
   unsigned long long smlf[2], smle[2];
   unsigned long long mmadone;
@@ -68,8 +65,8 @@ constexpr size_t GEMM_SMEM = sizeof(GemmSmem) + 1024;
 
 template <typename Epi>
 __global__ void __launch_bounds__(NTHREADS, 1)
-k_gemm_tc(const __grid_constant__ CUtensorMap tmX, const float* __restrict__ Yh, const float* __restrict__ Yl,
-          int64_t ldy, int M, int N, int K, long long budget, int* status, Epi epi) {
+k_gemm_tc(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmYh,
+          const __grid_constant__ CUtensorMap tmYl, int M, int N, int K, long long budget, int* status, Epi epi) {
   extern __shared__ uint8_t gt_raw[];
   GemmSmem& sm = *reinterpret_cast<GemmSmem*>((reinterpret_cast<uintptr_t>(gt_raw) + 1023) & ~(uintptr_t)1023);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -86,10 +83,7 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmX, const float* __restrict__ Yh,
     for (int b = 0; b < 2; ++b) {
       mbar_init(&sm.ofree[b], 1);
       mbar_init(&sm.osplit[b], NSPLIT);
-    }
-    for (int b = 0; b < QST; ++b) {
-      mbar_init(&sm.qfull[b], 32);
-      mbar_init(&sm.qfree[b], 1);
+      mbar_init(&sm.oy[b], 1);
     }
     for (int b = 0; b < NBIG; ++b) {
       mbar_init(&sm.bigf[b], 1);
@@ -113,7 +107,7 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmX, const float* __restrict__ Yh,
   __syncthreads();
   tc_fence_after();
   const uint32_t tbase = sm.tmem_base;
-  int issued = 0;
+  int issued = 0, yissued = 0;
 
   if (warp == 0) {
     if (lane == 0) {
@@ -137,13 +131,12 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmX, const float* __restrict__ Yh,
         const bool first = (s % CHUNK) == 0;
         if (gfirst && g >= NBIG && !mbar_wait(&sm.bige[b], (uint32_t)(g / NBIG - 1) & 1, abort, budget)) break;
         if (first && chunk >= 2 && !mbar_wait(&sm.smle[sb], (uint32_t)((chunk >> 1) - 1) & 1, abort, budget)) break;
-        const int ysl = s % QST;
         if (!mbar_wait(&sm.osplit[os], ouse & 1, abort, budget)) break;
-        if (!mbar_wait(&sm.qfull[ysl], (uint32_t)(s / QST) & 1, abort, budget)) break;
+        if (!mbar_wait(&sm.oy[os], ouse & 1, abort, budget)) break;
         tc_fence_after();
         const uint32_t txh = tbase + TA_COL + (uint32_t)(os * 2 * BK);   // X hi: 32 columns, then X lo
-        const uint64_t dyh = sw128_desc(smem_u32(sm.ys[ysl]));
-        const uint64_t dyl = sw128_desc(smem_u32(sm.ys[ysl] + B_BYTES));
+        const uint64_t dyh = sw128_desc(smem_u32(sm.ys[os]));
+        const uint64_t dyl = sw128_desc(smem_u32(sm.ys[os] + B_BYTES));
         const uint32_t dbig = tbase + (uint32_t)(b * BN);
         const uint32_t dsml = tbase + (uint32_t)(NBIG * BN + sb * BN);
 #pragma unroll
@@ -153,19 +146,25 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmX, const float* __restrict__ Yh,
           mma_tf32_ta(dsml, txh + BK + 8 * k, dyh + 2 * k, 1u);
         }
         mma_commit(&sm.ofree[os]);
-        mma_commit(&sm.qfree[ysl]);
         if (glast) mma_commit(&sm.bigf[b]);
         if ((s % CHUNK) == CHUNK - 1 || s == nk - 1) mma_commit(&sm.smlf[sb]);
       }
     }
   } else if (warp < 2 + NSPLIT / 32) {
     // split warps: one X row (a 128-byte swizzled row of the raw tile) per thread into
-    // TMEM lane 32 (warp % 4) + lane
+    // TMEM lane 32 (warp % 4) + lane; the first split thread requests the Y tiles
+    const int et = threadIdx.x - 64;
     const int row = 32 * (warp & 3) + lane;
     const uint32_t lane_off = (uint32_t)(32 * (warp & 3)) << 16;
     for (int s = 0; s < nk; ++s) {
       const int rs = s % GRAW, os = s & 1;
       if (s >= 2 && !mbar_wait(&sm.ofree[os], (uint32_t)((s >> 1) - 1) & 1, abort, budget)) break;
+      if (et == 0) {
+        mbar_expect_tx(&sm.oy[os], 2 * B_BYTES);
+        tma_load_2d(sm.ys[os], &tmYh, &sm.oy[os], s * BK, c0);
+        tma_load_2d(sm.ys[os] + B_BYTES, &tmYl, &sm.oy[os], s * BK, c0);
+        yissued = s + 1;
+      }
       if (!mbar_wait(&sm.rfull[rs], (uint32_t)(s / GRAW) & 1, abort, budget)) break;
       tc_fence_after();
       const uint8_t* rrow = sm.raw[rs] + row * 128;
@@ -186,8 +185,6 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmX, const float* __restrict__ Yh,
       mbar_arrive(&sm.rempty[rs]);
       mbar_arrive(&sm.osplit[os]);
     }
-  } else if (warp == LOADER_WARP) {
-    b_loader(sm.ys, sm.qfull, sm.qfree, Yh, Yl, ldy, c0, N, 0, nk, K, abort, budget);
   } else {
     const int dw = warp - 2 - NSPLIT / 32;  // 0..7
     const int q = warp & 3;                  // TMEM lane quarter of this warp
@@ -226,6 +223,10 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmX, const float* __restrict__ Yh,
     if (warp == 0 && lane == 0) {
       for (int s = issued - GRAW > 0 ? issued - GRAW : 0; s < issued; ++s)
         mbar_wait(&sm.rfull[s % GRAW], (uint32_t)(s / GRAW) & 1, never);
+    }
+    if (threadIdx.x == 64) {
+      for (int s = yissued - 2 > 0 ? yissued - 2 : 0; s < yissued; ++s)
+        mbar_wait(&sm.oy[s & 1], (uint32_t)(s >> 1) & 1, never);
     }
     if (warp == 1 && lane == 0) {
       mma_commit(&sm.mmadone);

@@ -154,8 +154,10 @@ extern "C" rbrp_status rbrp_sketch_gaussian_f32(rbrp_handle h, int l, int m, int
     if (s != RBRP_OK) return s;
     h->smem_attr_sketch_tc = true;
   }
-  CUtensorMap tmA;
+  CUtensorMap tmA, tmGh, tmGl;
   rbrp_status s = make_tmap_f32(h, &tmA, dA, m, n, lda, tc::BK, tc::BM);
+  if (s == RBRP_OK) s = make_tmap_f32(h, &tmGh, Gth, m, l, mp, tc::BK, tc::BN);
+  if (s == RBRP_OK) s = make_tmap_f32(h, &tmGl, Gtl, m, l, mp, tc::BK, tc::BN);
   if (s == RBRP_OK) s = cuda_check(h, cudaMemsetAsync(dstatus, 0, sizeof(int), h->stream), "clear status");
   if (s != RBRP_OK) return s;
   k_gt_split<<<dim3((l + 31) / 32, (m + 31) / 32), 256, 0, h->stream>>>(G, l, m, mp, Gth, Gtl);
@@ -163,7 +165,7 @@ extern "C" rbrp_status rbrp_sketch_gaussian_f32(rbrp_handle h, int l, int m, int
   EpiY epi{dY, ldy, l, n, vec};
   const long long budget = h->wait_budget > 0 ? h->wait_budget : kWaitBudgetDefault;
   tc::k_gemm_tc<EpiY><<<dim3((n + tc::BM - 1) / tc::BM, (l + tc::BN - 1) / tc::BN), tc::NTHREADS, tc::GEMM_SMEM,
-                        h->stream>>>(tmA, Gth, Gtl, mp, n, l, m, budget, dstatus, epi);
+                        h->stream>>>(tmA, tmGh, tmGl, n, l, m, budget, dstatus, epi);
   s = cuda_check(h, cudaGetLastError(), "sketch kernels");
   if (s != RBRP_OK) return s;
   int hs = 0;

@@ -12,12 +12,12 @@
 //            one TMEM accumulator and the two small ones (Ahi Qlo, Alo Qhi) to
 //            another.
 //   warps 2-5 split each raw tile (one column per thread) by tf32_split and store
-//            the hi / lo parts into one of two A slots in tensor memory.
+//            the hi / lo parts into one of two A slots in tensor memory; the first
+//            of them loads that stage's Q hi / lo tiles (64 x 32) into the slot's
+//            shared memory.
 //   warps 6-13 drain the large accumulator after every stage and the small one
 //            every 512 rows with tcgen05.ld into double-float registers; two
 //            warps share each TMEM lane quarter, one per half of the 64 columns.
-//   warp 14  B loader: each stage's Q hi / lo tiles (64 x 32) into a 4-slot ring in
-//            shared memory by cp.async (load_b_stage).
 //
 // Why the drains: the tensor core rounds its FP32 accumulator once per MMA and
 // the rounding is biased, so the error grows linearly with the number of MMAs
@@ -46,10 +46,7 @@ constexpr int A_BYTES = BM * BK * 4;     // 16 KB
 constexpr int B_BYTES = BN * BK * 4;     // 8 KB
 constexpr int NSPLIT = 128;              // 4 split warps
 constexpr int NDRAIN = 256;              // 8 drain warps
-constexpr int NTHREADS = 64 + NSPLIT + NDRAIN + 32;  // TMA warp, MMA warp, split, drain and B-loader warps
-constexpr int LOADER_WARP = 2 + (NSPLIT + NDRAIN) / 32;
-constexpr int QST = 4;                   // B-operand (Q or Y) slots in shared memory
-constexpr int QLEAD = 2;                 // B stages the loader warp keeps in flight
+constexpr int NTHREADS = 64 + NSPLIT + NDRAIN;  // TMA warp, MMA warp, split warps, drain warps
 constexpr int NBIG = 4;                   // large-product accumulators in the TMEM ring
 constexpr int TMEM_COLS = 512;            // large x4 + small x2 = 384 columns, + two A slots of 64
 constexpr int ST_ERR_TIMEOUT = 7;
@@ -156,64 +153,6 @@ __device__ __forceinline__ void tmem_st32(uint32_t taddr, const float (&v)[32]) 
       : "memory");
 }
 
-// The B operand of one stage (the hi and lo tiles: BN rows x 32 K values each,
-// K-major, 128-byte swizzled: 16-byte chunk c of row a at chunk c ^ (a % 8)) into
-// dst by cp.async from two column-major FP32 matrices, tile row a = column c0 + a
-// at Bh / Bl + (c0 + a) ldb, K values k0 .. k0 + 31; zero at and beyond K and N.
-// One warp; every instruction covers four columns' 128 contiguous bytes.  TMA
-// would take this path too, but the TMA unit moves a tile in about 250 cycles plus
-// 3.4 per 128-byte row, so two 64-row B tiles per stage beside the 128-row A tile
-// cost more than the stage's MMAs; the load / store units carry B instead.
-__device__ __forceinline__ void load_b_stage(uint8_t* dst, const float* __restrict__ Bh,
-                                             const float* __restrict__ Bl, int64_t ldb, int c0, int N, int k0,
-                                             int K) {
-  const int lane = threadIdx.x & 31;
-#pragma unroll 8
-  for (int j = 0; j < 2 * BN * 8 / 32; ++j) {
-    const int idx = lane + 32 * j;
-    const int t = idx >> 9;               // 0: hi, 1: lo
-    const int a = (idx >> 3) & (BN - 1);  // tile row = column c0 + a of B
-    const int c = idx & 7;                // chunk: K values k0 + 4c .. + 3
-    const int kk = k0 + 4 * c, col = c0 + a;
-    const int valid = col < N ? max(0, min(4, K - kk)) : 0;
-    const float* src = (t ? Bl : Bh) + (valid > 0 ? (int64_t)col * ldb + kk : 0);
-    const uint32_t d = smem_u32(dst + t * B_BYTES + a * 128 + ((c ^ (a & 7)) << 4));
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(4 * valid) : "memory");
-  }
-  asm volatile("cp.async.commit_group;" ::: "memory");
-}
-
-// The B-loader warp of k_proj_w_tc / k_gemm_tc: stage s into slot s % QST once the
-// MMAs of stage s - QST have released it, QLEAD stages in flight; each stage is
-// published on qfull (one arrival per lane) after its copies landed and a proxy
-// fence made them visible to the tensor core.  Returns false on abort; its copies
-// have landed either way.
-__device__ __forceinline__ bool b_loader(uint8_t (*qs)[2 * B_BYTES], unsigned long long* qfull,
-                                         unsigned long long* qfree, const float* Bh, const float* Bl,
-                                         int64_t ldb, int c0, int N, int kbase, int nk, int K, volatile int* abort,
-                                         long long budget) {
-  bool ok = true;
-  for (int s = 0; s < nk + QLEAD; ++s) {
-    if (s < nk) {
-      const int slot = s % QST;
-      if (s >= QST && !mbar_wait(&qfree[slot], (uint32_t)((s / QST) - 1) & 1, abort, budget)) {
-        ok = false;
-        break;
-      }
-      load_b_stage(qs[slot], Bh, Bl, ldb, c0, N, kbase + s * BK, K);
-    } else {
-      asm volatile("cp.async.commit_group;" ::: "memory");  // empty group: the count stays uniform
-    }
-    if (s >= QLEAD) {
-      asm volatile("cp.async.wait_group %0;" ::"n"(QLEAD) : "memory");
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      mbar_arrive(&qfull[(s - QLEAD) % QST]);
-    }
-  }
-  asm volatile("cp.async.wait_all;" ::: "memory");
-  return ok;
-}
-
 __device__ __forceinline__ void mma_commit(unsigned long long* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
                : "memory");
@@ -269,21 +208,20 @@ __device__ __forceinline__ void drain32(uint32_t taddr, float (&hi)[32], float (
 }
 
 // Shared memory of k_proj_w_tc.  The TMA ring holds raw A tiles only (16 KB a
-// stage: 128 KB of A in flight per SM).  The split warps write each tile's hi /
+// stage: 160 KB of A in flight per SM).  The split warps write each tile's hi /
 // lo parts straight into tensor memory (the MMAs read A from there), so shared
-// memory carries only the raw tiles and the loader warp's ring of Q hi / lo tiles.
+// memory carries only the raw tiles and, per operand slot, that stage's Q hi / lo.
 // An MMA whose A comes from shared memory re-reads its 4 KB per instruction at
 // about 128 bytes per clock (a probe: 51 clocks per M128 N64 K8 TF32 MMA); from
 // tensor memory only the 2 KB Q operand is read.
-constexpr int RAW = 8;                                   // raw A stages in flight
+constexpr int RAW = 10;                                  // raw A stages in flight
 constexpr uint32_t TA_COL = NBIG * BN + 2 * BN;          // TMEM columns of the A slots (after the accumulators)
 static_assert(TA_COL + 2 * 2 * BK <= TMEM_COLS, "TMEM budget: accumulators + two A slots of hi, lo");
 struct __align__(1024) ProjSmem {
   uint8_t raw[RAW][A_BYTES];
-  uint8_t qs[QST][2 * B_BYTES];                          // B slots: Q hi, Q lo (the loader warp's ring)
+  uint8_t qs[2][2 * B_BYTES];                            // per operand slot: Q hi, Q lo
   unsigned long long rfull[RAW], rempty[RAW];            // raw ring: TMA done / split done
-  unsigned long long ofree[2], osplit[2];                // A slots in TMEM: MMAs done / split done
-  unsigned long long qfull[QST], qfree[QST];             // B slots: landed / MMAs done
+  unsigned long long ofree[2], osplit[2], oq[2];         // operand slots: MMAs done / A in TMEM / Q landed
   unsigned long long bigf[NBIG], bige[NBIG];             // large accumulators: full (MMA done) / empty (drained)
   unsigned long long smlf[2], smle[2];                   // small accumulator
   unsigned long long mmadone;                            // abort path: every MMA this CTA issued has completed
@@ -293,9 +231,9 @@ struct __align__(1024) ProjSmem {
 constexpr size_t PROJ_SMEM = sizeof(ProjSmem) + 1024;    // + alignment slack of the dynamic window
 
 __global__ void __launch_bounds__(NTHREADS, 1)
-k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const float* __restrict__ Qh, const float* __restrict__ Ql,
-            int64_t ldq, State* st, int m, int n, int stages_per_split, float2* __restrict__ Wpart,
-            long long budget) {
+k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmQh,
+            const __grid_constant__ CUtensorMap tmQl, State* st, int m, int n, int stages_per_split,
+            float2* __restrict__ Wpart, long long budget) {
   extern __shared__ uint8_t p1_raw[];
   ProjSmem& sm = *reinterpret_cast<ProjSmem*>((reinterpret_cast<uintptr_t>(p1_raw) + 1023) & ~(uintptr_t)1023);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -317,10 +255,7 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const float* __restrict__ Q
     for (int b = 0; b < 2; ++b) {
       mbar_init(&sm.ofree[b], 1);
       mbar_init(&sm.osplit[b], NSPLIT);
-    }
-    for (int b = 0; b < QST; ++b) {
-      mbar_init(&sm.qfull[b], 32);
-      mbar_init(&sm.qfree[b], 1);
+      mbar_init(&sm.oq[b], 1);
     }
     for (int b = 0; b < NBIG; ++b) {
       mbar_init(&sm.bigf[b], 1);
@@ -345,6 +280,7 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const float* __restrict__ Q
   tc_fence_after();
   const uint32_t tbase = sm.tmem_base;
   int issued = 0;   // producer: stages whose A loads were issued
+  int qissued = 0;  // first split thread: stages whose Q loads were issued
 
   if (warp == 0) {
     if (lane == 0) {
@@ -366,13 +302,12 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const float* __restrict__ Q
         const bool first = (s % CHUNK) == 0;
         if (s >= NBIG && !mbar_wait(&sm.bige[b], (uint32_t)(s / NBIG - 1) & 1, abort, budget)) break;
         if (first && chunk >= 2 && !mbar_wait(&sm.smle[sb], (uint32_t)((chunk >> 1) - 1) & 1, abort, budget)) break;
-        const int qsl = s % QST;
         if (!mbar_wait(&sm.osplit[os], ouse & 1, abort, budget)) break;
-        if (!mbar_wait(&sm.qfull[qsl], (uint32_t)(s / QST) & 1, abort, budget)) break;
+        if (!mbar_wait(&sm.oq[os], ouse & 1, abort, budget)) break;
         tc_fence_after();
         const uint32_t tah = tbase + TA_COL + (uint32_t)(os * 2 * BK);   // A hi: 32 columns, then A lo
-        const uint64_t dqh = sw128_desc(smem_u32(sm.qs[qsl]));
-        const uint64_t dql = sw128_desc(smem_u32(sm.qs[qsl] + B_BYTES));
+        const uint64_t dqh = sw128_desc(smem_u32(sm.qs[os]));
+        const uint64_t dql = sw128_desc(smem_u32(sm.qs[os] + B_BYTES));
         const uint32_t dbig = tbase + (uint32_t)(b * BN);
         const uint32_t dsml = tbase + (uint32_t)(NBIG * BN + sb * BN);
 #pragma unroll
@@ -382,7 +317,6 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const float* __restrict__ Q
           mma_tf32_ta(dsml, tah + BK + 8 * k, dqh + 2 * k, 1u);
         }
         mma_commit(&sm.ofree[os]);
-        mma_commit(&sm.qfree[qsl]);
         mma_commit(&sm.bigf[b]);
         if ((s % CHUNK) == CHUNK - 1 || s == nk - 1) mma_commit(&sm.smlf[sb]);
       }
@@ -390,12 +324,20 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const float* __restrict__ Q
   } else if (warp < 2 + NSPLIT / 32) {
     // split warps: TMEM lane quarter warp % 4; a thread takes one position (a 128-byte
     // row of the swizzled raw tile: 16-byte chunk c of row r sits at chunk c ^ (r % 8)),
-    // splits its 32 values and stores hi / lo into the A slot of stage s
+    // splits its 32 values and stores hi / lo into the A slot of stage s; the first split
+    // thread requests that stage's Q tiles once the slot is free
+    const int et = threadIdx.x - 64;  // 0..NSPLIT-1
     const int row = 32 * (warp & 3) + lane;
     const uint32_t lane_off = (uint32_t)(32 * (warp & 3)) << 16;
     for (int s = 0; s < nk; ++s) {
       const int rs = s % RAW, os = s & 1;
       if (s >= 2 && !mbar_wait(&sm.ofree[os], (uint32_t)((s >> 1) - 1) & 1, abort, budget)) break;
+      if (et == 0) {
+        mbar_expect_tx(&sm.oq[os], 2 * B_BYTES);
+        tma_load_2d(sm.qs[os], &tmQh, &sm.oq[os], (s0 + s) * BK, 0);
+        tma_load_2d(sm.qs[os] + B_BYTES, &tmQl, &sm.oq[os], (s0 + s) * BK, 0);
+        qissued = s + 1;
+      }
       if (!mbar_wait(&sm.rfull[rs], (uint32_t)(s / RAW) & 1, abort, budget)) break;
       tc_fence_after();
       const uint8_t* rrow = sm.raw[rs] + row * 128;
@@ -416,8 +358,6 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const float* __restrict__ Q
       mbar_arrive(&sm.rempty[rs]);
       mbar_arrive(&sm.osplit[os]);
     }
-  } else if (warp == LOADER_WARP) {
-    b_loader(sm.qs, sm.qfull, sm.qfree, Qh, Ql, ldq, 0, BN, s0 * BK, nk, m, abort, budget);
   } else {
     // drain warps
     const int dw = warp - 2 - NSPLIT / 32;  // 0..7
@@ -470,6 +410,10 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const float* __restrict__ Q
     if (warp == 0 && lane == 0) {
       for (int s = issued - RAW > 0 ? issued - RAW : 0; s < issued; ++s)
         mbar_wait(&sm.rfull[s % RAW], (uint32_t)(s / RAW) & 1, never);
+    }
+    if (threadIdx.x == 64) {
+      for (int s = qissued - 2 > 0 ? qissued - 2 : 0; s < qissued; ++s)
+        mbar_wait(&sm.oq[s & 1], (uint32_t)(s >> 1) & 1, never);
     }
     if (warp == 1 && lane == 0) {
       mma_commit(&sm.mmadone);
