@@ -56,12 +56,14 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
   }
   cudaStream_t st = h->stream;
   const bool use_tc = RES && h->variant == 0;
-  CUtensorMap tmA, tmQh, tmQl, tmWth, tmWtl, tmQrh, tmQrl;
+  CUtensorMap tmA, tmQ, tmWth, tmWtl, tmQrh, tmQrl;
   if (use_tc) {  // TMA views: A_res (m x n) and the split basis (m x 64), boxes of 32 rows; for the
                  // update, W^T (64 per position, boxes of 64 positions) and the basis by rows (boxes of 128)
     s = make_tmap_f32(h, &tmA, h->Ares, m, n, L.ld_res, tc::BK, tc::BM);
-    if (s == RBRP_OK) s = make_tmap_f32(h, &tmQh, h->Qh, m, MAXB, L.ld_res, tc::BK, tc::BN);
-    if (s == RBRP_OK) s = make_tmap_f32(h, &tmQl, h->Ql, m, MAXB, L.ld_res, tc::BK, tc::BN);
+    // the split basis: Qh and Ql are adjacent workspace arrays (ld_res x 64 each), viewed as
+    // one m x 128 array so that one box fetches a stage's hi and lo tiles
+    if (h->Ql != h->Qh + L.ld_res * MAXB) return set_error(h, RBRP_ERR_INVALID_ARG, "basis hi / lo arrays not adjacent");
+    if (s == RBRP_OK) s = make_tmap_f32(h, &tmQ, h->Qh, m, 2 * MAXB, L.ld_res, tc::BK, 2 * tc::BN);
     if (s == RBRP_OK) s = make_tmap_f32(h, &tmWth, h->Wth, MAXB, n, MAXB, tc::BK, tc::U_POS);
     if (s == RBRP_OK) s = make_tmap_f32(h, &tmWtl, h->Wtl, MAXB, n, MAXB, tc::BK, tc::U_POS);
     if (s == RBRP_OK) s = make_tmap_f32(h, &tmQrh, h->Qrh, MAXB, m, MAXB, tc::BK, tc::U_ROWS);
@@ -180,7 +182,7 @@ rbrp_status run_rbrp(rbrp_handle h, int m, int n, const T* dA, int64_t lda, cons
           }
         }
         tc::k_proj_w_tc<<<dim3(ctiles, wsplit), tc::NTHREADS, tc::PROJ_SMEM, st>>>(
-            tmA, tmQh, tmQl, h->st, m, n, sps, reinterpret_cast<float2*>(h->Wpart),
+            tmA, tmQ, h->st, m, n, sps, reinterpret_cast<float2*>(h->Wpart),
             h->wait_budget > 0 ? h->wait_budget : kWaitBudgetDefault);
       } else {
         k_proj_w<<<(n - i + 63) / 64, 128, 0, st>>>((const float*)Q, L.ld_res, h->Ares, L.ld_res, h->st, m, n, h->R,

@@ -13,8 +13,8 @@
 //            another.
 //   warps 2-5 split each raw tile (one column per thread) by tf32_split and store
 //            the hi / lo parts into one of two A slots in tensor memory; the first
-//            of them loads that stage's Q hi / lo tiles (64 x 32) into the slot's
-//            shared memory.
+//            of them loads that stage's Q hi / lo tiles (64 x 32 each, one TMA box
+//            over the adjacent hi and lo arrays) into the slot's shared memory.
 //   warps 6-13 drain the large accumulator after every stage and the small one
 //            every 512 rows with tcgen05.ld into double-float registers; two
 //            warps share each TMEM lane quarter, one per half of the 64 columns.
@@ -231,8 +231,8 @@ struct __align__(1024) ProjSmem {
 constexpr size_t PROJ_SMEM = sizeof(ProjSmem) + 1024;    // + alignment slack of the dynamic window
 
 __global__ void __launch_bounds__(NTHREADS, 1)
-k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmQh,
-            const __grid_constant__ CUtensorMap tmQl, State* st, int m, int n, int stages_per_split,
+k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmQ, State* st, int m,
+            int n, int stages_per_split,
             float2* __restrict__ Wpart, long long budget) {
   extern __shared__ uint8_t p1_raw[];
   ProjSmem& sm = *reinterpret_cast<ProjSmem*>((reinterpret_cast<uintptr_t>(p1_raw) + 1023) & ~(uintptr_t)1023);
@@ -333,9 +333,8 @@ k_proj_w_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
       const int rs = s % RAW, os = s & 1;
       if (s >= 2 && !mbar_wait(&sm.ofree[os], (uint32_t)((s >> 1) - 1) & 1, abort, budget)) break;
       if (et == 0) {
-        mbar_expect_tx(&sm.oq[os], 2 * B_BYTES);
-        tma_load_2d(sm.qs[os], &tmQh, &sm.oq[os], (s0 + s) * BK, 0);
-        tma_load_2d(sm.qs[os] + B_BYTES, &tmQl, &sm.oq[os], (s0 + s) * BK, 0);
+        mbar_expect_tx(&sm.oq[os], 2 * B_BYTES);   // Q hi (64 rows) then Q lo: one box of 128
+        tma_load_2d(sm.qs[os], &tmQ, &sm.oq[os], (s0 + s) * BK, 0);
         qissued = s + 1;
       }
       if (!mbar_wait(&sm.rfull[rs], (uint32_t)(s / RAW) & 1, abort, budget)) break;
