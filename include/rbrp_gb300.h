@@ -133,9 +133,9 @@ rbrp_status rbrp_fixed_id_adjoint_f32(rbrp_handle h, int m, int n, const float* 
  * the cuBLAS GEMM of gpu/gemm.cu:9-15): dY (l x n, ldy >= l) = G A with
  * G (l x m) = scale * N(0, 1) from Philox4x64-10 (key seed) by Box-Muller.
  * The product runs on the tensor cores (tcgen05, 3xTF32: FP32-accurate) when dA
- * and lda are 16-byte aligned, else on a CUDA-core FP32 GEMM.  Returns after the
- * kernels have finished (a bounded device wait that runs out gives
- * RBRP_ERR_DEVICE_TIMEOUT). */
+ * and lda are 16-byte aligned; that path waits for its kernels to read their
+ * status (a bounded device wait that runs out gives RBRP_ERR_DEVICE_TIMEOUT).
+ * Otherwise a CUDA-core FP32 GEMM runs, asynchronously on the handle's stream. */
 rbrp_status rbrp_sketch_gaussian_f32(rbrp_handle h, int l, int m, int n, const float* dA, int64_t lda,
                                      uint64_t seed, float scale, float* dY, int64_t ldy);
 
