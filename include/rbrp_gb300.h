@@ -177,6 +177,16 @@ rbrp_status rbrp_CPQR(int m, int n, const double* dA, const int* ranks, int nran
 
 /* T (k x (n-k), column major) of the last run, into a device buffer with ldt >= k. */
 rbrp_status rbrp_copy_T(rbrp_handle h, double* dT, int64_t ldt);
+/* The notebook's L of the last run (python/RBRP.ipynb cell 11: L = A^T Q, one
+ * row per column of A in its original order, one column per basis vector), into
+ * a device buffer (n x k, column major, ldl >= n): L(perm[p], a) = R(a, p), the
+ * projection of the column at position p onto basis vector a, for p >= a, and 0
+ * for p < a (columns chosen before basis vector a, which the notebook leaves at
+ * 0 and which are orthogonal to it).  Each basis vector's sign follows a panel
+ * factor with a positive diagonal; LAPACK's QR in the notebook may flip it, which
+ * flips that column of L and leaves the interpolation matrix unchanged.
+ * Asynchronous on the handle's stream. */
+rbrp_status rbrp_copy_L(rbrp_handle h, double* dL, int64_t ldl);
 /* Device pointer of T of the last run (ld = k), valid until the next run. */
 rbrp_status rbrp_T_device(rbrp_handle h, const double** dT, int* ld);
 /* python/RBRP.ipynb cell 2 lines 111-126 (matdivide, A * pinv(B) from the SVD of

@@ -82,6 +82,7 @@ _SIGS = {
     "rbrp_id_f32": (c_int, [c_void_p, c_int, c_int, c_void_p, c_int64, ctypes.POINTER(Params), c_void_p,
                             ctypes.POINTER(Result)]),
     "rbrp_copy_T": (c_int, [c_void_p, c_void_p, c_int64]),
+    "rbrp_copy_L": (c_int, [c_void_p, c_void_p, c_int64]),
     "rbrp_T_device": (c_int, [c_void_p, ctypes.POINTER(c_void_p), ctypes.POINTER(c_int)]),
     "rbrp_get_trace": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int, ctypes.POINTER(c_int)]),
     "rbrp_id_error_f64": (c_int, [c_void_p, c_int, c_int, c_void_p, c_int64, ctypes.POINTER(c_double)]),

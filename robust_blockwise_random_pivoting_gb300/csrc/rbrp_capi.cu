@@ -879,6 +879,34 @@ rbrp_status rbrp_copy_T(rbrp_handle h, double* dT, int64_t ldt) {
                     "copy T");
 }
 
+namespace rbrp {
+namespace {
+// L(perm[p], a) = R(a, p) for p >= a, else 0 (R: k x n row major by position, ld n).
+__global__ void k_copy_L(const double* __restrict__ R, const int* __restrict__ perm, int n, int k,
+                         double* __restrict__ L, int64_t ldl) {
+  const int64_t total = (int64_t)n * k;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int a = (int)(idx / n), p = (int)(idx % n);
+    L[(int64_t)perm[p] + (int64_t)a * ldl] = p >= a ? R[(int64_t)a * n + p] : 0.0;
+  }
+}
+}  // namespace
+}  // namespace rbrp
+
+rbrp_status rbrp_copy_L(rbrp_handle h, double* dL, int64_t ldl) {
+  if (!h) return RBRP_ERR_INVALID_ARG;
+  if (!h->have_result) return set_error(h, RBRP_ERR_NOT_COMPUTED, "no successful run");
+  const int k = h->k, n = h->n;
+  if (k == 0 || n == 0) return RBRP_OK;
+  if (!dL || ldl < n) return set_error(h, RBRP_ERR_INVALID_ARG, "dL is NULL or ldl < n");
+  DeviceGuard g(h->device);
+  const int64_t total = (int64_t)n * k;
+  const int blocks = (int)std::min<int64_t>(4 * 1216, (total + 255) / 256);
+  k_copy_L<<<blocks, 256, 0, h->stream>>>(h->R, h->perm, n, k, dL, ldl);
+  return cuda_check(h, cudaGetLastError(), "copy L");
+}
+
 rbrp_status rbrp_T_device(rbrp_handle h, const double** dT, int* ld) {
   if (!h || !dT || !ld) return RBRP_ERR_INVALID_ARG;
   if (!h->have_result) return set_error(h, RBRP_ERR_NOT_COMPUTED, "no successful run");

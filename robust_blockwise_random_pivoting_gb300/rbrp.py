@@ -168,6 +168,20 @@ class Handle:
             check(self.lib.rbrp_copy_T(self.h, ctypes.c_void_p(out.data_ptr()), k), self.h)
         return out
 
+    def L(self):
+        """The notebook's L = A^T Q of the last run (python/RBRP.ipynb cell 11): an (n, k) FP64
+        CUDA tensor, row j for column j of A, column a for basis vector a; zero where the column
+        was chosen before basis vector a.  Basis vectors follow a positive-diagonal panel factor,
+        so a column may have the opposite sign of the notebook's (LAPACK) one; the interpolation
+        matrix derived from L does not depend on those signs."""
+        ptr, ld = ctypes.c_void_p(), ctypes.c_int()
+        check(self.lib.rbrp_T_device(self.h, ctypes.byref(ptr), ctypes.byref(ld)), self.h)
+        k, n = ld.value, self.n_last
+        out = torch.empty((k, n), dtype=torch.float64, device=f"cuda:{self.device}").t()
+        if k > 0 and n > 0:
+            check(self.lib.rbrp_copy_L(self.h, ctypes.c_void_p(out.data_ptr()), n), self.h)
+        return out
+
     def T_matdivide(self, tol=1e-12):
         """T of the last run as pinv_tol(R11) R12 (the notebook's ``matdivide``, python/RBRP.ipynb
         cell 2 lines 111-126): returns ``(T, rank)``, T a (k, n-k) column-major FP64 CUDA tensor
@@ -653,13 +667,15 @@ def rand_adap_rbrp(A, tol=1e-8, blk=16):
     return sk_t, rd_t, T_t, k, flops.value
 
 
-def blocked_rpid(X, k, b=20, tol=None, mode="rp", ortho=1, tol_loc=None, seed=0, handle=None):
+def blocked_rpid(X, k, b=20, tol=None, mode="rp", ortho=1, tol_loc=None, seed=0, handle=None, return_L=False):
     """The notebook's ``blocked_rpid`` contract on the GPU (rows of ``X`` are the items).
 
     ``X`` is an (n, d) CUDA tensor; the ID is the column ID of ``A = X.T``.
     Only ``ortho=1`` (RBRP) exists.  Returns ``(row_perm, T, residuals,
-    time_pivot, ranks)``; the notebook's ``L`` factor is replaced by the
-    interpolation matrix ``T`` (k x (n-k)) that the notebook derives from it.
+    time_pivot, ranks)``: the interpolation matrix ``T`` (k x (n-k)) that the
+    notebook derives from its ``L``.  With ``return_L=True`` the second entry is
+    the notebook's own ``L = X Q`` ((n, k), :meth:`Handle.L`) instead, so the
+    notebook's ``get_rpid_error`` / ``interpolation`` take the tuple unchanged.
     """
     if ortho != 1:
         raise ValueError("only ortho=1 (RBRP) is implemented")
@@ -667,5 +683,5 @@ def blocked_rpid(X, k, b=20, tol=None, mode="rp", ortho=1, tol_loc=None, seed=0,
     A = X.t()
     h = handle or Handle(A.device.index)
     r = h.column_id(A, b=b, tol=tol, kmax=k, seed=seed, sampler=sampler, tol_loc=tol_loc)
-    return (r.perm.cpu().numpy().astype(np.int64), r.T, r.residuals, r.t_ms * 1e-3,
+    return (r.perm.cpu().numpy().astype(np.int64), h.L() if return_L else r.T, r.residuals, r.t_ms * 1e-3,
             r.ranks.astype(np.int64))

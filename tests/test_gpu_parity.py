@@ -64,6 +64,43 @@ def check_against_oracle(h, A, b, tol, sampler="np", mode="rp", seed=0, kmax=Non
     return r, o
 
 
+def _notebook_T_from_L(L, perm, k):
+    """The interpolation matrix the notebook derives from L (T^T = L_rd L_S^{-1})."""
+    LS, Lrd = L[perm[:k]], L[perm[k:]]
+    return np.linalg.solve(LS.T, Lrd.T)
+
+
+@pytest.mark.parametrize("fp32", [False, True])
+def test_notebook_L_matches_oracle(handle, fp32):
+    """Handle.L() / blocked_rpid(return_L=True) is the notebook's L = A^T Q: equal to the oracle's
+    column by column up to each basis vector's sign (FP64 form to 1e-10 of |L|, the mixed form to
+    1e-5) over the positions where the two runs pick the same columns, zero where a column was
+    chosen before the basis vector, and the notebook's T from it is the library's T."""
+    from robust_blockwise_random_pivoting_gb300.rbrp import blocked_rpid
+    A = W.gaussian_exp(300, 420, decay=12.0, seed=5)
+    b, tol = 24, 1e-10
+    o = rbrp_column_id(A.astype(np.float32).astype(np.float64) if fp32 else A, b, tol=tol, seed=0)
+    X = dev(A, torch.float32 if fp32 else torch.float64).t()
+    row_perm, L, _, _, ranks = blocked_rpid(X, 300, b=b, tol=tol, seed=0, handle=handle, return_L=True)
+    k = int(ranks[-1])
+    L = L.cpu().numpy()
+    assert L.shape == (420, k)
+    if not fp32:
+        assert k == o["k"] and np.array_equal(row_perm, o["perm"])
+    kk = min(k, o["k"])
+    diff = np.nonzero(row_perm[:kk] != o["perm"][:kk])[0]
+    same = int(diff[0]) if diff.size else kk
+    assert same >= 10
+    Lo = o["L"][:, :same]
+    sign = np.sign(np.sum(L[:, :same] * Lo, axis=0))
+    np.testing.assert_allclose(L[:, :same] * sign, Lo, rtol=0, atol=(1e-5 if fp32 else 1e-10) * np.abs(Lo).max())
+    for a in range(k):  # columns chosen before basis vector a are exactly zero
+        assert np.all(L[row_perm[:a], a] == 0.0)
+    T = handle.T().cpu().numpy()
+    Tn = _notebook_T_from_L(L, row_perm, k)
+    np.testing.assert_allclose(Tn, T, rtol=0, atol=(1e-4 if fp32 else 1e-8) * max(1.0, np.abs(T).max()))
+
+
 def test_gexp1000_skeleton_bit_exact(handle):
     """The 1000 x 1000 FP64 workload, b = 40, squared tol 1e-12, Philox seed 0."""
     A = W.gaussian_exp()
