@@ -73,12 +73,15 @@ def _notebook_T_from_L(L, perm, k):
 @pytest.mark.parametrize("fp32", [False, True])
 def test_notebook_L_matches_oracle(handle, fp32):
     """Handle.L() / blocked_rpid(return_L=True) is the notebook's L = A^T Q: equal to the oracle's
-    column by column up to each basis vector's sign (FP64 form to 1e-10 of |L|, the mixed form to
+    column by column up to each basis vector's sign (FP64 form to 1e-8 of |L|, the mixed form to
     1e-5) over the positions where the two runs pick the same columns, zero where a column was
-    chosen before the basis vector, and the notebook's T from it is the library's T."""
+    chosen before the basis vector, and the notebook's T from it is the library's T.  The squared
+    tolerance 1e-6 keeps the skeleton's condition number near 1e3: deeper, the notebook's single
+    Gram-Schmidt pass loses orthogonality at ~eps cond^2 and the two bases part by more than
+    rounding (1e-4 of a column at k = 165 here), with the same T."""
     from robust_blockwise_random_pivoting_gb300.rbrp import blocked_rpid
     A = W.gaussian_exp(300, 420, decay=12.0, seed=5)
-    b, tol = 24, 1e-10
+    b, tol = 24, 1e-6
     o = rbrp_column_id(A.astype(np.float32).astype(np.float64) if fp32 else A, b, tol=tol, seed=0)
     X = dev(A, torch.float32 if fp32 else torch.float64).t()
     row_perm, L, _, _, ranks = blocked_rpid(X, 300, b=b, tol=tol, seed=0, handle=handle, return_L=True)
@@ -93,7 +96,7 @@ def test_notebook_L_matches_oracle(handle, fp32):
     assert same >= 10
     Lo = o["L"][:, :same]
     sign = np.sign(np.sum(L[:, :same] * Lo, axis=0))
-    np.testing.assert_allclose(L[:, :same] * sign, Lo, rtol=0, atol=(1e-5 if fp32 else 1e-10) * np.abs(Lo).max())
+    np.testing.assert_allclose(L[:, :same] * sign, Lo, rtol=0, atol=(1e-5 if fp32 else 1e-8) * np.abs(Lo).max())
     for a in range(k):  # columns chosen before basis vector a are exactly zero
         assert np.all(L[row_perm[:a], a] == 0.0)
     T = handle.T().cpu().numpy()
