@@ -284,6 +284,95 @@ __global__ void __launch_bounds__(256) k_trsm_T_df(const float2* __restrict__ R1
   }
 }
 
+// Right-looking form of the same double-float solve, for every shape: block row
+// b (64 rows from the bottom up) is solved for all columns at once, then its
+// product with R11(0:b0, b) is subtracted from every earlier row.  Each step has
+// work over rows and columns, so the whole GPU stays busy however few columns T
+// has (the left-looking k_trsm_T_df only has one CTA per tile of columns).
+//
+// k_trsm_rl_diag: X_b = R11(b, b)^{-1} B_b, one warp per column, lane l holding
+// rows l and l + 32 of the block; back substitution with the solved value
+// broadcast by shuffles, in double-float.
+__global__ void __launch_bounds__(256) k_trsm_rl_diag(const float2* __restrict__ R11, int k, int ncols, int b0, int bl,
+                                                      float2* __restrict__ T) {
+  __shared__ float2 Rd[64][65];
+  __shared__ float2 inv[64];
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  for (int idx = tid; idx < 64 * 64; idx += 256) {
+    const int xr = idx >> 6, y = idx & 63;
+    Rd[xr][y] = (xr < bl && y < bl && y >= xr) ? R11[(int64_t)(b0 + xr) * k + b0 + y] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  if (tid < bl) inv[tid] = df2_recip(Rd[tid][tid]);
+  __syncthreads();
+  const int c = blockIdx.x * 8 + w;
+  if (c >= ncols) return;
+  float2* col = T + b0 + (int64_t)c * k;
+  float2 v0 = lane < bl ? col[lane] : make_float2(0.f, 0.f);
+  float2 v1 = lane + 32 < bl ? col[lane + 32] : make_float2(0.f, 0.f);
+  for (int r = bl - 1; r >= 0; --r) {
+    // the owner of row r finishes it; every lane then removes its rows' share
+    const float2 mine = r < 32 ? v0 : v1;
+    const float2 xr = df2_mul(mine, inv[r]);
+    const float2 x = make_float2(__shfl_sync(0xffffffffu, xr.x, r & 31), __shfl_sync(0xffffffffu, xr.y, r & 31));
+    if (lane == (r & 31)) {
+      if (r < 32) v0 = x; else v1 = x;
+    }
+    if (lane < r) df_mac(v0.x, v0.y, make_float2(-Rd[lane][r].x, -Rd[lane][r].y), x);
+    if (lane + 32 < r) df_mac(v1.x, v1.y, make_float2(-Rd[lane + 32][r].x, -Rd[lane + 32][r].y), x);
+    // keep the low parts small, as the left-looking solve does after each block
+    if (lane < r) v0 = df2_fast(v0.x, v0.y);
+    if (lane + 32 < r) v1 = df2_fast(v1.x, v1.y);
+  }
+  if (lane < bl) col[lane] = v0;
+  if (lane + 32 < bl) col[lane + 32] = v1;
+}
+
+// k_trsm_rl_update: B(rows of tile, cols of tile) -= R11(rows, b) X_b for the
+// 64 x 32 tile (blockIdx.x: rows below b0, blockIdx.y: columns), in double-float:
+// each thread one row and 8 columns, the products summed as in k_trsm_T_df.
+struct TrsmRlSmem {
+  float2 Rs[64][65];
+  float2 Xs[64][33];
+};
+__global__ void __launch_bounds__(256) k_trsm_rl_update(const float2* __restrict__ R11, int k, int ncols, int b0,
+                                                        int bl, float2* __restrict__ T) {
+  extern __shared__ __align__(16) unsigned char dyn_smem[];
+  TrsmRlSmem& sm = *reinterpret_cast<TrsmRlSmem*>(dyn_smem);
+  const int tid = threadIdx.x;
+  const int r0 = blockIdx.x * 64, c0 = blockIdx.y * 32;
+  const int nc = min(32, ncols - c0);
+  for (int idx = tid; idx < 64 * 64; idx += 256) {
+    const int xr = idx >> 6, y = idx & 63;
+    const float2 v = y < bl ? R11[(int64_t)(r0 + xr) * k + b0 + y] : make_float2(0.f, 0.f);
+    sm.Rs[xr][y] = make_float2(-v.x, -v.y);
+  }
+  for (int idx = tid; idx < 64 * 32; idx += 256) {
+    const int y = idx & 63, c = idx >> 6;
+    sm.Xs[y][c] = (y < bl && c < nc) ? T[(b0 + y) + (int64_t)(c0 + c) * k] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  const int x = tid >> 2;
+  float sh[8], sl[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) sh[q] = sl[q] = 0.f;
+#pragma unroll 4
+  for (int y = 0; y < 64; ++y) {
+    const float2 r = sm.Rs[x][y];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) df_mac(sh[q], sl[q], r, sm.Xs[y][(tid & 3) + 4 * q]);
+  }
+  const int row = r0 + x;  // r0 + 63 < b0: every row of the tile exists
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const int c = (tid & 3) + 4 * q;
+    if (c < nc) {
+      float2* t = T + row + (int64_t)(c0 + c) * k;
+      *t = df2_add(*t, make_float2(sh[q], sl[q]));
+    }
+  }
+}
+
 // ===========================================================================
 // a11: ||A(:, rd) - A(:, S) T||_F^2 in FP64 (python/RBRP.ipynb cell 7 lines
 // 40-53; gpu/id_cpqr.cu:145-170).  Validation only: one FP64 GEMM.
@@ -504,49 +593,17 @@ rbrp_status solve_T(rbrp_handle h, int k, int n) {
     float2* R11df = static_cast<float2*>(h->df_buf);
     float2* Tdf = R11df + (size_t)k * k;
     k_split_df<<<1216, 256, 0, h->stream>>>(h->R, n, k, ncols, R11df, Tdf);
-    // tile width 4 NQ columns by a measured model: a CTA beside another one on its SM takes
-    // Tp ~ NQ + 2.5 (units), alone about 0.55 Tp (it is latency-bound; two CTAs per SM are
-    // issue-bound).  Full waves of two CTAs per SM cost Tp each; a remainder that fits one
-    // CTA per SM costs 0.55 Tp, a larger one Tp.  (16384 columns, k = 2030: 32 columns per
-    // tile 16.3 ms, 24 columns 16.9; 8192: 10.5 and 8.5.)
-    auto tsolve = [&](auto nq) -> rbrp_status {
-      constexpr int NQ = decltype(nq)::value;
-      return cuda_check(h, cudaFuncSetAttribute(k_trsm_T_df<NQ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                (int)sizeof(TrsmDfSmem)), "cudaFuncSetAttribute(k_trsm_T_df)");
-    };
-    auto per_sm = [&](auto nq) -> int {
-      constexpr int NQ = decltype(nq)::value;
-      int c = 0;
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_trsm_T_df<NQ>, 256, sizeof(TrsmDfSmem));
-      return std::max(1, c);
-    };
-    const std::integral_constant<int, 8> q8;
-    const std::integral_constant<int, 6> q6;
-    const std::integral_constant<int, 4> q4;
-    for (rbrp_status e : {tsolve(q8), tsolve(q6), tsolve(q4)})
-      if (e != RBRP_OK) return e;
-    int best_nq = 8;
-    double best = -1.0;
-    const int occ[3] = {per_sm(q8), per_sm(q6), per_sm(q4)};
-    const int nqs[3] = {8, 6, 4};
-    for (int v = 0; v < 3; ++v) {
-      const long tiles = (ncols + 4 * nqs[v] - 1) / (4 * nqs[v]);
-      const long full = (long)occ[v] * h->sms;
-      const long waves = tiles / full, rest = tiles - waves * full;
-      const double tail = rest == 0 ? 0.0 : (occ[v] > 1 && rest <= h->sms ? 0.55 : 1.0);
-      const double cost = ((double)waves + tail) * (nqs[v] + 2.5);
-      if (best < 0.0 || cost < best) {
-        best = cost;
-        best_nq = nqs[v];
-      }
+    s = cuda_check(h, cudaFuncSetAttribute(k_trsm_rl_update, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)sizeof(TrsmRlSmem)), "cudaFuncSetAttribute(k_trsm_rl_update)");
+    if (s != RBRP_OK) return s;
+    const int nbk = (k + 63) / 64;
+    for (int bi = nbk - 1; bi >= 0; --bi) {
+      const int b0 = bi * 64, bl = std::min(64, k - b0);
+      k_trsm_rl_diag<<<(ncols + 7) / 8, 256, 0, h->stream>>>(R11df, k, ncols, b0, bl, Tdf);
+      if (b0 > 0)
+        k_trsm_rl_update<<<dim3(b0 / 64, (ncols + 31) / 32), 256, sizeof(TrsmRlSmem), h->stream>>>(R11df, k, ncols,
+                                                                                                   b0, bl, Tdf);
     }
-    const int grid = (ncols + 4 * best_nq - 1) / (4 * best_nq);
-    if (best_nq == 8)
-      k_trsm_T_df<8><<<grid, 256, sizeof(TrsmDfSmem), h->stream>>>(R11df, k, ncols, Tdf);
-    else if (best_nq == 6)
-      k_trsm_T_df<6><<<grid, 256, sizeof(TrsmDfSmem), h->stream>>>(R11df, k, ncols, Tdf);
-    else
-      k_trsm_T_df<4><<<grid, 256, sizeof(TrsmDfSmem), h->stream>>>(R11df, k, ncols, Tdf);
     k_join_df<<<1216, 256, 0, h->stream>>>(Tdf, (int64_t)k * ncols, h->T);
   }
   return cuda_check(h, cudaGetLastError(), "T solve launch");
