@@ -10,8 +10,6 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
-#include <type_traits>
-
 #include "rbrp_internal.h"
 #include "../../include/rbrp_gb300_testing.h"
 
@@ -143,12 +141,6 @@ __global__ void k_join_df(const float2* __restrict__ Tdf, int64_t count, double*
   }
 }
 
-struct TrsmDfSmem {
-  float2 Rs[64][65];     // -R11 block (update) or R11 diagonal block (solve)
-  float2 Xs[64][33];     // solved T rows
-  float2 Acc[64][33];    // right-hand side / solution of the current block row
-};
-
 __device__ __forceinline__ float2 df2_two_sum(float a, float b) {
   const float s = a + b;
   const float bb = s - a;
@@ -186,109 +178,13 @@ __device__ __forceinline__ float2 df2_recip(float2 b) {
   return df2_fast(q, q * r.x);
 }
 
-// One CTA solves a tile of 4 NQ columns of T (NQ per thread: columns (tid & 3) + 4q).
-// The host picks NQ so that the tiles fill whole waves of CTAs: a CTA is bound by
-// its own latency chains, so it runs about as fast alone on an SM as beside a
-// second one, and a partial last wave costs a whole one.
-template <int NQ>
-__global__ void __launch_bounds__(256) k_trsm_T_df(const float2* __restrict__ R11, int k, int ncols,
-                                                   float2* __restrict__ T) {
-  constexpr int W = 4 * NQ;
-  extern __shared__ __align__(16) unsigned char dyn_smem[];
-  TrsmDfSmem& sm = *reinterpret_cast<TrsmDfSmem*>(dyn_smem);
-  const int tid = threadIdx.x;
-  const int c0 = blockIdx.x * W;
-  const int nc = min(W, ncols - c0);
-  const int nbk = (k + 63) / 64;
-  const int x = tid >> 2;
-  for (int bi = nbk - 1; bi >= 0; --bi) {
-    const int b0 = bi * 64, bl = min(64, k - b0);
-    for (int idx = tid; idx < 64 * W; idx += 256) {
-      const int xr = idx & 63, c = idx >> 6;
-      sm.Acc[xr][c] = (xr < bl && c < nc) ? T[(b0 + xr) + (int64_t)(c0 + c) * k] : make_float2(0.f, 0.f);
-    }
-    float sh[NQ], sl[NQ];
-#pragma unroll
-    for (int q = 0; q < NQ; ++q) sh[q] = sl[q] = 0.f;
-    // the tiles of step bj are fetched into registers during step bj - 1
-    float2 rpre[16], xpre[NQ];
-    auto fetch = [&](int bj) {
-      const int cr = bj * 64, cl = min(64, k - cr);
-#pragma unroll
-      for (int u = 0; u < 16; ++u) {
-        const int idx = tid + 256 * u, y = idx & 63, xr = idx >> 6;
-        const float2 v = (xr < bl && y < cl) ? R11[(int64_t)(b0 + xr) * k + cr + y] : make_float2(0.f, 0.f);
-        rpre[u] = make_float2(-v.x, -v.y);
-      }
-#pragma unroll
-      for (int u = 0; u < NQ; ++u) {
-        const int idx = tid + 256 * u, y = idx & 63, c = idx >> 6;
-        xpre[u] = (y < cl && c < nc) ? T[(cr + y) + (int64_t)(c0 + c) * k] : make_float2(0.f, 0.f);
-      }
-    };
-    if (bi + 1 < nbk) fetch(bi + 1);
-    for (int bj = bi + 1; bj < nbk; ++bj) {
-      __syncthreads();
-#pragma unroll
-      for (int u = 0; u < 16; ++u) {
-        const int idx = tid + 256 * u;
-        sm.Rs[idx >> 6][idx & 63] = rpre[u];
-      }
-#pragma unroll
-      for (int u = 0; u < NQ; ++u) {
-        const int idx = tid + 256 * u;
-        sm.Xs[idx & 63][idx >> 6] = xpre[u];
-      }
-      __syncthreads();
-      if (bj + 1 < nbk) fetch(bj + 1);
-#pragma unroll 4
-      for (int y = 0; y < 64; ++y) {
-        const float2 r = sm.Rs[x][y];
-#pragma unroll
-        for (int q = 0; q < NQ; ++q) df_mac(sh[q], sl[q], r, sm.Xs[y][(tid & 3) + 4 * q]);
-      }
-#pragma unroll
-      for (int q = 0; q < NQ; ++q) {  // renormalise so the low part stays small
-        const float t = sh[q] + sl[q];
-        sl[q] = sl[q] - (t - sh[q]);
-        sh[q] = t;
-      }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int q = 0; q < NQ; ++q) {
-      float2& a = sm.Acc[x][(tid & 3) + 4 * q];
-      a = df2_add(a, make_float2(sh[q], sl[q]));
-    }
-    for (int idx = tid; idx < 64 * 64; idx += 256) {
-      const int y = idx & 63, xr = idx >> 6;
-      sm.Rs[xr][y] = (xr < bl && y < bl && y >= xr) ? R11[(int64_t)(b0 + xr) * k + b0 + y] : make_float2(0.f, 0.f);
-    }
-    __syncthreads();
-    if (tid < nc) {  // back substitution on the diagonal block, one right-hand side per thread
-      for (int xr = bl - 1; xr >= 0; --xr) {
-        float vh = sm.Acc[xr][tid].x, vl = sm.Acc[xr][tid].y;
-        for (int y = xr + 1; y < bl; ++y) {
-          const float2 r = sm.Rs[xr][y];
-          df_mac(vh, vl, make_float2(-r.x, -r.y), sm.Acc[y][tid]);
-        }
-        sm.Acc[xr][tid] = df2_mul(df2_fast(vh, vl), df2_recip(sm.Rs[xr][xr]));
-      }
-    }
-    __syncthreads();
-    for (int idx = tid; idx < 64 * W; idx += 256) {
-      const int xr = idx & 63, c = idx >> 6;
-      if (xr < bl && c < nc) T[(b0 + xr) + (int64_t)(c0 + c) * k] = sm.Acc[xr][c];
-    }
-    __syncthreads();
-  }
-}
-
-// Right-looking form of the same double-float solve, for every shape: block row
-// b (64 rows from the bottom up) is solved for all columns at once, then its
-// product with R11(0:b0, b) is subtracted from every earlier row.  Each step has
-// work over rows and columns, so the whole GPU stays busy however few columns T
-// has (the left-looking k_trsm_T_df only has one CTA per tile of columns).
+// The double-float solve is right-looking: block row b (64 rows from the bottom
+// up) is solved for all columns at once, then its product with R11(0:b0, b) is
+// subtracted from every earlier row.  Each step has work over rows and columns,
+// so the whole GPU stays busy however few columns T has.  (A left-looking form,
+// one CTA per 32 columns for the whole solve, had as many CTAs as column tiles:
+// 120 for the adjoint's 3822 columns; it took 8.5 ms at 8192 x 8192, k = 2033,
+// against 7.6, and the same 16.2 ms at 16384.)
 //
 // k_trsm_rl_diag: X_b = R11(b, b)^{-1} B_b, one warp per column, lane l holding
 // rows l and l + 32 of the block; back substitution with the solved value
@@ -330,7 +226,8 @@ __global__ void __launch_bounds__(256) k_trsm_rl_diag(const float2* __restrict__
 
 // k_trsm_rl_update: B(rows of tile, cols of tile) -= R11(rows, b) X_b for the
 // 64 x 32 tile (blockIdx.x: rows below b0, blockIdx.y: columns), in double-float:
-// each thread one row and 8 columns, the products summed as in k_trsm_T_df.
+// each thread one row and 8 columns, each product exact (FMA split) and summed by
+// TwoSum in double-float.
 struct TrsmRlSmem {
   float2 Rs[64][65];
   float2 Xs[64][33];

@@ -284,9 +284,8 @@ def test_tensor_core_projection_matches_cuda_core(handle):
 
 @pytest.mark.parametrize("n", [900, 6400, 8400])
 def test_double_float_T_solve_matches_fp64(handle, n):
-    """T = R11^{-1} R12 with double-float block updates against the FP64-pipe solve.  The
-    double-float solve takes 16, 24 or 32 columns per CTA by the number of columns of T;
-    on 152 SMs these sizes (about 600, 6100 and 8100 columns) take the three widths."""
+    """T = R11^{-1} R12 with double-float block updates against the FP64-pipe solve, for
+    about 600, 6100 and 8100 columns of T (several 64-row blocks each)."""
     A = dev(W.gaussian_exp(500, n, decay=15.0, seed=17))
     Ts = []
     for fp64 in (True, False):
