@@ -9,8 +9,11 @@ where ``w`` holds one weight per column of A (the entries at S are ignored).
 :class:`FixedSkeletonIDLoss` is a ``torch.autograd.Function``: its forward runs
 the fixed-skeleton ID (``rbrp_fixed_id_f32``: the RBRP panels, swaps and
 updates with the sampler replaced by the given skeleton) and the loss kernels;
-its backward runs the forward again (nothing of the factorisation is stored)
-and the hand-written adjoint kernels of ``rbrp_fixed_id_adjoint_f32``:
+its backward runs the hand-written adjoint kernels of
+``rbrp_fixed_id_adjoint_f32`` on the forward's factorisation, which stays in the
+handle (R, T and the permutation of the last run) unless the handle did other
+work in between or the backward runs on another stream; then it runs the
+fixed-skeleton ID again first:
 
     dL/dB = 2 E + 2 (C z) w^T,   dL/dC = -2 E T^T - 2 (C z) u^T + 2 (E w) z^T,
     E = B - C T,  u = T w,  z = (C^T C)^{-1} u = R11^{-1} R11^{-T} u.
@@ -58,14 +61,18 @@ def fixed_skeleton_id(handle, A, S, b=64):
     return perm, r
 
 
-def fixed_skeleton_loss_and_grad(handle, A, S, w, b=64, grad=True, scale=1.0):
-    """Loss (float) and, if ``grad``, ``scale * dloss/dA`` (FP32, column major) for skeleton ``S``."""
+def fixed_skeleton_loss_and_grad(handle, A, S, w, b=64, grad=True, scale=1.0, reuse_epoch=None):
+    """Loss (float) and, if ``grad``, ``scale * dloss/dA`` (FP32, column major) for skeleton ``S``.
+
+    With ``reuse_epoch`` equal to ``handle.epoch`` (read right after a call for the same A, S
+    and b) the handle's factorisation is taken as it stands instead of being recomputed."""
     A = _as_f32_colmajor(A)
     m, n = A.shape
     w = w.to(device=A.device, dtype=torch.float32).contiguous()
     if w.numel() != n:
         raise ValueError("w needs one entry per column of A")
-    fixed_skeleton_id(handle, A, S, b)
+    if reuse_epoch is None or reuse_epoch != handle.epoch:
+        fixed_skeleton_id(handle, A, S, b)
     G = torch.empty((n, m), dtype=torch.float32, device=A.device).t() if grad else None
     loss = ctypes.c_double()
     check(handle.lib.rbrp_fixed_id_adjoint_f32(handle.h, m, n, ctypes.c_void_p(A.data_ptr()), _ld(A),
@@ -84,12 +91,15 @@ class FixedSkeletonIDLoss(torch.autograd.Function):
         loss, _ = fixed_skeleton_loss_and_grad(h, A.detach(), S, w, b, grad=False)
         ctx.save_for_backward(A.detach(), S, w)
         ctx.b, ctx.handle = b, h
+        ctx.epoch, ctx.stream = h.epoch, torch.cuda.current_stream(A.device).cuda_stream
         return torch.tensor(loss, dtype=torch.float64, device=A.device)
 
     @staticmethod
     def backward(ctx, g):
         A, S, w = ctx.saved_tensors
-        _, G = fixed_skeleton_loss_and_grad(ctx.handle, A, S, w, ctx.b, grad=True, scale=float(g))
+        same_stream = torch.cuda.current_stream(A.device).cuda_stream == ctx.stream
+        _, G = fixed_skeleton_loss_and_grad(ctx.handle, A, S, w, ctx.b, grad=True, scale=float(g),
+                                            reuse_epoch=ctx.epoch if same_stream else None)
         return G, None, None, None, None
 
 

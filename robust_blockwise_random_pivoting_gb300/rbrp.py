@@ -83,6 +83,9 @@ class Handle:
         check(self.lib.rbrp_create(ctypes.byref(h), self.device))
         self.h = h
         self.n_last = None
+        # work counter: advanced by every call that launches work or changes the last run's
+        # results, so a caller can tell whether those results are still the ones it made
+        self.epoch = 0
 
     def close(self):
         if getattr(self, "h", None):
@@ -115,8 +118,10 @@ class Handle:
         p.recompute = int(bool(recompute))
         return p
 
-    def _bind_stream(self, stream):
+    def _bind_stream(self, stream, work=True):
         check(self.lib.rbrp_set_stream(self.h, ctypes.c_void_p(stream.cuda_stream)), self.h)
+        if work:
+            self.epoch += 1
 
     def column_id(self, A, b=64, tol=1e-12, kmax=None, seed=0, sampler="np", tol_loc=None,
                   compute_T=True, recompute=True, stream=None):
@@ -188,6 +193,7 @@ class Handle:
         and rank the number of singular values of R11 above ``tol``.  Later ``T()`` calls
         return the same matrix until the next run."""
         rank = ctypes.c_int()
+        self.epoch += 1
         check(self.lib.rbrp_T_matdivide(self.h, float(tol), ctypes.byref(rank)), self.h)
         return self.T(), rank.value
 
@@ -199,6 +205,7 @@ class Handle:
         m, n = A.shape
         ch = ctypes.c_double()
         fn = self.lib.rbrp_refine_T_f64 if A.dtype == torch.float64 else self.lib.rbrp_refine_T_f32
+        self.epoch += 1
         check(fn(self.h, m, n, ctypes.c_void_p(A.data_ptr()), _ld(A), int(steps), float(tol), ctypes.byref(ch)),
               self.h)
         return ch.value

@@ -156,6 +156,34 @@ def test_lengthscale_gradient_fd_and_fp64(handle):
     assert abs(g_ours - g64) <= 1e-2 * abs(g64), (g_ours, g64)
 
 
+def test_backward_reuses_the_forward_factorisation(handle):
+    """The backward takes the handle's factorisation from the forward when nothing ran in
+    between (no second fixed-skeleton ID), and recomputes it when something did; the gradient
+    equals the one computed from scratch bit for bit either way."""
+    from robust_blockwise_random_pivoting_gb300.adjoint import (fixed_skeleton_id_loss, fixed_skeleton_loss_and_grad,
+                                                                gaussian_kernel_matrix)
+    P, ls = kernel_problem(384, seed=7)
+    A32 = colmajor(gaussian_kernel_matrix(P, ls).float())
+    S = skeleton(handle, A32)
+    w = torch.randn(384, generator=torch.Generator(device="cpu").manual_seed(3)).cuda()
+    loss_ref, G_ref = fixed_skeleton_loss_and_grad(handle, A32, S, w, b=64, grad=True)
+    # reuse: forward, then backward with nothing in between
+    A = A32.clone().requires_grad_(True)
+    loss = fixed_skeleton_id_loss(A, S, w, b=64, handle=handle)
+    e0 = handle.epoch
+    loss.backward()
+    assert handle.epoch == e0          # no fixed-skeleton ID ran in the backward
+    assert loss.item() == loss_ref and torch.equal(A.grad, G_ref)
+    # an intervening run on the handle: the backward recomputes
+    A2 = A32.clone().requires_grad_(True)
+    loss2 = fixed_skeleton_id_loss(A2, S, w, b=64, handle=handle)
+    handle.column_id(A32, b=32, tol=1e-6, seed=1)
+    e1 = handle.epoch
+    loss2.backward()
+    assert handle.epoch == e1 + 1      # the backward ran the fixed-skeleton ID again
+    assert torch.equal(A2.grad, G_ref)
+
+
 def test_adjoint_requires_matching_run(handle):
     from robust_blockwise_random_pivoting_gb300._lib import RBRPError
     from robust_blockwise_random_pivoting_gb300.adjoint import fixed_skeleton_id
