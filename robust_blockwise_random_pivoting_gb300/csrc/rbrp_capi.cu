@@ -150,14 +150,16 @@ __device__ __forceinline__ float2 df2_fast(float a, float b) {
   const float s = a + b;
   return make_float2(s, b - (s - a));
 }
-// (sh, sl) += a * b in double-float.
+// (sh, sl) += a * b in double-float: the exact product a.x b.x = p + e (FMA split)
+// and the cross terms go into the low part by FMAs, the high parts are added by
+// TwoSum with its error into the low part (12 FP32 operations).
 __device__ __forceinline__ void df_mac(float& sh, float& sl, float2 a, float2 b) {
   const float p = a.x * b.x;
   const float e = fmaf(a.x, b.x, -p);
-  const float c = fmaf(a.x, b.y, a.y * b.x);
+  sl = fmaf(a.y, b.x, fmaf(a.x, b.y, sl + e));
   const float t = sh + p;
   const float bb = t - sh;
-  sl += ((sh - (t - bb)) + (p - bb)) + (e + c);
+  sl += (sh - (t - bb)) + (p - bb);
   sh = t;
 }
 __device__ __forceinline__ float2 df2_add(float2 a, float2 b) {
@@ -225,47 +227,56 @@ __global__ void __launch_bounds__(256) k_trsm_rl_diag(const float2* __restrict__
 }
 
 // k_trsm_rl_update: B(rows of tile, cols of tile) -= R11(rows, b) X_b for the
-// 64 x 32 tile (blockIdx.x: rows below b0, blockIdx.y: columns), in double-float:
-// each thread one row and 8 columns, each product exact (FMA split) and summed by
-// TwoSum in double-float.
+// 64 x 64 tile (blockIdx.x: rows below b0, blockIdx.y: columns), in double-float:
+// each thread two rows (x, x + 32) and 8 columns, so every shared load of X feeds
+// two products; each product exact (FMA split) and summed by TwoSum.
 struct TrsmRlSmem {
   float2 Rs[64][65];
-  float2 Xs[64][33];
+  float2 Xs[64][65];
 };
 __global__ void __launch_bounds__(256) k_trsm_rl_update(const float2* __restrict__ R11, int k, int ncols, int b0,
                                                         int bl, float2* __restrict__ T) {
   extern __shared__ __align__(16) unsigned char dyn_smem[];
   TrsmRlSmem& sm = *reinterpret_cast<TrsmRlSmem*>(dyn_smem);
   const int tid = threadIdx.x;
-  const int r0 = blockIdx.x * 64, c0 = blockIdx.y * 32;
-  const int nc = min(32, ncols - c0);
+  const int r0 = blockIdx.x * 64, c0 = blockIdx.y * 64;
+  const int nc = min(64, ncols - c0);
   for (int idx = tid; idx < 64 * 64; idx += 256) {
     const int xr = idx >> 6, y = idx & 63;
     const float2 v = y < bl ? R11[(int64_t)(r0 + xr) * k + b0 + y] : make_float2(0.f, 0.f);
     sm.Rs[xr][y] = make_float2(-v.x, -v.y);
   }
-  for (int idx = tid; idx < 64 * 32; idx += 256) {
+  for (int idx = tid; idx < 64 * 64; idx += 256) {
     const int y = idx & 63, c = idx >> 6;
     sm.Xs[y][c] = (y < bl && c < nc) ? T[(b0 + y) + (int64_t)(c0 + c) * k] : make_float2(0.f, 0.f);
   }
   __syncthreads();
-  const int x = tid >> 2;
-  float sh[8], sl[8];
+  const int x = tid >> 3, cq = tid & 7;  // rows x and x + 32, columns cq + 8 q
+  float sh[2][8], sl[2][8];
 #pragma unroll
-  for (int q = 0; q < 8; ++q) sh[q] = sl[q] = 0.f;
-#pragma unroll 4
+  for (int h = 0; h < 2; ++h)
+#pragma unroll
+    for (int q = 0; q < 8; ++q) sh[h][q] = sl[h][q] = 0.f;
+#pragma unroll 2
   for (int y = 0; y < 64; ++y) {
-    const float2 r = sm.Rs[x][y];
+    const float2 ra = sm.Rs[x][y], rb = sm.Rs[x + 32][y];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) df_mac(sh[q], sl[q], r, sm.Xs[y][(tid & 3) + 4 * q]);
+    for (int q = 0; q < 8; ++q) {
+      const float2 xv = sm.Xs[y][cq + 8 * q];
+      df_mac(sh[0][q], sl[0][q], ra, xv);
+      df_mac(sh[1][q], sl[1][q], rb, xv);
+    }
   }
-  const int row = r0 + x;  // r0 + 63 < b0: every row of the tile exists
 #pragma unroll
-  for (int q = 0; q < 8; ++q) {
-    const int c = (tid & 3) + 4 * q;
-    if (c < nc) {
-      float2* t = T + row + (int64_t)(c0 + c) * k;
-      *t = df2_add(*t, make_float2(sh[q], sl[q]));
+  for (int h = 0; h < 2; ++h) {
+    const int row = r0 + x + 32 * h;  // r0 + 63 < b0: every row of the tile exists
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int c = cq + 8 * q;
+      if (c < nc) {
+        float2* t = T + row + (int64_t)(c0 + c) * k;
+        *t = df2_add(*t, make_float2(sh[h][q], sl[h][q]));
+      }
     }
   }
 }
@@ -498,7 +509,7 @@ rbrp_status solve_T(rbrp_handle h, int k, int n) {
       const int b0 = bi * 64, bl = std::min(64, k - b0);
       k_trsm_rl_diag<<<(ncols + 7) / 8, 256, 0, h->stream>>>(R11df, k, ncols, b0, bl, Tdf);
       if (b0 > 0)
-        k_trsm_rl_update<<<dim3(b0 / 64, (ncols + 31) / 32), 256, sizeof(TrsmRlSmem), h->stream>>>(R11df, k, ncols,
+        k_trsm_rl_update<<<dim3(b0 / 64, (ncols + 63) / 64), 256, sizeof(TrsmRlSmem), h->stream>>>(R11df, k, ncols,
                                                                                                    b0, bl, Tdf);
     }
     k_join_df<<<1216, 256, 0, h->stream>>>(Tdf, (int64_t)k * ncols, h->T);
