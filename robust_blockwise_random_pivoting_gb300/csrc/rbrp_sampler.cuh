@@ -59,7 +59,12 @@ __device__ void sample_block(State* st, const double* __restrict__ diags, const 
     double part = 0.0;
     for (int j = lo; j < hi; ++j) part += w[j];
     const double S = block_sum(part, shd);
-    const double invS = 1.0 / S;  // one FP64 division; per-entry divisions are ~1/64-rate work on GB300
+    // one FP64 division for the block, shared: per-thread or per-entry divisions are
+    // ~1/64-rate work on GB300
+    __shared__ double s_invS;
+    if (tid == 0) s_invS = 1.0 / S;
+    __syncthreads();
+    const double invS = s_invS;
     int npos = 0;
     for (int j = lo; j < hi; ++j) {
       const double pj = w[j] * invS;
@@ -79,7 +84,7 @@ __device__ void sample_block(State* st, const double* __restrict__ diags, const 
     // chunk: the index searchsorted(side='right') returns on the stored cdf.
     __shared__ double s_end[MAXT];
     __shared__ double s_off[MAXT];
-    __shared__ double s_last;
+    __shared__ double s_last, s_inv_last;
     double tot = 0.0;
     __syncthreads();
     // Rejection rounds.  Each round draws at least one new index unless every
@@ -109,10 +114,13 @@ __device__ void sample_block(State* st, const double* __restrict__ diags, const 
         tot = run;
       }
       const double off = block_exclusive_scan(tot, shd, (double*)nullptr);
-      if (lo < hi && hi == nrem) s_last = off + tot;
+      if (lo < hi && hi == nrem) {
+        s_last = off + tot;
+        s_inv_last = 1.0 / s_last;  // once, by the thread holding the last chunk
+      }
       s_off[tid] = off;
       __syncthreads();
-      const double inv_last = 1.0 / s_last;
+      const double inv_last = s_inv_last;
       s_end[tid] = lo < hi ? (hi == nrem ? 1.0 : (off + tot) * inv_last) : 2.0;
       __syncthreads();
       if (tid < need) {
