@@ -38,6 +38,7 @@ def test_null_arguments_rejected_without_gpu(rbrp_lib):
     r = _lib.Result()
     assert rbrp_lib.rbrp_id_f64(None, 4, 4, None, 4, None, None, ctypes.byref(r)) == 1
     assert rbrp_lib.rbrp_copy_T(None, None, 0) == 1
+    assert rbrp_lib.rbrp_copy_L(None, None, 0) == 1
 
 
 def test_create_without_gpu_fails_cleanly(rbrp_lib):
